@@ -1,0 +1,347 @@
+"""Benchmark of the Monte Carlo cycle: particle-steps per second.
+
+A step is one iteration of the reference main loop (liquid Euler step +
+cycleProcess: model update, contribution scatter, move, exit, division,
+compaction, merge) over the whole particle container of one scenario.
+Workload (default): 8x8x8 lattice with a toroidal recirculation, 4 liquid
+species, 1e7 particles, FP64 Monod + overflow model, glucose inlet at
+compartment 0, outlet at 511, dt 0.05 s.  Inputs are synthetic (seeded).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl bmc|reference]
+
+With N > 1 (torchrun, one process per GPU) every rank advances its own
+independent replica (different seed): the path has no data exchange, so
+the scaling is weak and the value is the sum of particle-steps over ranks
+divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "biocma-mcst_gb300"))
+
+METRIC = "particle-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="bmc", choices=["bmc", "reference"])
+    ap.add_argument("--workload", type=int, default=2)
+    ap.add_argument("--particles", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=50)
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload_config(scen):
+    return {
+        "workload": scen.name,
+        "n_particles": scen.n_particles,
+        "n_compartments": scen.net.n_c,
+        "max_neighbors": scen.net.K,
+        "n_species": scen.n_species,
+        "model": scen.model.name,
+        "state_dtype": "f64" if scen.model.f64 else "f32",
+        "n_var": scen.model.n_var,
+        "dt_s": scen.dt,
+        "feeds": [{"inlet": f.inlet, "outlet": f.outlet, "flow_m3_s": f.flow} for f in scen.feeds],
+        "l2": "inputs larger than L2: %.2f GB of particle state streamed per step"
+              % (scen.n_particles * scen.algorithmic_bytes() / 1e9),
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.12)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(scen):
+    """DRAM bytes per particle of the cycle kernel from the committed ncu
+    summary (profiles/k_cycle_<workload>.txt, line 'dram_bytes_per_particle:')."""
+    p = os.path.join(ROOT, "profiles", f"k_cycle_{scen.name}.txt")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def cpu_baseline(scen, steps: int, threads: int):
+    """The CPU restatement (port of the reference algorithm) on the host
+    cores: the same workload, `steps` steps, all `threads` threads."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(scen)
+    o.init_particles()
+    o.step(threads)  # first-touch of the arrays
+    n0 = o.n_used - int(o.s.inactive)
+    t0 = time.perf_counter()
+    o.run(steps, threads)
+    el = time.perf_counter() - t0
+    n1 = o.n_used - int(o.s.inactive)
+    return 0.5 * (n0 + n1) * steps / el, el
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from bmc import scenarios
+
+    threads = os.cpu_count() or 1
+    total = args.steps + args.warmup
+    full = scenarios.workload(args.workload, n_particles=args.particles)
+    # bounded sample: at most ~2e9 particle-steps for the whole run
+    n = min(full.n_particles, max(100_000, int(2e9 // max(total, 1))))
+    scen = scenarios.workload(args.workload, n_particles=n)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    o = oracle.Oracle(scen)
+    o.init_particles()
+    o.run(args.warmup, threads)
+    n0 = o.n_used - int(o.s.inactive)
+    t0 = time.perf_counter()
+    o.run(args.steps, threads)
+    el = time.perf_counter() - t0
+    n1 = o.n_used - int(o.s.inactive)
+    value = 0.5 * (n0 + n1) * args.steps / el
+    cfg = workload_config(full)
+    sample = f"{n} particles per step (full workload {full.n_particles}), {args.steps} timed steps"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": cfg["state_dtype"], "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference path (C, OpenMP); the reference itself needs "
+                "Kokkos 5.1.1, Eigen, MPI, meson and rcmtool, none of which is available",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args):
+    world, rank, local = dist_env()
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from bmc import scenarios, sim
+
+    sim.set_device(local)
+    scen = scenarios.workload(args.workload, n_particles=args.particles,
+                              seed=None if world == 1 else 2024 + rank)
+    g = sim.GpuScenario(scen)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up (graph capture, first touch)
+    g.run(max(args.warmup, 3))
+    st0 = g.stats()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = sim.launch_count()
+    barrier()
+    st1, ms = g.run_timed(args.steps)
+    barrier()
+    launches = sim.launch_count() - launches0
+    clk = clocks.stop()
+    alive0 = st0["n_used"] - st0["inactive"]
+    alive1 = st1["n_used"] - st1["inactive"]
+    psteps = 0.5 * (alive0 + alive1) * args.steps
+    t = ms / 1e3
+    if dist is not None:
+        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        pp = torch.tensor([psteps], dtype=torch.float64, device="cuda")
+        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+        t, psteps = float(tt.item()), float(pp.item())
+    value = psteps / t
+
+    # per-kernel durations (events between the six kernels of a step)
+    kms = []
+    alive_k = []
+    for _ in range(20):
+        s_, ms6 = g.step_timed()
+        kms.append(ms6)
+        alive_k.append(s_["n_used"] - s_["inactive"])
+    cyc_ms = statistics.mean(k[1] for k in kms)
+    step_ms = statistics.mean(sum(k) for k in kms)
+    B = scen.algorithmic_bytes()
+    achieved = B * statistics.mean(alive_k) / (cyc_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    tpp = profiled_traffic(scen)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
+                "traffic": (tpp * statistics.mean(alive_k)) if tpp else None,
+                "kernel": "k_cycle", "algorithmic_bytes_per_particle": B,
+                "kernel_ms": cyc_ms, "step_kernels_ms": step_ms,
+                "kernel_share_of_step": cyc_ms / step_ms}
+
+    # end to end through the public per-step API: host-side feed update
+    # (H2D), one step, concentrations + counters read back (D2H)
+    e2e = None
+    if args.e2e_steps > 0:
+        import ctypes as ct
+
+        import numpy as np
+
+        from bmc._lib import Feed, call
+
+        arr = (Feed * len(scen.feeds))()
+        for k, fd in enumerate(scen.feeds):
+            arr[k].inlet, arr[k].outlet, arr[k].flow = fd.inlet, fd.outlet, fd.flow
+            for sp in range(len(fd.conc)):
+                arr[k].conc[sp] = float(fd.conc[sp])
+        conc = np.zeros((scen.net.n_c, scen.n_species))
+        h0, d0 = sim.transfer_bytes()
+        barrier()
+        t0 = time.perf_counter()
+        a0 = g.stats()
+        ps = 0.0
+        for _ in range(args.e2e_steps):
+            call("bmc_set_feeds", g.handle, len(scen.feeds), arr)
+            s_ = g.step()
+            call("bmc_read_liquid", g.handle, ct.c_void_p(conc.ctypes.data), None, None)
+            ps += s_["n_used"] - s_["inactive"]
+        barrier()
+        te = time.perf_counter() - t0
+        h1, d1 = sim.transfer_bytes()
+        ev = ps / te
+        if dist is not None:
+            tt = torch.tensor([te], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            pp = torch.tensor([ps], dtype=torch.float64, device="cuda")
+            dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+            ev = float(pp.item()) / float(tt.item())
+        e2e = {"value": ev, "unit": METRIC,
+               "h2d_bytes_per_step": (h1 - h0) / args.e2e_steps,
+               "d2h_bytes_per_step": (d1 - d0) / args.e2e_steps,
+               "api": "bmc_set_feeds + bmc_step + bmc_read_liquid per step (C-ABI, host buffers)"}
+        del a0
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        csteps = 10
+        cval, cel = cpu_baseline(scen, csteps, threads)
+        cpu = {"value": cval, "unit": METRIC, "cores": threads, "kind": "port",
+               "sample": f"{scen.n_particles} particles x {csteps} steps of the same workload "
+                         f"({cel:.1f} s), C/OpenMP restatement of the reference path"}
+
+    if rank == 0:
+        cfg = workload_config(scen)
+        cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+        line = {
+            "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": cfg["state_dtype"], "data": "synthetic", "config": cfg,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    g.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

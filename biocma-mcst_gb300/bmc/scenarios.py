@@ -1,0 +1,197 @@
+"""Scenario descriptions: network + cell model + liquid state + feeds.
+
+A :class:`Scenario` is plain data (numpy arrays); both the GPU library and
+the CPU oracle are set up from the same object, so they see identical inputs.
+The five workloads of the benchmark are built by :func:`workload`.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .networks import Network, lattice_vortex, ring_network, single_compartment
+
+MODEL_MONOD = 1
+MODEL_OVERFLOW = 2
+MODEL_FIXED_LENGTH = 3
+
+MU_MAX = 0.77 / 3600.0  # 1/s
+
+
+@dataclass
+class ModelSpec:
+    """Cell model as the ModelType concept describes it (n_var, n_c, FloatType)."""
+
+    name: str
+    model_id: int
+    n_var: int
+    n_ctb: int
+    f64: bool
+    params: np.ndarray  # float64[16]
+    ctb_bound: np.ndarray  # float64[n_ctb]: bound on |contribution| per particle
+
+    @property
+    def itemsize(self) -> int:
+        return 8 if self.f64 else 4
+
+
+def monod(f64: bool = True, mu_max: float = MU_MAX, ks: float = 0.01, y: float = 0.5,
+          m_div: float = 2.0, m_lo: float = 0.9, m_span: float = 0.2) -> ModelSpec:
+    p = np.zeros(16)
+    p[:6] = [mu_max, ks, y, m_div, m_lo, m_span]
+    bound = np.array([mu_max * 4.0 * m_div / y])
+    return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, bound)
+
+
+def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
+    y_ox, y_of, y_ac, y_o, y_c, y_cof = 0.5, 0.15, 0.6, 0.6, 0.7, 0.3
+    qs_max = mu_max / y_ox
+    qo_max = 0.7 * qs_max
+    m_div = 2.0
+    p = np.zeros(16)
+    p[:13] = [qs_max, 0.01, qo_max, 1e-4, y_ox, y_of, y_ac, y_o, y_c, m_div, y_cof, 0.9, 0.2]
+    m = 4.0 * m_div
+    bound = np.array([qs_max * m, y_o * qo_max * m, y_ac * qs_max * m, (y_c + y_cof) * qs_max * m])
+    return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, bound)
+
+
+def fixed_length() -> ModelSpec:
+    """The reference's FixedLength model (float state, one contribution)."""
+    l_dot_max = np.float32(2e-6 / 3600.0)
+    d_m = np.float32(0.6e-6)
+    lin = np.float32(1000) * np.float32(math.pi) * d_m * d_m / np.float32(4.0)
+    phi = float((l_dot_max * lin) / np.float32(0.5))
+    p = np.zeros(16)
+    return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([4.0 * phi]))
+
+
+@dataclass
+class Feed:
+    inlet: int
+    outlet: int  # -1 when the feed has no outlet
+    flow: float  # m^3/s
+    conc: np.ndarray  # kg/m^3 per species
+
+
+@dataclass
+class Scenario:
+    name: str
+    net: Network
+    model: ModelSpec
+    n_particles: int
+    n_species: int
+    c0: np.ndarray  # [n_c, n_species]
+    feeds: list = field(default_factory=list)
+    dt: float = 0.1
+    n_steps: int = 100
+    seed: int = 42
+    x0: float = 0.5  # initial biomass concentration, kg/m^3 (sets the weight)
+    alloc_factor: float = 1.5
+    dead_ratio_threshold: float = 0.01
+    min_removal: int = 0
+    uniform_init: bool = True
+
+    @property
+    def capacity(self) -> int:
+        return int(math.ceil(self.n_particles * self.alloc_factor))
+
+    def ctb_exponents(self, weight: float) -> np.ndarray:
+        """Quantum exponent per contribution: |q| <= 2^42 for any particle."""
+        e = np.zeros(8, dtype=np.int32)
+        for j in range(self.model.n_ctb):
+            vmax = weight * float(self.model.ctb_bound[j])
+            e[j] = int(math.ceil(math.log2(vmax))) - 42 if vmax > 0 else -1074
+        return e
+
+    def algorithmic_bytes(self) -> int:
+        """Bytes per particle-step: state + u32 compartment + status + two f32
+        ages, each read and written once."""
+        return 2 * (self.model.n_var * self.model.itemsize + 4 + 1 + 8)
+
+
+CTB_QMAX = 1 << 42
+
+
+def weight_from_mass(total_mass: float, x0: float, total_volume: float) -> float:
+    """post_init_weight (apps/libs/mc/src/unit.cpp L233-L257): w = X0 V / m_tot."""
+    return (x0 * total_volume) / total_mass
+
+
+def workload(index: int, n_particles: int | None = None, n_steps: int | None = None,
+             seed: int | None = None, f64: bool | None = None) -> Scenario:
+    """Benchmark workloads (synthetic; no public dataset is involved).
+
+    1: ring of 10 + 2 random links, 1 species, 1e5 particles, FP64 Monod,
+       dt 0.1 s, 1000 steps, closed reactor.
+    2: 8^3 lattice vortex, 4 species, 1e7 particles, FP64 overflow model,
+       glucose inlet at 0, outlet at 511, D = 0.1/h, dt 0.05 s, 5000 steps.
+    3: 16^3 lattice vortex, 5e7 particles, FP32 overflow model, dt 0.05 s,
+       2000 steps.
+    """
+    if index == 1:
+        net = ring_network(10, 2, 1e-3, 0.5, 0.5e-3, 2e-3, seed=42 if seed is None else seed,
+                           max_courant=0.5, dt=0.1)
+        model = monod(f64=True if f64 is None else f64)
+        n_s = 1
+        c0 = np.full((net.n_c, n_s), 5.0)
+        return Scenario("ring10_monod_fp64", net, model, n_particles or 100_000, n_s, c0, [],
+                        dt=0.1, n_steps=n_steps or 1000, seed=42 if seed is None else seed)
+    if index in (2, 3):
+        n = 8 if index == 2 else 16
+        net = lattice_vortex(n, side=1.0, peak_velocity=0.5, noise=0.1,
+                             seed=7 if seed is None else seed)
+        use_f64 = (index == 2) if f64 is None else f64
+        model = overflow(f64=use_f64)
+        n_s = 4
+        c0 = np.zeros((net.n_c, n_s))
+        c0[:, 0] = 5.0
+        c0[:, 1] = 8e-3
+        flow = 0.1 / 3600.0 * net.total_volume
+        conc = np.zeros(n_s)
+        conc[0] = 20.0
+        feeds = [Feed(0, net.n_c - 1, flow, conc)]
+        npart = n_particles or (10_000_000 if index == 2 else 50_000_000)
+        steps = n_steps or (5000 if index == 2 else 2000)
+        name = "lattice512_overflow_fp64" if index == 2 else "lattice4096_overflow_fp32"
+        return Scenario(name, net, model, npart, n_s, c0, feeds, dt=0.05, n_steps=steps,
+                        seed=2024 if seed is None else seed)
+    raise ValueError(f"unknown workload {index}")
+
+
+def small_ring(n_particles: int = 4096, n_c: int = 10, seed: int = 3, f64: bool = True,
+               model: ModelSpec | None = None, n_steps: int = 20, dt: float = 0.1,
+               feeds: bool = False) -> Scenario:
+    """Small ring scenario for parity tests."""
+    net = ring_network(n_c, 2, 1e-3, 0.5, 0.5e-3, 2e-3, seed=seed, max_courant=0.5, dt=dt)
+    model = model or monod(f64=f64)
+    n_s = max(1, model.n_ctb)
+    c0 = np.zeros((n_c, n_s))
+    c0[:, 0] = 5.0
+    if n_s > 1:
+        c0[:, 1] = 8e-3
+    fl = []
+    if feeds:
+        conc = np.zeros(n_s)
+        conc[0] = 20.0
+        fl = [Feed(0, n_c - 1, 5e-5, conc)]
+    return Scenario(f"small_ring{n_c}", net, model, n_particles, n_s, c0, fl, dt=dt,
+                    n_steps=n_steps, seed=seed)
+
+
+def zero_d(n_particles: int = 4096, seed: int = 5, model: ModelSpec | None = None,
+           n_steps: int = 10, dt: float = 0.1, outlet: bool = True) -> Scenario:
+    """0-D reactor (one compartment): move disabled, optional outlet."""
+    net = single_compartment(1e-3)
+    model = model or monod(f64=True)
+    n_s = max(1, model.n_ctb)
+    c0 = np.zeros((1, n_s))
+    c0[:, 0] = 5.0
+    fl = []
+    if outlet:
+        conc = np.zeros(n_s)
+        conc[0] = 20.0
+        fl = [Feed(0, 0, 2e-4, conc)]
+    return Scenario("zero_d", net, model, n_particles, n_s, c0, fl, dt=dt, n_steps=n_steps,
+                    seed=seed)

@@ -1,0 +1,246 @@
+"""Host-side mirror of the reference's simulation-core objects for this path.
+
+``GpuScenario`` plays the role of SimulationUnit + ParticlesContainer +
+ReactorDomain + ScalarSimulation (apps/libs/simulation/public/simulation/
+simulation.hpp; apps/libs/mc/public/mc/particles_container.hpp): it creates
+a libbmc scenario from a :class:`bmc.scenarios.Scenario`, uploads the
+domain, transition, concentrations and feeds, initialises the particles
+and exposes cycleProcess / one main-loop step / n steps.  Every call goes
+through the C-ABI; nothing here computes the cycle.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+from ._lib import Feed, ScenarioDesc, StepStats, call
+
+
+def _p(a: np.ndarray):
+    return ct.c_void_p(a.ctypes.data)
+
+
+def scenario_desc(scen, capacity: int | None = None) -> ScenarioDesc:
+    m = scen.model
+    d = ScenarioDesc()
+    d.model.model = m.model_id
+    d.model.f64 = 1 if m.f64 else 0
+    d.model.n_var = m.n_var
+    d.model.n_ctb = m.n_ctb
+    for k in range(16):
+        d.model.params[k] = float(m.params[k])
+    d.n_species = scen.n_species
+    d.capacity = capacity or scen.capacity
+    d.seed = scen.seed
+    d.dead_ratio_threshold = scen.dead_ratio_threshold
+    d.min_removal = scen.min_removal
+    for j in range(m.n_ctb):
+        d.ctb_bound[j] = float(m.ctb_bound[j])
+    return d
+
+
+def transition_coo(net):
+    """COO of the transition matrix: off-diagonal F(i->j), diagonal -Q_out."""
+    rows = np.concatenate([net.src, np.arange(net.n_c)]).astype(np.uint64)
+    cols = np.concatenate([net.dst, np.arange(net.n_c)]).astype(np.uint64)
+    vals = np.concatenate([net.flow, -net.out_flow]).astype(np.float64)
+    return rows, cols, vals
+
+
+class GpuScenario:
+    def __init__(self, scen, capacity: int | None = None, init: bool = True,
+                 n_particles: int | None = None):
+        self.scen = scen
+        self.lib = _lib.load()
+        self.handle = ct.c_void_p()
+        desc = scenario_desc(scen, capacity)
+        call("bmc_scenario_create", ct.byref(desc), ct.byref(self.handle))
+        self.cap = (int(desc.capacity) + 1023) // 1024 * 1024  # slots, rounded to whole tiles
+        net = scen.net
+        vol = np.ascontiguousarray(net.volume, dtype=np.float64)
+        nbr = np.ascontiguousarray(net.neighbors, dtype=np.uint64)
+        outf = np.ascontiguousarray(net.out_flow, dtype=np.float64)
+        cdf = np.ascontiguousarray(net.cdf, dtype=np.float64)
+        call("bmc_domain_update", self.handle, net.n_c, net.K, _p(vol), _p(nbr), _p(outf), _p(cdf))
+        r, c, v = transition_coo(net)
+        call("bmc_set_transition_coo", self.handle, net.n_c, len(v), _p(r), _p(c), _p(v))
+        c0 = np.ascontiguousarray(scen.c0, dtype=np.float64)
+        call("bmc_set_concentrations", self.handle, _p(c0))
+        if scen.feeds:
+            arr = (Feed * len(scen.feeds))()
+            for k, fd in enumerate(scen.feeds):
+                arr[k].inlet = fd.inlet
+                arr[k].outlet = fd.outlet
+                arr[k].flow = fd.flow
+                for sp in range(len(fd.conc)):
+                    arr[k].conc[sp] = float(fd.conc[sp])
+            call("bmc_set_feeds", self.handle, len(scen.feeds), arr)
+        self.weight = None
+        if init:
+            self.init_particles(n_particles)
+
+    def close(self):
+        if self.handle:
+            _lib.load().bmc_scenario_destroy(self.handle)
+            self.handle = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- set-up ---------------------------------------------------------------
+    def init_particles(self, n: int | None = None) -> float:
+        n = self.scen.n_particles if n is None else n
+        w = ct.c_double()
+        call("bmc_init_particles", self.handle, n, 1 if self.scen.uniform_init else 0,
+             self.scen.x0, ct.byref(w))
+        self.weight = w.value
+        return self.weight
+
+    def set_weight(self, w: float):
+        call("bmc_set_weight", self.handle, w)
+        self.weight = w
+
+    def set_particles(self, parts: dict, next_id: int):
+        m = self.scen.model
+        ft = np.float64 if m.f64 else np.float32
+        st = np.ascontiguousarray(parts["state"], dtype=ft)
+        n = st.shape[1]
+        arrs = [np.ascontiguousarray(parts[k], dtype=t) for k, t in
+                (("pos", np.uint32), ("status", np.uint8), ("age_h", np.float32),
+                 ("age_d", np.float32), ("id", np.uint32))]
+        call("bmc_set_particles", self.handle, n, _p(st), *[_p(a) for a in arrs], next_id)
+
+    # -- stepping ---------------------------------------------------------------
+    def cycle(self, dt: float | None = None) -> dict:
+        st = StepStats()
+        call("bmc_cycle", self.handle, dt or self.scen.dt, ct.byref(st))
+        return st.as_dict()
+
+    def step(self, dt: float | None = None) -> dict:
+        st = StepStats()
+        call("bmc_step", self.handle, dt or self.scen.dt, ct.byref(st))
+        return st.as_dict()
+
+    def step_timed(self, dt: float | None = None):
+        """One step with per-kernel CUDA-event durations (ms): liquid, cycle,
+        plan, divide, compact, merge."""
+        st = StepStats()
+        ms = (ct.c_float * 6)()
+        call("bmc_step_timed", self.handle, dt or self.scen.dt, ct.byref(st), ms)
+        return st.as_dict(), list(ms)
+
+    def run(self, n_steps: int, dt: float | None = None) -> dict:
+        st = StepStats()
+        call("bmc_run", self.handle, dt or self.scen.dt, n_steps, ct.byref(st))
+        return st.as_dict()
+
+    def run_timed(self, n_steps: int, dt: float | None = None):
+        """n_steps graph-replayed steps; device time (ms) from CUDA events
+        recorded on the scenario's own stream around them."""
+        st = StepStats()
+        ms = ct.c_float()
+        call("bmc_run_timed", self.handle, dt or self.scen.dt, n_steps, ct.byref(st), ct.byref(ms))
+        return st.as_dict(), ms.value
+
+    def run_async(self, n_steps: int, dt: float | None = None):
+        call("bmc_run_async", self.handle, dt or self.scen.dt, n_steps)
+
+    def synchronize(self):
+        call("bmc_synchronize", self.handle)
+
+    def stats(self) -> dict:
+        st = StepStats()
+        call("bmc_read_stats", self.handle, ct.byref(st))
+        return st.as_dict()
+
+    # -- readback -----------------------------------------------------------------
+    def particles(self) -> dict:
+        n = self.stats()["n_used"]
+        m = self.scen.model
+        ft = np.float64 if m.f64 else np.float32
+        st = np.zeros((m.n_var, max(n, 1)), dtype=ft)
+        pos = np.zeros(max(n, 1), np.uint32)
+        status = np.zeros(max(n, 1), np.uint8)
+        ah = np.zeros(max(n, 1), np.float32)
+        ad = np.zeros(max(n, 1), np.float32)
+        pid = np.zeros(max(n, 1), np.uint32)
+        got = ct.c_uint64()
+        call("bmc_read_particles", self.handle, max(n, 1), _p(st), _p(pos), _p(status), _p(ah),
+             _p(ad), _p(pid), ct.byref(got))
+        n = got.value
+        return dict(state=st[:, :n], pos=pos[:n], status=status[:n], age_h=ah[:n], age_d=ad[:n],
+                    id=pid[:n])
+
+    def liquid(self) -> dict:
+        shape = (self.scen.net.n_c, self.scen.n_species)
+        C = np.zeros(shape)
+        M = np.zeros(shape)
+        S = np.zeros(shape)
+        call("bmc_read_liquid", self.handle, _p(C), _p(M), _p(S))
+        return dict(C=C, M=M, src=S)
+
+    def repartition(self) -> np.ndarray:
+        out = np.zeros(self.scen.net.n_c, dtype=np.uint64)
+        call("bmc_repartition", self.handle, _p(out))
+        return out
+
+    def force_remove_dead(self):
+        call("bmc_force_remove_dead", self.handle)
+
+
+def debug_draws(seed: int, ids: np.ndarray, step: int, purpose: int) -> np.ndarray:
+    ids = np.ascontiguousarray(ids, dtype=np.uint32)
+    out = np.zeros((len(ids), 4), dtype=np.float32)
+    call("bmc_debug_draws", seed, _p(ids), len(ids), step, purpose, _p(out))
+    return out
+
+
+def transfer_bytes() -> tuple[int, int]:
+    h, d = ct.c_uint64(), ct.c_uint64()
+    call("bmc_transfer_bytes", ct.byref(h), ct.byref(d))
+    return h.value, d.value
+
+
+def set_device(device: int):
+    call("bmc_set_device", device)
+
+
+def launch_count() -> int:
+    v = ct.c_uint64()
+    call("bmc_launch_count", ct.byref(v))
+    return v.value
+
+
+class GpuBatch:
+    """Many scenarios advanced by one set of launches per step."""
+
+    def __init__(self, scenarios: list[GpuScenario]):
+        self.members = scenarios
+        arr = (ct.c_void_p * len(scenarios))(*[s.handle.value for s in scenarios])
+        self.handle = ct.c_void_p()
+        call("bmc_batch_create", arr, len(scenarios), ct.byref(self.handle))
+
+    def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
+        call("bmc_batch_set_shape", self.handle, threads, ppt, blocks_per_sm)
+
+    def run(self, n_steps: int, dt: float):
+        call("bmc_batch_run", self.handle, dt, n_steps)
+
+    def synchronize(self):
+        call("bmc_batch_synchronize", self.handle)
+
+    def close(self):
+        if self.handle:
+            _lib.load().bmc_batch_destroy(self.handle)
+            self.handle = ct.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,1017 @@
+// bmc_api.cu -- the C-ABI of libbmc (declared in include/bmc.h).
+//
+// Host-side responsibilities: device memory of each scenario (one arena for
+// the particle container, one for the domain and liquid state), the
+// scenario descriptor the kernels read, the per-dt quantities (move
+// probabilities on the device, outlet thresholds exp(-dt F / V) on the
+// host), the step sequence and its CUDA graph, readback.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bmc.h"
+#include "bmc_launch.h"
+
+using bmc::BatchCtl;
+using bmc::Control;
+using bmc::kTile;
+using bmc::ScenDev;
+
+namespace {
+
+thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
+std::atomic<unsigned long long> g_h2d{0}, g_d2h{0};
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define BMC_CUDA(call)                                                                  \
+  do {                                                                                  \
+    cudaError_t _e = (call);                                                            \
+    if (_e != cudaSuccess)                                                              \
+      return fail(BMC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));      \
+  } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+void count_copy(size_t n, cudaMemcpyKind kind) {
+  if (kind == cudaMemcpyHostToDevice) g_h2d += n;
+  if (kind == cudaMemcpyDeviceToHost) g_d2h += n;
+}
+cudaError_t counted_memcpy_async(void* dst, const void* src, size_t n, cudaMemcpyKind kind, cudaStream_t st) {
+  count_copy(n, kind);
+  return cudaMemcpyAsync(dst, src, n, kind, st);
+}
+cudaError_t counted_memcpy(void* dst, const void* src, size_t n, cudaMemcpyKind kind) {
+  count_copy(n, kind);
+  return cudaMemcpy(dst, src, n, kind);
+}
+
+// Carves 256-byte aligned arrays out of one allocation.
+struct Carver {
+  size_t off = 0;
+  std::vector<std::pair<void**, size_t>> items;
+  template <class T>
+  void add(T** p, size_t n_elems) {
+    items.emplace_back(reinterpret_cast<void**>(p), off);
+    off = align_up(off + std::max<size_t>(n_elems, 1) * sizeof(T), 256);
+  }
+  void add_raw(void** p, size_t bytes) {
+    items.emplace_back(p, off);
+    off = align_up(off + std::max<size_t>(bytes, 1), 256);
+  }
+  void bind(void* base) {
+    for (auto& it : items) *it.first = static_cast<char*>(base) + it.second;
+  }
+};
+
+// ceil(log2(v)) computed exactly with frexp.
+int ceil_log2(double v) {
+  int ex = 0;
+  const double m = std::frexp(v, &ex);
+  return m == 0.5 ? ex - 1 : ex;
+}
+
+}  // namespace
+
+struct bmc_scenario {
+  bmc_scenario_desc desc{};
+  const bmc::KernelSet* ks = nullptr;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  void* parena = nullptr;  // particle container
+  void* darena = nullptr;  // domain + liquid
+  void* tarena = nullptr;  // transition CSR
+  ScenDev h{};             // host mirror of the descriptor
+  ScenDev* d_desc = nullptr;
+  Control* d_ctl = nullptr;
+  BatchCtl* d_bctl = nullptr;
+  Control* h_ctl = nullptr;  // pinned
+  bool has_domain = false, has_transition = false, has_conc = false, has_weight = false;
+  std::vector<double> volume;
+  std::vector<bmc_feed> feeds;
+  double dt = -1.0;
+  // launch shape of the cycle kernel
+  unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_smem = 0;
+};
+
+struct bmc_batch {
+  std::vector<bmc_scenario*> scen;
+  const bmc::KernelSet* ks = nullptr;
+  cudaStream_t stream = nullptr;
+  ScenDev* d_table = nullptr;
+  BatchCtl* d_bctl = nullptr;
+  std::vector<ScenDev> table;
+  unsigned total_tiles = 0;
+  unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
+  cudaGraphExec_t graph = nullptr;
+  size_t graph_smem = 0;
+  double dt = -1.0;
+};
+
+namespace {
+
+int ppt_of(unsigned idx) { return idx == 0 ? 1 : (idx == 1 ? 2 : 4); }
+
+int upload_desc(bmc_scenario* s) {
+  BMC_CUDA(counted_memcpy_async(s->d_desc, &s->h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream));
+  return BMC_OK;
+}
+
+// Outlets follow the feeds in order (SimulationUnit::update_feed assigns the
+// leaving-flow slots in feed order); thresholds exp(-(dt*F)/V).
+void derive_outlets(bmc_scenario* s) {
+  s->h.n_feeds = (uint32_t)s->feeds.size();
+  s->h.n_outlets = 0;
+  for (size_t f = 0; f < s->feeds.size(); ++f) {
+    const bmc_feed& fd = s->feeds[f];
+    s->h.feed_in[f] = fd.inlet;
+    s->h.feed_out[f] = fd.outlet;
+    s->h.feed_flow[f] = fd.flow;
+    for (int sp = 0; sp < bmc::kMaxSpecies; ++sp) s->h.feed_conc[f * bmc::kMaxSpecies + sp] = fd.conc[sp];
+    if (fd.outlet >= 0) {
+      const unsigned o = s->h.n_outlets++;
+      s->h.outlet_idx[o] = (uint32_t)fd.outlet;
+      s->h.outlet_flow[o] = fd.flow;
+      const double vol = s->volume[(size_t)fd.outlet];
+      s->h.outlet_thr[o] = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
+    }
+  }
+}
+
+int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
+  if (!(dt > 0.0)) return fail(BMC_E_INVALID, "dt must be > 0");
+  if (dt == s->dt) return BMC_OK;
+  s->dt = dt;
+  s->h.dt = dt;
+  derive_outlets(s);
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  if (launch_pmove) {
+    bmc::launch_pmove(1, s->stream, s->d_desc);
+    g_launches++;
+    BMC_CUDA(cudaGetLastError());
+  }
+  return BMC_OK;
+}
+
+size_t cycle_smem(const ScenDev& h, int n_ctb) { return (size_t)h.n_c * n_ctb * sizeof(unsigned long long); }
+
+int prepare_cycle(const bmc::KernelSet* ks, unsigned threads, unsigned ppt_index, unsigned bps_req,
+                  size_t smem, int sm_count, unsigned* grid_out) {
+  const void* fn = ks->cycle_fn[ppt_index];
+  if (smem > 227 * 1024)
+    return fail(BMC_E_UNSUPPORTED, "n_compartments * n_contributions too large for the shared accumulator");
+  BMC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int bps = 0;
+  BMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, (int)threads, smem));
+  if (bps < 1) return fail(BMC_E_UNSUPPORTED, "cycle kernel cannot be resident with this shape");
+  if (bps_req > 0) bps = std::min<int>(bps, (int)bps_req);
+  *grid_out = (unsigned)(sm_count * bps);
+  return BMC_OK;
+}
+
+// Enqueue one step (liquid step optional) for a table of scenarios.
+int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, BatchCtl* d_bctl,
+                 int do_scalar, unsigned threads, unsigned ppt_index, unsigned grid, size_t smem,
+                 int sm_count) {
+  const int ppt = ppt_of(ppt_index);
+  if (kTile % (int)(threads * ppt) != 0) return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
+  bmc::launch_liquid(n_scen, st, d_table, d_bctl, do_scalar);
+  ks->cycle[ppt_index](dim3(grid), dim3(threads), smem, st, d_table, n_scen, d_bctl);
+  bmc::launch_plan(n_scen, st, d_table);
+  ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
+  ks->compact(dim3(sm_count * 2), st, d_table, n_scen);
+  ks->merge(dim3(sm_count * 2), st, d_table, n_scen);
+  g_launches += 6;
+  BMC_CUDA(cudaGetLastError());
+  return BMC_OK;
+}
+
+int read_ctl(bmc_scenario* s, bmc_step_stats* out) {
+  BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  if (out) {
+    const Control& c = *s->h_ctl;
+    std::memset(out, 0, sizeof(*out));
+    out->n_used = c.n_used;
+    out->inactive = c.inactive;
+    out->births = c.last_births;
+    out->exits = c.last_exits;
+    out->moves = c.last_moves;
+    out->overflow = c.last_overflow;
+    out->requested_divisions = c.last_req_div;
+    out->clamped = c.clamped;
+    out->next_id = c.next_id;
+    out->step = c.step;
+    out->compacted = c.last_compacted;
+    out->error = c.error;
+    for (int k = 0; k < 8; ++k) out->mass_balance[k] = c.mass_balance[k];
+  }
+  if (s->h_ctl->error) return fail(BMC_E_DEVICE, "device error word set: " + std::to_string(s->h_ctl->error));
+  return BMC_OK;
+}
+
+int check_ready(bmc_scenario* s, bool need_liquid) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update)");
+  if (!s->has_conc) return fail(BMC_E_STATE, "concentrations not set (bmc_set_concentrations)");
+  if (!s->has_weight) return fail(BMC_E_STATE, "particles not initialised (bmc_init_particles / bmc_set_weight)");
+  if (need_liquid && !s->has_transition) return fail(BMC_E_STATE, "transition not set (bmc_set_transition_coo)");
+  return BMC_OK;
+}
+
+int set_quanta(bmc_scenario* s) {
+  for (int j = 0; j < bmc::kMaxSpecies; ++j) {
+    int e = -1074 + 64;
+    if (j < (int)s->h.n_ctb) {
+      const double vmax = s->h.weight * s->desc.ctb_bound[j];
+      if (!(vmax > 0.0) || !std::isfinite(vmax)) return fail(BMC_E_INVALID, "contribution bound must be > 0");
+      e = ceil_log2(vmax) - 42;
+    }
+    s->h.ctb_exp[j] = e;
+    s->h.ctb_scale[j] = std::ldexp(1.0, -e);
+    s->h.ctb_scale_up[j] = std::ldexp(1.0, e);
+  }
+  return BMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmc_version(int32_t* major, int32_t* minor) {
+  if (major) *major = BMC_VERSION_MAJOR;
+  if (minor) *minor = BMC_VERSION_MINOR;
+  return BMC_OK;
+}
+
+const char* bmc_last_error(void) { return g_last_error.c_str(); }
+
+int bmc_device_sm_count(int32_t* sm_count) {
+  int dev = 0;
+  BMC_CUDA(cudaGetDevice(&dev));
+  int n = 0;
+  BMC_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+  if (sm_count) *sm_count = n;
+  return BMC_OK;
+}
+
+int bmc_set_device(int32_t device) {
+  BMC_CUDA(cudaSetDevice(device));
+  return BMC_OK;
+}
+
+int bmc_transfer_bytes(uint64_t* h2d, uint64_t* d2h) {
+  if (h2d) *h2d = g_h2d.load();
+  if (d2h) *d2h = g_d2h.load();
+  return BMC_OK;
+}
+
+int bmc_launch_count(uint64_t* count) {
+  if (count) *count = g_launches.load();
+  return BMC_OK;
+}
+
+int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
+  if (!desc || !out) return fail(BMC_E_INVALID, "null argument");
+  const bmc::KernelSet* ks = bmc::kernel_set(desc->model.model, desc->model.f64);
+  if (!ks) return fail(BMC_E_UNSUPPORTED, "model / precision not compiled in");
+  if ((int)desc->model.n_var != ks->n_var || (int)desc->model.n_ctb != ks->n_ctb)
+    return fail(BMC_E_INVALID, "n_var / n_ctb do not match the compiled model");
+  if (desc->n_species < (uint32_t)ks->n_ctb || desc->n_species > (uint32_t)bmc::kMaxSpecies)
+    return fail(BMC_E_INVALID, "n_species must be in [n_ctb, 8]");
+  if (desc->capacity == 0 || desc->capacity > 0xFFFFFFFFull - kTile)
+    return fail(BMC_E_INVALID, "capacity must be in [1, 2^32 - 1024]");
+  auto* s = new bmc_scenario();
+  s->desc = *desc;
+  s->ks = ks;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete s;
+    return fail(BMC_E_CUDA, std::string("device set-up: ") + cudaGetErrorString(e));
+  }
+  const unsigned long long cap = align_up(desc->capacity, kTile);
+  const size_t fsz = desc->model.f64 ? 8 : 4;
+  const unsigned n_tiles = (unsigned)(cap / kTile);
+  ScenDev& h = s->h;
+  h.cap = cap;
+  h.n_tiles = n_tiles;
+  h.tile_base = 0;
+  Carver cv;
+  cv.add_raw(&h.state, fsz * ks->n_var * cap);
+  cv.add(&h.pos, cap);
+  cv.add(&h.status, cap);
+  cv.add(&h.age_h, cap);
+  cv.add(&h.age_d, cap);
+  cv.add(&h.id, cap);
+  cv.add_raw(&h.child_state, fsz * ks->n_var * cap);
+  cv.add(&h.child_pos, cap);
+  cv.add(&h.tile_births, n_tiles);
+  cv.add(&h.tile_inactive, n_tiles);
+  cv.add(&h.tile_boff, n_tiles);
+  cv.add(&h.tile_goff, n_tiles);
+  cv.add(&h.tile_soff, n_tiles);
+  cv.add(&h.bmask, cap / 32);
+  cv.add(&h.bpos, cap);
+  cv.add(&h.gap_slot, cap);
+  cv.add(&h.src_slot, cap);
+  Control* ctl_tmp = nullptr;
+  cv.add(&ctl_tmp, 1);
+  ScenDev* desc_tmp = nullptr;
+  cv.add(&desc_tmp, 1);
+  BatchCtl* bctl_tmp = nullptr;
+  cv.add(&bctl_tmp, 1);
+  e = cudaMalloc(&s->parena, cv.off);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return fail(BMC_E_CUDA, std::string("cudaMalloc particle arena: ") + cudaGetErrorString(e));
+  }
+  cv.bind(s->parena);
+  s->d_ctl = ctl_tmp;
+  s->d_desc = desc_tmp;
+  s->d_bctl = bctl_tmp;
+  h.ctl = s->d_ctl;
+  h.n_var = ks->n_var;
+  h.n_ctb = ks->n_ctb;
+  h.n_s = desc->n_species;
+  h.f64 = desc->model.f64;
+  for (int k = 0; k < 16; ++k) h.params[k] = desc->model.params[k];
+  h.seed = desc->seed;
+  h.dead_ratio = desc->dead_ratio_threshold;
+  h.min_removal = desc->min_removal;
+  e = cudaMallocHost(&s->h_ctl, sizeof(Control));
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->parena, 0, cv.off, s->stream);
+  if (e == cudaSuccess) {
+    BatchCtl b{0u, n_tiles};
+    e = counted_memcpy_async(s->d_bctl, &b, sizeof(b), cudaMemcpyHostToDevice, s->stream);
+  }
+  if (e == cudaSuccess) e = counted_memcpy_async(s->d_desc, &h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    cudaFree(s->parena);
+    if (s->h_ctl) cudaFreeHost(s->h_ctl);
+    cudaStreamDestroy(s->stream);
+    delete s;
+    return fail(BMC_E_CUDA, std::string("scenario set-up: ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return BMC_OK;
+}
+
+int bmc_scenario_destroy(bmc_scenario* s) {
+  if (!s) return BMC_OK;
+  cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->parena) cudaFree(s->parena);
+  if (s->darena) cudaFree(s->darena);
+  if (s->tarena) cudaFree(s->tarena);
+  if (s->h_ctl) cudaFreeHost(s->h_ctl);
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return BMC_OK;
+}
+
+int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* volume, const uint64_t* neighbors,
+                      const double* out_flows, const double* cdf) {
+  if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
+  if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
+  std::vector<uint32_t> nbr((size_t)n_c * K, 0u);
+  std::vector<double> cd((size_t)n_c * K, 1.0);
+  for (size_t k = 0; k < (size_t)n_c * K; ++k) {
+    if (neighbors) {
+      if (neighbors[k] >= n_c) return fail(BMC_E_INVALID, "neighbor index out of range");
+      nbr[k] = (uint32_t)neighbors[k];
+    } else {
+      nbr[k] = (uint32_t)(k / K);
+    }
+    if (cdf) cd[k] = cdf[k];
+  }
+  std::vector<double> vol(volume, volume + n_c), outf(out_flows, out_flows + n_c), vinv(n_c), diag(n_c);
+  for (uint32_t j = 0; j < n_c; ++j) {
+    if (!(vol[j] > 0.0)) return fail(BMC_E_INVALID, "volumes must be > 0");
+    if (!(outf[j] >= 0.0)) return fail(BMC_E_INVALID, "out flows must be >= 0");
+    vinv[j] = 1.0 / vol[j];
+    diag[j] = -outf[j];
+  }
+  ScenDev& h = s->h;
+  const bool resize = !s->has_domain || h.n_c != n_c || h.K != K;
+  if (resize) {
+    cudaStreamSynchronize(s->stream);
+    if (s->darena) cudaFree(s->darena);
+    s->darena = nullptr;
+    const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_ctb;
+    Carver cv;
+    cv.add(&h.pmove, n_c);
+    double* p_vol = nullptr;
+    cv.add(&p_vol, n_c);
+    double* p_out = nullptr;
+    cv.add(&p_out, n_c);
+    double* p_cdf = nullptr;
+    cv.add(&p_cdf, (size_t)n_c * K);
+    uint32_t* p_nbr = nullptr;
+    cv.add(&p_nbr, (size_t)n_c * K);
+    double* p_diag = nullptr;
+    cv.add(&p_diag, n_c);
+    double* p_vinv = nullptr;
+    cv.add(&p_vinv, n_c);
+    cv.add(&h.C, ne);
+    cv.add(&h.M, ne);
+    cv.add(&h.src, ne);
+    cv.add(&h.acc_hi, na);
+    cv.add(&h.acc_lo, na);
+    BMC_CUDA(cudaMalloc(&s->darena, cv.off));
+    cv.bind(s->darena);
+    h.volume = p_vol;
+    h.out_flow = p_out;
+    h.cdf = p_cdf;
+    h.nbr = p_nbr;
+    h.diag = p_diag;
+    h.vinv = p_vinv;
+    BMC_CUDA(cudaMemsetAsync(s->darena, 0, cv.off, s->stream));
+    s->has_conc = false;
+    s->has_transition = false;
+  }
+  h.n_c = n_c;
+  h.K = K;
+  BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.volume), vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.cdf), cd.data(), cd.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<uint32_t*>(h.nbr), nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.vinv), vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  if (!s->has_transition)
+    BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.diag), diag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  s->volume = vol;
+  s->has_domain = true;
+  const double dt = s->dt;
+  s->dt = -1.0;
+  int rc = BMC_OK;
+  if (dt > 0)
+    rc = set_dt(s, dt, true);
+  else {
+    derive_outlets(s);
+    rc = upload_desc(s);
+  }
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
+                           const double* values) {
+  if (!s || (nnz && (!rows || !cols || !values))) return fail(BMC_E_INVALID, "bad transition arguments");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  if (n != s->h.n_c) return fail(BMC_E_INVALID, "transition size differs from n_compartments");
+  // incoming lists by destination column, sources ascending, duplicates summed
+  std::vector<std::pair<std::pair<uint32_t, uint32_t>, double>> off;
+  std::vector<double> diag(n, 0.0);
+  off.reserve(nnz);
+  for (uint64_t k = 0; k < nnz; ++k) {
+    if (rows[k] >= n || cols[k] >= n) return fail(BMC_E_INVALID, "transition index out of range");
+    if (rows[k] == cols[k])
+      diag[rows[k]] += values[k];
+    else
+      off.push_back({{(uint32_t)cols[k], (uint32_t)rows[k]}, values[k]});
+  }
+  std::stable_sort(off.begin(), off.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  std::vector<uint32_t> ptr(n + 1, 0u), idx;
+  std::vector<double> val;
+  for (size_t k = 0; k < off.size(); ++k) {
+    if (!idx.empty() && k > 0 && off[k].first == off[k - 1].first) {
+      val.back() += off[k].second;
+      continue;
+    }
+    idx.push_back(off[k].first.second);
+    val.push_back(off[k].second);
+    ptr[off[k].first.first + 1]++;
+  }
+  for (uint32_t j = 0; j < n; ++j) ptr[j + 1] += ptr[j];
+  cudaStreamSynchronize(s->stream);
+  if (s->tarena) cudaFree(s->tarena);
+  s->tarena = nullptr;
+  Carver cv;
+  uint32_t* p_ptr = nullptr;
+  uint32_t* p_idx = nullptr;
+  double* p_val = nullptr;
+  cv.add(&p_ptr, n + 1);
+  cv.add(&p_idx, idx.size());
+  cv.add(&p_val, val.size());
+  BMC_CUDA(cudaMalloc(&s->tarena, cv.off));
+  cv.bind(s->tarena);
+  BMC_CUDA(counted_memcpy_async(p_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+  if (!idx.empty()) {
+    BMC_CUDA(counted_memcpy_async(p_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_val, val.data(), val.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  }
+  BMC_CUDA(counted_memcpy_async(const_cast<double*>(s->h.diag), diag.data(), n * 8, cudaMemcpyHostToDevice, s->stream));
+  s->h.in_ptr = p_ptr;
+  s->h.in_idx = p_idx;
+  s->h.in_flow = p_val;
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  s->has_transition = true;
+  return BMC_OK;
+}
+
+int bmc_set_concentrations(bmc_scenario* s, const double* conc) {
+  if (!s || !conc) return fail(BMC_E_INVALID, "null argument");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  const size_t n_c = s->h.n_c, ns = s->h.n_s;
+  std::vector<double> C(conc, conc + n_c * ns), M(n_c * ns);
+  for (size_t j = 0; j < n_c; ++j) {
+    for (size_t sp = 0; sp < ns; ++sp) {
+      if (!(C[j * ns + sp] >= 0.0)) return fail(BMC_E_INVALID, "concentrations must be >= 0");
+      M[j * ns + sp] = C[j * ns + sp] * s->volume[j];
+    }
+  }
+  BMC_CUDA(counted_memcpy_async(s->h.C, C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.M, M.data(), M.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(cudaMemsetAsync(s->h.src, 0, C.size() * 8, s->stream));
+  BMC_CUDA(cudaMemsetAsync(s->h.acc_hi, 0, n_c * s->h.n_ctb * 8, s->stream));
+  BMC_CUDA(cudaMemsetAsync(s->h.acc_lo, 0, n_c * s->h.n_ctb * 8, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  s->has_conc = true;
+  return BMC_OK;
+}
+
+int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
+  if (!s || (n_feeds && !feeds)) return fail(BMC_E_INVALID, "null argument");
+  if (n_feeds > (uint32_t)bmc::kMaxOutlets) return fail(BMC_E_INVALID, "at most 8 feeds");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  for (uint32_t f = 0; f < n_feeds; ++f) {
+    if (feeds[f].inlet >= s->h.n_c || feeds[f].outlet >= (int32_t)s->h.n_c || feeds[f].outlet < -1)
+      return fail(BMC_E_INVALID, "feed position out of range");
+    if (!(feeds[f].flow >= 0.0)) return fail(BMC_E_INVALID, "feed flow must be >= 0");
+  }
+  s->feeds.assign(feeds, feeds + n_feeds);
+  derive_outlets(s);
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_set_weight(bmc_scenario* s, double weight) {
+  if (!s || !(weight > 0.0)) return fail(BMC_E_INVALID, "weight must be > 0");
+  s->h.weight = weight;
+  int rc = set_quanta(s);
+  if (rc) return rc;
+  rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  s->has_weight = true;
+  return BMC_OK;
+}
+
+static int write_ctl_fresh(bmc_scenario* s, unsigned long long n, unsigned long long next_id,
+                           unsigned long long inactive) {
+  BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  Control c = *s->h_ctl;
+  c.n_used = n;
+  c.next_id = next_id;
+  c.inactive = inactive;
+  BMC_CUDA(counted_memcpy_async(s->d_ctl, &c, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_init_particles(bmc_scenario* s, uint64_t n, int32_t uniform_init, double x0, double* weight_out) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  if (n > s->h.cap) return fail(BMC_E_CAPACITY, "more particles than capacity");
+  if (n == 0) return fail(BMC_E_INVALID, "n must be > 0");
+  double* d_mass = nullptr;
+  BMC_CUDA(cudaMalloc(&d_mass, n * sizeof(double)));
+  const uint32_t span = uniform_init ? s->h.n_c : 1u;
+  s->ks->init(dim3(s->sm_count * 8), s->stream, s->d_desc, n, 0u, span, d_mass);
+  g_launches++;
+  std::vector<double> mass(n);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = counted_memcpy_async(mass.data(), d_mass, n * 8, cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(d_mass);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("init: ") + cudaGetErrorString(e));
+  double total = 0.0;
+  for (uint64_t i = 0; i < n; ++i) total += mass[i];
+  double vtot = 0.0;
+  for (double v : s->volume) vtot += v;
+  const double w = (x0 * vtot) / total;
+  if (!(w > 0.0) || !std::isfinite(w)) return fail(BMC_E_INVALID, "initial weight is not positive");
+  int rc = write_ctl_fresh(s, n, n, 0ull);
+  if (rc) return rc;
+  rc = bmc_set_weight(s, w);
+  if (rc) return rc;
+  if (weight_out) *weight_out = w;
+  return BMC_OK;
+}
+
+int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint32_t* pos, const uint8_t* status,
+                      const float* age_h, const float* age_d, const uint32_t* id, uint64_t next_id) {
+  if (!s || !state || !pos || !status || !age_h || !age_d || !id) return fail(BMC_E_INVALID, "null argument");
+  if (n > s->h.cap) return fail(BMC_E_CAPACITY, "more particles than capacity");
+  const size_t fsz = s->h.f64 ? 8 : 4;
+  for (int v = 0; v < (int)s->h.n_var; ++v)
+    BMC_CUDA(counted_memcpy_async(static_cast<char*>(s->h.state) + (size_t)v * s->h.cap * fsz,
+                             static_cast<const char*>(state) + (size_t)v * n * fsz, n * fsz, cudaMemcpyHostToDevice,
+                             s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.pos, pos, n * 4, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.status, status, n, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.age_h, age_h, n * 4, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.age_d, age_d, n * 4, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.id, id, n * 4, cudaMemcpyHostToDevice, s->stream));
+  unsigned long long inactive = 0;
+  for (uint64_t i = 0; i < n; ++i) inactive += status[i] != BMC_STATUS_IDLE;
+  return write_ctl_fresh(s, n, next_id, inactive);
+}
+
+static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
+  if (s->graph && s->graph_smem == smem) return BMC_OK;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  cudaGraph_t g = nullptr;
+  BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  const unsigned long long before = g_launches.load();
+  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->d_bctl, 1, s->threads, s->ppt_index, grid, smem,
+                        s->sm_count);
+  g_launches = before;
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  s->graph_smem = smem;
+  return BMC_OK;
+}
+
+static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_scalar, bool use_graph) {
+  int rc = check_ready(s, do_scalar != 0);
+  if (rc) return rc;
+  rc = set_dt(s, dt, true);
+  if (rc) return rc;
+  const size_t smem = cycle_smem(s->h, s->ks->n_ctb);
+  unsigned grid = 0;
+  rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
+  if (rc) return rc;
+  if (use_graph && do_scalar) {
+    rc = ensure_graph(s, grid, smem);
+    if (rc) return rc;
+    for (uint32_t k = 0; k < n_steps; ++k) {
+      BMC_CUDA(cudaGraphLaunch(s->graph, s->stream));
+      g_launches += 6;
+    }
+    return BMC_OK;
+  }
+  for (uint32_t k = 0; k < n_steps; ++k) {
+    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->d_bctl, do_scalar, s->threads, s->ppt_index, grid, smem,
+                      s->sm_count);
+    if (rc) return rc;
+  }
+  return BMC_OK;
+}
+
+int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats) {
+  int rc = scenario_steps(s, dt, 1, 0, false);
+  if (rc) return rc;
+  return read_ctl(s, stats);
+}
+
+int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
+  int rc = scenario_steps(s, dt, 1, 1, false);
+  if (rc) return rc;
+  return read_ctl(s, stats);
+}
+
+int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats) {
+  int rc = scenario_steps(s, dt, n_steps, 1, true);
+  if (rc) return rc;
+  return read_ctl(s, stats);
+}
+
+int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps) { return scenario_steps(s, dt, n_steps, 1, true); }
+
+int bmc_run_timed(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats, float* elapsed_ms) {
+  int rc = check_ready(s, true);
+  if (rc) return rc;
+  rc = set_dt(s, dt, true);  // outside the timed region
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  BMC_CUDA(cudaEventCreate(&e0));
+  BMC_CUDA(cudaEventCreate(&e1));
+  BMC_CUDA(cudaEventRecord(e0, s->stream));
+  rc = scenario_steps(s, dt, n_steps, 1, true);
+  cudaEventRecord(e1, s->stream);
+  if (rc == BMC_OK) rc = read_ctl(s, stats);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  if (elapsed_ms) *elapsed_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+int bmc_synchronize(bmc_scenario* s) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_read_stats(bmc_scenario* s, bmc_step_stats* stats) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  return read_ctl(s, stats);
+}
+
+int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* pos, uint8_t* status, float* age_h,
+                       float* age_d, uint32_t* id, uint64_t* n_out) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  const uint64_t n = s->h_ctl->n_used;
+  if (n_out) *n_out = n;
+  if (n > max_n) return fail(BMC_E_CAPACITY, "host buffers smaller than n_used");
+  const size_t fsz = s->h.f64 ? 8 : 4;
+  if (state)
+    for (int v = 0; v < (int)s->h.n_var; ++v)
+      BMC_CUDA(counted_memcpy_async(static_cast<char*>(state) + (size_t)v * n * fsz,
+                               static_cast<const char*>(s->h.state) + (size_t)v * s->h.cap * fsz, n * fsz,
+                               cudaMemcpyDeviceToHost, s->stream));
+  if (pos) BMC_CUDA(counted_memcpy_async(pos, s->h.pos, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (status) BMC_CUDA(counted_memcpy_async(status, s->h.status, n, cudaMemcpyDeviceToHost, s->stream));
+  if (age_h) BMC_CUDA(counted_memcpy_async(age_h, s->h.age_h, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (age_d) BMC_CUDA(counted_memcpy_async(age_d, s->h.age_d, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (id) BMC_CUDA(counted_memcpy_async(id, s->h.id, n * 4, cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  if (conc) BMC_CUDA(counted_memcpy_async(conc, s->h.C, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (mass) BMC_CUDA(counted_memcpy_async(mass, s->h.M, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (sources) BMC_CUDA(counted_memcpy_async(sources, s->h.src, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_repartition(bmc_scenario* s, uint64_t* counts) {
+  if (!s || !counts) return fail(BMC_E_INVALID, "null argument");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  unsigned long long* d = nullptr;
+  BMC_CUDA(cudaMalloc(&d, s->h.n_c * 8ull));
+  cudaError_t e = cudaMemsetAsync(d, 0, s->h.n_c * 8ull, s->stream);
+  if (e == cudaSuccess) {
+    bmc::launch_repartition(s->stream, s->d_desc, d, s->sm_count * 4);
+    g_launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = counted_memcpy_async(counts, d, s->h.n_c * 8ull, cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("repartition: ") + cudaGetErrorString(e));
+  return BMC_OK;
+}
+
+int bmc_force_remove_dead(bmc_scenario* s) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  int rc = read_ctl(s, nullptr);
+  if (rc) return rc;
+  const uint64_t n = s->h_ctl->n_used;
+  const size_t fsz = s->h.f64 ? 8 : 4;
+  const int nv = (int)s->h.n_var;
+  std::vector<char> st((size_t)nv * n * fsz);
+  std::vector<uint32_t> pos(n), id(n);
+  std::vector<uint8_t> status(n);
+  std::vector<float> ah(n), ad(n);
+  uint64_t got = 0;
+  rc = bmc_read_particles(s, n, st.data(), pos.data(), status.data(), ah.data(), ad.data(), id.data(), &got);
+  if (rc) return rc;
+  uint64_t r = 0;
+  for (uint64_t i = 0; i < n; ++i) r += status[i] != BMC_STATUS_IDLE;
+  if (r == 0) return BMC_OK;
+  const uint64_t head = n - r;
+  std::vector<uint64_t> gaps, srcs;
+  for (uint64_t i = 0; i < head; ++i)
+    if (status[i] != BMC_STATUS_IDLE) gaps.push_back(i);
+  for (uint64_t i = n; i-- > head;)
+    if (status[i] == BMC_STATUS_IDLE) srcs.push_back(i);
+  for (size_t j = 0; j < gaps.size(); ++j) {
+    const uint64_t d = gaps[j], src = srcs[j];
+    for (int v = 0; v < nv; ++v) std::memcpy(&st[((size_t)v * n + d) * fsz], &st[((size_t)v * n + src) * fsz], fsz);
+    pos[d] = pos[src];
+    status[d] = BMC_STATUS_IDLE;
+    ah[d] = ah[src];
+    ad[d] = ad[src];
+    id[d] = id[src];
+  }
+  // repack the state with the new count as row stride
+  std::vector<char> st2((size_t)nv * head * fsz);
+  for (int v = 0; v < nv; ++v) std::memcpy(&st2[(size_t)v * head * fsz], &st[(size_t)v * n * fsz], head * fsz);
+  return bmc_set_particles(s, head, st2.data(), pos.data(), status.data(), ah.data(), ad.data(), id.data(),
+                           s->h_ctl->next_id);
+}
+
+// ---- batching ------------------------------------------------------------------
+
+int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out) {
+  if (!scenarios || n == 0 || !out) return fail(BMC_E_INVALID, "empty batch");
+  auto* b = new bmc_batch();
+  b->scen.assign(scenarios, scenarios + n);
+  b->ks = scenarios[0]->ks;
+  for (uint32_t i = 0; i < n; ++i) {
+    if (!scenarios[i] || scenarios[i]->ks != b->ks) {
+      delete b;
+      return fail(BMC_E_INVALID, "all scenarios of a batch must share model and precision");
+    }
+    int rc = check_ready(scenarios[i], true);
+    if (rc) {
+      delete b;
+      return rc;
+    }
+    cudaStreamSynchronize(scenarios[i]->stream);
+  }
+  b->ppt_index = b->ks->f64 ? 1 : 2;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(ScenDev) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_bctl, sizeof(BatchCtl));
+  if (e != cudaSuccess) {
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return fail(BMC_E_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+  }
+  *out = b;
+  return BMC_OK;
+}
+
+int bmc_batch_destroy(bmc_batch* b) {
+  if (!b) return BMC_OK;
+  cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_table);
+  cudaFree(b->d_bctl);
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return BMC_OK;
+}
+
+int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
+  if (!b) return fail(BMC_E_INVALID, "null batch");
+  if (threads) {
+    if (threads % 32 || threads > 256) return fail(BMC_E_INVALID, "threads must be a multiple of 32, <= 256");
+    b->threads = threads;
+  }
+  if (ppt) {
+    if (ppt != 1 && ppt != 2 && ppt != 4) return fail(BMC_E_INVALID, "ppt must be 1, 2 or 4");
+    b->ppt_index = ppt == 1 ? 0 : (ppt == 2 ? 1 : 2);
+  }
+  b->blocks_per_sm = blocks_per_sm;
+  if (kTile % (int)(b->threads * ppt_of(b->ppt_index)) != 0)
+    return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  return BMC_OK;
+}
+
+int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
+  if (!b) return fail(BMC_E_INVALID, "null batch");
+  const int n = (int)b->scen.size();
+  bool table_changed = b->table.size() != (size_t)n;
+  b->table.resize(n);
+  unsigned tiles = 0;
+  size_t smem = 0;
+  for (int i = 0; i < n; ++i) {
+    bmc_scenario* s = b->scen[i];
+    int rc = set_dt(s, dt, false);
+    if (rc) return rc;
+    ScenDev d = s->h;
+    d.tile_base = tiles;
+    tiles += d.n_tiles;
+    smem = std::max(smem, cycle_smem(d, b->ks->n_ctb));
+    if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
+    b->table[i] = d;
+  }
+  if (table_changed || b->dt != dt) {
+    BMC_CUDA(cudaStreamSynchronize(b->stream));
+    BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
+    BatchCtl bc{0u, tiles};
+    BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
+    bmc::launch_pmove(n, b->stream, b->d_table);
+    g_launches++;
+    BMC_CUDA(cudaGetLastError());
+    b->dt = dt;
+    b->total_tiles = tiles;
+  }
+  unsigned grid = 0;
+  int rc = prepare_cycle(b->ks, b->threads, b->ppt_index, b->blocks_per_sm, smem, b->scen[0]->sm_count, &grid);
+  if (rc) return rc;
+  if (!b->graph || b->graph_smem != smem) {
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+    cudaGraph_t g = nullptr;
+    BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const unsigned long long before = g_launches.load();
+    rc = enqueue_step(b->ks, b->stream, b->d_table, n, b->d_bctl, 1, b->threads, b->ppt_index, grid, smem,
+                      b->scen[0]->sm_count);
+    g_launches = before;
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    b->graph_smem = smem;
+  }
+  for (uint32_t k = 0; k < n_steps; ++k) {
+    BMC_CUDA(cudaGraphLaunch(b->graph, b->stream));
+    g_launches += 6;
+  }
+  return BMC_OK;
+}
+
+int bmc_batch_synchronize(bmc_batch* b) {
+  if (!b) return fail(BMC_E_INVALID, "null batch");
+  BMC_CUDA(cudaStreamSynchronize(b->stream));
+  return BMC_OK;
+}
+
+// ---- diagnostics -----------------------------------------------------------------
+
+int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* kernel_ms) {
+  int rc = check_ready(s, true);
+  if (rc) return rc;
+  rc = set_dt(s, dt, true);
+  if (rc) return rc;
+  const size_t smem = cycle_smem(s->h, s->ks->n_ctb);
+  unsigned grid = 0;
+  rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
+  if (rc) return rc;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
+  cudaStream_t st = s->stream;
+  const int ppt_index = (int)s->ppt_index;
+  BMC_CUDA(cudaEventRecord(ev[0], st));
+  bmc::launch_liquid(1, st, s->d_desc, s->d_bctl, 1);
+  BMC_CUDA(cudaEventRecord(ev[1], st));
+  s->ks->cycle[ppt_index](dim3(grid), dim3(s->threads), smem, st, s->d_desc, 1, s->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[2], st));
+  bmc::launch_plan(1, st, s->d_desc);
+  BMC_CUDA(cudaEventRecord(ev[3], st));
+  s->ks->divide(dim3(s->sm_count * 4), st, s->d_desc, 1, s->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[4], st));
+  s->ks->compact(dim3(s->sm_count * 2), st, s->d_desc, 1);
+  BMC_CUDA(cudaEventRecord(ev[5], st));
+  s->ks->merge(dim3(s->sm_count * 2), st, s->d_desc, 1);
+  BMC_CUDA(cudaEventRecord(ev[6], st));
+  g_launches += 6;
+  BMC_CUDA(cudaGetLastError());
+  rc = read_ctl(s, stats);
+  for (int k = 0; k < 6 && kernel_ms; ++k) cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
+}
+
+int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, uint32_t purpose, float* out) {
+  if (!ids || !out || n == 0) return fail(BMC_E_INVALID, "bad arguments");
+  uint32_t* d_ids = nullptr;
+  float* d_out = nullptr;
+  BMC_CUDA(cudaMalloc(&d_ids, n * 4));
+  cudaError_t e = cudaMalloc(&d_out, n * 16);
+  if (e == cudaSuccess) e = counted_memcpy(d_ids, ids, n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    bmc::launch_debug_draws(0, seed, d_ids, n, step, purpose, d_out);
+    g_launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = counted_memcpy(out, d_out, n * 16, cudaMemcpyDeviceToHost);
+  cudaFree(d_ids);
+  if (d_out) cudaFree(d_out);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug draws: ") + cudaGetErrorString(e));
+  return BMC_OK;
+}
+
+}  // extern "C"

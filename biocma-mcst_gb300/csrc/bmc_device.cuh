@@ -1,0 +1,348 @@
+// bmc_device.cuh -- device-side data layout, draw source and model plugins.
+//
+// Layout in HBM, per scenario (one arena, every array 256-byte aligned):
+//   state   F[n_var][cap]      SoA particle state (ModelType::SelfParticle)
+//   pos     u32[cap]           compartment (reference ParticlePositions, u64)
+//   status  u8[cap]            MC::Status
+//   age_h   f32[cap]           reference ages(i,0), hydraulic time
+//   age_d   f32[cap]           reference ages(i,1), time since division
+//   id      u32[cap]           particle identity, keys the draws
+//   child   F[n_var][cap] + u32[cap]   division buffer (children in rank order)
+//   tile_*  u32[cap/TILE]      per-tile counters (births, inactive, offsets)
+//   bmask   u32[cap/32]        birth-request bits, slot order
+//   bpos    u32[cap]           compartment of a mother when it asked to divide
+//   gap/src u32[cap]           compaction lists
+//   liquid  C, M, src: f64[n_c][n_s]; acc_hi/acc_lo: i64/u64[n_c][n_ctb]
+//   domain  pmove f64[n_c], cdf f64[n_c][K], nbr u32[n_c][K], incoming CSR
+#pragma once
+#include <cstdint>
+
+namespace bmc {
+
+constexpr int kMaxOutlets = 8;
+constexpr int kMaxSpecies = 8;
+constexpr int kMaxVar = 8;
+constexpr long long kQMax = 1LL << 42;  // |quantised contribution| bound
+// A block flushes its shared-memory accumulator before it has summed more
+// than 2^20 particles, so |partial| <= 2^62 and no int64 sum can overflow.
+constexpr unsigned kFlushParticles = 1u << 20;
+
+enum : uint8_t { kIdle = 0, kDivision = 1, kExit = 2, kDead = 3 };
+
+// Per-scenario control block, written by the kernels (device memory).
+struct Control {
+  unsigned long long n_used;
+  unsigned long long inactive;
+  unsigned long long next_id;
+  unsigned int step;
+  unsigned int error;
+  // counters of the current step (reset by the liquid step)
+  unsigned long long req_div;
+  unsigned long long exits;
+  unsigned long long moves;
+  unsigned long long clamped;
+  // plan of the current step (written by the plan kernel)
+  unsigned long long plan_n_old;
+  unsigned long long plan_to_remove;
+  unsigned long long plan_n_after;
+  unsigned long long plan_births;
+  unsigned long long plan_overflow;
+  unsigned long long plan_next_id;
+  unsigned long long plan_gaps;
+  unsigned int plan_step;
+  unsigned int plan_compact;
+  // results of the last completed step
+  unsigned long long last_births;
+  unsigned long long last_exits;
+  unsigned long long last_moves;
+  unsigned long long last_overflow;
+  unsigned long long last_req_div;
+  unsigned int last_compacted;
+  unsigned int pad;
+  double mass_balance[kMaxSpecies];
+};
+
+// Scenario descriptor as the kernels see it (one per scenario, device memory).
+struct ScenDev {
+  // particle container
+  void* state;
+  uint32_t* pos;
+  uint8_t* status;
+  float* age_h;
+  float* age_d;
+  uint32_t* id;
+  void* child_state;
+  uint32_t* child_pos;
+  uint32_t* tile_births;
+  uint32_t* tile_inactive;
+  uint32_t* tile_boff;
+  uint32_t* tile_goff;
+  uint32_t* tile_soff;
+  uint32_t* bmask;
+  uint32_t* bpos;
+  uint32_t* gap_slot;
+  uint32_t* src_slot;
+  unsigned long long cap;
+  uint32_t n_tiles;
+  uint32_t tile_base;  // first global tile of this scenario in its batch
+  // domain
+  double* pmove;
+  const double* volume;
+  const double* out_flow;
+  const double* cdf;
+  const uint32_t* nbr;
+  const uint32_t* in_ptr;
+  const uint32_t* in_idx;
+  const double* in_flow;
+  const double* diag;
+  const double* vinv;
+  uint32_t n_c;
+  uint32_t K;
+  uint32_t n_s;
+  uint32_t n_ctb;
+  uint32_t n_var;
+  uint32_t n_outlets;
+  uint32_t outlet_idx[kMaxOutlets];
+  double outlet_flow[kMaxOutlets];
+  double outlet_thr[kMaxOutlets];
+  // feeds
+  uint32_t n_feeds;
+  uint32_t feed_in[kMaxOutlets];
+  int32_t feed_out[kMaxOutlets];
+  double feed_flow[kMaxOutlets];
+  double feed_conc[kMaxOutlets * kMaxSpecies];
+  // liquid
+  double* C;
+  double* M;
+  double* src;
+  long long* acc_hi;
+  unsigned long long* acc_lo;
+  double ctb_scale[kMaxSpecies];     // 2^-e: value -> quanta
+  double ctb_scale_up[kMaxSpecies];  // 2^e: quanta -> value
+  int32_t ctb_exp[kMaxSpecies];
+  // model
+  double params[16];
+  double weight;
+  double dt;
+  unsigned long long seed;
+  double dead_ratio;
+  unsigned long long min_removal;
+  Control* ctl;
+  int32_t f64;
+  int32_t pad0;
+};
+
+// ---------------------------------------------------------------------------
+// Draw source: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), keyed by
+// the scenario seed, counter (particle id, step, purpose, 0).
+struct Draws {
+  float u[4];
+};
+
+__device__ __forceinline__ Draws philox_draws(unsigned long long seed, uint32_t id, uint32_t step,
+                                              uint32_t purpose) {
+  uint32_t c0 = id, c1 = step, c2 = purpose, c3 = 0u;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c0;
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0;
+    const uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  Draws d;
+  // odd 24-bit integer * 2^-24: exact, in (0, 1)
+  d.u[0] = (float)((c0 >> 8) | 1u) * 0x1p-24f;
+  d.u[1] = (float)((c1 >> 8) | 1u) * 0x1p-24f;
+  d.u[2] = (float)((c2 >> 8) | 1u) * 0x1p-24f;
+  d.u[3] = (float)((c3 >> 8) | 1u) * 0x1p-24f;
+  return d;
+}
+
+__device__ __forceinline__ void philox_raw(unsigned long long seed, uint32_t id, uint32_t step,
+                                           uint32_t purpose, uint32_t out[4]) {
+  uint32_t c0 = id, c1 = step, c2 = purpose, c3 = 0u;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t lo0 = 0xD2511F53u * c0;
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0;
+    const uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+// ---------------------------------------------------------------------------
+// Model plugins.  A plugin is a struct template over the float type F with
+//   n_var, n_ctb                              sizes (ModelType::n_var, n_c)
+//   update(dt, x, c, ctb, p) -> status        Model::update
+//   division(x, child, d, p)                  Model::division
+//   init(x, d, p)                             Model::init
+//   mass(x, p) -> double                      Model::mass
+// x is the particle's state in registers, c the concentrations of its
+// compartment (double), ctb its contributions, p the parameter vector, d
+// the draws of the particle.  Reference concept: apps/libs/mc/public/mc/
+// traits.hpp L67-L133.  Every expression keeps the operation order of the
+// CPU restatement so that both round identically (no contraction).
+
+template <class F>
+struct MonodModel {
+  static constexpr int n_var = 2;
+  static constexpr int n_ctb = 1;
+  static constexpr int model_id = 1;
+  __device__ __forceinline__ static int update(F dt, F* x, const double* c, F* ctb, const double* p) {
+    const F mu_max = (F)p[0], ks = (F)p[1], y = (F)p[2], mdiv = (F)p[3];
+    F s = (F)__ldg(c);
+    if (s < (F)0) s = (F)0;
+    const F g = s / (ks + s);
+    const F mu = mu_max * g;
+    const F growth = mu * x[0];
+    ctb[0] = -(growth / y);
+    x[0] = x[0] + dt * growth;
+    x[1] = x[1] + dt;
+    return x[0] >= mdiv ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static void division(F* x, F* child, const float* d, const double* p) {
+    (void)d;
+    (void)p;
+    const F half = x[0] * (F)0.5;
+    x[0] = half;
+    x[1] = (F)0;
+    child[0] = half;
+    child[1] = (F)0;
+  }
+  __device__ __forceinline__ static void init(F* x, const float* d, const double* p) {
+    x[0] = (F)p[4] + (F)p[5] * (F)d[1];
+    x[1] = (F)0;
+  }
+  __device__ __forceinline__ static double mass(const F* x, const double* p) {
+    (void)p;
+    return (double)x[0];
+  }
+};
+
+template <class F>
+struct OverflowModel {
+  static constexpr int n_var = 6;
+  static constexpr int n_ctb = 4;
+  static constexpr int model_id = 2;
+  __device__ __forceinline__ static int update(F dt, F* x, const double* c, F* ctb, const double* p) {
+    const F qs_max = (F)p[0], ks = (F)p[1], qo_max = (F)p[2], ko = (F)p[3];
+    const F y_ox = (F)p[4], y_of = (F)p[5], y_ac = (F)p[6], y_o = (F)p[7];
+    const F y_c = (F)p[8], mdiv = (F)p[9], y_cof = (F)p[10];
+    F s = (F)__ldg(c);
+    if (s < (F)0) s = (F)0;
+    F o = (F)__ldg(c + 1);
+    if (o < (F)0) o = (F)0;
+    const F q_s = qs_max * (s / (ks + s));
+    const F q_cap = qo_max * (o / (ko + o));
+    const F q_ox = q_s < q_cap ? q_s : q_cap;
+    const F q_of = q_s - q_ox;
+    const F mu = y_ox * q_ox + y_of * q_of;
+    const F q_ac = y_ac * q_of;
+    const F q_o2 = y_o * q_ox;
+    const F q_co2 = y_c * q_ox + y_cof * q_of;
+    const F m = x[0];
+    ctb[0] = -(q_s * m);
+    ctb[1] = -(q_o2 * m);
+    ctb[2] = q_ac * m;
+    ctb[3] = q_co2 * m;
+    x[0] = m + dt * (mu * m);
+    x[1] = x[1] + dt;
+    x[2] = mu;
+    x[3] = q_s;
+    x[4] = q_o2;
+    x[5] = q_ac;
+    return x[0] >= mdiv ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static void division(F* x, F* child, const float* d, const double* p) {
+    (void)d;
+    (void)p;
+    const F half = x[0] * (F)0.5;
+    x[0] = half;
+    x[1] = (F)0;
+    child[0] = half;
+    child[1] = (F)0;
+#pragma unroll
+    for (int v = 2; v < 6; ++v) child[v] = x[v];
+  }
+  __device__ __forceinline__ static void init(F* x, const float* d, const double* p) {
+    x[0] = (F)p[11] + (F)p[12] * (F)d[1];
+#pragma unroll
+    for (int v = 1; v < 6; ++v) x[v] = (F)0;
+  }
+  __device__ __forceinline__ static double mass(const F* x, const double* p) {
+    (void)p;
+    return (double)x[0];
+  }
+};
+
+// The reference's FixedLength model (apps/libs/models/public/models/
+// fixed_length.hpp L19-L161), float state {length, l_max}, one contribution.
+struct FixedLengthModel {
+  static constexpr int n_var = 2;
+  static constexpr int n_ctb = 1;
+  static constexpr int model_id = 3;
+  __device__ __forceinline__ static float lin_density() {
+    const float d_m = (float)0.6e-6;
+    return (float)1000 * (float)3.14159265358979323846 * d_m * d_m / (float)4.;
+  }
+  __device__ __forceinline__ static float l_dot_max() { return (float)(2e-6 / 3600.); }
+  __device__ __forceinline__ static float phi_s_max() { return (l_dot_max() * lin_density()) / (float)0.5; }
+  __device__ __forceinline__ static int update(float dt, float* x, const double* c, float* ctb,
+                                               const double* p) {
+    (void)p;
+    const float k = (float)1e-3;
+    const float s = (float)__ldg(c);
+    const float g = s / (k + s);
+    const float phi_s = phi_s_max() * g;
+    const float ldot = l_dot_max() * g;
+    x[0] += dt * ldot;
+    ctb[0] = -phi_s;
+    return x[0] >= x[1] ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static void division(float* x, float* child, const float* d,
+                                                  const double* p) {
+    (void)d;
+    (void)p;
+    const float l_max_m = (float)2e-6;
+    const float nl = x[0] / 2.F;
+    x[0] = nl;
+    x[1] = l_max_m;
+    child[0] = nl;
+    child[1] = l_max_m;
+  }
+  __device__ __forceinline__ static void init(float* x, const float* d, const double* p) {
+    (void)p;
+    const float l_max_m = (float)2e-6;
+    const float l_min_m = l_max_m / (float)2.;
+    x[0] = l_min_m + (l_max_m - l_min_m) * d[1];
+    x[1] = l_max_m;
+  }
+  __device__ __forceinline__ static double mass(const float* x, const double* p) {
+    (void)p;
+    return (double)(x[0] * lin_density());
+  }
+};
+
+}  // namespace bmc

@@ -1,0 +1,758 @@
+// bmc_kernels.cu -- kernels of the Monte Carlo cycle and their launchers.
+//
+// Reference behaviour (BioCMA-MCST paths):
+//   model + division request   apps/libs/simulation/public/simulation/kernels/
+//                              model_kernel.hpp L164-L268
+//   contribution scatter       contribution_kernel.hpp L146-L186
+//   move                       move_kernel.hpp L62-L103, L393-L437
+//   exit                       move_kernel.hpp L348-L359, L588-L648
+//   leave tests                apps/libs/simulation/public/simulation/
+//                              probability_leaving.hpp L18-L35
+//   division / compaction /    apps/libs/mc/public/mc/particles_container.hpp
+//   merge                      L541-L600, L737-L795
+//   liquid step                apps/libs/simulation/src/implScalar.cpp L251
+//   feeds                      apps/libs/simulation/src/simulation.model.cpp L73
+#include <cstdio>
+
+#include "bmc_kernels.cuh"
+#include "bmc_launch.h"
+
+namespace bmc {
+
+// ---------------------------------------------------------------------------
+// k_liquid: feeds into sources/sink, explicit Euler step of the liquid
+// scalars (M += dt (C T - C sink + src); C = M / V), mass-balance residual.
+// One block per scenario.  Also resets the step counters and the tile
+// scheduler for the cycle that follows.
+__global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
+  const ScenDev& S = sc[blockIdx.x];
+  Control* ctl = S.ctl;
+  if (blockIdx.x == 0 && threadIdx.x == 0) bctl->ticket = 0u;
+  if (threadIdx.x == 0) {
+    ctl->req_div = 0ull;
+    ctl->exits = 0ull;
+    ctl->moves = 0ull;
+  }
+  if (!do_scalar) return;
+  const unsigned nsp = S.n_s;
+  const unsigned n_e = S.n_c * nsp;
+  const double dt = S.dt;
+  double m_new[kMaxSpecies], m_exp[kMaxSpecies];
+#pragma unroll
+  for (int k = 0; k < kMaxSpecies; ++k) m_new[k] = m_exp[k] = 0.0;
+  for (unsigned e = threadIdx.x; e < n_e; e += blockDim.x) {
+    const unsigned j = e / nsp;
+    const unsigned sp = e - j * nsp;
+    double srcv = S.src[e];
+    double sinkj = 0.0;
+    for (unsigned f = 0; f < S.n_feeds; ++f) {
+      if (S.feed_in[f] == j) {
+        const double cf = S.feed_conc[f * kMaxSpecies + sp];
+        if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
+      }
+      if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
+    }
+    S.src[e] = srcv;
+    double acc = 0.0;
+    const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
+    for (unsigned q = e0; q < e1; ++q)
+      acc = __dadd_rn(acc, __dmul_rn(S.C[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
+    const double cj = S.C[e];
+    acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
+    const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
+    const double mold = S.M[e];
+    const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
+    S.M[e] = mnew;
+    for (unsigned k = 0; k < nsp && k < kMaxSpecies; ++k) {
+      if (k == sp) {
+        m_new[k] += mnew;
+        m_exp[k] += mold + dt * (srcv - cj * sinkj);
+      }
+    }
+  }
+  __syncthreads();
+  for (unsigned e = threadIdx.x; e < n_e; e += blockDim.x) {
+    const unsigned j = e / nsp;
+    S.C[e] = __dmul_rn(S.M[e], S.vinv[j]);
+  }
+  // mass-balance residual per species (diagnostic, block tree reduction)
+  __shared__ double red[2][32];
+  for (unsigned k = 0; k < nsp && k < kMaxSpecies; ++k) {
+    double a = m_new[k], b = m_exp[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = a;
+      red[1][threadIdx.x >> 5] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double ta = 0.0, tb = 0.0;
+      for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) {
+        ta += red[0][w];
+        tb += red[1][w];
+      }
+      const double den = fabs(ta) > 1e-300 ? fabs(ta) : 1e-300;
+      ctl->mass_balance[k] = fabs(ta - tb) / den;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_cycle: the fused per-particle hot path.  A persistent grid takes tiles
+// of 1024 slots from a ticket counter (tiles are ordered scenario after
+// scenario).  For each Idle particle:
+//   ages(i,1) += dt; status = Model::update(..., C(:, pos))
+//   contributions -> shared-memory fixed-point accumulator at the pre-move
+//     compartment (exact integer sums, flushed to two-limb global sums)
+//   move:  leave iff dt*Q/V > u1; next = first k with u2 <= CDF(pos, k)
+//   exit:  ages(i,0) += dt; leave the reactor iff u3 > exp(-dt F / V)
+// A division request sets a bit of the tile's birth mask; the division
+// itself runs in k_divide once the slot-order ranks are known.
+template <class Model, class F, int PPT>
+__global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, int n_scen,
+                                              BatchCtl* __restrict__ bctl) {
+  extern __shared__ unsigned long long sacc[];
+  __shared__ unsigned s_tile;
+  __shared__ unsigned s_tile_births, s_tile_inactive;
+  __shared__ unsigned long long s_cnt[5];
+  constexpr int NV = Model::n_var;
+  constexpr int NC = Model::n_ctb;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const unsigned total_tiles = bctl->total_tiles;
+  const int passes = kTile / (blockDim.x * PPT);
+  int cur = -1;
+  unsigned since_flush = 0;
+  unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
+  unsigned my_err = 0;
+
+  for (;;) {
+    if (tid == 0) {
+      s_tile = atomicAdd(&bctl->ticket, 1u);
+      s_tile_births = 0u;
+      s_tile_inactive = 0u;
+    }
+    __syncthreads();
+    const unsigned g = s_tile;
+    __syncthreads();  // every thread has read the ticket before thread 0 takes the next
+    const bool done = g >= total_tiles;
+    const int s = done ? -1 : scen_of_tile(sc, n_scen, g, cur);
+    if (s != cur || since_flush + kTile > kFlushParticles) {
+      if (cur >= 0) {
+        // flush the accumulator and the counters of scenario `cur`
+        const ScenDev& P = sc[cur];
+        const unsigned n_ent = P.n_c * NC;
+        for (unsigned e = tid; e < n_ent; e += blockDim.x) {
+          const long long p = (long long)sacc[e];
+          if (p != 0) {
+            atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
+            atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
+          }
+        }
+        if (tid < 5) s_cnt[tid] = 0ull;
+        __syncthreads();
+        const unsigned long long r0 = warp_sum_u64(my_req), r1 = warp_sum_u64(my_exit);
+        const unsigned long long r2 = warp_sum_u64(my_move), r3 = warp_sum_u64(my_clamp);
+        unsigned e4 = my_err;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) e4 |= __shfl_xor_sync(0xffffffffu, e4, o);
+        if (lane == 0) {
+          atomicAdd(&s_cnt[0], r0);
+          atomicAdd(&s_cnt[1], r1);
+          atomicAdd(&s_cnt[2], r2);
+          atomicAdd(&s_cnt[3], r3);
+          atomicOr(reinterpret_cast<unsigned*>(&s_cnt[4]), e4);
+        }
+        __syncthreads();
+        if (tid == 0) {
+          Control* c = P.ctl;
+          if (s_cnt[0]) atomicAdd(&c->req_div, s_cnt[0]);
+          if (s_cnt[1]) atomicAdd(&c->exits, s_cnt[1]);
+          if (s_cnt[2]) atomicAdd(&c->moves, s_cnt[2]);
+          if (s_cnt[3]) atomicAdd(&c->clamped, s_cnt[3]);
+          const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
+          if (ev) atomicOr(&c->error, ev);
+        }
+        my_req = my_exit = my_move = my_clamp = 0ull;
+        my_err = 0u;
+      }
+      if (done) break;
+      const unsigned n_ent = sc[s].n_c * NC;
+      for (unsigned e = tid; e < n_ent; e += blockDim.x) sacc[e] = 0ull;
+      cur = s;
+      since_flush = 0;
+      __syncthreads();
+    }
+    const ScenDev& S = sc[s];
+    const unsigned t = g - S.tile_base;
+    const unsigned long long n_used = S.ctl->n_used;
+    const unsigned long long base = (unsigned long long)t * kTile;
+    if (base >= n_used) continue;
+    since_flush += kTile;
+
+    const unsigned long long cap = S.cap;
+    const unsigned n_c = S.n_c, K = S.K, nsp = S.n_s;
+    const unsigned step = S.ctl->step;
+    const double dt = S.dt;
+    const F dtF = (F)dt;
+    const bool do_move = n_c > 1;
+    const unsigned n_out = S.n_outlets;
+    F* __restrict__ state = reinterpret_cast<F*>(S.state);
+
+    for (int pass = 0; pass < passes; ++pass) {
+      const unsigned long long first = base + ((unsigned long long)pass * blockDim.x + tid) * PPT;
+      uint8_t stv[PPT];
+      ld_stream<uint8_t, PPT>(S.status + first, stv);
+      bool idle[PPT];
+      bool any = false;
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) {
+        idle[k] = (first + k < n_used) && stv[k] == kIdle;
+        any |= idle[k];
+      }
+      unsigned bits = 0u;
+      unsigned n_inact = 0u;
+      if (any) {
+        uint32_t pv[PPT], idv[PPT];
+        float ah[PPT], ad[PPT];
+        F x[NV][PPT];
+        ld_stream<uint32_t, PPT>(S.pos + first, pv);
+        ld_stream<uint32_t, PPT>(S.id + first, idv);
+        ld_stream<float, PPT>(S.age_h + first, ah);
+        ld_stream<float, PPT>(S.age_d + first, ad);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        bool st_changed = false;
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          if (!idle[k]) continue;
+          const uint32_t p0 = pv[k];
+          if (p0 >= n_c) {
+            my_err |= 1u;
+            continue;
+          }
+          const Draws d = philox_draws(S.seed, idv[k], step, 0u);
+          if constexpr (sizeof(F) == 8)
+            ad[k] = (float)__dadd_rn((double)ad[k], dt);
+          else
+            ad[k] = __fadd_rn(ad[k], (float)dt);
+          F xx[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
+          F ctb[NC];
+          const int r = Model::update(dtF, xx, S.C + (size_t)p0 * nsp, ctb, S.params);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) x[v][k] = xx[v];
+          if (r == kDivision) {
+            bits |= 1u << k;
+            S.bpos[first + k] = p0;
+            ++my_req;
+          }
+#pragma unroll
+          for (int j = 0; j < NC; ++j) {
+            const double val = __dmul_rn(S.weight, (double)ctb[j]);
+            double q = rint(__dmul_rn(val, S.ctb_scale[j]));
+            if (q > (double)kQMax) {
+              q = (double)kQMax;
+              ++my_clamp;
+              my_err |= 2u;
+            } else if (q < -(double)kQMax) {
+              q = -(double)kQMax;
+              ++my_clamp;
+              my_err |= 2u;
+            }
+            atomicAdd(&sacc[p0 * NC + j], (unsigned long long)(long long)q);
+          }
+          uint32_t p = p0;
+          if (do_move) {
+            if (__ldg(S.pmove + p0) > (double)d.u[0]) {
+              const double u2 = (double)d.u[1];
+              const double* row = S.cdf + (size_t)p0 * K;
+              int left = 0, right = (int)K - 1;
+              while (left < right) {
+                const int mid = (left + right) >> 1;
+                if (u2 > __ldg(row + mid))
+                  left = mid + 1;
+                else
+                  right = mid;
+              }
+              p = __ldg(S.nbr + (size_t)p0 * K + left);
+              ++my_move;
+            }
+            pv[k] = p;
+          }
+          if (n_out > 0) {
+            ah[k] = (float)__dadd_rn((double)ah[k], dt);
+            for (unsigned o = 0; o < n_out; ++o) {
+              if (S.outlet_idx[o] == p) {
+                if (S.outlet_flow[o] != 0.0 && (double)d.u[2] > S.outlet_thr[o]) {
+                  stv[k] = kExit;
+                  ah[k] = 0.0f;
+                  ++my_exit;
+                  st_changed = true;
+                }
+                break;
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) st_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        if (do_move) st_stream<uint32_t, PPT>(S.pos + first, pv);
+        if (n_out > 0) st_stream<float, PPT>(S.age_h + first, ah);
+        st_stream<float, PPT>(S.age_d + first, ad);
+        if (st_changed) st_stream<uint8_t, PPT>(S.status + first, stv);
+      }
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) n_inact += (first + k < n_used && stv[k] != kIdle) ? 1u : 0u;
+      // birth-request bits: slot first+k -> bit (first+k) % 32 of word (first+k) / 32
+      constexpr int lanes_per_word = 32 / PPT;
+      unsigned w = bits << ((lane % lanes_per_word) * PPT);
+#pragma unroll
+      for (int o = 1; o < lanes_per_word; o <<= 1) w |= __shfl_xor_sync(0xffffffffu, w, o);
+      if (lane % lanes_per_word == 0) S.bmask[first >> 5] = w;
+      const unsigned nb = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));
+      const unsigned ni = __reduce_add_sync(0xffffffffu, n_inact);
+      if (lane == 0) {
+        if (nb) atomicAdd(&s_tile_births, nb);
+        if (ni) atomicAdd(&s_tile_inactive, ni);
+      }
+    }
+    __syncthreads();
+    if (tid == 0) {
+      S.tile_births[t] = s_tile_births;
+      S.tile_inactive[t] = s_tile_inactive;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_plan: per scenario (one block of 1024 threads):
+//  1. exact contribution totals -> sources (double), accumulators cleared;
+//  2. post_cycle decisions: inactive += exits; compaction iff inactive >
+//     max(min_removal, n * ratio) (update_and_remove_inactive); room for
+//     births = capacity - live particles after compaction;
+//  3. scans of the per-tile counters (birth ranks, gap ranks ascending,
+//     source ranks from the end);
+//  4. control block advanced to the state after the step.
+__global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
+  const ScenDev& S = sc[blockIdx.x];
+  Control* ctl = S.ctl;
+  const int tid = threadIdx.x;
+  __shared__ unsigned long long sh64[33];
+  __shared__ unsigned long long p_n, p_req, p_rm, p_after;
+  __shared__ int p_compact;
+
+  const unsigned nsp = S.n_s, nc = S.n_ctb;
+  const unsigned n_e = S.n_c * nsp;
+  for (unsigned e = tid; e < n_e; e += blockDim.x) {
+    const unsigned j = e / nsp;
+    const unsigned sp = e - j * nsp;
+    double v = 0.0;
+    if (sp < nc) {
+      const unsigned idx = j * nc + sp;
+      v = fixed_to_double(S.acc_hi[idx], S.acc_lo[idx], S.ctb_scale_up[sp]);
+      S.acc_hi[idx] = 0;
+      S.acc_lo[idx] = 0ull;
+    }
+    S.src[e] = v;
+  }
+  if (tid == 0) {
+    const unsigned long long n = ctl->n_used;
+    const unsigned long long req = ctl->req_div;
+    const unsigned long long inactive_after = ctl->inactive + ctl->exits;
+    const unsigned long long ratio_thr = (unsigned long long)((double)n * S.dead_ratio);
+    const unsigned long long thr = S.min_removal > ratio_thr ? S.min_removal : ratio_thr;
+    int compact = inactive_after > thr ? 1 : 0;
+    unsigned long long rm = compact ? inactive_after : 0ull;
+    if (rm > n) {
+      ctl->error |= 8u;
+      rm = 0ull;
+      compact = 0;
+    }
+    const unsigned long long after = n - rm;
+    const unsigned long long room = S.cap > after ? S.cap - after : 0ull;
+    const unsigned long long births = req < room ? req : room;
+    p_n = n;
+    p_req = req;
+    p_rm = rm;
+    p_after = after;
+    p_compact = compact;
+    ctl->plan_n_old = n;
+    ctl->plan_to_remove = rm;
+    ctl->plan_n_after = after;
+    ctl->plan_births = births;
+    ctl->plan_overflow = req - births;
+    ctl->plan_next_id = ctl->next_id;
+    ctl->plan_step = ctl->step;
+    ctl->plan_compact = (unsigned)compact;
+    ctl->plan_gaps = 0ull;
+    if (ctl->next_id + births > 0x100000000ull) ctl->error |= 4u;
+    ctl->n_used = after + births;
+    ctl->inactive = compact ? 0ull : inactive_after;
+    ctl->next_id += births;
+    ctl->step += 1u;
+    ctl->last_births = births;
+    ctl->last_exits = ctl->exits;
+    ctl->last_moves = ctl->moves;
+    ctl->last_overflow = req - births;
+    ctl->last_req_div = req;
+    ctl->last_compacted = (unsigned)compact;
+  }
+  __syncthreads();
+  const unsigned long long n = p_n;
+  const unsigned n_t = (unsigned)((n + kTile - 1) / kTile);
+  const unsigned chunk = (n_t + blockDim.x - 1) / blockDim.x;
+  const unsigned t0 = tid * chunk;
+  const unsigned t1 = min(t0 + chunk, n_t);
+  unsigned long long tot;
+  if (p_req > 0) {
+    unsigned long long local = 0;
+    for (unsigned t = t0; t < t1; ++t) local += S.tile_births[t];
+    unsigned long long off = block_exscan_u64(local, sh64, &tot);
+    for (unsigned t = t0; t < t1; ++t) {
+      S.tile_boff[t] = (unsigned)off;
+      off += S.tile_births[t];
+    }
+  }
+  if (p_compact && p_after > 0 && p_rm < n) {
+    const unsigned long long after = p_after;
+    // gap offsets for tiles t <= after / kTile (ascending prefix of inactive)
+    const unsigned tg_end = min((unsigned)(after / kTile) + 1u, n_t);
+    unsigned long long local = 0;
+    for (unsigned t = t0; t < t1 && t < tg_end; ++t) local += S.tile_inactive[t];
+    unsigned long long off = block_exscan_u64(local, sh64, &tot);
+    for (unsigned t = t0; t < t1 && t < tg_end; ++t) {
+      S.tile_goff[t] = (unsigned)off;
+      off += S.tile_inactive[t];
+    }
+    // source offsets for tiles t >= after / kTile: idle slots in later tiles
+    const unsigned ts_begin = (unsigned)(after / kTile);
+    unsigned long long local2 = 0;
+    for (unsigned t = t0; t < t1; ++t) {
+      if (t < ts_begin) continue;
+      const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
+      local2 += valid - S.tile_inactive[t];
+    }
+    unsigned long long tot2;
+    unsigned long long pre = block_exscan_u64(local2, sh64, &tot2);
+    for (unsigned t = t0; t < t1; ++t) {
+      if (t < ts_begin) continue;
+      const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
+      pre += valid - S.tile_inactive[t];
+      S.tile_soff[t] = (unsigned)(tot2 - pre);  // idle slots in tiles after t
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_divide: (a) Model::division for the requests of this step, in slot
+// order, the first `plan_births` succeeding (handle_division,
+// particles_container.hpp L561-L575: mother updated in place, child into the
+// buffer, ages(mother,1) = 0); (b) the compaction lists: j-th non-Idle slot
+// of [0, n_after) and j-th Idle slot of [n_after, n) counted from the end
+// (CompactParticlesFunctor run in slot order).  256 threads x 4 slots.
+template <class Model, class F>
+__global__ void __launch_bounds__(256) k_divide(const ScenDev* __restrict__ sc, int n_scen,
+                                               const BatchCtl* __restrict__ bctl) {
+  constexpr int NV = Model::n_var;
+  __shared__ unsigned sh[33];
+  const unsigned total_tiles = bctl->total_tiles;
+  const int tid = threadIdx.x;
+  int s = -1;
+  for (unsigned g = blockIdx.x; g < total_tiles; g += gridDim.x) {
+    s = scen_of_tile(sc, n_scen, g, s);
+    const ScenDev& S = sc[s];
+    const Control* ctl = S.ctl;
+    const unsigned long long n_old = ctl->plan_n_old;
+    const unsigned t = g - S.tile_base;
+    const unsigned long long base = (unsigned long long)t * kTile;
+    if (base >= n_old) continue;
+    const unsigned long long req = ctl->plan_births + ctl->plan_overflow;
+    const bool cmp = ctl->plan_compact != 0u && ctl->plan_n_after > 0ull && ctl->plan_to_remove < n_old;
+    if (req == 0ull && !cmp) continue;
+    const unsigned long long first = base + (unsigned long long)tid * 4ull;
+    const unsigned long long cap = S.cap;
+    if (req > 0ull && S.tile_births[t] > 0u) {
+      const unsigned word = S.bmask[first >> 5];
+      const unsigned bits = (word >> (first & 31ull)) & 0xFu;
+      unsigned tot;
+      unsigned rank = S.tile_boff[t] + block_exscan_u32((unsigned)__popc(bits), sh, &tot);
+      const unsigned long long births = ctl->plan_births;
+      F* state = reinterpret_cast<F*>(S.state);
+      F* child_state = reinterpret_cast<F*>(S.child_state);
+      for (int k = 0; k < 4; ++k) {
+        if (!((bits >> k) & 1u)) continue;
+        const unsigned long long slot = first + k;
+        if (rank < births) {
+          F x[NV], y[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) x[v] = state[(size_t)v * cap + slot];
+          const Draws d = philox_draws(S.seed, S.id[slot], ctl->plan_step, 1u);
+          Model::division(x, y, d.u, S.params);
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            state[(size_t)v * cap + slot] = x[v];
+            child_state[(size_t)v * cap + rank] = y[v];
+          }
+          S.child_pos[rank] = S.bpos[slot];
+          S.age_d[slot] = 0.0f;
+        }
+        ++rank;
+      }
+    }
+    if (cmp) {
+      const unsigned long long after = ctl->plan_n_after;
+      unsigned gbits = 0u, sbits = 0u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const unsigned long long slot = first + k;
+        if (slot >= n_old) continue;
+        const bool idle = S.status[slot] == kIdle;
+        if (slot < after && !idle) gbits |= 1u << k;
+        if (slot >= after && idle) sbits |= 1u << k;
+      }
+      unsigned gtot, stot;
+      const unsigned gpre = block_exscan_u32((unsigned)__popc(gbits), sh, &gtot);
+      const unsigned spre = block_exscan_u32((unsigned)__popc(sbits), sh, &stot);
+      if (gbits) {
+        unsigned r = S.tile_goff[t] + gpre;
+        for (int k = 0; k < 4; ++k)
+          if ((gbits >> k) & 1u) S.gap_slot[r++] = (uint32_t)(first + k);
+      }
+      if (sbits) {
+        unsigned i_loc = 0;
+        for (int k = 0; k < 4; ++k) {
+          if (!((sbits >> k) & 1u)) continue;
+          const unsigned larger = stot - spre - i_loc - 1u;  // sources after this slot in the tile
+          S.src_slot[S.tile_soff[t] + larger] = (uint32_t)(first + k);
+          ++i_loc;
+        }
+      }
+      if (t == (unsigned)(after / kTile) && tid == 0) {
+        Control* c = const_cast<Control*>(ctl);
+        c->plan_gaps = (unsigned long long)S.tile_goff[t] + gtot;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_compact: copy the j-th source particle into the j-th gap (all fields);
+// k_merge: append the children after the live particles with ages 0 and
+// fresh ids (InsertFunctor, particles_container.hpp L403-L447).
+template <int NV, class F>
+__global__ void __launch_bounds__(256) k_compact(const ScenDev* __restrict__ sc, int n_scen) {
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (int s = 0; s < n_scen; ++s) {
+    const ScenDev& S = sc[s];
+    const Control* ctl = S.ctl;
+    if (!ctl->plan_compact) continue;
+    const unsigned long long gaps = ctl->plan_gaps;
+    const unsigned long long cap = S.cap;
+    const unsigned long long after = ctl->plan_n_after, n_old = ctl->plan_n_old;
+    F* state = reinterpret_cast<F*>(S.state);
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < gaps; j += stride) {
+      const unsigned long long dst = S.gap_slot[j], src = S.src_slot[j];
+      if (dst >= after || src < after || src >= n_old) {  // lists inconsistent: record, skip
+        atomicOr(&S.ctl->error, 8u);
+        continue;
+      }
+#pragma unroll
+      for (int v = 0; v < NV; ++v) state[(size_t)v * cap + dst] = state[(size_t)v * cap + src];
+      S.pos[dst] = S.pos[src];
+      S.status[dst] = kIdle;
+      S.age_h[dst] = S.age_h[src];
+      S.age_d[dst] = S.age_d[src];
+      S.id[dst] = S.id[src];
+    }
+  }
+}
+
+template <int NV, class F>
+__global__ void __launch_bounds__(256) k_merge(const ScenDev* __restrict__ sc, int n_scen) {
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (int s = 0; s < n_scen; ++s) {
+    const ScenDev& S = sc[s];
+    const Control* ctl = S.ctl;
+    const unsigned long long births = ctl->plan_births;
+    if (births == 0ull) continue;
+    const unsigned long long after = ctl->plan_n_after;
+    const unsigned long long id0 = ctl->plan_next_id;
+    const unsigned long long cap = S.cap;
+    F* state = reinterpret_cast<F*>(S.state);
+    const F* child = reinterpret_cast<const F*>(S.child_state);
+    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < births; j += stride) {
+      const unsigned long long dst = after + j;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) state[(size_t)v * cap + dst] = child[(size_t)v * cap + j];
+      S.pos[dst] = S.child_pos[j];
+      S.status[dst] = kIdle;
+      S.age_h[dst] = 0.0f;
+      S.age_d[dst] = 0.0f;
+      S.id[dst] = (uint32_t)(id0 + j);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Set-up and diagnostics.
+
+// InitFunctor (apps/libs/mc/src/unit.cpp L102-L137): model init from the
+// particle's draws, position = lo + floor(u32 * span / 2^32), mass out.
+template <class Model, class F>
+__global__ void k_init(const ScenDev* __restrict__ sc, unsigned long long n, uint32_t lo, uint32_t span,
+                       double* __restrict__ mass_out) {
+  const ScenDev& S = *sc;
+  constexpr int NV = Model::n_var;
+  F* state = reinterpret_cast<F*>(S.state);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t r[4];
+    philox_raw(S.seed, (uint32_t)i, 0xFFFFFFFFu, 2u, r);
+    float d[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) d[k] = (float)((r[k] >> 8) | 1u) * 0x1p-24f;
+    F x[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) x[v] = (F)0;
+    Model::init(x, d, S.params);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) state[(size_t)v * S.cap + i] = x[v];
+    S.pos[i] = lo + __umulhi(r[0], span);
+    S.status[i] = kIdle;
+    S.age_h[i] = 0.0f;
+    S.age_d[i] = 0.0f;
+    S.id[i] = (uint32_t)i;
+    mass_out[i] = Model::mass(x, S.params);
+  }
+}
+
+template <class Model, class F>
+__global__ void k_mass(const ScenDev* __restrict__ sc, unsigned long long n, double* __restrict__ mass_out) {
+  const ScenDev& S = *sc;
+  constexpr int NV = Model::n_var;
+  const F* state = reinterpret_cast<const F*>(S.state);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    F x[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) x[v] = state[(size_t)v * S.cap + i];
+    mass_out[i] = S.status[i] == kIdle ? Model::mass(x, S.params) : 0.0;
+  }
+}
+
+__global__ void k_pmove(ScenDev* __restrict__ sc) {
+  const ScenDev& S = sc[blockIdx.y];
+  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x)
+    S.pmove[c] = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
+}
+
+__global__ void k_repartition(const ScenDev* __restrict__ sc, unsigned long long* __restrict__ counts) {
+  const ScenDev& S = *sc;
+  const unsigned long long n = S.ctl->n_used;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint32_t p = S.pos[i];
+    if (S.status[i] == kIdle && p < S.n_c) atomicAdd(counts + p, 1ull);
+  }
+}
+
+__global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restrict__ ids, unsigned long long n,
+                              uint32_t step, uint32_t purpose, float* __restrict__ out) {
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const Draws d = philox_draws(seed, ids[i], step, purpose);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) out[4 * i + k] = d.u[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Launchers and the per-model dispatch table.
+
+namespace {
+template <class Model, class F, int PPT>
+void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
+                    BatchCtl* b) {
+  k_cycle<Model, F, PPT><<<grid, block, smem, st>>>(sc, n, b);
+}
+template <class Model, class F>
+void launch_divide_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
+  k_divide<Model, F><<<grid, 256, 0, st>>>(sc, n, b);
+}
+template <class Model, class F>
+void launch_compact_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n) {
+  k_compact<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n);
+}
+template <class Model, class F>
+void launch_merge_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n) {
+  k_merge<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n);
+}
+template <class Model, class F>
+void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long long n, uint32_t lo,
+                   uint32_t span, double* mass) {
+  k_init<Model, F><<<grid, 256, 0, st>>>(sc, n, lo, span, mass);
+}
+template <class Model, class F>
+void launch_mass_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long long n, double* mass) {
+  k_mass<Model, F><<<grid, 256, 0, st>>>(sc, n, mass);
+}
+template <class Model, class F, int PPT>
+const void* cycle_fn_t() {
+  return reinterpret_cast<const void*>(&k_cycle<Model, F, PPT>);
+}
+
+template <class Model, class F>
+KernelSet make_set() {
+  KernelSet k{};
+  k.n_var = Model::n_var;
+  k.n_ctb = Model::n_ctb;
+  k.model = Model::model_id;
+  k.f64 = sizeof(F) == 8;
+  k.cycle[0] = &launch_cycle_t<Model, F, 1>;
+  k.cycle[1] = &launch_cycle_t<Model, F, 2>;
+  k.cycle[2] = &launch_cycle_t<Model, F, 4>;
+  k.cycle_fn[0] = cycle_fn_t<Model, F, 1>();
+  k.cycle_fn[1] = cycle_fn_t<Model, F, 2>();
+  k.cycle_fn[2] = cycle_fn_t<Model, F, 4>();
+  k.divide = &launch_divide_t<Model, F>;
+  k.compact = &launch_compact_t<Model, F>;
+  k.merge = &launch_merge_t<Model, F>;
+  k.init = &launch_init_t<Model, F>;
+  k.mass = &launch_mass_t<Model, F>;
+  return k;
+}
+
+const KernelSet g_sets[] = {
+    make_set<MonodModel<double>, double>(),    make_set<MonodModel<float>, float>(),
+    make_set<OverflowModel<double>, double>(), make_set<OverflowModel<float>, float>(),
+    make_set<FixedLengthModel, float>(),
+};
+}  // namespace
+
+const KernelSet* kernel_set(int model, int f64) {
+  for (const KernelSet& k : g_sets)
+    if (k.model == model && k.f64 == (f64 != 0)) return &k;
+  return nullptr;
+}
+
+void launch_liquid(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
+  k_liquid<<<n_scen, 1024, 0, st>>>(sc, b, do_scalar);
+}
+void launch_plan(int n_scen, cudaStream_t st, ScenDev* sc) { k_plan<<<n_scen, 1024, 0, st>>>(sc); }
+void launch_pmove(int n_scen, cudaStream_t st, ScenDev* sc) { k_pmove<<<dim3(4, n_scen), 256, 0, st>>>(sc); }
+void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {
+  k_repartition<<<grid, 256, 0, st>>>(sc, counts);
+}
+void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
+                        uint32_t step, uint32_t purpose, float* out) {
+  k_debug_draws<<<256, 256, 0, st>>>(seed, ids, n, step, purpose, out);
+}
+
+}  // namespace bmc

@@ -1,0 +1,40 @@
+// bmc_launch.h -- host-side view of the kernels: one KernelSet per compiled
+// model plugin and precision, plus the model-independent launchers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "bmc_device.cuh"
+#include "bmc_kernels.cuh"
+
+namespace bmc {
+
+using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
+using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
+using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int);
+using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
+                            double*);
+using MassLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, double*);
+
+struct KernelSet {
+  int model;
+  bool f64;
+  int n_var;
+  int n_ctb;
+  CycleLaunch cycle[3];      // particles per thread 1, 2, 4
+  const void* cycle_fn[3];   // for occupancy queries / attributes
+  DivideLaunch divide;
+  CopyLaunch compact;
+  CopyLaunch merge;
+  InitLaunch init;
+  MassLaunch mass;
+};
+
+const KernelSet* kernel_set(int model, int f64);
+void launch_liquid(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar);
+void launch_plan(int n_scen, cudaStream_t st, ScenDev* sc);
+void launch_pmove(int n_scen, cudaStream_t st, ScenDev* sc);
+void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
+void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
+                        uint32_t step, uint32_t purpose, float* out);
+
+}  // namespace bmc

@@ -1,0 +1,250 @@
+/*
+ * bmc.h -- C-ABI of the GB300 Monte Carlo cycle library (libbmc.so).
+ *
+ * The library replaces the BioCMA-MCST Monte Carlo cycle: the per-particle
+ * model update, the compartment move and outlet exit, the contribution
+ * scatter, and division / removal / compaction of the particle container,
+ * plus the liquid-scalar Euler step that consumes the contributions.  Every
+ * entry point takes plain pointers and sizes, returns 0 on success and a
+ * negative BMC_E* code on failure (bmc_last_error() then holds a message),
+ * mirroring apps/api/public/api/api_raw.h of the reference (int return
+ * codes, opaque handle).  Host pointers are read during the call only.
+ *
+ * Reference paths below are relative to the BioCMA-MCST tree.
+ */
+#ifndef BMC_H
+#define BMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BMC_VERSION_MAJOR 1
+#define BMC_VERSION_MINOR 0
+
+/* Return codes (reference: ApiResult::to_c_ret_code,
+ * apps/api/public/api/results.hpp; ErrorCodes,
+ * apps/libs/simulation/public/simulation/simulation_exception.hpp L10). */
+#define BMC_OK 0
+#define BMC_E_INVALID -1     /* bad argument / size mismatch */
+#define BMC_E_CUDA -2        /* CUDA runtime error */
+#define BMC_E_STATE -3       /* call out of order (e.g. no domain yet) */
+#define BMC_E_CAPACITY -4    /* more particles than the container can hold */
+#define BMC_E_DEVICE -5      /* device error word set (see bmc_step_stats.error) */
+#define BMC_E_UNSUPPORTED -6 /* model / precision not compiled in */
+
+/* Particle status, reference MC::Status (apps/libs/mc/public/mc/alias.hpp
+ * L124-L130). */
+#define BMC_STATUS_IDLE 0
+#define BMC_STATUS_DIVISION 1
+#define BMC_STATUS_EXIT 2
+#define BMC_STATUS_DEAD 3
+
+/* Compiled model plugins (the ModelType concept,
+ * apps/libs/mc/public/mc/traits.hpp L67-L133).  FIXED_LENGTH restates the
+ * reference's FixedLength model (apps/libs/models/public/models/
+ * fixed_length.hpp); MONOD and OVERFLOW are the benchmark's Monod uptake and
+ * Monod + overflow-to-acetate models written against the same concept. */
+#define BMC_MODEL_MONOD 1
+#define BMC_MODEL_OVERFLOW 2
+#define BMC_MODEL_FIXED_LENGTH 3
+
+/* Device error word bits (copied back with the step statistics). */
+#define BMC_ERR_POSITION 1u  /* compartment index out of range */
+#define BMC_ERR_CLAMP 2u     /* a contribution exceeded its quantum range */
+#define BMC_ERR_IDS 4u       /* particle id space (2^32) exhausted */
+#define BMC_ERR_COMPACT 8u   /* compaction lists disagree (internal) */
+
+typedef struct bmc_scenario bmc_scenario;
+typedef struct bmc_batch bmc_batch;
+
+/* Model descriptor: the host-side metadata of the reference's ModelType
+ * (n_var, n_c, FloatType) plus the parameter vector the device plugin reads.
+ * Reference: traits.hpp L80-L100 (n_var, n_c, FloatType), and the UDF
+ * metadata queries set_nvar_udf / set_nc_udf
+ * (apps/libs/models/ext/udf_includes.hpp L29-L30). */
+typedef struct bmc_model_desc {
+  int32_t model;      /* BMC_MODEL_* */
+  int32_t f64;        /* 1: double state and arithmetic, 0: float */
+  uint32_t n_var;     /* must equal the plugin's n_var */
+  uint32_t n_ctb;     /* must equal the plugin's contribution count */
+  double params[16];  /* plugin parameters */
+} bmc_model_desc;
+
+/* Scenario descriptor: one reactor = one particle container + domain +
+ * liquid scalars.  Reference: ParticlesContainer(RuntimeParameters, n, ...)
+ * (apps/libs/mc/public/mc/particles_container.hpp L25-L43, L700) and
+ * MC::load_tuning_constant (apps/libs/mc/src/unit.cpp L309-L343). */
+typedef struct bmc_scenario_desc {
+  bmc_model_desc model;
+  uint32_t n_species;
+  uint64_t capacity;               /* particle slots allocated on the device */
+  uint64_t seed;                   /* Philox key */
+  double dead_ratio_threshold;     /* BIOMC_MC_REMOVE_RATIO_THRESHOLD, 0.01 */
+  uint64_t min_removal;            /* BIOMC_MC_MINIMUM_REMOVAL, 0 */
+  double ctb_bound[8];             /* bound on |contribution| per particle */
+} bmc_scenario_desc;
+
+/* A liquid feed, reference Simulation::Feed::FeedDescriptor
+ * (apps/libs/simulation/public/simulation/feed_descriptor.hpp L91-L100):
+ * constant flow, one concentration per species at the inlet, optional
+ * outlet (-1 for none) that becomes a leaving flow of the particles and a
+ * sink of the liquid scalars. */
+typedef struct bmc_feed {
+  uint32_t inlet;
+  int32_t outlet;
+  double flow;
+  double conc[8];
+} bmc_feed;
+
+/* Per-step statistics.  Reference: CycleReduceType {waiting_allocation,
+ * dead} and the out counter returned by CycleFunctors::get_host_reduction
+ * (apps/libs/simulation/public/simulation/kernels/kernels.hpp L80-L89), the
+ * event tallies of MC::EventContainer (apps/libs/mc/public/mc/events.hpp
+ * L17-L26) and ParticlesContainer::n_particles / get_inactive. */
+typedef struct bmc_step_stats {
+  uint64_t n_used;      /* slots in use (Idle + not yet removed) */
+  uint64_t inactive;    /* non-Idle slots not yet removed */
+  uint64_t births;      /* NewParticle events of the last step */
+  uint64_t exits;       /* Exit events of the last step */
+  uint64_t moves;       /* Move events of the last step */
+  uint64_t overflow;    /* divisions refused for lack of room (Overflow) */
+  uint64_t requested_divisions;
+  uint64_t clamped;     /* contributions clamped to the quantum range (total) */
+  uint64_t next_id;
+  uint32_t step;
+  uint32_t compacted;   /* 1 if the last step removed inactive particles */
+  uint32_t error;       /* BMC_ERR_* bits, sticky */
+  uint32_t pad;
+  double mass_balance[8]; /* relative liquid mass-balance residual per species */
+} bmc_step_stats;
+
+/* ---- library ---------------------------------------------------------- */
+int bmc_version(int32_t* major, int32_t* minor);
+const char* bmc_last_error(void);
+/* Number of SMs of the current device and the library's default device. */
+int bmc_device_sm_count(int32_t* sm_count);
+
+/* ---- scenario lifetime -------------------------------------------------- */
+/* Replaces the construction of MC::ParticlesContainer + ReactorDomain +
+ * ScalarSimulation in SimulationUnit's constructor
+ * (apps/libs/simulation/src/simulation.cpp L47-L81). */
+int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out);
+int bmc_scenario_destroy(bmc_scenario* s);
+
+/* ReactorDomain::update (apps/libs/mc/src/domain.cpp L44-L74):
+ * liquid volumes [n_c], neighbours [n_c*K] (row-major, std::size_t in the
+ * reference), total out-flows per compartment (diag_transition) [n_c] and
+ * the cumulative destination probabilities [n_c*K]. */
+int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* volume,
+                      const uint64_t* neighbors, const double* out_flows, const double* cdf);
+
+/* ScalarSimulation::set_transition (apps/libs/simulation/src/implScalar.cpp
+ * L323-L330): the liquid transition matrix in COO form; diagonal entries are
+ * T(j,j) = -sum of out-flows. */
+int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint64_t* rows,
+                           const uint64_t* cols, const double* values);
+
+/* ScalarSimulation::deep_copy_concentration + set_mass
+ * (implScalar.cpp L299-L320): concentrations [n_c][n_species]
+ * (the reference's LayoutLeft n_species x n_c matrix), M = C * V. */
+int bmc_set_concentrations(bmc_scenario* s, const double* conc);
+
+/* Feeds (SimulationUnit::update_feed, simulation.model.cpp L73-L111, with
+ * ReactorDomain::set_leaving_flow, domain.cpp L97-L108). At most 8. */
+int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds);
+
+/* MC::init + post_init_weight (apps/libs/mc/src/unit.cpp L102-L163,
+ * L233-L306): n particles, model init, position uniform in [0, n_c) (or 0
+ * when uniform_init == 0), weight = x0 * V_total / total mass.  Writes the
+ * weight if weight_out is not NULL. */
+int bmc_init_particles(bmc_scenario* s, uint64_t n, int32_t uniform_init, double x0,
+                       double* weight_out);
+int bmc_set_weight(bmc_scenario* s, double weight);
+
+/* Upload an explicit container (n particles, SoA state [n_var][n]); used by
+ * callers that hold particles already (serde load, tests). */
+int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint32_t* pos,
+                      const uint8_t* status, const float* age_h, const float* age_d,
+                      const uint32_t* id, uint64_t next_id);
+
+/* ---- the hot path -------------------------------------------------------- */
+/* SimulationUnit::cycleProcess (apps/libs/simulation/public/simulation/
+ * simulation.hpp L184-L239) with CycleFunctors::launch_model /
+ * launch_move (kernels.hpp L124-L224) and post_cycle: model update,
+ * contribution scatter, move, exit, division, compaction, merge.  Uses the
+ * concentrations currently on the device; leaves the contributions of this
+ * cycle as the sources of the next liquid step. */
+int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats);
+
+/* One iteration of the reference main loop (apps/core/src/host_specific.cpp
+ * L280-L291): update_feed, ode_step (ScalarSimulation::performStep,
+ * implScalar.cpp L251-L264), clearContribution, cycleProcess. */
+int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
+
+/* n_steps iterations on the device without host round trips (one captured
+ * CUDA graph replayed).  Statistics are those of the last step. */
+int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats);
+
+/* Enqueue n_steps iterations without waiting (bmc_synchronize waits). */
+int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps);
+int bmc_synchronize(bmc_scenario* s);
+
+/* ---- readback ------------------------------------------------------------ */
+int bmc_read_stats(bmc_scenario* s, bmc_step_stats* stats);
+/* Host buffers sized for n_used particles (state as [n_var][n_used]). */
+int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* pos,
+                       uint8_t* status, float* age_h, float* age_d, uint32_t* id,
+                       uint64_t* n_out);
+int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources);
+/* MonteCarloUnit::getRepartition (apps/libs/mc/src/unit.cpp L191-L230). */
+int bmc_repartition(bmc_scenario* s, uint64_t* counts);
+/* Force removal of every inactive particle (ParticlesContainer::
+ * force_remove_dead, particles_container.hpp L460-L465). */
+int bmc_force_remove_dead(bmc_scenario* s);
+
+/* ---- batching: many scenarios advanced by one set of launches ----------- */
+/* All scenarios of a batch share model and precision; each keeps its own
+ * domain, liquid state, parameters, seed and step counter. */
+int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out);
+int bmc_batch_destroy(bmc_batch* b);
+/* Advance every scenario of the batch by n_steps (captured graph). */
+int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps);
+/* Kernel shape (threads per block, particles per thread, blocks per SM); 0
+ * keeps the default.  Used by the autotuner. */
+int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
+int bmc_batch_synchronize(bmc_batch* b);
+
+/* ---- diagnostics ---------------------------------------------------------- */
+/* Fill out[4*n] with the four uniform draws of (seed, id[k], step, purpose)
+ * computed on the device (checks the draw source against the oracle). */
+int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step,
+                    uint32_t purpose, float* out);
+/* One main-loop iteration like bmc_step, with CUDA events recorded on the
+ * scenario's stream between its six kernels; kernel_ms[0..5] receive the
+ * durations of: liquid step, cycle, plan, divide, compact, merge.
+ * Reference counterpart: the Kokkos-tools region timers of the cycle
+ * (tools/benchs/benchmark.py L145-L229). */
+int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* kernel_ms);
+
+/* bmc_run with CUDA events recorded on the scenario's stream before the
+ * first and after the last step; *elapsed_ms receives the device time. */
+int bmc_run_timed(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats, float* elapsed_ms);
+
+/* Select the CUDA device used by scenarios created afterwards on this host
+ * thread (one process per GPU). */
+int bmc_set_device(int32_t device);
+
+/* Bytes the library has copied host->device and device->host so far. */
+int bmc_transfer_bytes(uint64_t* h2d, uint64_t* d2h);
+
+/* Number of kernels this library has launched so far (all scenarios). */
+int bmc_launch_count(uint64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,574 @@
+/*
+ * bmc_oracle.c -- CPU restatement of the BioCMA-MCST Monte Carlo cycle.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker).  The product never links this file.
+ * Reference citations for every function are in bmc_oracle.h and beside each
+ * function below.  Compile with -ffp-contract=off: the GPU path is compiled
+ * without multiply-add contraction, so both sides round every operation the
+ * same way and integer outcomes (positions, statuses, counts) match bit for
+ * bit.
+ */
+#include "bmc_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Draw source.  The reference draws from Kokkos::Random_XorShift1024_Pool
+ * (apps/libs/mc/public/mc/alias.hpp L98), which cannot be replayed outside
+ * Kokkos.  Both this oracle and the GPU path use Philox4x32-10 (Salmon et al.,
+ * SC'11, "Parallel random numbers: as easy as 1, 2, 3"), keyed by the
+ * scenario seed and countered by (particle id, step, purpose). */
+
+static inline void mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  *hi = (uint32_t)(p >> 32);
+  *lo = (uint32_t)p;
+}
+
+void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(0xD2511F53u, c0, &hi0, &lo0);
+    mulhilo32(0xCD9E8D57u, c2, &hi1, &lo1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+/* Uniform float on the open interval (0,1): an odd 24-bit integer times
+ * 2^-24, exactly representable, never 0 or 1. */
+float orc_u01(uint32_t x) { return (float)((x >> 8) | 1u) * 0x1p-24f; }
+
+void orc_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]) {
+  uint32_t ctr[4] = {id, step, purpose, 0u};
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t r[4];
+  orc_philox4x32_10(ctr, key, r);
+  for (int k = 0; k < 4; ++k) out[k] = orc_u01(r[k]);
+}
+
+/* Independent stream for the free-running statistical comparison: a
+ * splitmix64-seeded xorshift64* generator per (particle id, step), so that
+ * the oracle does not share a single draw with the GPU path. */
+static void xorshift_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]) {
+  uint64_t z = seed ^ ((uint64_t)id << 20) ^ ((uint64_t)step << 42) ^ ((uint64_t)purpose << 60);
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  if (z == 0) z = 0x2545F4914F6CDD1Dull;
+  for (int k = 0; k < 4; ++k) {
+    z ^= z >> 12;
+    z ^= z << 25;
+    z ^= z >> 27;
+    uint64_t v = z * 0x2545F4914F6CDD1Dull;
+    out[k] = orc_u01((uint32_t)(v >> 32));
+  }
+}
+
+static inline void draws_for(const orc_state* s, uint32_t id, uint32_t purpose, float out[4]) {
+  if (s->draw_mode == ORC_DRAW_XORSHIFT)
+    xorshift_draws(s->seed, id, s->step, purpose, out);
+  else
+    orc_draws(s->seed, id, s->step, purpose, out);
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* Exact contribution sums.  v is rounded to the nearest multiple of 2^e
+ * (ties to even), clamped to |q| <= qmax.  Integer sums are independent of
+ * summation order, so every parallel decomposition gives the same total. */
+int64_t orc_quantize(double v, int32_t e, int64_t qmax, int* clamped) {
+  double x = rint(ldexp(v, -e));
+  if (x > (double)qmax) {
+    *clamped = 1;
+    return qmax;
+  }
+  if (x < -(double)qmax) {
+    *clamped = 1;
+    return -qmax;
+  }
+  return (int64_t)x;
+}
+
+/* Total t (an integer number of quanta) to double, rounded once:
+ * t = hi * 2^32 + lo with 0 <= lo < 2^32; hi*2^32 and lo are exact doubles
+ * while |t| < 2^85, so the single addition is the only rounding. */
+double orc_fixed_to_double(__int128 t, int32_t e) {
+  const __int128 lo = t & (__int128)0xFFFFFFFFu;
+  const __int128 hi = (t - lo) / ((__int128)1 << 32);
+  const double d = (double)(int64_t)hi * 0x1p32 + (double)(uint64_t)lo;
+  return ldexp(d, e);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Models, restated per the ModelType concept
+ * (apps/libs/mc/public/mc/traits.hpp L67-L133): update returns Idle or
+ * Division and writes the particle's contributions; division splits a mother
+ * into mother + child.  Each model is instantiated for double and float. */
+
+#define ORC_F double
+#define ORC_SFX _f64
+#include "bmc_oracle_models.inc"
+#undef ORC_F
+#undef ORC_SFX
+#define ORC_F float
+#define ORC_SFX _f32
+#include "bmc_oracle_models.inc"
+#undef ORC_F
+#undef ORC_SFX
+
+static int model_update(const orc_state* s, double dt, uint64_t i, const double* c, double* ctb) {
+  const uint64_t cap = s->phys_capacity;
+  if (s->f64) {
+    double* st = (double*)s->state;
+    double x[8];
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    int r;
+    switch (s->model) {
+      case ORC_MODEL_MONOD: r = monod_update_f64(dt, x, c, ctb, s->params); break;
+      case ORC_MODEL_OVERFLOW: r = overflow_update_f64(dt, x, c, ctb, s->params); break;
+      default: r = ORC_IDLE; break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+    return r;
+  } else {
+    float* st = (float*)s->state;
+    float x[8];
+    float cf[8] = {0};
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    int r;
+    switch (s->model) {
+      case ORC_MODEL_MONOD: r = monod_update_f32((float)dt, x, c, cf, s->params); break;
+      case ORC_MODEL_OVERFLOW: r = overflow_update_f32((float)dt, x, c, cf, s->params); break;
+      case ORC_MODEL_FIXED_LENGTH: r = fixed_length_update_f32((float)dt, x, c, cf, s->params); break;
+      default: r = ORC_IDLE; break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+    for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = (double)cf[j];
+    return r;
+  }
+}
+
+static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) {
+  const uint64_t cap = s->phys_capacity;
+  float d[4];
+  draws_for(s, s->id[i], 1u, d);
+  if (s->f64) {
+    double* st = (double*)s->state;
+    double* ch = (double*)s->child_state;
+    double x[8], y[8] = {0};
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    switch (s->model) {
+      case ORC_MODEL_MONOD: monod_division_f64(x, y, d, s->params); break;
+      case ORC_MODEL_OVERFLOW: overflow_division_f64(x, y, d, s->params); break;
+      default: break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) {
+      st[v * cap + i] = x[v];
+      ch[v * cap + child_slot] = y[v];
+    }
+  } else {
+    float* st = (float*)s->state;
+    float* ch = (float*)s->child_state;
+    float x[8], y[8] = {0};
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    switch (s->model) {
+      case ORC_MODEL_MONOD: monod_division_f32(x, y, d, s->params); break;
+      case ORC_MODEL_OVERFLOW: overflow_division_f32(x, y, d, s->params); break;
+      case ORC_MODEL_FIXED_LENGTH: fixed_length_division_f32(x, y, d, s->params); break;
+      default: break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) {
+      st[v * cap + i] = x[v];
+      ch[v * cap + child_slot] = y[v];
+    }
+  }
+}
+
+static void model_init(const orc_state* s, uint64_t i, const float* d) {
+  const uint64_t cap = s->phys_capacity;
+  if (s->f64) {
+    double* st = (double*)s->state;
+    double x[8] = {0};
+    switch (s->model) {
+      case ORC_MODEL_MONOD: monod_init_f64(x, d, s->params); break;
+      case ORC_MODEL_OVERFLOW: overflow_init_f64(x, d, s->params); break;
+      default: break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+  } else {
+    float* st = (float*)s->state;
+    float x[8] = {0};
+    switch (s->model) {
+      case ORC_MODEL_MONOD: monod_init_f32(x, d, s->params); break;
+      case ORC_MODEL_OVERFLOW: overflow_init_f32(x, d, s->params); break;
+      case ORC_MODEL_FIXED_LENGTH: fixed_length_init_f32(x, d, s->params); break;
+      default: break;
+    }
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+  }
+}
+
+static double model_mass(const orc_state* s, uint64_t i) {
+  const uint64_t cap = s->phys_capacity;
+  if (s->f64) return ((const double*)s->state)[i];
+  if (s->model == ORC_MODEL_FIXED_LENGTH) {
+    float lin_density = fixed_length_lin_density();
+    return (double)(((const float*)s->state)[i] * lin_density);
+  }
+  (void)cap;
+  return (double)((const float*)s->state)[i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* Initialisation: apps/libs/mc/src/unit.cpp L102-L163 (InitFunctor: model
+ * init, position = uniform integer in [min_c, max_c), mass reduction). */
+void orc_init_particles(orc_state* s, uint64_t n, uint32_t pos_lo, uint32_t pos_hi) {
+  const uint32_t span = pos_hi - pos_lo;
+  for (uint64_t i = 0; i < n; ++i) {
+    float d[4];
+    const uint32_t pid = (uint32_t)i;
+    uint32_t ctr[4] = {pid, 0xFFFFFFFFu, 2u, 0u};
+    uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
+    uint32_t r[4];
+    orc_philox4x32_10(ctr, key, r);
+    for (int k = 0; k < 4; ++k) d[k] = orc_u01(r[k]);
+    model_init(s, i, d);
+    s->pos[i] = pos_lo + (uint32_t)(((uint64_t)r[0] * (uint64_t)span) >> 32);
+    s->status[i] = ORC_IDLE;
+    s->age_h[i] = 0.0f;
+    s->age_d[i] = 0.0f;
+    s->id[i] = pid;
+  }
+  s->n_used = n;
+  s->next_id = n;
+  s->inactive = 0;
+}
+
+double orc_total_mass(const orc_state* s) {
+  double m = 0.0;
+  for (uint64_t i = 0; i < s->n_used; ++i)
+    if (s->status[i] == ORC_IDLE) m += model_mass(s, i);
+  return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Move: apps/libs/simulation/public/simulation/kernels/move_kernel.hpp
+ * L62-L103.  First k with u <= CDF(c, k) over the K slots; the search is the
+ * reference's branchless bisection (left=0, right=K-1). */
+uint32_t orc_find_next(const orc_state* s, uint32_t c, double u) {
+  const double* row = s->cdf + (uint64_t)c * s->K;
+  int left = 0;
+  int right = (int)s->K - 1;
+  while (left < right) {
+    const int mid = (left + right) >> 1;
+    if (u > row[mid])
+      left = mid + 1;
+    else
+      right = mid;
+  }
+  return s->neighbors[(uint64_t)c * s->K + (uint32_t)left];
+}
+
+/* Liquid step, apps/libs/simulation/src/implScalar.cpp L251-L264:
+ *   M += dt * (C*T - C*sink + Src);  C = M * diag(1/V)
+ * with T(i,j) = F(i->j) off the diagonal and T(j,j) = -sum_k F(j->k). */
+void orc_scalar_step(orc_state* s, double dt) {
+  const uint32_t ns = s->n_s;
+  for (uint32_t j = 0; j < s->n_c; ++j) {
+    for (uint32_t sp = 0; sp < ns; ++sp) {
+      double acc = 0.0;
+      for (uint32_t e = s->in_ptr[j]; e < s->in_ptr[j + 1]; ++e)
+        acc += s->C[(uint64_t)s->in_idx[e] * ns + sp] * s->in_flow[e];
+      const double cj = s->C[(uint64_t)j * ns + sp];
+      acc += cj * (-s->out_flow[j]);
+      const double dmdt = acc - cj * s->sink[j] + s->src[(uint64_t)j * ns + sp];
+      s->M[(uint64_t)j * ns + sp] += dt * dmdt;
+    }
+  }
+  for (uint32_t j = 0; j < s->n_c; ++j)
+    for (uint32_t sp = 0; sp < ns; ++sp)
+      s->C[(uint64_t)j * ns + sp] = s->M[(uint64_t)j * ns + sp] * s->vinv[j];
+}
+
+/* ------------------------------------------------------------------------ */
+/* One cycle over the container (reference CycleFunctors::launch_model then
+ * launch_move, kernels.hpp L124-L224).  Per Idle particle:
+ *   ages(i,1) += dt; status = Model::update(...)       model_kernel.hpp L193
+ *   S(:, pos) += w * contribs                          contribution_kernel.hpp
+ *   move: leave iff dt*Q/V > u1, next = CDF search(u2) move_kernel.hpp L393
+ *   ages(i,0) += dt; exit iff dt*F > -ln(u3)*V          move_kernel.hpp L588
+ * The exit test is evaluated as u3 > exp(-(dt*F)/V), the same inequality
+ * after exponentiation, with the threshold computed once per outlet.
+ * Division requests are recorded here and carried out in slot order by
+ * orc_post_cycle, which is where the reference's buffer order becomes
+ * deterministic. */
+void orc_cycle(orc_state* s, double dt, int n_threads) {
+  const uint64_t n = s->n_used;
+  const uint32_t ns = s->n_s;
+  const uint32_t nctb = s->n_ctb;
+  const int do_move = s->n_c > 1;
+  const int do_leave = s->n_outlets > 0;
+  double pmove_small[1];
+  double* pmove = s->n_c > 1 ? (double*)malloc(sizeof(double) * s->n_c) : pmove_small;
+  for (uint32_t c = 0; c < s->n_c && do_move; ++c) pmove[c] = (dt * s->out_flow[c]) / s->volume[c];
+  double thr[ORC_MAX_OUTLETS];
+  for (uint32_t o = 0; o < s->n_outlets; ++o) thr[o] = exp(-(dt * s->outlet_flow[o]) / s->outlet_volume[o]);
+
+  /* Optional emulation of the reference's Tag3D contribution loop
+   * (contribution_kernel.hpp L167-L185): a team thread walks 32 consecutive
+   * particles and returns at the first non-Idle one, so the Idle particles
+   * after it in that chunk do not contribute.  Off by default; used only to
+   * quantify the deviation of the intended semantics from the shipped one. */
+  uint8_t* contrib_ok = NULL;
+  if (s->quirk_tag3d) {
+    contrib_ok = (uint8_t*)malloc(n ? n : 1);
+    for (uint64_t c0 = 0; c0 < n; c0 += 32) {
+      int alive = 1;
+      for (uint64_t i = c0; i < c0 + 32 && i < n; ++i) {
+        if (s->status[i] != ORC_IDLE) alive = 0;
+        contrib_ok[i] = (uint8_t)alive;
+      }
+    }
+  }
+  uint64_t moves = 0, exits = 0, reqdiv = 0;
+  const size_t src_len = (size_t)s->n_c * ns;
+  if (n_threads < 1) n_threads = 1;
+  uint64_t clamped = 0;
+#ifdef _OPENMP
+  __int128* partial = (__int128*)calloc((size_t)n_threads * src_len, sizeof(__int128));
+#pragma omp parallel num_threads(n_threads) reduction(+ : moves, exits, reqdiv, clamped)
+  {
+    const int tid = omp_get_thread_num();
+    __int128* acc = partial + (size_t)tid * src_len;
+#pragma omp for schedule(static)
+    for (uint64_t i = 0; i < n; ++i) {
+#else
+  __int128* partial = (__int128*)calloc(src_len, sizeof(__int128));
+  {
+    __int128* acc = partial;
+    for (uint64_t i = 0; i < n; ++i) {
+#endif
+      if (s->status[i] != ORC_IDLE) continue;
+      float d[4];
+      draws_for(s, s->id[i], 0u, d);
+      if (s->f64)
+        s->age_d[i] = (float)((double)s->age_d[i] + dt);
+      else
+        s->age_d[i] = s->age_d[i] + (float)dt;
+      const uint32_t p0 = s->pos[i];
+      double ctb[8];
+      const int st = model_update(s, dt, i, s->C + (uint64_t)p0 * ns, ctb);
+      if (st == ORC_DIVISION) {
+        s->div_flag[i] = 1;
+        s->div_pos[i] = p0;
+        reqdiv++;
+      }
+      if (!contrib_ok || contrib_ok[i])
+        for (uint32_t j = 0; j < nctb; ++j) {
+          int cl = 0;
+          acc[(uint64_t)p0 * ns + j] += orc_quantize(s->weight * ctb[j], s->ctb_exp[j], s->ctb_qmax, &cl);
+          clamped += (uint64_t)cl;
+        }
+      uint32_t p = p0;
+      if (do_move) {
+        if (pmove[p] > (double)d[0]) {
+          p = orc_find_next(s, p, (double)d[1]);
+          moves++;
+        }
+        s->pos[i] = p;
+      }
+      if (do_leave) {
+        s->age_h[i] = (float)((double)s->age_h[i] + dt);
+        for (uint32_t o = 0; o < s->n_outlets; ++o) {
+          if (s->outlet_index[o] == p) {
+            if (s->outlet_flow[o] != 0.0 && (double)d[2] > thr[o]) {
+              s->status[i] = ORC_EXIT;
+              s->age_h[i] = 0.0f;
+              exits++;
+            }
+            break;
+          }
+        }
+      }
+    }
+  }
+#ifndef _OPENMP
+  n_threads = 1;
+#endif
+  for (uint32_t c = 0; c < s->n_c; ++c) {
+    for (uint32_t j = 0; j < nctb; ++j) {
+      const size_t k = (size_t)c * ns + j;
+      __int128 t = 0;
+      for (int th = 0; th < n_threads; ++th) t += partial[(size_t)th * src_len + k];
+      s->src[k] = orc_fixed_to_double(t, s->ctb_exp[j]);
+    }
+  }
+  s->ctb_clamped += clamped;
+  free(partial);
+  free(contrib_ok);
+  if (pmove != pmove_small) free(pmove);
+  s->moves = moves;
+  s->exits = exits;
+  s->requested_divisions = reqdiv;
+}
+
+/* Gap filling of remove_inactive_particles (particles_container.hpp L737-L795
+ * with CompactParticlesFunctor L292-L383) in single-threaded order: the j-th
+ * non-Idle slot of [0, n-r) receives the j-th Idle particle counted from the
+ * end of [n-r, n). */
+void orc_remove_inactive(orc_state* s, uint64_t to_remove) {
+  if (to_remove == 0) return;
+  if (to_remove == s->n_used) {
+    s->n_used = 0;
+    s->inactive = 0;
+    return;
+  }
+  if (to_remove > s->n_used) {
+    s->error = 1;
+    return;
+  }
+  const uint64_t n = s->n_used;
+  const uint64_t head = n - to_remove;
+  uint64_t g = 0;
+  for (uint64_t i = 0; i < head; ++i)
+    if (s->status[i] != ORC_IDLE) s->gap_slot[g++] = (uint32_t)i;
+  uint64_t q = 0;
+  for (uint64_t i = n; i-- > head;)
+    if (s->status[i] == ORC_IDLE) s->src_slot[q++] = (uint32_t)i;
+  if (q != g) {
+    s->error = 2;
+    return;
+  }
+  const uint64_t cap = s->phys_capacity;
+  for (uint64_t j = 0; j < g; ++j) {
+    const uint64_t dst = s->gap_slot[j], src = s->src_slot[j];
+    for (uint32_t v = 0; v < s->n_var; ++v) {
+      if (s->f64)
+        ((double*)s->state)[v * cap + dst] = ((double*)s->state)[v * cap + src];
+      else
+        ((float*)s->state)[v * cap + dst] = ((float*)s->state)[v * cap + src];
+    }
+    s->pos[dst] = s->pos[src];
+    s->status[dst] = ORC_IDLE;
+    s->age_h[dst] = s->age_h[src];
+    s->age_d[dst] = s->age_d[src];
+    s->id[dst] = s->id[src];
+    s->div_flag[dst] = 0;
+  }
+  s->n_used = head;
+  s->inactive -= to_remove;
+}
+
+/* Post-cycle (reference SimulationUnit::post_cycle, simulation.hpp L215):
+ *   1. divisions in slot order, limited by free room (handle_division);
+ *   2. inactive += out (+ dead); compaction when above the threshold
+ *      max(min_removal, n_used * ratio) (update_and_remove_inactive);
+ *   3. children appended after the live particles with ages 0
+ *      (merge_buffer / InsertFunctor). */
+void orc_post_cycle(orc_state* s) {
+  const uint64_t n = s->n_used;
+  uint64_t inactive_after = s->inactive + s->exits;
+  const uint64_t ratio_thr = (uint64_t)((double)n * s->dead_ratio_threshold);
+  const uint64_t threshold = s->min_removal > ratio_thr ? s->min_removal : ratio_thr;
+  const int compact = inactive_after > threshold;
+  const uint64_t n_after = compact ? n - inactive_after : n;
+  const uint64_t room = s->phys_capacity > n_after ? s->phys_capacity - n_after : 0;
+
+  uint64_t births = 0, overflow = 0;
+  for (uint64_t i = 0; i < n; ++i) {
+    if (!s->div_flag[i]) continue;
+    s->div_flag[i] = 0;
+    if (births < room) {
+      model_division(s, i, births);
+      s->child_pos[births] = s->div_pos[i];
+      s->age_d[i] = 0.0f;
+      births++;
+    } else {
+      overflow++;
+    }
+  }
+  s->inactive = inactive_after;
+  s->compacted = 0;
+  if (compact) {
+    orc_remove_inactive(s, inactive_after);
+    s->compacted = 1;
+  }
+  const uint64_t base = s->n_used;
+  const uint64_t cap = s->phys_capacity;
+  for (uint64_t b = 0; b < births; ++b) {
+    const uint64_t dst = base + b;
+    for (uint32_t v = 0; v < s->n_var; ++v) {
+      if (s->f64)
+        ((double*)s->state)[v * cap + dst] = ((double*)s->child_state)[v * cap + b];
+      else
+        ((float*)s->state)[v * cap + dst] = ((float*)s->child_state)[v * cap + b];
+    }
+    s->pos[dst] = s->child_pos[b];
+    s->status[dst] = ORC_IDLE;
+    s->age_h[dst] = 0.0f;
+    s->age_d[dst] = 0.0f;
+    s->id[dst] = (uint32_t)(s->next_id + b);
+  }
+  s->n_used = base + births;
+  s->next_id += births;
+  s->births = births;
+  s->overflow = overflow;
+}
+
+/* One main-loop iteration, apps/core/src/host_specific.cpp L280-L291:
+ * update_feed -> ode_step -> clearContribution -> cycleProcess. */
+void orc_step(orc_state* s, double dt, int n_threads) {
+  const uint32_t ns = s->n_s;
+  for (uint32_t j = 0; j < s->n_c; ++j) s->sink[j] = 0.0;
+  s->n_outlets = 0;
+  for (uint32_t f = 0; f < s->n_feeds; ++f) {
+    for (uint32_t sp = 0; sp < ns; ++sp) {
+      const double cf = s->feed_conc[f * 8 + sp];
+      if (cf != 0.0) s->src[(uint64_t)s->feed_in[f] * ns + sp] += s->feed_flow[f] * cf;
+    }
+    if (s->feed_out[f] >= 0) {
+      const uint32_t o = (uint32_t)s->feed_out[f];
+      s->sink[o] += s->feed_flow[f];
+      s->outlet_index[s->n_outlets] = o;
+      s->outlet_flow[s->n_outlets] = s->feed_flow[f];
+      s->outlet_volume[s->n_outlets] = s->volume[o];
+      s->n_outlets++;
+    }
+  }
+  orc_scalar_step(s, dt);
+  memset(s->src, 0, sizeof(double) * (size_t)s->n_c * ns);
+  orc_cycle(s, dt, n_threads);
+  orc_post_cycle(s);
+  s->step++;
+}
+
+void orc_run(orc_state* s, double dt, uint32_t n_steps, int n_threads) {
+  for (uint32_t k = 0; k < n_steps; ++k) orc_step(s, dt, n_threads);
+}
+
+/* Occupancy per compartment of Idle particles (MonteCarloUnit::getRepartition,
+ * apps/libs/mc/src/unit.cpp L191-L230). */
+void orc_repartition(const orc_state* s, uint64_t* counts) {
+  for (uint32_t c = 0; c < s->n_c; ++c) counts[c] = 0;
+  for (uint64_t i = 0; i < s->n_used; ++i)
+    if (s->status[i] == ORC_IDLE) counts[s->pos[i]]++;
+}

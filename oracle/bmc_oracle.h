@@ -1,0 +1,158 @@
+/*
+ * bmc_oracle.h -- CPU restatement of the BioCMA-MCST Monte Carlo cycle.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file and bmc_oracle.c are the checker the
+ * GPU path is compared against; the product (libbmc) never links, loads or
+ * calls them.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+ * baseline leg use the oracle.
+ *
+ * What it restates (reference paths are relative to the BioCMA-MCST tree):
+ *   - per-particle cycle: apps/libs/simulation/public/simulation/kernels/
+ *       model_kernel.hpp L164-L268 (ages(i,1)+=dt, Model::update, division)
+ *       contribution_kernel.hpp L146-L186 (S(j,pos) += w*contribs(p,j))
+ *       move_kernel.hpp L62-L103 (__find_next_compartment), L393-L437
+ *       (handle_move), L348-L359 + L588-L648 (TagLeave / handle_exit)
+ *     apps/libs/simulation/public/simulation/probability_leaving.hpp L18-L35
+ *   - division buffer, compaction, merge: apps/libs/mc/public/mc/
+ *       particles_container.hpp L541-L575 (update_and_remove_inactive,
+ *       handle_division), L577-L600 (merge_buffer), L737-L795
+ *       (remove_inactive_particles) and L292-L383 (CompactParticlesFunctor,
+ *       whose single-threaded execution order is the one restated here)
+ *   - liquid step: apps/libs/simulation/src/implScalar.cpp L251-L264
+ *       (performStep), apps/libs/simulation/src/simulation.model.cpp L73-L111
+ *       (update_feed), ordering from apps/core/src/host_specific.cpp L257-L313
+ *
+ * Parity status: the reference ships no golden vectors for the cycle, the
+ * move, the scatter or the liquid step (its own tests cover feed arithmetic
+ * and container counts only).  The oracle is pinned against those tests, the
+ * published Philox4x32-10 known-answer vectors, and hand-derived cases
+ * worked from the reference source; see tests/golden/.
+ */
+#ifndef BMC_ORACLE_H
+#define BMC_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_IDLE = 0, ORC_DIVISION = 1, ORC_EXIT = 2, ORC_DEAD = 3 };
+enum { ORC_MODEL_MONOD = 1, ORC_MODEL_OVERFLOW = 2, ORC_MODEL_FIXED_LENGTH = 3 };
+enum { ORC_DRAW_PHILOX = 0, ORC_DRAW_XORSHIFT = 1 };
+
+#define ORC_MAX_OUTLETS 8
+#define ORC_MAX_PARAMS 16
+
+/* Every array is owned by the caller.  Particle arrays have `phys_capacity`
+ * slots; `state` is SoA: state[v * phys_capacity + i], element type double
+ * when f64 != 0 else float. */
+typedef struct orc_state {
+  /* particle container */
+  uint64_t n_used;
+  uint64_t phys_capacity;
+  uint64_t inactive;
+  uint64_t next_id;
+  void* state;
+  uint32_t* pos;
+  uint8_t* status;
+  float* age_h; /* reference ages(i,0): hydraulic time */
+  float* age_d; /* reference ages(i,1): time since division */
+  uint32_t* id;
+  uint8_t* div_flag;     /* scratch, phys_capacity */
+  uint32_t* div_pos;     /* scratch, phys_capacity */
+  void* child_state;     /* scratch, n_var * phys_capacity */
+  uint32_t* child_pos;   /* scratch */
+  uint32_t* gap_slot;    /* scratch */
+  uint32_t* src_slot;    /* scratch */
+
+  /* model */
+  int32_t model;
+  int32_t f64;
+  uint32_t n_var;
+  uint32_t n_ctb;
+  double params[ORC_MAX_PARAMS];
+  double weight;
+
+  /* domain: liquid_volume, diag_transition (out flows), neighbors, CDF */
+  uint32_t n_c;
+  uint32_t K;
+  uint32_t n_s;
+  const double* volume;
+  const double* out_flow;
+  const uint32_t* neighbors; /* n_c * K, row-major */
+  const double* cdf;         /* n_c * K, row-major */
+  uint32_t n_outlets;
+  uint32_t outlet_index[ORC_MAX_OUTLETS];
+  double outlet_flow[ORC_MAX_OUTLETS];
+  double outlet_volume[ORC_MAX_OUTLETS];
+
+  /* liquid scalars, layout [compartment][species] (reference LayoutLeft of
+   * an n_species x n_compartments matrix) */
+  double* C;
+  double* M;
+  double* src;      /* contributions of the last cycle (+ feed during a step) */
+  double* sink;     /* per compartment */
+  const double* vinv;
+  const uint32_t* in_ptr;  /* incoming-flow CSR by destination column */
+  const uint32_t* in_idx;
+  const double* in_flow;
+  /* feeds: constant flow * concentration at an inlet, optional outlet sink */
+  uint32_t n_feeds;
+  uint32_t feed_in[ORC_MAX_OUTLETS];
+  int32_t feed_out[ORC_MAX_OUTLETS];
+  double feed_flow[ORC_MAX_OUTLETS];
+  double feed_conc[ORC_MAX_OUTLETS * 8]; /* [feed][species] */
+
+  /* randomness */
+  int32_t draw_mode;
+  uint64_t seed;
+  uint32_t step;
+
+  /* runtime parameters (reference MC::RuntimeParameters) */
+  double dead_ratio_threshold;
+  uint64_t min_removal;
+
+  /* Contribution quantum: a particle's contribution v = weight * ctb[j] is
+   * rounded to the integer q = rint(v * 2^-ctb_exp[j]) with |q| <= ctb_qmax,
+   * and the sums are exact integer sums (see orc_fixed_to_double). */
+  int32_t ctb_exp[8];
+  int64_t ctb_qmax;
+  uint64_t ctb_clamped;
+
+  /* quirk emulation: 1 = reference Tag3D contribution early return */
+  int32_t quirk_tag3d;
+
+  /* per-step outputs */
+  uint64_t births;
+  uint64_t exits;
+  uint64_t moves;
+  uint64_t overflow;
+  uint64_t requested_divisions;
+  int32_t compacted;
+  int32_t error;
+} orc_state;
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+float orc_u01(uint32_t x);
+void orc_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]);
+
+void orc_init_particles(orc_state* s, uint64_t n, uint32_t pos_lo, uint32_t pos_hi);
+double orc_total_mass(const orc_state* s);
+
+void orc_scalar_step(orc_state* s, double dt);
+void orc_cycle(orc_state* s, double dt, int n_threads);
+void orc_post_cycle(orc_state* s);
+void orc_step(orc_state* s, double dt, int n_threads);
+void orc_run(orc_state* s, double dt, uint32_t n_steps, int n_threads);
+void orc_remove_inactive(orc_state* s, uint64_t to_remove);
+
+int64_t orc_quantize(double v, int32_t e, int64_t qmax, int* clamped);
+double orc_fixed_to_double(__int128 t, int32_t e);
+uint32_t orc_find_next(const orc_state* s, uint32_t c, double u);
+void orc_repartition(const orc_state* s, uint64_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,163 @@
+"""GPU path (libbmc through its C-ABI) against the CPU restatement.
+
+Integer outcomes (compartments, statuses, ids, counts) and every floating
+value (state, ages, concentrations, masses, sources) are compared bit for
+bit: the draws are the same Philox stream on both sides, contribution sums
+are exact integer sums, and both sides round each operation the same way.
+"""
+import numpy as np
+import pytest
+
+from bmc import scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(oracle_mod, scen, capacity=None):
+    from bmc.sim import GpuScenario
+
+    g = GpuScenario(scen, capacity=capacity)
+    o = oracle_mod.Oracle(scen, phys_capacity=g.cap)
+    w = o.init_particles()
+    assert abs(w - g.weight) <= 1e-14 * g.weight
+    o.set_weight(g.weight)
+    return g, o
+
+
+def assert_same_particles(g, o, where=""):
+    pg, po = g.particles(), o.particles()
+    assert len(pg["pos"]) == len(po["pos"]), where
+    for k in ("pos", "status", "id"):
+        assert np.array_equal(pg[k], po[k]), f"{where}: {k}"
+    for k in ("age_h", "age_d"):
+        assert np.array_equal(pg[k].view(np.uint32), po[k].view(np.uint32)), f"{where}: {k}"
+    sg, so = pg["state"], po["state"]
+    ui = np.uint64 if sg.dtype == np.float64 else np.uint32
+    assert np.array_equal(sg.view(ui), so.view(ui)), f"{where}: state"
+
+
+def assert_same_liquid(g, o, where=""):
+    lq = g.liquid()
+    for k, ref in (("C", o.C), ("M", o.M), ("src", o.src)):
+        assert np.array_equal(lq[k].view(np.uint64), ref.view(np.uint64)), f"{where}: {k}"
+
+
+def assert_same_stats(gs, os_, where=""):
+    for k in ("n_used", "births", "exits", "moves", "overflow"):
+        assert gs[k] == os_[k], f"{where}: {k} gpu={gs[k]} cpu={os_[k]}"
+    assert gs["error"] == 0, where
+
+
+def test_draws_match_oracle(oracle_mod):
+    from bmc.sim import debug_draws
+
+    ids = np.arange(0, 5000, 7, dtype=np.uint32)
+    for step, purpose in ((0, 0), (123, 1), (0xFFFFFFFF, 2)):
+        got = debug_draws(0x1234ABCD5678, ids, step, purpose)
+        ref = np.stack([oracle_mod.draws(0x1234ABCD5678, int(i), step, purpose) for i in ids])
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
+def test_init_identical(oracle_mod):
+    g, o = make_pair(oracle_mod, scenarios.small_ring(5000))
+    assert_same_particles(g, o, "init")
+
+
+@pytest.mark.parametrize("f64", [True, False])
+def test_ring_monod_steps(oracle_mod, f64):
+    sc = scenarios.small_ring(6000, f64=f64, feeds=True)
+    g, o = make_pair(oracle_mod, sc)
+    for k in range(12):
+        gs = g.step()
+        os_ = o.step()
+        assert_same_stats(gs, os_, f"step {k}")
+        assert_same_liquid(g, o, f"step {k}")
+    assert_same_particles(g, o, "end")
+
+
+def test_cycle_only_uses_given_concentrations(oracle_mod):
+    sc = scenarios.small_ring(3000, feeds=False)
+    g, o = make_pair(oracle_mod, sc)
+    gs = g.cycle()
+    o.cycle()
+    o.post_cycle()
+    o.s.step += 1
+    assert gs["moves"] == o.s.moves
+    assert_same_particles(g, o, "cycle")
+    assert np.array_equal(g.liquid()["src"].view(np.uint64), o.src.view(np.uint64))
+
+
+@pytest.mark.parametrize("f64", [True, False])
+def test_lattice_overflow_model(oracle_mod, f64):
+    sc = scenarios.workload(2, n_particles=40000, n_steps=6, f64=f64)
+    sc.net = __import__("bmc.networks", fromlist=["x"]).lattice_vortex(4, seed=7)
+    sc.c0 = sc.c0[: sc.net.n_c]
+    sc.feeds[0].outlet = sc.net.n_c - 1
+    sc.feeds[0].flow = 2e-4
+    g, o = make_pair(oracle_mod, sc)
+    for k in range(6):
+        gs = g.step()
+        os_ = o.step(4)
+        assert_same_stats(gs, os_, f"step {k}")
+    assert_same_liquid(g, o, "end")
+    assert_same_particles(g, o, "end")
+
+
+def test_fixed_length_reference_model(oracle_mod):
+    sc = scenarios.small_ring(4000, model=scenarios.fixed_length(), feeds=True)
+    sc.dt = 5.0  # lengths grow visibly; many divisions
+    g, o = make_pair(oracle_mod, sc)
+    births = 0
+    for k in range(40):
+        gs = g.step()
+        os_ = o.step()
+        assert_same_stats(gs, os_, f"step {k}")
+        births += gs["births"]
+    assert births > 0
+    assert_same_particles(g, o, "end")
+    assert_same_liquid(g, o, "end")
+
+
+def test_divisions_overflow_and_compaction(oracle_mod):
+    # division mass inside the initial range: many births, refusals once full
+    m = scenarios.monod(f64=True, m_div=1.0)
+    sc = scenarios.zero_d(3000, model=m, outlet=True)
+    sc.feeds[0].flow = 1e-3  # strong outlet: exits trigger compaction
+    g, o = make_pair(oracle_mod, sc, capacity=4096)
+    saw = {"births": 0, "overflow": 0, "compacted": 0}
+    for k in range(25):
+        gs = g.step()
+        os_ = o.step()
+        assert_same_stats(gs, os_, f"step {k}")
+        assert gs["compacted"] == os_["compacted"], f"step {k}"
+        saw["births"] += gs["births"]
+        saw["overflow"] += gs["overflow"]
+        saw["compacted"] += gs["compacted"]
+        assert_same_particles(g, o, f"step {k}")
+    assert saw["births"] > 0 and saw["compacted"] > 0
+    assert_same_liquid(g, o, "end")
+
+
+def test_graph_run_equals_steps(oracle_mod):
+    sc = scenarios.small_ring(5000, feeds=True)
+    g, o = make_pair(oracle_mod, sc)
+    gs = g.run(15)
+    o.run(15)
+    assert gs["n_used"] == o.n_used and gs["step"] == 15
+    assert_same_particles(g, o, "run")
+    assert_same_liquid(g, o, "run")
+
+
+def test_repartition_and_force_remove(oracle_mod):
+    sc = scenarios.small_ring(4096, feeds=True)
+    sc.feeds[0].flow = 2e-3
+    g, o = make_pair(oracle_mod, sc)
+    for _ in range(5):
+        g.step()
+        o.step()
+    assert np.array_equal(g.repartition(), o.repartition())
+    g.force_remove_dead()
+    import ctypes as ct
+
+    oracle_mod.lib().orc_remove_inactive(ct.byref(o.s), o.s.inactive)
+    assert_same_particles(g, o, "force_remove_dead")
