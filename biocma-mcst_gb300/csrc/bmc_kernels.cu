@@ -188,6 +188,7 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
       since_flush = 0;
       __syncthreads();
     }
+    if (done) break;  // a block that never received a tile (cur == -1) ends here
     const ScenDev& S = sc[s];
     const unsigned t = g - S.tile_base;
     const unsigned long long n_used = S.ctl->n_used;
