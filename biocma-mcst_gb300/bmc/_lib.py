@@ -69,6 +69,7 @@ SIGNATURES = {
     "bmc_read_particles": [VP, c_u64, VP, VP, VP, VP, VP, VP, VP],
     "bmc_read_liquid": [VP, VP, VP, VP],
     "bmc_repartition": [VP, VP],
+    "bmc_repartition_static": [VP, VP],
     "bmc_force_remove_dead": [VP],
     "bmc_batch_create": [VP, c_u32, VP],
     "bmc_batch_destroy": [VP],

@@ -8,7 +8,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -790,6 +792,47 @@ int bmc_repartition(bmc_scenario* s, uint64_t* counts) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   cudaFree(d);
   if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("repartition: ") + cudaGetErrorString(e));
+  return BMC_OK;
+}
+
+// ---- allocation-free repartition --------------------------------------------------
+// Per-compartment counters of bmc_repartition_static.  The name below is a
+// host-side stand-in in host code: the device address is looked up once per
+// device with cudaGetSymbolAddress and passed to the kernel.
+static __device__ __align__(256) unsigned long long g_repartition_scratch[BMC_REPARTITION_STATIC_MAX];
+
+namespace {
+std::mutex g_scratch_mu;
+std::array<unsigned long long*, 64> g_scratch_ptr{};  // by device ordinal
+}  // namespace
+
+int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
+  if (!s || !counts) return fail(BMC_E_INVALID, "null argument");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  if (s->h.n_c > BMC_REPARTITION_STATIC_MAX)
+    return fail(BMC_E_CAPACITY, "bmc_repartition_static: " + std::to_string(s->h.n_c) +
+                                    " compartments exceed the static scratch of " +
+                                    std::to_string(BMC_REPARTITION_STATIC_MAX));
+  int dev = 0;
+  BMC_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= (int)g_scratch_ptr.size()) return fail(BMC_E_INVALID, "device ordinal out of range");
+  unsigned long long* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+      void* p = nullptr;
+      BMC_CUDA(cudaGetSymbolAddress(&p, g_repartition_scratch));
+      g_scratch_ptr[dev] = static_cast<unsigned long long*>(p);
+    }
+    scratch = g_scratch_ptr[dev];
+  }
+  const size_t bytes = (size_t)s->h.n_c * sizeof(unsigned long long);
+  BMC_CUDA(cudaMemsetAsync(scratch, 0, bytes, s->stream));
+  bmc::launch_repartition(s->stream, s->d_desc, scratch, s->sm_count * 4);
+  g_launches++;
+  BMC_CUDA(cudaGetLastError());
+  BMC_CUDA(counted_memcpy_async(counts, scratch, bytes, cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
   return BMC_OK;
 }
 
