@@ -223,6 +223,10 @@ def run_gpu(args):
         if dist is not None:
             dist.barrier()
 
+    # launch shape chosen by the autotuner (its timed steps are warm-up steps)
+    from bmc import autotune
+
+    shape, tune_ms = autotune.tune_scenario(g)
     # warm-up (graph capture, first touch)
     g.run(max(args.warmup, 3))
     st0 = g.stats()
@@ -265,6 +269,9 @@ def run_gpu(args):
                 "traffic": (tpp * statistics.mean(alive_k)) if tpp else None,
                 "kernel": "k_cycle", "algorithmic_bytes_per_particle": B,
                 "kernel_ms": cyc_ms, "step_kernels_ms": step_ms,
+                "step_breakdown_ms": dict(zip(["liquid", "cycle", "plan", "divide", "compact", "merge"],
+                                              [round(statistics.mean(k[i] for k in kms), 5)
+                                               for i in range(6)])),
                 "kernel_share_of_step": cyc_ms / step_ms}
 
     # end to end through the public per-step API: host-side feed update
@@ -321,6 +328,10 @@ def run_gpu(args):
     if rank == 0:
         cfg = workload_config(scen)
         cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
+        cfg["launch_shape"] = {"threads": shape[0], "particles_per_thread": shape[1],
+                               "blocks_per_sm": shape[2] or "max",
+                               "autotune_ms_per_step": {f"{a}x{b}x{c}": round(v, 4)
+                                                        for (a, b, c), v in tune_ms.items()}}
         line = {
             "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,

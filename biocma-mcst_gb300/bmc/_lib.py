@@ -20,7 +20,7 @@ class ModelDesc(ct.Structure):
 
 class ScenarioDesc(ct.Structure):
     _fields_ = [("model", ModelDesc), ("n_species", c_u32), ("capacity", c_u64), ("seed", c_u64),
-                ("dead_ratio_threshold", c_dbl), ("min_removal", c_u64), ("ctb_bound", c_dbl * 8)]
+                ("dead_ratio_threshold", c_dbl), ("min_removal", c_u64), ("value_bound", c_dbl * 8)]
 
 
 class Feed(ct.Structure):
@@ -75,6 +75,7 @@ SIGNATURES = {
     "bmc_batch_destroy": [VP],
     "bmc_batch_run": [VP, c_dbl, c_u32],
     "bmc_batch_set_shape": [VP, c_u32, c_u32, c_u32],
+    "bmc_set_shape": [VP, c_u32, c_u32, c_u32],
     "bmc_batch_synchronize": [VP],
     "bmc_debug_draws": [c_u64, VP, c_u64, c_u32, c_u32, VP],
     "bmc_launch_count": [VP],

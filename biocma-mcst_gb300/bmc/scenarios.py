@@ -16,6 +16,7 @@ from .networks import Network, lattice_vortex, ring_network, single_compartment
 MODEL_MONOD = 1
 MODEL_OVERFLOW = 2
 MODEL_FIXED_LENGTH = 3
+MODEL_FIXED_LENGTH_GENERAL = 4
 
 MU_MAX = 0.77 / 3600.0  # 1/s
 
@@ -30,7 +31,11 @@ class ModelSpec:
     n_ctb: int
     f64: bool
     params: np.ndarray  # float64[16]
-    ctb_bound: np.ndarray  # float64[n_ctb]: bound on |contribution| per particle
+    # separable models: [bound on |basis|]; general models: bound on
+    # |contribution j| of one particle
+    value_bound: np.ndarray
+    separable: bool = True
+    read_vars: int = 2  # state variables the update reads (the others are outputs)
 
     @property
     def itemsize(self) -> int:
@@ -41,8 +46,8 @@ def monod(f64: bool = True, mu_max: float = MU_MAX, ks: float = 0.01, y: float =
           m_div: float = 2.0, m_lo: float = 0.9, m_span: float = 0.2) -> ModelSpec:
     p = np.zeros(16)
     p[:6] = [mu_max, ks, y, m_div, m_lo, m_span]
-    bound = np.array([mu_max * 4.0 * m_div / y])
-    return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, bound)
+    # contribution = -(mu / Y) * mass: the basis is the particle mass
+    return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, np.array([4.0 * m_div]))
 
 
 def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
@@ -52,19 +57,23 @@ def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
     m_div = 2.0
     p = np.zeros(16)
     p[:13] = [qs_max, 0.01, qo_max, 1e-4, y_ox, y_of, y_ac, y_o, y_c, m_div, y_cof, 0.9, 0.2]
-    m = 4.0 * m_div
-    bound = np.array([qs_max * m, y_o * qo_max * m, y_ac * qs_max * m, (y_c + y_cof) * qs_max * m])
-    return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, bound)
+    # every contribution is a rate of the compartment times the mass
+    return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, np.array([4.0 * m_div]))
 
 
-def fixed_length() -> ModelSpec:
-    """The reference's FixedLength model (float state, one contribution)."""
+def fixed_length(general: bool = False) -> ModelSpec:
+    """The reference's FixedLength model (float state, one contribution).
+    ``general`` runs it through the per-particle contribution path."""
     l_dot_max = np.float32(2e-6 / 3600.0)
     d_m = np.float32(0.6e-6)
     lin = np.float32(1000) * np.float32(math.pi) * d_m * d_m / np.float32(4.0)
     phi = float((l_dot_max * lin) / np.float32(0.5))
     p = np.zeros(16)
-    return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([4.0 * phi]))
+    if general:
+        return ModelSpec("fixed_length_general", MODEL_FIXED_LENGTH_GENERAL, 2, 1, False, p,
+                         np.array([4.0 * phi]), separable=False)
+    # contribution = -phi_s(C) per particle: basis 1
+    return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([1.0]))
 
 
 @dataclass
@@ -97,12 +106,17 @@ class Scenario:
     def capacity(self) -> int:
         return int(math.ceil(self.n_particles * self.alloc_factor))
 
-    def ctb_exponents(self, weight: float) -> np.ndarray:
-        """Quantum exponent per contribution: |q| <= 2^42 for any particle."""
+    def quantum_exponents(self, weight: float) -> np.ndarray:
+        """Exponent e of the accumulator quantum 2^e per column, chosen so
+        that the value bound is 2^42 quanta (ceil(log2) taken exactly)."""
         e = np.zeros(8, dtype=np.int32)
-        for j in range(self.model.n_ctb):
-            vmax = weight * float(self.model.ctb_bound[j])
-            e[j] = int(math.ceil(math.log2(vmax))) - 42 if vmax > 0 else -1074
+        cols = 1 if self.model.separable else self.model.n_ctb
+        for j in range(cols):
+            vmax = float(self.model.value_bound[j])
+            if not self.model.separable:
+                vmax *= weight
+            m, ex = math.frexp(vmax)
+            e[j] = (ex - 1 if m == 0.5 else ex) - 42
         return e
 
     def algorithmic_bytes(self) -> int:

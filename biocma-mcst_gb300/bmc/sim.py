@@ -36,8 +36,8 @@ def scenario_desc(scen, capacity: int | None = None) -> ScenarioDesc:
     d.seed = scen.seed
     d.dead_ratio_threshold = scen.dead_ratio_threshold
     d.min_removal = scen.min_removal
-    for j in range(m.n_ctb):
-        d.ctb_bound[j] = float(m.ctb_bound[j])
+    for j in range(len(m.value_bound)):
+        d.value_bound[j] = float(m.value_bound[j])
     return d
 
 
@@ -104,6 +104,9 @@ class GpuScenario:
     def set_weight(self, w: float):
         call("bmc_set_weight", self.handle, w)
         self.weight = w
+
+    def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
+        call("bmc_set_shape", self.handle, threads, ppt, blocks_per_sm)
 
     def set_particles(self, parts: dict, next_id: int):
         m = self.scen.model

@@ -106,6 +106,7 @@ struct bmc_scenario {
   unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
+  unsigned graph_grid = 0;
 };
 
 struct bmc_batch {
@@ -119,6 +120,7 @@ struct bmc_batch {
   unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
+  unsigned graph_grid = 0;
   double dt = -1.0;
 };
 
@@ -147,7 +149,10 @@ void derive_outlets(bmc_scenario* s) {
       s->h.outlet_idx[o] = (uint32_t)fd.outlet;
       s->h.outlet_flow[o] = fd.flow;
       const double vol = s->volume[(size_t)fd.outlet];
-      s->h.outlet_thr[o] = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
+      // leave the reactor iff dt*F > -ln(u)*V  <=>  u > exp(-(dt*F)/V)
+      // <=>  x > floor(2^24 exp(-(dt*F)/V)) for the integer draw x = u 2^24
+      const double thr = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
+      s->h.exit_thr[o] = (uint32_t)std::min(16777216.0, std::floor(thr * 16777216.0));
     }
   }
 }
@@ -161,14 +166,14 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
   int rc = upload_desc(s);
   if (rc) return rc;
   if (launch_pmove) {
-    bmc::launch_pmove(1, s->stream, s->d_desc);
+    bmc::launch_move_thr(1, s->stream, s->d_desc);
     g_launches++;
     BMC_CUDA(cudaGetLastError());
   }
   return BMC_OK;
 }
 
-size_t cycle_smem(const ScenDev& h, int n_ctb) { return (size_t)h.n_c * n_ctb * sizeof(unsigned long long); }
+size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(unsigned long long); }
 
 int prepare_cycle(const bmc::KernelSet* ks, unsigned threads, unsigned ppt_index, unsigned bps_req,
                   size_t smem, int sm_count, unsigned* grid_out) {
@@ -190,9 +195,9 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
                  int sm_count) {
   const int ppt = ppt_of(ppt_index);
   if (kTile % (int)(threads * ppt) != 0) return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
-  bmc::launch_liquid(n_scen, st, d_table, d_bctl, do_scalar);
+  ks->liquid(n_scen, st, d_table, d_bctl, do_scalar);
   ks->cycle[ppt_index](dim3(grid), dim3(threads), smem, st, d_table, n_scen, d_bctl);
-  bmc::launch_plan(n_scen, st, d_table);
+  ks->plan(n_scen, st, d_table);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen);
   ks->merge(dim3(sm_count * 2), st, d_table, n_scen);
@@ -235,16 +240,20 @@ int check_ready(bmc_scenario* s, bool need_liquid) {
 }
 
 int set_quanta(bmc_scenario* s) {
+  // Separable models accumulate one basis value per particle (column 0,
+  // bounded by value_bound[0]); general models accumulate weight *
+  // contribution j per particle (column j, bounded by weight *
+  // value_bound[j]).  The quantum 2^e puts the bound at 2^42 quanta.
+  const int cols = s->ks->separable ? 1 : s->ks->n_ctb;
   for (int j = 0; j < bmc::kMaxSpecies; ++j) {
-    int e = -1074 + 64;
-    if (j < (int)s->h.n_ctb) {
-      const double vmax = s->h.weight * s->desc.ctb_bound[j];
-      if (!(vmax > 0.0) || !std::isfinite(vmax)) return fail(BMC_E_INVALID, "contribution bound must be > 0");
+    int e = 0;
+    if (j < cols) {
+      const double vmax = s->ks->separable ? s->desc.value_bound[j] : s->h.weight * s->desc.value_bound[j];
+      if (!(vmax > 0.0) || !std::isfinite(vmax)) return fail(BMC_E_INVALID, "value bounds must be > 0");
       e = ceil_log2(vmax) - 42;
     }
-    s->h.ctb_exp[j] = e;
-    s->h.ctb_scale[j] = std::ldexp(1.0, -e);
-    s->h.ctb_scale_up[j] = std::ldexp(1.0, e);
+    s->h.q_scale[j] = std::ldexp(1.0, -e);
+    s->h.q_scale_up[j] = std::ldexp(1.0, e);
   }
   return BMC_OK;
 }
@@ -351,6 +360,7 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   h.ctl = s->d_ctl;
   h.n_var = ks->n_var;
   h.n_ctb = ks->n_ctb;
+  h.n_acc = ks->separable ? 1u : (uint32_t)ks->n_ctb;
   h.n_s = desc->n_species;
   h.f64 = desc->model.f64;
   for (int k = 0; k < 16; ++k) h.params[k] = desc->model.params[k];
@@ -394,7 +404,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
   if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
   std::vector<uint32_t> nbr((size_t)n_c * K, 0u);
-  std::vector<double> cd((size_t)n_c * K, 1.0);
+  std::vector<int32_t> cthr((size_t)n_c * K, 1 << 24);
   for (size_t k = 0; k < (size_t)n_c * K; ++k) {
     if (neighbors) {
       if (neighbors[k] >= n_c) return fail(BMC_E_INVALID, "neighbor index out of range");
@@ -402,7 +412,11 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     } else {
       nbr[k] = (uint32_t)(k / K);
     }
-    if (cdf) cd[k] = cdf[k];
+    if (cdf) {
+      // u > CDF  <=>  x > floor(2^24 CDF) for the integer draw x = u 2^24
+      const double v = std::floor(cdf[k] * 16777216.0);
+      cthr[k] = (int32_t)std::max(-1.0, std::min(16777216.0, v));
+    }
   }
   std::vector<double> vol(volume, volume + n_c), outf(out_flows, out_flows + n_c), vinv(n_c), diag(n_c);
   for (uint32_t j = 0; j < n_c; ++j) {
@@ -417,21 +431,23 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     cudaStreamSynchronize(s->stream);
     if (s->darena) cudaFree(s->darena);
     s->darena = nullptr;
-    const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_ctb;
+    const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_acc;
     Carver cv;
-    cv.add(&h.pmove, n_c);
+    cv.add(&h.move_thr, n_c);
+    int32_t* p_cthr = nullptr;
+    cv.add(&p_cthr, (size_t)n_c * K);
     double* p_vol = nullptr;
     cv.add(&p_vol, n_c);
     double* p_out = nullptr;
     cv.add(&p_out, n_c);
-    double* p_cdf = nullptr;
-    cv.add(&p_cdf, (size_t)n_c * K);
     uint32_t* p_nbr = nullptr;
     cv.add(&p_nbr, (size_t)n_c * K);
     double* p_diag = nullptr;
     cv.add(&p_diag, n_c);
     double* p_vinv = nullptr;
     cv.add(&p_vinv, n_c);
+    double* p_rates = nullptr;
+    cv.add(&p_rates, (size_t)n_c * bmc::kMaxRates);
     cv.add(&h.C, ne);
     cv.add(&h.M, ne);
     cv.add(&h.src, ne);
@@ -439,12 +455,13 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     cv.add(&h.acc_lo, na);
     BMC_CUDA(cudaMalloc(&s->darena, cv.off));
     cv.bind(s->darena);
+    h.cdf_thr = p_cthr;
     h.volume = p_vol;
     h.out_flow = p_out;
-    h.cdf = p_cdf;
     h.nbr = p_nbr;
     h.diag = p_diag;
     h.vinv = p_vinv;
+    h.rates = p_rates;
     BMC_CUDA(cudaMemsetAsync(s->darena, 0, cv.off, s->stream));
     s->has_conc = false;
     s->has_transition = false;
@@ -453,7 +470,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   h.K = K;
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.volume), vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
-  BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.cdf), cd.data(), cd.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<int32_t*>(h.cdf_thr), cthr.data(), cthr.size() * 4, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<uint32_t*>(h.nbr), nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.vinv), vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   if (!s->has_transition)
@@ -545,8 +562,8 @@ int bmc_set_concentrations(bmc_scenario* s, const double* conc) {
   BMC_CUDA(counted_memcpy_async(s->h.C, C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(s->h.M, M.data(), M.size() * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(cudaMemsetAsync(s->h.src, 0, C.size() * 8, s->stream));
-  BMC_CUDA(cudaMemsetAsync(s->h.acc_hi, 0, n_c * s->h.n_ctb * 8, s->stream));
-  BMC_CUDA(cudaMemsetAsync(s->h.acc_lo, 0, n_c * s->h.n_ctb * 8, s->stream));
+  BMC_CUDA(cudaMemsetAsync(s->h.acc_hi, 0, n_c * s->h.n_acc * 8, s->stream));
+  BMC_CUDA(cudaMemsetAsync(s->h.acc_lo, 0, n_c * s->h.n_acc * 8, s->stream));
   BMC_CUDA(cudaStreamSynchronize(s->stream));
   s->has_conc = true;
   return BMC_OK;
@@ -644,7 +661,7 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
 }
 
 static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
-  if (s->graph && s->graph_smem == smem) return BMC_OK;
+  if (s->graph && s->graph_smem == smem && s->graph_grid == grid) return BMC_OK;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
   cudaGraph_t g = nullptr;
@@ -663,6 +680,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   s->graph_smem = smem;
+  s->graph_grid = grid;
   return BMC_OK;
 }
 
@@ -671,7 +689,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   if (rc) return rc;
   rc = set_dt(s, dt, true);
   if (rc) return rc;
-  const size_t smem = cycle_smem(s->h, s->ks->n_ctb);
+  const size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
   rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
   if (rc) return rc;
@@ -919,6 +937,24 @@ int bmc_batch_destroy(bmc_batch* b) {
   return BMC_OK;
 }
 
+int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  unsigned th = threads ? threads : s->threads;
+  unsigned pi = s->ppt_index;
+  if (threads && (threads % 32 || threads > 256)) return fail(BMC_E_INVALID, "threads must be a multiple of 32, <= 256");
+  if (ppt) {
+    if (ppt != 1 && ppt != 2 && ppt != 4) return fail(BMC_E_INVALID, "ppt must be 1, 2 or 4");
+    pi = ppt == 1 ? 0 : (ppt == 2 ? 1 : 2);
+  }
+  if (kTile % (int)(th * ppt_of(pi)) != 0) return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
+  s->threads = th;
+  s->ppt_index = pi;
+  s->blocks_per_sm = blocks_per_sm;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  return BMC_OK;
+}
+
 int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!b) return fail(BMC_E_INVALID, "null batch");
   if (threads) {
@@ -951,7 +987,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     ScenDev d = s->h;
     d.tile_base = tiles;
     tiles += d.n_tiles;
-    smem = std::max(smem, cycle_smem(d, b->ks->n_ctb));
+    smem = std::max(smem, cycle_smem(d));
     if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
     b->table[i] = d;
   }
@@ -960,7 +996,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
     BatchCtl bc{0u, tiles};
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
-    bmc::launch_pmove(n, b->stream, b->d_table);
+    bmc::launch_move_thr(n, b->stream, b->d_table);
     g_launches++;
     BMC_CUDA(cudaGetLastError());
     b->dt = dt;
@@ -969,7 +1005,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   unsigned grid = 0;
   int rc = prepare_cycle(b->ks, b->threads, b->ppt_index, b->blocks_per_sm, smem, b->scen[0]->sm_count, &grid);
   if (rc) return rc;
-  if (!b->graph || b->graph_smem != smem) {
+  if (!b->graph || b->graph_smem != smem || b->graph_grid != grid) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
@@ -988,6 +1024,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     b->graph_smem = smem;
+    b->graph_grid = grid;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     BMC_CUDA(cudaGraphLaunch(b->graph, b->stream));
@@ -1009,7 +1046,7 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   if (rc) return rc;
   rc = set_dt(s, dt, true);
   if (rc) return rc;
-  const size_t smem = cycle_smem(s->h, s->ks->n_ctb);
+  const size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
   rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
   if (rc) return rc;
@@ -1018,11 +1055,11 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   cudaStream_t st = s->stream;
   const int ppt_index = (int)s->ppt_index;
   BMC_CUDA(cudaEventRecord(ev[0], st));
-  bmc::launch_liquid(1, st, s->d_desc, s->d_bctl, 1);
+  s->ks->liquid(1, st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
   s->ks->cycle[ppt_index](dim3(grid), dim3(s->threads), smem, st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[2], st));
-  bmc::launch_plan(1, st, s->d_desc);
+  s->ks->plan(1, st, s->d_desc);
   BMC_CUDA(cudaEventRecord(ev[3], st));
   s->ks->divide(dim3(s->sm_count * 4), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[4], st));

@@ -1,19 +1,23 @@
 // bmc_device.cuh -- device-side data layout, draw source and model plugins.
 //
-// Layout in HBM, per scenario (one arena, every array 256-byte aligned):
-//   state   F[n_var][cap]      SoA particle state (ModelType::SelfParticle)
-//   pos     u32[cap]           compartment (reference ParticlePositions, u64)
-//   status  u8[cap]            MC::Status
-//   age_h   f32[cap]           reference ages(i,0), hydraulic time
-//   age_d   f32[cap]           reference ages(i,1), time since division
-//   id      u32[cap]           particle identity, keys the draws
-//   child   F[n_var][cap] + u32[cap]   division buffer (children in rank order)
-//   tile_*  u32[cap/TILE]      per-tile counters (births, inactive, offsets)
-//   bmask   u32[cap/32]        birth-request bits, slot order
-//   bpos    u32[cap]           compartment of a mother when it asked to divide
-//   gap/src u32[cap]           compaction lists
-//   liquid  C, M, src: f64[n_c][n_s]; acc_hi/acc_lo: i64/u64[n_c][n_ctb]
-//   domain  pmove f64[n_c], cdf f64[n_c][K], nbr u32[n_c][K], incoming CSR
+// Layout in HBM, per scenario (one arena per kind, arrays 256-byte aligned):
+//   state    F[n_var][cap]    SoA particle state (ModelType::SelfParticle)
+//   pos      u32[cap]         compartment (reference ParticlePositions, u64)
+//   status   u8[cap]          MC::Status
+//   age_h    f32[cap]         reference ages(i,0), hydraulic time
+//   age_d    f32[cap]         reference ages(i,1), time since division
+//   id       u32[cap]         particle identity, keys the draws
+//   child    F[n_var][cap] + u32[cap]   division buffer (children in rank order)
+//   tile_*   u32[cap/1024]    per-tile counters (births, inactive, offsets)
+//   bmask    u32[cap/32]      birth-request bits, slot order
+//   bpos     u32[cap]         compartment of a mother when it asked to divide
+//   gap/src  u32[cap]         compaction lists
+// Domain and liquid state, per compartment:
+//   move_thr u32[n_c]         leave iff draw < move_thr (= ceil(2^24 dt Q/V))
+//   cdf_thr  i32[n_c][K]      next = first k with draw <= cdf_thr[k]
+//   nbr      u32[n_c][K]      neighbours
+//   rates    F[n_c][8]        model rates of the compartment (from C)
+//   C, M, src f64[n_c][n_s];  acc_hi/acc_lo i64/u64[n_c][n_acc] fixed point
 #pragma once
 #include <cstdint>
 
@@ -22,7 +26,8 @@ namespace bmc {
 constexpr int kMaxOutlets = 8;
 constexpr int kMaxSpecies = 8;
 constexpr int kMaxVar = 8;
-constexpr long long kQMax = 1LL << 42;  // |quantised contribution| bound
+constexpr int kMaxRates = 8;
+constexpr long long kQMax = 1LL << 42;  // |quantised value| bound
 // A block flushes its shared-memory accumulator before it has summed more
 // than 2^20 particles, so |partial| <= 2^62 and no int64 sum can overflow.
 constexpr unsigned kFlushParticles = 1u << 20;
@@ -86,25 +91,27 @@ struct ScenDev {
   uint32_t n_tiles;
   uint32_t tile_base;  // first global tile of this scenario in its batch
   // domain
-  double* pmove;
+  uint32_t* move_thr;
+  const int32_t* cdf_thr;
+  const uint32_t* nbr;
   const double* volume;
   const double* out_flow;
-  const double* cdf;
-  const uint32_t* nbr;
   const uint32_t* in_ptr;
   const uint32_t* in_idx;
   const double* in_flow;
   const double* diag;
   const double* vinv;
+  void* rates;
   uint32_t n_c;
   uint32_t K;
   uint32_t n_s;
   uint32_t n_ctb;
   uint32_t n_var;
+  uint32_t n_acc;  // accumulator entries per compartment (1 when separable)
   uint32_t n_outlets;
   uint32_t outlet_idx[kMaxOutlets];
+  uint32_t exit_thr[kMaxOutlets];  // leave the reactor iff draw > exit_thr
   double outlet_flow[kMaxOutlets];
-  double outlet_thr[kMaxOutlets];
   // feeds
   uint32_t n_feeds;
   uint32_t feed_in[kMaxOutlets];
@@ -117,9 +124,8 @@ struct ScenDev {
   double* src;
   long long* acc_hi;
   unsigned long long* acc_lo;
-  double ctb_scale[kMaxSpecies];     // 2^-e: value -> quanta
-  double ctb_scale_up[kMaxSpecies];  // 2^e: quanta -> value
-  int32_t ctb_exp[kMaxSpecies];
+  double q_scale[kMaxSpecies];     // 2^-e per accumulator column: value -> quanta
+  double q_scale_up[kMaxSpecies];  // 2^e: quanta -> value
   // model
   double params[16];
   double weight;
@@ -192,35 +198,59 @@ __device__ __forceinline__ void philox_raw(unsigned long long seed, uint32_t id,
   out[3] = c3;
 }
 
+// Integer form of a draw: the odd 24-bit integer x with u = x * 2^-24.
+__device__ __forceinline__ uint32_t draw_int(uint32_t r) { return (r >> 8) | 1u; }
+
 // ---------------------------------------------------------------------------
-// Model plugins.  A plugin is a struct template over the float type F with
-//   n_var, n_ctb                              sizes (ModelType::n_var, n_c)
-//   update(dt, x, c, ctb, p) -> status        Model::update
-//   division(x, child, d, p)                  Model::division
-//   init(x, d, p)                             Model::init
-//   mass(x, p) -> double                      Model::mass
-// x is the particle's state in registers, c the concentrations of its
-// compartment (double), ctb its contributions, p the parameter vector, d
-// the draws of the particle.  Reference concept: apps/libs/mc/public/mc/
-// traits.hpp L67-L133.  Every expression keeps the operation order of the
-// CPU restatement so that both round identically (no contraction).
+// Model plugins.  The ModelType concept of the reference
+// (apps/libs/mc/public/mc/traits.hpp L67-L133) split for a GPU:
+//   n_var, n_ctb, n_rates                   sizes
+//   read_mask                               state variables update() reads
+//   separable                               contributions are coef(c)*basis(x)
+//   rates(c, p, r)                          per compartment, from C(:, j):
+//                                           every factor of Model::update that
+//                                           depends on the concentrations only
+//   update(dt, x, r, basis|ctb, p) -> st    Model::update of one particle
+//   coef(r, j)                              contribution j per unit basis
+//   division(x, child, d, p)                Model::division
+//   init(x, d, p)                           Model::init
+//   mass(x, p) -> double                    Model::mass
+// A separable model's contribution to species j is coef_j(C) * basis(x);
+// the cycle then sums one basis value per compartment and the coefficients
+// are applied once per compartment.  A general model (separable = false)
+// writes its n_ctb contributions per particle.  Every expression keeps the
+// operation order of the CPU restatement, so both round identically.
 
 template <class F>
 struct MonodModel {
   static constexpr int n_var = 2;
   static constexpr int n_ctb = 1;
+  static constexpr int n_rates = 2;
   static constexpr int model_id = 1;
-  __device__ __forceinline__ static int update(F dt, F* x, const double* c, F* ctb, const double* p) {
-    const F mu_max = (F)p[0], ks = (F)p[1], y = (F)p[2], mdiv = (F)p[3];
-    F s = (F)__ldg(c);
+  static constexpr bool separable = true;
+  static constexpr unsigned read_mask = 0x3u;
+  // r = {mu, -(mu / Y)}
+  __device__ __forceinline__ static void rates(const double* c, const double* p, F* r) {
+    const F mu_max = (F)p[0], ks = (F)p[1], y = (F)p[2];
+    F s = (F)c[0];
     if (s < (F)0) s = (F)0;
     const F g = s / (ks + s);
     const F mu = mu_max * g;
-    const F growth = mu * x[0];
-    ctb[0] = -(growth / y);
-    x[0] = x[0] + dt * growth;
+    r[0] = mu;
+    r[1] = -(mu / y);
+  }
+  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const double* p) {
+    const F mdiv = (F)p[3];
+    const F m = x[0];
+    basis = m;
+    const F growth = r[0] * m;
+    x[0] = m + dt * growth;
     x[1] = x[1] + dt;
     return x[0] >= mdiv ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static F coef(const F* r, int j) {
+    (void)j;
+    return r[1];
   }
   __device__ __forceinline__ static void division(F* x, F* child, const float* d, const double* p) {
     (void)d;
@@ -245,35 +275,44 @@ template <class F>
 struct OverflowModel {
   static constexpr int n_var = 6;
   static constexpr int n_ctb = 4;
+  static constexpr int n_rates = 5;
   static constexpr int model_id = 2;
-  __device__ __forceinline__ static int update(F dt, F* x, const double* c, F* ctb, const double* p) {
+  static constexpr bool separable = true;
+  static constexpr unsigned read_mask = 0x3u;  // mass and age; the rest is output
+  // r = {mu, q_s, q_o2, q_ac, q_co2}
+  __device__ __forceinline__ static void rates(const double* c, const double* p, F* r) {
     const F qs_max = (F)p[0], ks = (F)p[1], qo_max = (F)p[2], ko = (F)p[3];
     const F y_ox = (F)p[4], y_of = (F)p[5], y_ac = (F)p[6], y_o = (F)p[7];
-    const F y_c = (F)p[8], mdiv = (F)p[9], y_cof = (F)p[10];
-    F s = (F)__ldg(c);
+    const F y_c = (F)p[8], y_cof = (F)p[10];
+    F s = (F)c[0];
     if (s < (F)0) s = (F)0;
-    F o = (F)__ldg(c + 1);
+    F o = (F)c[1];
     if (o < (F)0) o = (F)0;
     const F q_s = qs_max * (s / (ks + s));
     const F q_cap = qo_max * (o / (ko + o));
     const F q_ox = q_s < q_cap ? q_s : q_cap;
     const F q_of = q_s - q_ox;
-    const F mu = y_ox * q_ox + y_of * q_of;
-    const F q_ac = y_ac * q_of;
-    const F q_o2 = y_o * q_ox;
-    const F q_co2 = y_c * q_ox + y_cof * q_of;
+    r[0] = y_ox * q_ox + y_of * q_of;
+    r[1] = q_s;
+    r[2] = y_o * q_ox;
+    r[3] = y_ac * q_of;
+    r[4] = y_c * q_ox + y_cof * q_of;
+  }
+  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const double* p) {
+    const F mdiv = (F)p[9];
     const F m = x[0];
-    ctb[0] = -(q_s * m);
-    ctb[1] = -(q_o2 * m);
-    ctb[2] = q_ac * m;
-    ctb[3] = q_co2 * m;
-    x[0] = m + dt * (mu * m);
+    basis = m;
+    x[0] = m + dt * (r[0] * m);
     x[1] = x[1] + dt;
-    x[2] = mu;
-    x[3] = q_s;
-    x[4] = q_o2;
-    x[5] = q_ac;
+    x[2] = r[0];
+    x[3] = r[1];
+    x[4] = r[2];
+    x[5] = r[3];
     return x[0] >= mdiv ? kDivision : kIdle;
+  }
+  // glucose and O2 consumed, acetate and CO2 produced
+  __device__ __forceinline__ static F coef(const F* r, int j) {
+    return j == 0 ? -r[1] : (j == 1 ? -r[2] : (j == 2 ? r[3] : r[4]));
   }
   __device__ __forceinline__ static void division(F* x, F* child, const float* d, const double* p) {
     (void)d;
@@ -298,31 +337,52 @@ struct OverflowModel {
 };
 
 // The reference's FixedLength model (apps/libs/models/public/models/
-// fixed_length.hpp L19-L161), float state {length, l_max}, one contribution.
-struct FixedLengthModel {
+// fixed_length.hpp L19-L161), float state {length, l_max}, one
+// contribution -phi_s(C) per particle (basis 1).  Separable = false
+// instantiates the same model through the general per-particle path.
+template <bool Separable>
+struct FixedLengthModelT {
   static constexpr int n_var = 2;
   static constexpr int n_ctb = 1;
-  static constexpr int model_id = 3;
+  static constexpr int n_rates = 2;
+  static constexpr int model_id = Separable ? 3 : 4;
+  static constexpr bool separable = Separable;
+  static constexpr unsigned read_mask = 0x3u;
   __device__ __forceinline__ static float lin_density() {
     const float d_m = (float)0.6e-6;
     return (float)1000 * (float)3.14159265358979323846 * d_m * d_m / (float)4.;
   }
   __device__ __forceinline__ static float l_dot_max() { return (float)(2e-6 / 3600.); }
   __device__ __forceinline__ static float phi_s_max() { return (l_dot_max() * lin_density()) / (float)0.5; }
-  __device__ __forceinline__ static int update(float dt, float* x, const double* c, float* ctb,
-                                               const double* p) {
+  // r = {ldot, -phi_s}
+  __device__ __forceinline__ static void rates(const double* c, const double* p, float* r) {
     (void)p;
     const float k = (float)1e-3;
-    const float s = (float)__ldg(c);
+    const float s = (float)c[0];
     const float g = s / (k + s);
     const float phi_s = phi_s_max() * g;
-    const float ldot = l_dot_max() * g;
-    x[0] += dt * ldot;
-    ctb[0] = -phi_s;
+    r[0] = l_dot_max() * g;
+    r[1] = -phi_s;
+  }
+  __device__ __forceinline__ static int update(float dt, float* x, const float* r, float& basis,
+                                               const double* p) {
+    (void)p;
+    basis = 1.0f;
+    x[0] += dt * r[0];
     return x[0] >= x[1] ? kDivision : kIdle;
   }
-  __device__ __forceinline__ static void division(float* x, float* child, const float* d,
-                                                  const double* p) {
+  __device__ __forceinline__ static int update_general(float dt, float* x, const float* r, float* ctb,
+                                                       const double* p) {
+    (void)p;
+    x[0] += dt * r[0];
+    ctb[0] = r[1];
+    return x[0] >= x[1] ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static float coef(const float* r, int j) {
+    (void)j;
+    return r[1];
+  }
+  __device__ __forceinline__ static void division(float* x, float* child, const float* d, const double* p) {
     (void)d;
     (void)p;
     const float l_max_m = (float)2e-6;

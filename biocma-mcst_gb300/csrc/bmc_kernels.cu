@@ -20,10 +20,26 @@
 namespace bmc {
 
 // ---------------------------------------------------------------------------
+// Rates of every compartment (Model::rates) from C, by the calling block.
+template <class Model, class F>
+__device__ __forceinline__ void model_rates(const ScenDev& S) {
+  __syncthreads();
+  F* rates = reinterpret_cast<F*>(S.rates);
+  for (unsigned j = threadIdx.x; j < S.n_c; j += blockDim.x) {
+    F r[kMaxRates];
+    Model::rates(S.C + (size_t)j * S.n_s, S.params, r);
+#pragma unroll
+    for (int k = 0; k < Model::n_rates; ++k) rates[(size_t)j * kMaxRates + k] = r[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // k_liquid: feeds into sources/sink, explicit Euler step of the liquid
-// scalars (M += dt (C T - C sink + src); C = M / V), mass-balance residual.
-// One block per scenario.  Also resets the step counters and the tile
-// scheduler for the cycle that follows.
+// scalars (M += dt (C T - C sink + src); C = M / V), mass-balance residual,
+// then the model's rates of every compartment from the new C.  One block per
+// scenario.  Also resets the step counters and the tile scheduler for the
+// cycle that follows.  With do_scalar == 0 only the resets and the rates.
+template <class Model, class F>
 __global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
   const ScenDev& S = sc[blockIdx.x];
   Control* ctl = S.ctl;
@@ -33,7 +49,10 @@ __global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, Batch
     ctl->exits = 0ull;
     ctl->moves = 0ull;
   }
-  if (!do_scalar) return;
+  if (!do_scalar) {
+    model_rates<Model, F>(S);
+    return;
+  }
   const unsigned nsp = S.n_s;
   const unsigned n_e = S.n_c * nsp;
   const double dt = S.dt;
@@ -63,8 +82,9 @@ __global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, Batch
     const double mold = S.M[e];
     const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
     S.M[e] = mnew;
-    for (unsigned k = 0; k < nsp && k < kMaxSpecies; ++k) {
-      if (k == sp) {
+#pragma unroll
+    for (int k = 0; k < kMaxSpecies; ++k) {
+      if ((unsigned)k == sp) {
         m_new[k] += mnew;
         m_exp[k] += mold + dt * (srcv - cj * sinkj);
       }
@@ -77,7 +97,9 @@ __global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, Batch
   }
   // mass-balance residual per species (diagnostic, block tree reduction)
   __shared__ double red[2][32];
-  for (unsigned k = 0; k < nsp && k < kMaxSpecies; ++k) {
+#pragma unroll
+  for (int k = 0; k < kMaxSpecies; ++k) {
+    if ((unsigned)k >= nsp) break;
     double a = m_new[k], b = m_exp[k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -100,28 +122,64 @@ __global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, Batch
     }
     __syncthreads();
   }
+  model_rates<Model, F>(S);
+}
+
+// ---------------------------------------------------------------------------
+// Quantisation of a value to the accumulator's fixed point: the nearest
+// integer multiple of 2^e (ties to even), |q| <= 2^42.  For a float value
+// the scaling by a power of two and the rounding are exact in float, which
+// gives the same integer as the double computation.
+__device__ __forceinline__ long long quantize(double v, double scale, unsigned long long& clamped, unsigned& err) {
+  double q = rint(__dmul_rn(v, scale));
+  if (fabs(q) > (double)kQMax) {
+    q = q > 0 ? (double)kQMax : -(double)kQMax;
+    ++clamped;
+    err |= 2u;
+  }
+  return (long long)q;
+}
+__device__ __forceinline__ long long quantize(float v, double scale, unsigned long long& clamped, unsigned& err) {
+  float q = rintf(__fmul_rn(v, (float)scale));
+  if (fabsf(q) > (float)kQMax) {
+    q = q > 0 ? (float)kQMax : -(float)kQMax;
+    ++clamped;
+    err |= 2u;
+  }
+  return (long long)q;
 }
 
 // ---------------------------------------------------------------------------
 // k_cycle: the fused per-particle hot path.  A persistent grid takes tiles
 // of 1024 slots from a ticket counter (tiles are ordered scenario after
-// scenario).  For each Idle particle:
-//   ages(i,1) += dt; status = Model::update(..., C(:, pos))
-//   contributions -> shared-memory fixed-point accumulator at the pre-move
-//     compartment (exact integer sums, flushed to two-limb global sums)
-//   move:  leave iff dt*Q/V > u1; next = first k with u2 <= CDF(pos, k)
-//   exit:  ages(i,0) += dt; leave the reactor iff u3 > exp(-dt F / V)
+// scenario).  For each Idle particle (draws: one Philox block, integers
+// x_k = (r_k >> 8) | 1 with u_k = x_k 2^-24):
+//   ages(i,1) += dt; Model::update(dt, x, rates(pos))
+//   contribution basis (or contributions) -> shared-memory fixed-point
+//     accumulator of the pre-move compartment (exact integer sums)
+//   move:  leave iff x_0 < ceil(2^24 dt Q/V)       (<=> dt Q / V > u_0)
+//          next = first k with x_1 <= floor(2^24 CDF(pos,k))
+//                                                  (<=> u_1 <= CDF(pos,k))
+//   exit:  ages(i,0) += dt; leave the reactor iff x_2 > floor(2^24 e^{-dt F/V})
+//                                                  (<=> dt F > -ln(u_2) V)
 // A division request sets a bit of the tile's birth mask; the division
 // itself runs in k_divide once the slot-order ranks are known.
+// Resident blocks of 256 threads per SM the register budget is cut for.
+template <int PPT>
+struct CycleOccupancy {
+  static constexpr int value = PPT == 1 ? 4 : (PPT == 2 ? 3 : 2);
+};
+
 template <class Model, class F, int PPT>
-__global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, int n_scen,
-                                              BatchCtl* __restrict__ bctl) {
+__global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
+    k_cycle(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   extern __shared__ unsigned long long sacc[];
   __shared__ unsigned s_tile;
   __shared__ unsigned s_tile_births, s_tile_inactive;
   __shared__ unsigned long long s_cnt[5];
   constexpr int NV = Model::n_var;
   constexpr int NC = Model::n_ctb;
+  constexpr int NA = Model::separable ? 1 : NC;  // accumulator columns
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const unsigned total_tiles = bctl->total_tiles;
@@ -146,7 +204,7 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
       if (cur >= 0) {
         // flush the accumulator and the counters of scenario `cur`
         const ScenDev& P = sc[cur];
-        const unsigned n_ent = P.n_c * NC;
+        const unsigned n_ent = P.n_c * NA;
         for (unsigned e = tid; e < n_ent; e += blockDim.x) {
           const long long p = (long long)sacc[e];
           if (p != 0) {
@@ -182,7 +240,7 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
         my_err = 0u;
       }
       if (done) break;
-      const unsigned n_ent = sc[s].n_c * NC;
+      const unsigned n_ent = sc[s].n_c * NA;
       for (unsigned e = tid; e < n_ent; e += blockDim.x) sacc[e] = 0ull;
       cur = s;
       since_flush = 0;
@@ -197,12 +255,15 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
     since_flush += kTile;
 
     const unsigned long long cap = S.cap;
-    const unsigned n_c = S.n_c, K = S.K, nsp = S.n_s;
+    const unsigned n_c = S.n_c, K = S.K;
     const unsigned step = S.ctl->step;
+    const unsigned long long seed = S.seed;
     const double dt = S.dt;
     const F dtF = (F)dt;
+    const float dtf = (float)dt;
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
+    const F* __restrict__ rates = reinterpret_cast<const F*>(S.rates);
     F* __restrict__ state = reinterpret_cast<F*>(S.state);
 
     for (int pass = 0; pass < passes; ++pass) {
@@ -210,11 +271,12 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
       uint8_t stv[PPT];
       ld_stream<uint8_t, PPT>(S.status + first, stv);
       bool idle[PPT];
-      bool any = false;
+      bool any = false, all = true;
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
         idle[k] = (first + k < n_used) && stv[k] == kIdle;
         any |= idle[k];
+        all &= idle[k];
       }
       unsigned bits = 0u;
       unsigned n_inact = 0u;
@@ -224,10 +286,14 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
         F x[NV][PPT];
         ld_stream<uint32_t, PPT>(S.pos + first, pv);
         ld_stream<uint32_t, PPT>(S.id + first, idv);
-        ld_stream<float, PPT>(S.age_h + first, ah);
+        if (n_out > 0) ld_stream<float, PPT>(S.age_h + first, ah);
         ld_stream<float, PPT>(S.age_d + first, ad);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        for (int v = 0; v < NV; ++v) {
+          // variables the update only writes are read back solely when some
+          // slot of the vector keeps its old value
+          if (((Model::read_mask >> v) & 1u) || !all) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        }
         bool st_changed = false;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
@@ -237,47 +303,45 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
             my_err |= 1u;
             continue;
           }
-          const Draws d = philox_draws(S.seed, idv[k], step, 0u);
-          if constexpr (sizeof(F) == 8)
-            ad[k] = (float)__dadd_rn((double)ad[k], dt);
-          else
-            ad[k] = __fadd_rn(ad[k], (float)dt);
+          uint32_t r[4];
+          philox_raw(seed, idv[k], step, 0u, r);
+          ad[k] = __fadd_rn(ad[k], dtf);
+          const F* rr = rates + (size_t)p0 * kMaxRates;
           F xx[NV];
 #pragma unroll
           for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
-          F ctb[NC];
-          const int r = Model::update(dtF, xx, S.C + (size_t)p0 * nsp, ctb, S.params);
+          int st;
+          if constexpr (Model::separable) {
+            F basis;
+            st = Model::update(dtF, xx, rr, basis, S.params);
+            const long long q = quantize(basis, S.q_scale[0], my_clamp, my_err);
+            atomicAdd(&sacc[p0], (unsigned long long)q);
+          } else {
+            F ctb[NC];
+            st = Model::update_general(dtF, xx, rr, ctb, S.params);
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+              const double val = __dmul_rn(S.weight, (double)ctb[j]);
+              const long long q = quantize(val, S.q_scale[j], my_clamp, my_err);
+              atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
+            }
+          }
 #pragma unroll
           for (int v = 0; v < NV; ++v) x[v][k] = xx[v];
-          if (r == kDivision) {
+          if (st == kDivision) {
             bits |= 1u << k;
             S.bpos[first + k] = p0;
             ++my_req;
           }
-#pragma unroll
-          for (int j = 0; j < NC; ++j) {
-            const double val = __dmul_rn(S.weight, (double)ctb[j]);
-            double q = rint(__dmul_rn(val, S.ctb_scale[j]));
-            if (q > (double)kQMax) {
-              q = (double)kQMax;
-              ++my_clamp;
-              my_err |= 2u;
-            } else if (q < -(double)kQMax) {
-              q = -(double)kQMax;
-              ++my_clamp;
-              my_err |= 2u;
-            }
-            atomicAdd(&sacc[p0 * NC + j], (unsigned long long)(long long)q);
-          }
           uint32_t p = p0;
           if (do_move) {
-            if (__ldg(S.pmove + p0) > (double)d.u[0]) {
-              const double u2 = (double)d.u[1];
-              const double* row = S.cdf + (size_t)p0 * K;
+            if (draw_int(r[0]) < __ldg(S.move_thr + p0)) {
+              const int x1 = (int)draw_int(r[1]);
+              const int32_t* row = S.cdf_thr + (size_t)p0 * K;
               int left = 0, right = (int)K - 1;
               while (left < right) {
                 const int mid = (left + right) >> 1;
-                if (u2 > __ldg(row + mid))
+                if (x1 > __ldg(row + mid))
                   left = mid + 1;
                 else
                   right = mid;
@@ -288,10 +352,10 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
             pv[k] = p;
           }
           if (n_out > 0) {
-            ah[k] = (float)__dadd_rn((double)ah[k], dt);
+            ah[k] = __fadd_rn(ah[k], dtf);
             for (unsigned o = 0; o < n_out; ++o) {
               if (S.outlet_idx[o] == p) {
-                if (S.outlet_flow[o] != 0.0 && (double)d.u[2] > S.outlet_thr[o]) {
+                if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
                   stv[k] = kExit;
                   ah[k] = 0.0f;
                   ++my_exit;
@@ -334,13 +398,17 @@ __global__ void __launch_bounds__(256) k_cycle(const ScenDev* __restrict__ sc, i
 
 // ---------------------------------------------------------------------------
 // k_plan: per scenario (one block of 1024 threads):
-//  1. exact contribution totals -> sources (double), accumulators cleared;
+//  1. exact accumulator totals -> sources: for a separable model
+//     src(j, s) = (w * coef_s(rates_j)) * B_j with B_j the basis total of
+//     compartment j; for a general model src(j, s) = total of w * ctb_s;
+//     accumulators cleared;
 //  2. post_cycle decisions: inactive += exits; compaction iff inactive >
 //     max(min_removal, n * ratio) (update_and_remove_inactive); room for
 //     births = capacity - live particles after compaction;
 //  3. scans of the per-tile counters (birth ranks, gap ranks ascending,
 //     source ranks from the end);
 //  4. control block advanced to the state after the step.
+template <class Model, class F>
 __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
   const ScenDev& S = sc[blockIdx.x];
   Control* ctl = S.ctl;
@@ -349,19 +417,35 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
   __shared__ unsigned long long p_n, p_req, p_rm, p_after;
   __shared__ int p_compact;
 
-  const unsigned nsp = S.n_s, nc = S.n_ctb;
+  const unsigned nsp = S.n_s;
   const unsigned n_e = S.n_c * nsp;
-  for (unsigned e = tid; e < n_e; e += blockDim.x) {
-    const unsigned j = e / nsp;
-    const unsigned sp = e - j * nsp;
-    double v = 0.0;
-    if (sp < nc) {
-      const unsigned idx = j * nc + sp;
-      v = fixed_to_double(S.acc_hi[idx], S.acc_lo[idx], S.ctb_scale_up[sp]);
-      S.acc_hi[idx] = 0;
-      S.acc_lo[idx] = 0ull;
+  const F* rates = reinterpret_cast<const F*>(S.rates);
+  if constexpr (Model::separable) {
+    for (unsigned j = tid; j < S.n_c; j += blockDim.x) {
+      const double B = fixed_to_double(S.acc_hi[j], S.acc_lo[j], S.q_scale_up[0]);
+      S.acc_hi[j] = 0;
+      S.acc_lo[j] = 0ull;
+      const F* rr = rates + (size_t)j * kMaxRates;
+      for (unsigned sp = 0; sp < nsp; ++sp) {
+        double v = 0.0;
+        if (sp < (unsigned)Model::n_ctb) v = __dmul_rn(__dmul_rn(S.weight, (double)Model::coef(rr, (int)sp)), B);
+        S.src[(size_t)j * nsp + sp] = v;
+      }
     }
-    S.src[e] = v;
+  } else {
+    const unsigned nc = Model::n_ctb;
+    for (unsigned e = tid; e < n_e; e += blockDim.x) {
+      const unsigned j = e / nsp;
+      const unsigned sp = e - j * nsp;
+      double v = 0.0;
+      if (sp < nc) {
+        const unsigned idx = j * nc + sp;
+        v = fixed_to_double(S.acc_hi[idx], S.acc_lo[idx], S.q_scale_up[sp]);
+        S.acc_hi[idx] = 0;
+        S.acc_lo[idx] = 0ull;
+      }
+      S.src[e] = v;
+    }
   }
   if (tid == 0) {
     const unsigned long long n = ctl->n_used;
@@ -451,7 +535,6 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
   }
 }
 
-// ---------------------------------------------------------------------------
 // k_divide: (a) Model::division for the requests of this step, in slot
 // order, the first `plan_births` succeeding (handle_division,
 // particles_container.hpp L561-L575: mother updated in place, child into the
@@ -618,7 +701,7 @@ __global__ void k_init(const ScenDev* __restrict__ sc, unsigned long long n, uin
     philox_raw(S.seed, (uint32_t)i, 0xFFFFFFFFu, 2u, r);
     float d[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) d[k] = (float)((r[k] >> 8) | 1u) * 0x1p-24f;
+    for (int k = 0; k < 4; ++k) d[k] = (float)draw_int(r[k]) * 0x1p-24f;
     F x[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) x[v] = (F)0;
@@ -634,24 +717,21 @@ __global__ void k_init(const ScenDev* __restrict__ sc, unsigned long long n, uin
   }
 }
 
-template <class Model, class F>
-__global__ void k_mass(const ScenDev* __restrict__ sc, unsigned long long n, double* __restrict__ mass_out) {
-  const ScenDev& S = *sc;
-  constexpr int NV = Model::n_var;
-  const F* state = reinterpret_cast<const F*>(S.state);
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    F x[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) x[v] = state[(size_t)v * S.cap + i];
-    mass_out[i] = S.status[i] == kIdle ? Model::mass(x, S.params) : 0.0;
-  }
-}
-
-__global__ void k_pmove(ScenDev* __restrict__ sc) {
+// Move thresholds of every compartment for the current dt:
+// leave iff u < p = dt*Q/V, i.e. x < ceil(2^24 p) for the integer draw x.
+__global__ void k_move_thr(ScenDev* __restrict__ sc) {
   const ScenDev& S = sc[blockIdx.y];
-  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x)
-    S.pmove[c] = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
+  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x) {
+    const double p = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
+    uint32_t t;
+    if (p >= 1.0)
+      t = (1u << 24) + 1u;
+    else if (!(p > 0.0))
+      t = 0u;
+    else
+      t = (uint32_t)ceil(__dmul_rn(p, 16777216.0));
+    S.move_thr[c] = t;
+  }
 }
 
 __global__ void k_repartition(const ScenDev* __restrict__ sc, unsigned long long* __restrict__ counts) {
@@ -684,6 +764,14 @@ void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const S
   k_cycle<Model, F, PPT><<<grid, block, smem, st>>>(sc, n, b);
 }
 template <class Model, class F>
+void launch_liquid_t(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
+  k_liquid<Model, F><<<n_scen, 1024, 0, st>>>(sc, b, do_scalar);
+}
+template <class Model, class F>
+void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc) {
+  k_plan<Model, F><<<n_scen, 1024, 0, st>>>(sc);
+}
+template <class Model, class F>
 void launch_divide_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
   k_divide<Model, F><<<grid, 256, 0, st>>>(sc, n, b);
 }
@@ -700,10 +788,6 @@ void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long 
                    uint32_t span, double* mass) {
   k_init<Model, F><<<grid, 256, 0, st>>>(sc, n, lo, span, mass);
 }
-template <class Model, class F>
-void launch_mass_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long long n, double* mass) {
-  k_mass<Model, F><<<grid, 256, 0, st>>>(sc, n, mass);
-}
 template <class Model, class F, int PPT>
 const void* cycle_fn_t() {
   return reinterpret_cast<const void*>(&k_cycle<Model, F, PPT>);
@@ -716,24 +800,26 @@ KernelSet make_set() {
   k.n_ctb = Model::n_ctb;
   k.model = Model::model_id;
   k.f64 = sizeof(F) == 8;
+  k.separable = Model::separable;
   k.cycle[0] = &launch_cycle_t<Model, F, 1>;
   k.cycle[1] = &launch_cycle_t<Model, F, 2>;
   k.cycle[2] = &launch_cycle_t<Model, F, 4>;
   k.cycle_fn[0] = cycle_fn_t<Model, F, 1>();
   k.cycle_fn[1] = cycle_fn_t<Model, F, 2>();
   k.cycle_fn[2] = cycle_fn_t<Model, F, 4>();
+  k.liquid = &launch_liquid_t<Model, F>;
+  k.plan = &launch_plan_t<Model, F>;
   k.divide = &launch_divide_t<Model, F>;
   k.compact = &launch_compact_t<Model, F>;
   k.merge = &launch_merge_t<Model, F>;
   k.init = &launch_init_t<Model, F>;
-  k.mass = &launch_mass_t<Model, F>;
   return k;
 }
 
 const KernelSet g_sets[] = {
     make_set<MonodModel<double>, double>(),    make_set<MonodModel<float>, float>(),
     make_set<OverflowModel<double>, double>(), make_set<OverflowModel<float>, float>(),
-    make_set<FixedLengthModel, float>(),
+    make_set<FixedLengthModelT<true>, float>(), make_set<FixedLengthModelT<false>, float>(),
 };
 }  // namespace
 
@@ -743,11 +829,7 @@ const KernelSet* kernel_set(int model, int f64) {
   return nullptr;
 }
 
-void launch_liquid(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
-  k_liquid<<<n_scen, 1024, 0, st>>>(sc, b, do_scalar);
-}
-void launch_plan(int n_scen, cudaStream_t st, ScenDev* sc) { k_plan<<<n_scen, 1024, 0, st>>>(sc); }
-void launch_pmove(int n_scen, cudaStream_t st, ScenDev* sc) { k_pmove<<<dim3(4, n_scen), 256, 0, st>>>(sc); }
+void launch_move_thr(int n_scen, cudaStream_t st, ScenDev* sc) { k_move_thr<<<dim3(4, n_scen), 256, 0, st>>>(sc); }
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {
   k_repartition<<<grid, 256, 0, st>>>(sc, counts);
 }

@@ -13,26 +13,28 @@ using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const Bat
 using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int);
 using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
                             double*);
-using MassLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, double*);
+
+using LiquidLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*, int);
+using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*);
 
 struct KernelSet {
   int model;
   bool f64;
+  bool separable;
   int n_var;
   int n_ctb;
+  LiquidLaunch liquid;
+  PlanLaunch plan;
   CycleLaunch cycle[3];      // particles per thread 1, 2, 4
   const void* cycle_fn[3];   // for occupancy queries / attributes
   DivideLaunch divide;
   CopyLaunch compact;
   CopyLaunch merge;
   InitLaunch init;
-  MassLaunch mass;
 };
 
 const KernelSet* kernel_set(int model, int f64);
-void launch_liquid(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar);
-void launch_plan(int n_scen, cudaStream_t st, ScenDev* sc);
-void launch_pmove(int n_scen, cudaStream_t st, ScenDev* sc);
+void launch_move_thr(int n_scen, cudaStream_t st, ScenDev* sc);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);

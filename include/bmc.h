@@ -51,6 +51,8 @@ extern "C" {
 #define BMC_MODEL_MONOD 1
 #define BMC_MODEL_OVERFLOW 2
 #define BMC_MODEL_FIXED_LENGTH 3
+/* FixedLength through the general per-particle contribution path. */
+#define BMC_MODEL_FIXED_LENGTH_GENERAL 4
 
 /* Device error word bits (copied back with the step statistics). */
 #define BMC_ERR_POSITION 1u  /* compartment index out of range */
@@ -85,7 +87,13 @@ typedef struct bmc_scenario_desc {
   uint64_t seed;                   /* Philox key */
   double dead_ratio_threshold;     /* BIOMC_MC_REMOVE_RATIO_THRESHOLD, 0.01 */
   uint64_t min_removal;            /* BIOMC_MC_MINIMUM_REMOVAL, 0 */
-  double ctb_bound[8];             /* bound on |contribution| per particle */
+  /* Bounds that fix the quanta of the exact contribution sums: for a
+   * separable model (contribution j = coef_j(C) * basis(particle)),
+   * value_bound[0] bounds |basis| (the mass for the Monod models, 1 for
+   * FixedLength); for a general model value_bound[j] bounds |contribution
+   * j| of one particle.  Values above the bound are clamped and flagged
+   * (BMC_ERR_CLAMP). */
+  double value_bound[8];
 } bmc_scenario_desc;
 
 /* A liquid feed, reference Simulation::Feed::FeedDescriptor
@@ -188,6 +196,11 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
 /* n_steps iterations on the device without host round trips (one captured
  * CUDA graph replayed).  Statistics are those of the last step. */
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats);
+
+/* Launch shape of the scenario's cycle kernel: threads per block (multiple
+ * of 32, <= 256), particles per thread (1, 2, 4), resident blocks per SM
+ * (0 = as many as fit); 0 keeps the current value. */
+int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 
 /* Enqueue n_steps iterations without waiting (bmc_synchronize waits). */
 int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps);

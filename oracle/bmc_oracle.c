@@ -135,35 +135,69 @@ double orc_fixed_to_double(__int128 t, int32_t e) {
 #undef ORC_F
 #undef ORC_SFX
 
-static int model_update(const orc_state* s, double dt, uint64_t i, const double* c, double* ctb) {
+static int is_fixed_length(const orc_state* s) {
+  return s->model == ORC_MODEL_FIXED_LENGTH || s->model == ORC_MODEL_FIXED_LENGTH_GENERAL;
+}
+
+/* Rates of compartment c into r[8] (element type of the model's float). */
+static void model_rates(const orc_state* s, const double* c, void* r) {
+  if (s->f64) {
+    double* rr = (double*)r;
+    if (s->model == ORC_MODEL_MONOD) monod_rates_f64(c, s->params, rr);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_rates_f64(c, s->params, rr);
+  } else {
+    float* rr = (float*)r;
+    if (s->model == ORC_MODEL_MONOD) monod_rates_f32(c, s->params, rr);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_rates_f32(c, s->params, rr);
+    if (is_fixed_length(s)) fixed_length_rates(c, s->params, rr);
+  }
+}
+
+/* Contribution coefficient j of a compartment (as double). */
+static double model_coef(const orc_state* s, const void* r, int j) {
+  if (s->f64) {
+    const double* rr = (const double*)r;
+    if (s->model == ORC_MODEL_MONOD) return monod_coef_f64(rr, j);
+    return overflow_coef_f64(rr, j);
+  }
+  const float* rr = (const float*)r;
+  if (s->model == ORC_MODEL_MONOD) return (double)monod_coef_f32(rr, j);
+  if (s->model == ORC_MODEL_OVERFLOW) return (double)overflow_coef_f32(rr, j);
+  return (double)fixed_length_coef(rr, j);
+}
+
+/* Per-particle update.  Separable models return their basis (as double,
+ * with *basis_is_float set when it is a float); the general FixedLength
+ * writes its contribution w-free into ctb[0]. */
+static int model_update(const orc_state* s, double dt, uint64_t i, const void* r, double* basis, double* ctb) {
   const uint64_t cap = s->phys_capacity;
   if (s->f64) {
     double* st = (double*)s->state;
     double x[8];
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    int r;
-    switch (s->model) {
-      case ORC_MODEL_MONOD: r = monod_update_f64(dt, x, c, ctb, s->params); break;
-      case ORC_MODEL_OVERFLOW: r = overflow_update_f64(dt, x, c, ctb, s->params); break;
-      default: r = ORC_IDLE; break;
-    }
+    double b = 0.0;
+    int res = ORC_IDLE;
+    if (s->model == ORC_MODEL_MONOD) res = monod_update_f64(dt, x, (const double*)r, &b, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) res = overflow_update_f64(dt, x, (const double*)r, &b, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
-    return r;
+    *basis = b;
+    return res;
   } else {
     float* st = (float*)s->state;
     float x[8];
-    float cf[8] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    int r;
-    switch (s->model) {
-      case ORC_MODEL_MONOD: r = monod_update_f32((float)dt, x, c, cf, s->params); break;
-      case ORC_MODEL_OVERFLOW: r = overflow_update_f32((float)dt, x, c, cf, s->params); break;
-      case ORC_MODEL_FIXED_LENGTH: r = fixed_length_update_f32((float)dt, x, c, cf, s->params); break;
-      default: r = ORC_IDLE; break;
-    }
+    float b = 0.0f, cf[8] = {0};
+    int res = ORC_IDLE;
+    const float* rr = (const float*)r;
+    const float dtf = (float)dt;
+    if (s->model == ORC_MODEL_MONOD) res = monod_update_f32(dtf, x, rr, &b, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) res = overflow_update_f32(dtf, x, rr, &b, s->params);
+    if (s->model == ORC_MODEL_FIXED_LENGTH) res = fixed_length_update(dtf, x, rr, &b, s->params);
+    if (s->model == ORC_MODEL_FIXED_LENGTH_GENERAL) res = fixed_length_update_general(dtf, x, rr, cf, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+    *basis = (double)b;
     for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = (double)cf[j];
-    return r;
+    return res;
   }
 }
 
@@ -176,11 +210,8 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
     double* ch = (double*)s->child_state;
     double x[8], y[8] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    switch (s->model) {
-      case ORC_MODEL_MONOD: monod_division_f64(x, y, d, s->params); break;
-      case ORC_MODEL_OVERFLOW: overflow_division_f64(x, y, d, s->params); break;
-      default: break;
-    }
+    if (s->model == ORC_MODEL_MONOD) monod_division_f64(x, y, d, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_division_f64(x, y, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) {
       st[v * cap + i] = x[v];
       ch[v * cap + child_slot] = y[v];
@@ -190,12 +221,9 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
     float* ch = (float*)s->child_state;
     float x[8], y[8] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    switch (s->model) {
-      case ORC_MODEL_MONOD: monod_division_f32(x, y, d, s->params); break;
-      case ORC_MODEL_OVERFLOW: overflow_division_f32(x, y, d, s->params); break;
-      case ORC_MODEL_FIXED_LENGTH: fixed_length_division_f32(x, y, d, s->params); break;
-      default: break;
-    }
+    if (s->model == ORC_MODEL_MONOD) monod_division_f32(x, y, d, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_division_f32(x, y, d, s->params);
+    if (is_fixed_length(s)) fixed_length_division(x, y, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) {
       st[v * cap + i] = x[v];
       ch[v * cap + child_slot] = y[v];
@@ -208,33 +236,22 @@ static void model_init(const orc_state* s, uint64_t i, const float* d) {
   if (s->f64) {
     double* st = (double*)s->state;
     double x[8] = {0};
-    switch (s->model) {
-      case ORC_MODEL_MONOD: monod_init_f64(x, d, s->params); break;
-      case ORC_MODEL_OVERFLOW: overflow_init_f64(x, d, s->params); break;
-      default: break;
-    }
+    if (s->model == ORC_MODEL_MONOD) monod_init_f64(x, d, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_init_f64(x, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
   } else {
     float* st = (float*)s->state;
     float x[8] = {0};
-    switch (s->model) {
-      case ORC_MODEL_MONOD: monod_init_f32(x, d, s->params); break;
-      case ORC_MODEL_OVERFLOW: overflow_init_f32(x, d, s->params); break;
-      case ORC_MODEL_FIXED_LENGTH: fixed_length_init_f32(x, d, s->params); break;
-      default: break;
-    }
+    if (s->model == ORC_MODEL_MONOD) monod_init_f32(x, d, s->params);
+    if (s->model == ORC_MODEL_OVERFLOW) overflow_init_f32(x, d, s->params);
+    if (is_fixed_length(s)) fixed_length_init(x, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
   }
 }
 
 static double model_mass(const orc_state* s, uint64_t i) {
-  const uint64_t cap = s->phys_capacity;
   if (s->f64) return ((const double*)s->state)[i];
-  if (s->model == ORC_MODEL_FIXED_LENGTH) {
-    float lin_density = fixed_length_lin_density();
-    return (double)(((const float*)s->state)[i] * lin_density);
-  }
-  (void)cap;
+  if (is_fixed_length(s)) return (double)(((const float*)s->state)[i] * fixed_length_lin_density());
   return (double)((const float*)s->state)[i];
 }
 
@@ -325,13 +342,19 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
   const uint64_t n = s->n_used;
   const uint32_t ns = s->n_s;
   const uint32_t nctb = s->n_ctb;
+  const uint32_t ncol = s->separable ? 1u : nctb;
   const int do_move = s->n_c > 1;
   const int do_leave = s->n_outlets > 0;
+  const size_t rsz = s->f64 ? sizeof(double) : sizeof(float);
+  /* the model's rates of every compartment, from the concentrations */
+  char* rates = (char*)malloc((size_t)s->n_c * 8 * rsz);
+  for (uint32_t c = 0; c < s->n_c; ++c) model_rates(s, s->C + (uint64_t)c * ns, rates + (size_t)c * 8 * rsz);
   double pmove_small[1];
   double* pmove = s->n_c > 1 ? (double*)malloc(sizeof(double) * s->n_c) : pmove_small;
   for (uint32_t c = 0; c < s->n_c && do_move; ++c) pmove[c] = (dt * s->out_flow[c]) / s->volume[c];
   double thr[ORC_MAX_OUTLETS];
   for (uint32_t o = 0; o < s->n_outlets; ++o) thr[o] = exp(-(dt * s->outlet_flow[o]) / s->outlet_volume[o]);
+  const float dtf = (float)dt;
 
   /* Optional emulation of the reference's Tag3D contribution loop
    * (contribution_kernel.hpp L167-L185): a team thread walks 32 consecutive
@@ -350,19 +373,19 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
     }
   }
   uint64_t moves = 0, exits = 0, reqdiv = 0;
-  const size_t src_len = (size_t)s->n_c * ns;
+  const size_t acc_len = (size_t)s->n_c * ncol;
   if (n_threads < 1) n_threads = 1;
   uint64_t clamped = 0;
 #ifdef _OPENMP
-  __int128* partial = (__int128*)calloc((size_t)n_threads * src_len, sizeof(__int128));
+  __int128* partial = (__int128*)calloc((size_t)n_threads * acc_len, sizeof(__int128));
 #pragma omp parallel num_threads(n_threads) reduction(+ : moves, exits, reqdiv, clamped)
   {
     const int tid = omp_get_thread_num();
-    __int128* acc = partial + (size_t)tid * src_len;
+    __int128* acc = partial + (size_t)tid * acc_len;
 #pragma omp for schedule(static)
     for (uint64_t i = 0; i < n; ++i) {
 #else
-  __int128* partial = (__int128*)calloc(src_len, sizeof(__int128));
+  __int128* partial = (__int128*)calloc(acc_len, sizeof(__int128));
   {
     __int128* acc = partial;
     for (uint64_t i = 0; i < n; ++i) {
@@ -370,24 +393,28 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
       if (s->status[i] != ORC_IDLE) continue;
       float d[4];
       draws_for(s, s->id[i], 0u, d);
-      if (s->f64)
-        s->age_d[i] = (float)((double)s->age_d[i] + dt);
-      else
-        s->age_d[i] = s->age_d[i] + (float)dt;
+      s->age_d[i] = s->age_d[i] + dtf;
       const uint32_t p0 = s->pos[i];
-      double ctb[8];
-      const int st = model_update(s, dt, i, s->C + (uint64_t)p0 * ns, ctb);
+      double basis = 0.0, ctb[8] = {0};
+      const int st = model_update(s, dt, i, rates + (size_t)p0 * 8 * rsz, &basis, ctb);
       if (st == ORC_DIVISION) {
         s->div_flag[i] = 1;
         s->div_pos[i] = p0;
         reqdiv++;
       }
-      if (!contrib_ok || contrib_ok[i])
-        for (uint32_t j = 0; j < nctb; ++j) {
-          int cl = 0;
-          acc[(uint64_t)p0 * ns + j] += orc_quantize(s->weight * ctb[j], s->ctb_exp[j], s->ctb_qmax, &cl);
+      if (!contrib_ok || contrib_ok[i]) {
+        int cl = 0;
+        if (s->separable) {
+          acc[p0] += orc_quantize(basis, s->q_exp[0], s->q_max, &cl);
           clamped += (uint64_t)cl;
+        } else {
+          for (uint32_t j = 0; j < nctb; ++j) {
+            cl = 0;
+            acc[(uint64_t)p0 * ncol + j] += orc_quantize(s->weight * ctb[j], s->q_exp[j], s->q_max, &cl);
+            clamped += (uint64_t)cl;
+          }
         }
+      }
       uint32_t p = p0;
       if (do_move) {
         if (pmove[p] > (double)d[0]) {
@@ -397,7 +424,7 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
         s->pos[i] = p;
       }
       if (do_leave) {
-        s->age_h[i] = (float)((double)s->age_h[i] + dt);
+        s->age_h[i] = s->age_h[i] + dtf;
         for (uint32_t o = 0; o < s->n_outlets; ++o) {
           if (s->outlet_index[o] == p) {
             if (s->outlet_flow[o] != 0.0 && (double)d[2] > thr[o]) {
@@ -414,17 +441,33 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
 #ifndef _OPENMP
   n_threads = 1;
 #endif
+  /* exact totals -> sources: separable src(c,j) = (w * coef_j(c)) * B(c) */
   for (uint32_t c = 0; c < s->n_c; ++c) {
-    for (uint32_t j = 0; j < nctb; ++j) {
-      const size_t k = (size_t)c * ns + j;
+    if (s->separable) {
       __int128 t = 0;
-      for (int th = 0; th < n_threads; ++th) t += partial[(size_t)th * src_len + k];
-      s->src[k] = orc_fixed_to_double(t, s->ctb_exp[j]);
+      for (int th = 0; th < n_threads; ++th) t += partial[(size_t)th * acc_len + c];
+      const double B = orc_fixed_to_double(t, s->q_exp[0]);
+      for (uint32_t sp = 0; sp < ns; ++sp) {
+        double v = 0.0;
+        if (sp < nctb) v = (s->weight * model_coef(s, rates + (size_t)c * 8 * rsz, (int)sp)) * B;
+        s->src[(size_t)c * ns + sp] = v;
+      }
+    } else {
+      for (uint32_t sp = 0; sp < ns; ++sp) {
+        double v = 0.0;
+        if (sp < nctb) {
+          __int128 t = 0;
+          for (int th = 0; th < n_threads; ++th) t += partial[(size_t)th * acc_len + (size_t)c * ncol + sp];
+          v = orc_fixed_to_double(t, s->q_exp[sp]);
+        }
+        s->src[(size_t)c * ns + sp] = v;
+      }
     }
   }
   s->ctb_clamped += clamped;
   free(partial);
   free(contrib_ok);
+  free(rates);
   if (pmove != pmove_small) free(pmove);
   s->moves = moves;
   s->exits = exits;

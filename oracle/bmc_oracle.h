@@ -38,7 +38,7 @@ extern "C" {
 #endif
 
 enum { ORC_IDLE = 0, ORC_DIVISION = 1, ORC_EXIT = 2, ORC_DEAD = 3 };
-enum { ORC_MODEL_MONOD = 1, ORC_MODEL_OVERFLOW = 2, ORC_MODEL_FIXED_LENGTH = 3 };
+enum { ORC_MODEL_MONOD = 1, ORC_MODEL_OVERFLOW = 2, ORC_MODEL_FIXED_LENGTH = 3, ORC_MODEL_FIXED_LENGTH_GENERAL = 4 };
 enum { ORC_DRAW_PHILOX = 0, ORC_DRAW_XORSHIFT = 1 };
 
 #define ORC_MAX_OUTLETS 8
@@ -113,11 +113,15 @@ typedef struct orc_state {
   double dead_ratio_threshold;
   uint64_t min_removal;
 
-  /* Contribution quantum: a particle's contribution v = weight * ctb[j] is
-   * rounded to the integer q = rint(v * 2^-ctb_exp[j]) with |q| <= ctb_qmax,
-   * and the sums are exact integer sums (see orc_fixed_to_double). */
-  int32_t ctb_exp[8];
-  int64_t ctb_qmax;
+  /* Exact contribution sums.  Separable models (contribution j =
+   * coef_j(C) * basis(particle)): each particle's basis is rounded to the
+   * integer q = rint(basis * 2^-q_exp[0]), |q| <= q_max, summed exactly per
+   * compartment, and src(c, j) = (weight * coef_j(c)) * total.  General
+   * models: weight * contribution j of each particle is quantised with
+   * q_exp[j] and summed exactly.  See orc_quantize / orc_fixed_to_double. */
+  int32_t separable;
+  int32_t q_exp[8];
+  int64_t q_max;
   uint64_t ctb_clamped;
 
   /* quirk emulation: 1 = reference Tag3D contribution early return */

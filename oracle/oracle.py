@@ -42,7 +42,8 @@ class OrcState(ct.Structure):
         ("feed_flow", ct.c_double * MAXO), ("feed_conc", ct.c_double * (MAXO * 8)),
         ("draw_mode", ct.c_int32), ("seed", ct.c_uint64), ("step", ct.c_uint32),
         ("dead_ratio_threshold", ct.c_double), ("min_removal", ct.c_uint64),
-        ("ctb_exp", ct.c_int32 * 8), ("ctb_qmax", ct.c_int64), ("ctb_clamped", ct.c_uint64),
+        ("separable", ct.c_int32), ("q_exp", ct.c_int32 * 8), ("q_max", ct.c_int64),
+        ("ctb_clamped", ct.c_uint64),
         ("quirk_tag3d", ct.c_int32),
         ("births", ct.c_uint64), ("exits", ct.c_uint64), ("moves", ct.c_uint64),
         ("overflow", ct.c_uint64), ("requested_divisions", ct.c_uint64),
@@ -171,7 +172,8 @@ class Oracle:
         s.step = 0
         s.dead_ratio_threshold = scen.dead_ratio_threshold
         s.min_removal = scen.min_removal
-        s.ctb_qmax = 1 << 42
+        s.q_max = 1 << 42
+        s.separable = 1 if m.separable else 0
         s.quirk_tag3d = 1 if quirk_tag3d else 0
         self.s = s
         self.weight = None
@@ -189,9 +191,9 @@ class Oracle:
     def set_weight(self, w: float):
         self.weight = w
         self.s.weight = w
-        e = self.scen.ctb_exponents(w)
+        e = self.scen.quantum_exponents(w)
         for j in range(8):
-            self.s.ctb_exp[j] = int(e[j])
+            self.s.q_exp[j] = int(e[j])
 
     # -- stepping -------------------------------------------------------------
     def step(self, n_threads: int = 1):

@@ -110,8 +110,9 @@ def test_lattice_overflow_model(oracle_mod, f64):
     assert_same_particles(g, o, "end")
 
 
-def test_fixed_length_reference_model(oracle_mod):
-    sc = scenarios.small_ring(16000, model=scenarios.fixed_length(), feeds=True)
+@pytest.mark.parametrize("general", [False, True])
+def test_fixed_length_reference_model(oracle_mod, general):
+    sc = scenarios.small_ring(16000, model=scenarios.fixed_length(general=general), feeds=True)
     g, o = make_pair(oracle_mod, sc)
     births = 0
     for k in range(60):
@@ -168,3 +169,19 @@ def test_repartition_and_force_remove(oracle_mod):
 
     oracle_mod.lib().orc_remove_inactive(ct.byref(o.s), o.s.inactive)
     assert_same_particles(g, o, "force_remove_dead")
+
+
+@pytest.mark.parametrize("shape", [(256, 1, 0), (256, 2, 0), (128, 4, 0), (256, 4, 1)])
+def test_launch_shapes_bit_identical(oracle_mod, shape):
+    """Results do not depend on the launch shape: sums are exact."""
+    sc = scenarios.workload(2, n_particles=30000, f64=True)
+    sc.net = __import__("bmc.networks", fromlist=["x"]).lattice_vortex(4, seed=9)
+    sc.c0 = sc.c0[: sc.net.n_c]
+    sc.feeds[0].outlet = sc.net.n_c - 1
+    sc.feeds[0].flow = 3e-4
+    g, o = make_pair(oracle_mod, sc)
+    g.set_shape(*shape)
+    g.run(7)
+    o.run(7, 2)
+    assert_same_particles(g, o, f"shape {shape}")
+    assert_same_liquid(g, o, f"shape {shape}")
