@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--shape", default=None,
+                    help="threads,particles_per_thread,blocks_per_sm (skips the autotuner)")
     return ap.parse_args()
 
 
@@ -226,7 +228,12 @@ def run_gpu(args):
     # launch shape chosen by the autotuner (its timed steps are warm-up steps)
     from bmc import autotune
 
-    shape, tune_ms = autotune.tune_scenario(g)
+    if args.shape:
+        shape = tuple(int(v) for v in args.shape.split(","))
+        g.set_shape(*shape)
+        tune_ms = {}
+    else:
+        shape, tune_ms = autotune.tune_scenario(g)
     # warm-up (graph capture, first touch)
     g.run(max(args.warmup, 3))
     st0 = g.stats()

@@ -1,8 +1,8 @@
 """Launch-shape autotuner for the cycle kernel.
 
-The cycle kernel has three instantiated shapes per model (1, 2 or 4
-particles per thread, each compiled for its own register budget) and a
-free choice of resident blocks per SM.  The autotuner times each candidate
+The cycle kernel has five instantiated shapes per model (256 threads with
+1, 2 or 4 particles per thread, 512 x 2 and 1024 x 1, each compiled for
+its own register budget) and a free choice of resident blocks per SM.  The autotuner times each candidate
 on the live scenario (or batch) for a few steps -- every timed step is a
 real step of the simulation, so tuning doubles as warm-up -- and keeps the
 fastest.  Results are remembered per workload key (compartment-count
@@ -14,7 +14,8 @@ from __future__ import annotations
 import math
 import time
 
-CANDIDATES = [(256, 1, 0), (256, 2, 0), (256, 4, 0), (128, 4, 0), (256, 2, 2), (256, 4, 1)]
+# (threads per block, particles per thread, resident blocks per SM; 0 = max)
+CANDIDATES = [(256, 1, 0), (256, 2, 0), (256, 4, 0), (512, 2, 0), (1024, 1, 0)]
 
 _cache: dict = {}
 

@@ -103,7 +103,7 @@ struct bmc_scenario {
   std::vector<bmc_feed> feeds;
   double dt = -1.0;
   // launch shape of the cycle kernel
-  unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
+  unsigned variant = 0, blocks_per_sm = 0;  // cycle launch variant (bmc_launch.h)
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
   unsigned graph_grid = 0;
@@ -117,7 +117,7 @@ struct bmc_batch {
   BatchCtl* d_bctl = nullptr;
   std::vector<ScenDev> table;
   unsigned total_tiles = 0;
-  unsigned threads = 256, ppt_index = 2, blocks_per_sm = 0;
+  unsigned variant = 0, blocks_per_sm = 0;  // cycle launch variant (bmc_launch.h)
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
   unsigned graph_grid = 0;
@@ -126,7 +126,12 @@ struct bmc_batch {
 
 namespace {
 
-int ppt_of(unsigned idx) { return idx == 0 ? 1 : (idx == 1 ? 2 : 4); }
+// Variant index of (threads, particles per thread); -1 if not compiled.
+int variant_of(unsigned threads, unsigned ppt) {
+  for (int v = 0; v < bmc::kCycleVariants; ++v)
+    if (bmc::kVariantThreads[v] == threads && bmc::kVariantPPT[v] == ppt) return v;
+  return -1;
+}
 
 int upload_desc(bmc_scenario* s) {
   BMC_CUDA(counted_memcpy_async(s->d_desc, &s->h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream));
@@ -166,7 +171,7 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
   int rc = upload_desc(s);
   if (rc) return rc;
   if (launch_pmove) {
-    bmc::launch_move_thr(1, s->stream, s->d_desc);
+    s->ks->move_thr(1, s->stream, s->d_desc);
     g_launches++;
     BMC_CUDA(cudaGetLastError());
   }
@@ -175,9 +180,10 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
 
 size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(unsigned long long); }
 
-int prepare_cycle(const bmc::KernelSet* ks, unsigned threads, unsigned ppt_index, unsigned bps_req,
-                  size_t smem, int sm_count, unsigned* grid_out) {
-  const void* fn = ks->cycle_fn[ppt_index];
+int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t smem, int sm_count,
+                  unsigned* grid_out) {
+  const void* fn = ks->cycle_fn[variant];
+  const unsigned threads = bmc::kVariantThreads[variant];
   if (smem > 227 * 1024)
     return fail(BMC_E_UNSUPPORTED, "n_compartments * n_contributions too large for the shared accumulator");
   BMC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -190,13 +196,10 @@ int prepare_cycle(const bmc::KernelSet* ks, unsigned threads, unsigned ppt_index
 }
 
 // Enqueue one step (liquid step optional) for a table of scenarios.
-int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, BatchCtl* d_bctl,
-                 int do_scalar, unsigned threads, unsigned ppt_index, unsigned grid, size_t smem,
-                 int sm_count) {
-  const int ppt = ppt_of(ppt_index);
-  if (kTile % (int)(threads * ppt) != 0) return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
-  ks->liquid(n_scen, st, d_table, d_bctl, do_scalar);
-  ks->cycle[ppt_index](dim3(grid), dim3(threads), smem, st, d_table, n_scen, d_bctl);
+int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned max_nc,
+                 BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count) {
+  ks->liquid(n_scen, max_nc, st, d_table, d_bctl, do_scalar);
+  ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl);
   ks->plan(n_scen, st, d_table);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen);
@@ -252,7 +255,7 @@ int set_quanta(bmc_scenario* s) {
       if (!(vmax > 0.0) || !std::isfinite(vmax)) return fail(BMC_E_INVALID, "value bounds must be > 0");
       e = ceil_log2(vmax) - 42;
     }
-    s->h.q_scale[j] = std::ldexp(1.0, -e);
+    s->h.q_exp[j] = e;
     s->h.q_scale_up[j] = std::ldexp(1.0, e);
   }
   return BMC_OK;
@@ -403,19 +406,26 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
                       const double* out_flows, const double* cdf) {
   if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
   if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
-  std::vector<uint32_t> nbr((size_t)n_c * K, 0u);
-  std::vector<int32_t> cthr((size_t)n_c * K, 1 << 24);
-  for (size_t k = 0; k < (size_t)n_c * K; ++k) {
-    if (neighbors) {
-      if (neighbors[k] >= n_c) return fail(BMC_E_INVALID, "neighbor index out of range");
-      nbr[k] = (uint32_t)neighbors[k];
-    } else {
-      nbr[k] = (uint32_t)(k / K);
-    }
-    if (cdf) {
-      // u > CDF  <=>  x > floor(2^24 CDF) for the integer draw x = u 2^24
-      const double v = std::floor(cdf[k] * 16777216.0);
-      cthr[k] = (int32_t)std::max(-1.0, std::min(16777216.0, v));
+  // rows {floor(2^24 CDF(k)), neighbour(k)}: u > CDF <=> x > floor(2^24 CDF)
+  // for the integer draw x = u 2^24; rows must be non-decreasing
+  std::vector<int2> mrow((size_t)n_c * K);
+  for (uint32_t i = 0; i < n_c; ++i) {
+    int32_t prev = -2;
+    for (uint32_t k = 0; k < K; ++k) {
+      const size_t q = (size_t)i * K + k;
+      uint32_t nb = i;
+      if (neighbors) {
+        if (neighbors[q] >= n_c) return fail(BMC_E_INVALID, "neighbor index out of range");
+        nb = (uint32_t)neighbors[q];
+      }
+      int32_t th = 1 << 24;
+      if (cdf) {
+        if (!(cdf[q] == cdf[q])) return fail(BMC_E_INVALID, "cumulative probability is NaN");
+        th = (int32_t)std::max(-1.0, std::min(16777216.0, std::floor(cdf[q] * 16777216.0)));
+      }
+      if (th < prev) return fail(BMC_E_INVALID, "cumulative probability rows must be non-decreasing");
+      prev = th;
+      mrow[q] = make_int2(th, (int)nb);
     }
   }
   std::vector<double> vol(volume, volume + n_c), outf(out_flows, out_flows + n_c), vinv(n_c), diag(n_c);
@@ -433,35 +443,31 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     s->darena = nullptr;
     const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_acc;
     Carver cv;
-    cv.add(&h.move_thr, n_c);
-    int32_t* p_cthr = nullptr;
-    cv.add(&p_cthr, (size_t)n_c * K);
+    int2* p_mrow = nullptr;
+    cv.add(&p_mrow, (size_t)n_c * K);
     double* p_vol = nullptr;
     cv.add(&p_vol, n_c);
     double* p_out = nullptr;
     cv.add(&p_out, n_c);
-    uint32_t* p_nbr = nullptr;
-    cv.add(&p_nbr, (size_t)n_c * K);
     double* p_diag = nullptr;
     cv.add(&p_diag, n_c);
     double* p_vinv = nullptr;
     cv.add(&p_vinv, n_c);
-    double* p_rates = nullptr;
-    cv.add(&p_rates, (size_t)n_c * bmc::kMaxRates);
-    cv.add(&h.C, ne);
+    double* p_rec = nullptr;
+    cv.add(&p_rec, (size_t)n_c * 8);
+    cv.add(&h.C, 2 * ne);
     cv.add(&h.M, ne);
     cv.add(&h.src, ne);
     cv.add(&h.acc_hi, na);
     cv.add(&h.acc_lo, na);
     BMC_CUDA(cudaMalloc(&s->darena, cv.off));
     cv.bind(s->darena);
-    h.cdf_thr = p_cthr;
+    h.mrow = p_mrow;
     h.volume = p_vol;
     h.out_flow = p_out;
-    h.nbr = p_nbr;
     h.diag = p_diag;
     h.vinv = p_vinv;
-    h.rates = p_rates;
+    h.crec = p_rec;
     BMC_CUDA(cudaMemsetAsync(s->darena, 0, cv.off, s->stream));
     s->has_conc = false;
     s->has_transition = false;
@@ -470,8 +476,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   h.K = K;
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.volume), vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
-  BMC_CUDA(counted_memcpy_async(const_cast<int32_t*>(h.cdf_thr), cthr.data(), cthr.size() * 4, cudaMemcpyHostToDevice, s->stream));
-  BMC_CUDA(counted_memcpy_async(const_cast<uint32_t*>(h.nbr), nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(const_cast<int2*>(h.mrow), mrow.data(), mrow.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.vinv), vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   if (!s->has_transition)
     BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.diag), diag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
@@ -560,6 +565,7 @@ int bmc_set_concentrations(bmc_scenario* s, const double* conc) {
     }
   }
   BMC_CUDA(counted_memcpy_async(s->h.C, C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.C + C.size(), C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(s->h.M, M.data(), M.size() * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(cudaMemsetAsync(s->h.src, 0, C.size() * 8, s->stream));
   BMC_CUDA(cudaMemsetAsync(s->h.acc_hi, 0, n_c * s->h.n_acc * 8, s->stream));
@@ -667,7 +673,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   cudaGraph_t g = nullptr;
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
-  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->d_bctl, 1, s->threads, s->ppt_index, grid, smem,
+  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->h.n_c, s->d_bctl, 1, s->variant, grid, smem,
                         s->sm_count);
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
@@ -691,7 +697,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   if (rc) return rc;
   const size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
+  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, &grid);
   if (rc) return rc;
   if (use_graph && do_scalar) {
     rc = ensure_graph(s, grid, smem);
@@ -703,7 +709,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
     return BMC_OK;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
-    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->d_bctl, do_scalar, s->threads, s->ppt_index, grid, smem,
+    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->h.n_c, s->d_bctl, do_scalar, s->variant, grid, smem,
                       s->sm_count);
     if (rc) return rc;
   }
@@ -788,7 +794,10 @@ int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
-  if (conc) BMC_CUDA(counted_memcpy_async(conc, s->h.C, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  const double* cur = s->h.C + (s->h_ctl->step & 1u) * ne;
+  if (conc) BMC_CUDA(counted_memcpy_async(conc, cur, ne * 8, cudaMemcpyDeviceToHost, s->stream));
   if (mass) BMC_CUDA(counted_memcpy_async(mass, s->h.M, ne * 8, cudaMemcpyDeviceToHost, s->stream));
   if (sources) BMC_CUDA(counted_memcpy_async(sources, s->h.src, ne * 8, cudaMemcpyDeviceToHost, s->stream));
   BMC_CUDA(cudaStreamSynchronize(s->stream));
@@ -912,7 +921,6 @@ int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out
     }
     cudaStreamSynchronize(scenarios[i]->stream);
   }
-  b->ppt_index = b->ks->f64 ? 1 : 2;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(ScenDev) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bctl, sizeof(BatchCtl));
@@ -939,16 +947,11 @@ int bmc_batch_destroy(bmc_batch* b) {
 
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!s) return fail(BMC_E_INVALID, "null scenario");
-  unsigned th = threads ? threads : s->threads;
-  unsigned pi = s->ppt_index;
-  if (threads && (threads % 32 || threads > 256)) return fail(BMC_E_INVALID, "threads must be a multiple of 32, <= 256");
-  if (ppt) {
-    if (ppt != 1 && ppt != 2 && ppt != 4) return fail(BMC_E_INVALID, "ppt must be 1, 2 or 4");
-    pi = ppt == 1 ? 0 : (ppt == 2 ? 1 : 2);
-  }
-  if (kTile % (int)(th * ppt_of(pi)) != 0) return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
-  s->threads = th;
-  s->ppt_index = pi;
+  const unsigned th = threads ? threads : bmc::kVariantThreads[s->variant];
+  const unsigned pp = ppt ? ppt : bmc::kVariantPPT[s->variant];
+  const int v = variant_of(th, pp);
+  if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
+  s->variant = (unsigned)v;
   s->blocks_per_sm = blocks_per_sm;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
@@ -957,17 +960,12 @@ int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t bloc
 
 int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!b) return fail(BMC_E_INVALID, "null batch");
-  if (threads) {
-    if (threads % 32 || threads > 256) return fail(BMC_E_INVALID, "threads must be a multiple of 32, <= 256");
-    b->threads = threads;
-  }
-  if (ppt) {
-    if (ppt != 1 && ppt != 2 && ppt != 4) return fail(BMC_E_INVALID, "ppt must be 1, 2 or 4");
-    b->ppt_index = ppt == 1 ? 0 : (ppt == 2 ? 1 : 2);
-  }
+  const unsigned th = threads ? threads : bmc::kVariantThreads[b->variant];
+  const unsigned pp = ppt ? ppt : bmc::kVariantPPT[b->variant];
+  const int v = variant_of(th, pp);
+  if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
+  b->variant = (unsigned)v;
   b->blocks_per_sm = blocks_per_sm;
-  if (kTile % (int)(b->threads * ppt_of(b->ppt_index)) != 0)
-    return fail(BMC_E_INVALID, "threads * ppt must divide 1024");
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
   return BMC_OK;
@@ -978,7 +976,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   const int n = (int)b->scen.size();
   bool table_changed = b->table.size() != (size_t)n;
   b->table.resize(n);
-  unsigned tiles = 0;
+  unsigned tiles = 0, max_nc = 0;
   size_t smem = 0;
   for (int i = 0; i < n; ++i) {
     bmc_scenario* s = b->scen[i];
@@ -987,6 +985,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     ScenDev d = s->h;
     d.tile_base = tiles;
     tiles += d.n_tiles;
+    max_nc = std::max(max_nc, d.n_c);
     smem = std::max(smem, cycle_smem(d));
     if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
     b->table[i] = d;
@@ -996,14 +995,14 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
     BatchCtl bc{0u, tiles};
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
-    bmc::launch_move_thr(n, b->stream, b->d_table);
+    b->ks->move_thr(n, b->stream, b->d_table);
     g_launches++;
     BMC_CUDA(cudaGetLastError());
     b->dt = dt;
     b->total_tiles = tiles;
   }
   unsigned grid = 0;
-  int rc = prepare_cycle(b->ks, b->threads, b->ppt_index, b->blocks_per_sm, smem, b->scen[0]->sm_count, &grid);
+  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, smem, b->scen[0]->sm_count, &grid);
   if (rc) return rc;
   if (!b->graph || b->graph_smem != smem || b->graph_grid != grid) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -1011,7 +1010,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     cudaGraph_t g = nullptr;
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
-    rc = enqueue_step(b->ks, b->stream, b->d_table, n, b->d_bctl, 1, b->threads, b->ppt_index, grid, smem,
+    rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->variant, grid, smem,
                       b->scen[0]->sm_count);
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -1048,16 +1047,16 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   if (rc) return rc;
   const size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->threads, s->ppt_index, s->blocks_per_sm, smem, s->sm_count, &grid);
+  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, &grid);
   if (rc) return rc;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = s->stream;
-  const int ppt_index = (int)s->ppt_index;
+  const unsigned variant = s->variant;
   BMC_CUDA(cudaEventRecord(ev[0], st));
-  s->ks->liquid(1, st, s->d_desc, s->d_bctl, 1);
+  s->ks->liquid(1, s->h.n_c, st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
-  s->ks->cycle[ppt_index](dim3(grid), dim3(s->threads), smem, st, s->d_desc, 1, s->d_bctl);
+  s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[2], st));
   s->ks->plan(1, st, s->d_desc);
   BMC_CUDA(cudaEventRecord(ev[3], st));

@@ -13,11 +13,13 @@
 //   bpos     u32[cap]         compartment of a mother when it asked to divide
 //   gap/src  u32[cap]         compaction lists
 // Domain and liquid state, per compartment:
-//   move_thr u32[n_c]         leave iff draw < move_thr (= ceil(2^24 dt Q/V))
-//   cdf_thr  i32[n_c][K]      next = first k with draw <= cdf_thr[k]
-//   nbr      u32[n_c][K]      neighbours
-//   rates    F[n_c][8]        model rates of the compartment (from C)
-//   C, M, src f64[n_c][n_s];  acc_hi/acc_lo i64/u64[n_c][n_acc] fixed point
+//   crec     F[n_c][8]        compartment record: model rates (slots 0..6,
+//                             from C) and the move threshold (slot 7 bits):
+//                             leave iff draw < ceil(2^24 dt Q/V)
+//   mrow     i32x2[n_c][K]    {floor(2^24 CDF(k)), neighbour(k)}: next =
+//                             neighbour of the first k with draw <= thr
+//   C        f64[2][n_c][n_s] double-buffered concentrations (step parity)
+//   M, src   f64[n_c][n_s];   acc_hi/acc_lo i64/u64[n_c][n_acc] fixed point
 #pragma once
 #include <cstdint>
 
@@ -65,6 +67,9 @@ struct Control {
   unsigned int last_compacted;
   unsigned int pad;
   double mass_balance[kMaxSpecies];
+  // per-species sums of the liquid step (new mass, expected mass)
+  double mb_new[kMaxSpecies];
+  double mb_exp[kMaxSpecies];
 };
 
 // Scenario descriptor as the kernels see it (one per scenario, device memory).
@@ -91,9 +96,7 @@ struct ScenDev {
   uint32_t n_tiles;
   uint32_t tile_base;  // first global tile of this scenario in its batch
   // domain
-  uint32_t* move_thr;
-  const int32_t* cdf_thr;
-  const uint32_t* nbr;
+  const int2* mrow;
   const double* volume;
   const double* out_flow;
   const uint32_t* in_ptr;
@@ -101,7 +104,7 @@ struct ScenDev {
   const double* in_flow;
   const double* diag;
   const double* vinv;
-  void* rates;
+  void* crec;
   uint32_t n_c;
   uint32_t K;
   uint32_t n_s;
@@ -119,12 +122,12 @@ struct ScenDev {
   double feed_flow[kMaxOutlets];
   double feed_conc[kMaxOutlets * kMaxSpecies];
   // liquid
-  double* C;
+  double* C;  // two buffers of n_c * n_s; the current one is C + (step & 1) * n_c * n_s
   double* M;
   double* src;
   long long* acc_hi;
   unsigned long long* acc_lo;
-  double q_scale[kMaxSpecies];     // 2^-e per accumulator column: value -> quanta
+  int32_t q_exp[kMaxSpecies];      // e per accumulator column: quantum 2^e
   double q_scale_up[kMaxSpecies];  // 2^e: quanta -> value
   // model
   double params[16];
@@ -205,12 +208,14 @@ __device__ __forceinline__ uint32_t draw_int(uint32_t r) { return (r >> 8) | 1u;
 // Model plugins.  The ModelType concept of the reference
 // (apps/libs/mc/public/mc/traits.hpp L67-L133) split for a GPU:
 //   n_var, n_ctb, n_rates                   sizes
+//   n_upd                                   leading rates update() reads
 //   read_mask                               state variables update() reads
 //   separable                               contributions are coef(c)*basis(x)
 //   rates(c, p, r)                          per compartment, from C(:, j):
 //                                           every factor of Model::update that
 //                                           depends on the concentrations only
-//   update(dt, x, r, basis|ctb, p) -> st    Model::update of one particle
+//   update(dt, x, r, basis|ctb, pf) -> st   Model::update of one particle
+//                                           (pf: the parameters converted to F)
 //   coef(r, j)                              contribution j per unit basis
 //   division(x, child, d, p)                Model::division
 //   init(x, d, p)                           Model::init
@@ -226,6 +231,7 @@ struct MonodModel {
   static constexpr int n_var = 2;
   static constexpr int n_ctb = 1;
   static constexpr int n_rates = 2;
+  static constexpr int n_upd = 1;  // leading rates update() reads
   static constexpr int model_id = 1;
   static constexpr bool separable = true;
   static constexpr unsigned read_mask = 0x3u;
@@ -239,8 +245,8 @@ struct MonodModel {
     r[0] = mu;
     r[1] = -(mu / y);
   }
-  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const double* p) {
-    const F mdiv = (F)p[3];
+  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const F* pf) {
+    const F mdiv = pf[3];
     const F m = x[0];
     basis = m;
     const F growth = r[0] * m;
@@ -276,6 +282,7 @@ struct OverflowModel {
   static constexpr int n_var = 6;
   static constexpr int n_ctb = 4;
   static constexpr int n_rates = 5;
+  static constexpr int n_upd = 4;
   static constexpr int model_id = 2;
   static constexpr bool separable = true;
   static constexpr unsigned read_mask = 0x3u;  // mass and age; the rest is output
@@ -298,8 +305,8 @@ struct OverflowModel {
     r[3] = y_ac * q_of;
     r[4] = y_c * q_ox + y_cof * q_of;
   }
-  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const double* p) {
-    const F mdiv = (F)p[9];
+  __device__ __forceinline__ static int update(F dt, F* x, const F* r, F& basis, const F* pf) {
+    const F mdiv = pf[9];
     const F m = x[0];
     basis = m;
     x[0] = m + dt * (r[0] * m);
@@ -345,6 +352,7 @@ struct FixedLengthModelT {
   static constexpr int n_var = 2;
   static constexpr int n_ctb = 1;
   static constexpr int n_rates = 2;
+  static constexpr int n_upd = 2;
   static constexpr int model_id = Separable ? 3 : 4;
   static constexpr bool separable = Separable;
   static constexpr unsigned read_mask = 0x3u;
@@ -365,15 +373,15 @@ struct FixedLengthModelT {
     r[1] = -phi_s;
   }
   __device__ __forceinline__ static int update(float dt, float* x, const float* r, float& basis,
-                                               const double* p) {
-    (void)p;
+                                               const float* pf) {
+    (void)pf;
     basis = 1.0f;
     x[0] += dt * r[0];
     return x[0] >= x[1] ? kDivision : kIdle;
   }
   __device__ __forceinline__ static int update_general(float dt, float* x, const float* r, float* ctb,
-                                                       const double* p) {
-    (void)p;
+                                                       const float* pf) {
+    (void)pf;
     x[0] += dt * r[0];
     ctb[0] = r[1];
     return x[0] >= x[1] ? kDivision : kIdle;

@@ -20,133 +20,192 @@
 namespace bmc {
 
 // ---------------------------------------------------------------------------
-// Rates of every compartment (Model::rates) from C, by the calling block.
+// k_liquid: one thread per compartment j (grid x over compartments, grid y
+// over scenarios).  Feeds into sources and sink, explicit Euler step of the
+// liquid scalars of j
+//   M(j,:) += dt (sum_i C(i,:) T(i,j) - C(j,:) sink(j) + src(j,:)),
+//   C'(j,:) = M(j,:) / V(j),
+// then Model::rates of j from C'(j,:) into the compartment record.  C is
+// double-buffered by step parity (C' goes to the other buffer), so no block
+// waits for another.  With do_scalar == 0 only the rates (and C carried to
+// the next buffer).  Block (0, s) resets the step counters of scenario s;
+// block (0, 0) resets the tile scheduler.
 template <class Model, class F>
-__device__ __forceinline__ void model_rates(const ScenDev& S) {
-  __syncthreads();
-  F* rates = reinterpret_cast<F*>(S.rates);
-  for (unsigned j = threadIdx.x; j < S.n_c; j += blockDim.x) {
-    F r[kMaxRates];
-    Model::rates(S.C + (size_t)j * S.n_s, S.params, r);
-#pragma unroll
-    for (int k = 0; k < Model::n_rates; ++k) rates[(size_t)j * kMaxRates + k] = r[k];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// k_liquid: feeds into sources/sink, explicit Euler step of the liquid
-// scalars (M += dt (C T - C sink + src); C = M / V), mass-balance residual,
-// then the model's rates of every compartment from the new C.  One block per
-// scenario.  Also resets the step counters and the tile scheduler for the
-// cycle that follows.  With do_scalar == 0 only the resets and the rates.
-template <class Model, class F>
-__global__ void __launch_bounds__(1024) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
-  const ScenDev& S = sc[blockIdx.x];
+__global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
+  const ScenDev& S = sc[blockIdx.y];
   Control* ctl = S.ctl;
-  if (blockIdx.x == 0 && threadIdx.x == 0) bctl->ticket = 0u;
-  if (threadIdx.x == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (blockIdx.y == 0) bctl->ticket = 0u;
     ctl->req_div = 0ull;
     ctl->exits = 0ull;
     ctl->moves = 0ull;
   }
-  if (!do_scalar) {
-    model_rates<Model, F>(S);
-    return;
-  }
+  const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned nsp = S.n_s;
-  const unsigned n_e = S.n_c * nsp;
-  const double dt = S.dt;
-  double m_new[kMaxSpecies], m_exp[kMaxSpecies];
+  const size_t ne = (size_t)S.n_c * nsp;
+  const unsigned parity = ctl->step & 1u;
+  const double* __restrict__ Cold = S.C + parity * ne;
+  double* __restrict__ Cnew = S.C + (parity ^ 1u) * ne;
+  double cn[kMaxSpecies];
+  double mn[kMaxSpecies], mx[kMaxSpecies];
 #pragma unroll
-  for (int k = 0; k < kMaxSpecies; ++k) m_new[k] = m_exp[k] = 0.0;
-  for (unsigned e = threadIdx.x; e < n_e; e += blockDim.x) {
-    const unsigned j = e / nsp;
-    const unsigned sp = e - j * nsp;
-    double srcv = S.src[e];
-    double sinkj = 0.0;
-    for (unsigned f = 0; f < S.n_feeds; ++f) {
-      if (S.feed_in[f] == j) {
-        const double cf = S.feed_conc[f * kMaxSpecies + sp];
-        if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
+  for (int k = 0; k < kMaxSpecies; ++k) mn[k] = mx[k] = 0.0;
+  if (j < S.n_c) {
+    if (!do_scalar) {
+      for (unsigned sp = 0; sp < nsp; ++sp) {
+        cn[sp] = Cold[(size_t)j * nsp + sp];
+        Cnew[(size_t)j * nsp + sp] = cn[sp];
       }
-      if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
+    } else {
+      const double dt = S.dt;
+      double sinkj = 0.0;
+      for (unsigned f = 0; f < S.n_feeds; ++f)
+        if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
+      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
+      const double vinv = S.vinv[j], dg = S.diag[j];
+      for (unsigned sp = 0; sp < nsp; ++sp) {
+        const size_t e = (size_t)j * nsp + sp;
+        double srcv = S.src[e];
+        for (unsigned f = 0; f < S.n_feeds; ++f) {
+          if (S.feed_in[f] == j) {
+            const double cf = S.feed_conc[f * kMaxSpecies + sp];
+            if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
+          }
+        }
+        S.src[e] = srcv;
+        double acc = 0.0;
+        for (unsigned q = e0; q < e1; ++q)
+          acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
+        const double cj = Cold[e];
+        acc = __dadd_rn(acc, __dmul_rn(cj, dg));
+        const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
+        const double mold = S.M[e];
+        const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
+        S.M[e] = mnew;
+        cn[sp] = __dmul_rn(mnew, vinv);
+        Cnew[e] = cn[sp];
+#pragma unroll
+        for (int k = 0; k < kMaxSpecies; ++k) {
+          if ((unsigned)k == sp) {
+            mn[k] = mnew;
+            mx[k] = mold + dt * (srcv - cj * sinkj);
+          }
+        }
+      }
     }
-    S.src[e] = srcv;
-    double acc = 0.0;
-    const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
-    for (unsigned q = e0; q < e1; ++q)
-      acc = __dadd_rn(acc, __dmul_rn(S.C[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
-    const double cj = S.C[e];
-    acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
-    const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
-    const double mold = S.M[e];
-    const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
-    S.M[e] = mnew;
+    F r[kMaxRates];
+    Model::rates(cn, S.params, r);
+    F* rec = reinterpret_cast<F*>(S.crec) + (size_t)j * 8;
+#pragma unroll
+    for (int k = 0; k < Model::n_rates; ++k) rec[k] = r[k];
+  }
+  if (do_scalar) {
+    // mass-balance sums (diagnostic): block reduction, one atomic per species
+    __shared__ double red[2][8];
 #pragma unroll
     for (int k = 0; k < kMaxSpecies; ++k) {
-      if ((unsigned)k == sp) {
-        m_new[k] += mnew;
-        m_exp[k] += mold + dt * (srcv - cj * sinkj);
-      }
-    }
-  }
-  __syncthreads();
-  for (unsigned e = threadIdx.x; e < n_e; e += blockDim.x) {
-    const unsigned j = e / nsp;
-    S.C[e] = __dmul_rn(S.M[e], S.vinv[j]);
-  }
-  // mass-balance residual per species (diagnostic, block tree reduction)
-  __shared__ double red[2][32];
+      if ((unsigned)k >= nsp) break;
+      double a = mn[k], b = mx[k];
 #pragma unroll
-  for (int k = 0; k < kMaxSpecies; ++k) {
-    if ((unsigned)k >= nsp) break;
-    double a = m_new[k], b = m_exp[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) {
-      red[0][threadIdx.x >> 5] = a;
-      red[1][threadIdx.x >> 5] = b;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double ta = 0.0, tb = 0.0;
-      for (unsigned w = 0; w < (blockDim.x + 31) / 32; ++w) {
-        ta += red[0][w];
-        tb += red[1][w];
+      for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
       }
-      const double den = fabs(ta) > 1e-300 ? fabs(ta) : 1e-300;
-      ctl->mass_balance[k] = fabs(ta - tb) / den;
+      if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = a;
+        red[1][threadIdx.x >> 5] = b;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double ta = 0.0, tb = 0.0;
+        for (unsigned w = 0; w < blockDim.x / 32; ++w) {
+          ta += red[0][w];
+          tb += red[1][w];
+        }
+        atomicAdd(&ctl->mb_new[k], ta);
+        atomicAdd(&ctl->mb_exp[k], tb);
+      }
+      __syncthreads();
     }
-    __syncthreads();
   }
-  model_rates<Model, F>(S);
 }
 
 // ---------------------------------------------------------------------------
 // Quantisation of a value to the accumulator's fixed point: the nearest
-// integer multiple of 2^e (ties to even), |q| <= 2^42.  For a float value
-// the scaling by a power of two and the rounding are exact in float, which
-// gives the same integer as the double computation.
-__device__ __forceinline__ long long quantize(double v, double scale, unsigned long long& clamped, unsigned& err) {
-  double q = rint(__dmul_rn(v, scale));
-  if (fabs(q) > (double)kQMax) {
-    q = q > 0 ? (double)kQMax : -(double)kQMax;
+// integer multiple of 2^e (ties to even), clamped to |q| <= 2^42.  Done on
+// the integer pipe from the IEEE fields of v, so no FP64 instruction is
+// spent per particle; the result equals rint(v * 2^-e) evaluated in double.
+template <int MBITS, int EBITS, int BIAS, class U>
+__device__ __forceinline__ long long quantize_bits(U bits, int e, unsigned long long& clamped, unsigned& err) {
+  const bool neg = (bits >> (MBITS + EBITS)) & 1u;
+  const int ex = (int)((bits >> MBITS) & (((U)1 << EBITS) - 1));
+  const unsigned long long mant = (unsigned long long)(bits & (((U)1 << MBITS) - 1));
+  long long q;
+  if (ex == 0) {
+    q = 0;  // zero or subnormal: far below any quantum in use
+  } else if (ex == (1 << EBITS) - 1) {
+    q = kQMax;  // inf / nan
     ++clamped;
     err |= 2u;
+  } else {
+    const unsigned long long m = mant | (1ull << MBITS);  // value = m * 2^(ex - BIAS - MBITS)
+    const int sh = ex - BIAS - MBITS - e;                  // value / 2^e = m * 2^sh
+    if (sh >= 0) {
+      q = sh > 62 - MBITS ? kQMax + 1 : (long long)(m << sh);
+    } else {
+      const int r = -sh;
+      if (r > MBITS + 1) {
+        q = 0;  // below half a quantum
+      } else {
+        const unsigned long long t = m >> r;
+        const unsigned long long rem = m & ((1ull << r) - 1ull);
+        const unsigned long long half = 1ull << (r - 1);
+        q = (long long)(t + ((rem > half || (rem == half && (t & 1ull))) ? 1ull : 0ull));
+      }
+    }
+    if (q > kQMax) {
+      q = kQMax;
+      ++clamped;
+      err |= 2u;
+    }
   }
-  return (long long)q;
+  return neg ? -q : q;
 }
-__device__ __forceinline__ long long quantize(float v, double scale, unsigned long long& clamped, unsigned& err) {
-  float q = rintf(__fmul_rn(v, (float)scale));
-  if (fabsf(q) > (float)kQMax) {
-    q = q > 0 ? (float)kQMax : -(float)kQMax;
-    ++clamped;
-    err |= 2u;
+
+__device__ __forceinline__ long long quantize(double v, int e, unsigned long long& clamped, unsigned& err) {
+  return quantize_bits<52, 11, 1023>((unsigned long long)__double_as_longlong(v), e, clamped, err);
+}
+__device__ __forceinline__ long long quantize(float v, int e, unsigned long long& clamped, unsigned& err) {
+  return quantize_bits<23, 8, 127>((unsigned)__float_as_uint(v), e, clamped, err);
+}
+
+// Move threshold stored in slot 7 of a compartment record.
+__device__ __forceinline__ uint32_t rec_move_thr(float v) { return __float_as_uint(v); }
+__device__ __forceinline__ uint32_t rec_move_thr(double v) { return (uint32_t)__double_as_longlong(v); }
+
+// Loads the first NU slots of a compartment record (vector loads through
+// the read-only path) and its move threshold (slot 7, same 32-byte sector
+// for float records).
+template <int NU, class F>
+__device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
+  if constexpr (sizeof(F) == 4) {
+    if constexpr (NU > 2) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(p));
+      out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    } else {
+      const float2 a = __ldg(reinterpret_cast<const float2*>(p));
+      out[0] = a.x; out[1] = a.y;
+    }
+    static_assert(NU <= 4, "float records: update may read at most 4 rates");
+  } else {
+#pragma unroll
+    for (int k = 0; k < (NU + 1) / 2; ++k) {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(p) + k);
+      out[2 * k] = a.x;
+      out[2 * k + 1] = a.y;
+    }
   }
-  return (long long)q;
+  return rec_move_thr(__ldg(p + 7));
 }
 
 // ---------------------------------------------------------------------------
@@ -164,26 +223,24 @@ __device__ __forceinline__ long long quantize(float v, double scale, unsigned lo
 //                                                  (<=> dt F > -ln(u_2) V)
 // A division request sets a bit of the tile's birth mask; the division
 // itself runs in k_divide once the slot-order ranks are known.
-// Resident blocks of 256 threads per SM the register budget is cut for.
-template <int PPT>
-struct CycleOccupancy {
-  static constexpr int value = PPT == 1 ? 4 : (PPT == 2 ? 3 : 2);
-};
-
-template <class Model, class F, int PPT>
-__global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
+// Launch variants: THREADS per block, PPT consecutive particles per thread
+// (THREADS * PPT divides the 1024-slot tile) and MINB resident blocks per SM
+// the register budget is cut for.
+template <class Model, class F, int PPT, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
     k_cycle(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   extern __shared__ unsigned long long sacc[];
   __shared__ unsigned s_tile;
   __shared__ unsigned s_tile_births, s_tile_inactive;
   __shared__ unsigned long long s_cnt[5];
+  __shared__ F s_pf[16];  // parameters of the current scenario, as F
   constexpr int NV = Model::n_var;
   constexpr int NC = Model::n_ctb;
   constexpr int NA = Model::separable ? 1 : NC;  // accumulator columns
   const int tid = threadIdx.x;
   const int lane = tid & 31;
   const unsigned total_tiles = bctl->total_tiles;
-  const int passes = kTile / (blockDim.x * PPT);
+  constexpr int passes = kTile / (THREADS * PPT);
   int cur = -1;
   unsigned since_flush = 0;
   unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
@@ -242,6 +299,7 @@ __global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
       if (done) break;
       const unsigned n_ent = sc[s].n_c * NA;
       for (unsigned e = tid; e < n_ent; e += blockDim.x) sacc[e] = 0ull;
+      if (tid < 16) s_pf[tid] = (F)sc[s].params[tid];
       cur = s;
       since_flush = 0;
       __syncthreads();
@@ -263,11 +321,13 @@ __global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
     const float dtf = (float)dt;
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
-    const F* __restrict__ rates = reinterpret_cast<const F*>(S.rates);
+    const F* __restrict__ crec = reinterpret_cast<const F*>(S.crec);
+    const int2* __restrict__ mrow = S.mrow;
     F* __restrict__ state = reinterpret_cast<F*>(S.state);
 
+#pragma unroll 1
     for (int pass = 0; pass < passes; ++pass) {
-      const unsigned long long first = base + ((unsigned long long)pass * blockDim.x + tid) * PPT;
+      const unsigned long long first = base + ((unsigned long long)pass * THREADS + tid) * PPT;
       uint8_t stv[PPT];
       ld_stream<uint8_t, PPT>(S.status + first, stv);
       bool idle[PPT];
@@ -306,23 +366,24 @@ __global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
           uint32_t r[4];
           philox_raw(seed, idv[k], step, 0u, r);
           ad[k] = __fadd_rn(ad[k], dtf);
-          const F* rr = rates + (size_t)p0 * kMaxRates;
+          F rr[(Model::n_upd + 1) & ~1];
+          const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
           F xx[NV];
 #pragma unroll
           for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
           int st;
           if constexpr (Model::separable) {
             F basis;
-            st = Model::update(dtF, xx, rr, basis, S.params);
-            const long long q = quantize(basis, S.q_scale[0], my_clamp, my_err);
+            st = Model::update(dtF, xx, rr, basis, s_pf);
+            const long long q = quantize(basis, S.q_exp[0], my_clamp, my_err);
             atomicAdd(&sacc[p0], (unsigned long long)q);
           } else {
             F ctb[NC];
-            st = Model::update_general(dtF, xx, rr, ctb, S.params);
+            st = Model::update_general(dtF, xx, rr, ctb, s_pf);
 #pragma unroll
             for (int j = 0; j < NC; ++j) {
               const double val = __dmul_rn(S.weight, (double)ctb[j]);
-              const long long q = quantize(val, S.q_scale[j], my_clamp, my_err);
+              const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
               atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
             }
           }
@@ -335,18 +396,26 @@ __global__ void __launch_bounds__(256, CycleOccupancy<PPT>::value)
           }
           uint32_t p = p0;
           if (do_move) {
-            if (draw_int(r[0]) < __ldg(S.move_thr + p0)) {
+            if (draw_int(r[0]) < mthr) {
+              // the reference's bisection (move_kernel.hpp L89-L101) over the
+              // {threshold, neighbour} pairs of the row; the neighbour of the
+              // answer comes with the probe that set `right`, or with the
+              // last pair, loaded ahead
               const int x1 = (int)draw_int(r[1]);
-              const int32_t* row = S.cdf_thr + (size_t)p0 * K;
+              const int2* row = mrow + (size_t)p0 * K;
+              int nb = __ldg(row + (K - 1)).y;
               int left = 0, right = (int)K - 1;
               while (left < right) {
                 const int mid = (left + right) >> 1;
-                if (x1 > __ldg(row + mid))
+                const int2 pm = __ldg(row + mid);
+                if (x1 > pm.x) {
                   left = mid + 1;
-                else
+                } else {
                   right = mid;
+                  nb = pm.y;
+                }
               }
-              p = __ldg(S.nbr + (size_t)p0 * K + left);
+              p = (uint32_t)nb;
               ++my_move;
             }
             pv[k] = p;
@@ -419,13 +488,20 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
 
   const unsigned nsp = S.n_s;
   const unsigned n_e = S.n_c * nsp;
-  const F* rates = reinterpret_cast<const F*>(S.rates);
+  const F* rates = reinterpret_cast<const F*>(S.crec);
+  if (tid < (int)nsp && tid < kMaxSpecies) {
+    const double a = ctl->mb_new[tid], b = ctl->mb_exp[tid];
+    const double den = fabs(a) > 1e-300 ? fabs(a) : 1e-300;
+    ctl->mass_balance[tid] = fabs(a - b) / den;
+    ctl->mb_new[tid] = 0.0;
+    ctl->mb_exp[tid] = 0.0;
+  }
   if constexpr (Model::separable) {
     for (unsigned j = tid; j < S.n_c; j += blockDim.x) {
       const double B = fixed_to_double(S.acc_hi[j], S.acc_lo[j], S.q_scale_up[0]);
       S.acc_hi[j] = 0;
       S.acc_lo[j] = 0ull;
-      const F* rr = rates + (size_t)j * kMaxRates;
+      const F* rr = rates + (size_t)j * 8;
       for (unsigned sp = 0; sp < nsp; ++sp) {
         double v = 0.0;
         if (sp < (unsigned)Model::n_ctb) v = __dmul_rn(__dmul_rn(S.weight, (double)Model::coef(rr, (int)sp)), B);
@@ -717,10 +793,13 @@ __global__ void k_init(const ScenDev* __restrict__ sc, unsigned long long n, uin
   }
 }
 
-// Move thresholds of every compartment for the current dt:
-// leave iff u < p = dt*Q/V, i.e. x < ceil(2^24 p) for the integer draw x.
+// Move thresholds of every compartment for the current dt, into slot 7 of
+// the compartment record: leave iff u < p = dt*Q/V, i.e. x < ceil(2^24 p)
+// for the integer draw x.
+template <class F>
 __global__ void k_move_thr(ScenDev* __restrict__ sc) {
   const ScenDev& S = sc[blockIdx.y];
+  F* rec = reinterpret_cast<F*>(S.crec);
   for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x) {
     const double p = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
     uint32_t t;
@@ -730,7 +809,10 @@ __global__ void k_move_thr(ScenDev* __restrict__ sc) {
       t = 0u;
     else
       t = (uint32_t)ceil(__dmul_rn(p, 16777216.0));
-    S.move_thr[c] = t;
+    if constexpr (sizeof(F) == 4)
+      rec[(size_t)c * 8 + 7] = __uint_as_float(t);
+    else
+      rec[(size_t)c * 8 + 7] = __longlong_as_double((long long)t);
   }
 }
 
@@ -758,14 +840,15 @@ __global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restric
 // Launchers and the per-model dispatch table.
 
 namespace {
-template <class Model, class F, int PPT>
+template <class Model, class F, int PPT, int THREADS, int MINB>
 void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
                     BatchCtl* b) {
-  k_cycle<Model, F, PPT><<<grid, block, smem, st>>>(sc, n, b);
+  (void)block;
+  k_cycle<Model, F, PPT, THREADS, MINB><<<grid, THREADS, smem, st>>>(sc, n, b);
 }
 template <class Model, class F>
-void launch_liquid_t(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
-  k_liquid<Model, F><<<n_scen, 1024, 0, st>>>(sc, b, do_scalar);
+void launch_liquid_t(int n_scen, unsigned max_nc, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
+  k_liquid<Model, F><<<dim3((max_nc + 255) / 256, n_scen), 256, 0, st>>>(sc, b, do_scalar);
 }
 template <class Model, class F>
 void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc) {
@@ -788,9 +871,13 @@ void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long 
                    uint32_t span, double* mass) {
   k_init<Model, F><<<grid, 256, 0, st>>>(sc, n, lo, span, mass);
 }
-template <class Model, class F, int PPT>
+template <class Model, class F, int PPT, int THREADS, int MINB>
 const void* cycle_fn_t() {
-  return reinterpret_cast<const void*>(&k_cycle<Model, F, PPT>);
+  return reinterpret_cast<const void*>(&k_cycle<Model, F, PPT, THREADS, MINB>);
+}
+template <class F>
+void launch_move_thr_t(int n_scen, cudaStream_t st, ScenDev* sc) {
+  k_move_thr<F><<<dim3(4, n_scen), 256, 0, st>>>(sc);
 }
 
 template <class Model, class F>
@@ -801,12 +888,17 @@ KernelSet make_set() {
   k.model = Model::model_id;
   k.f64 = sizeof(F) == 8;
   k.separable = Model::separable;
-  k.cycle[0] = &launch_cycle_t<Model, F, 1>;
-  k.cycle[1] = &launch_cycle_t<Model, F, 2>;
-  k.cycle[2] = &launch_cycle_t<Model, F, 4>;
-  k.cycle_fn[0] = cycle_fn_t<Model, F, 1>();
-  k.cycle_fn[1] = cycle_fn_t<Model, F, 2>();
-  k.cycle_fn[2] = cycle_fn_t<Model, F, 4>();
+  k.cycle[0] = &launch_cycle_t<Model, F, 1, 256, 4>;
+  k.cycle[1] = &launch_cycle_t<Model, F, 2, 256, 3>;
+  k.cycle[2] = &launch_cycle_t<Model, F, 4, 256, 2>;
+  k.cycle[3] = &launch_cycle_t<Model, F, 2, 512, 2>;
+  k.cycle[4] = &launch_cycle_t<Model, F, 1, 1024, 1>;
+  k.cycle_fn[0] = cycle_fn_t<Model, F, 1, 256, 4>();
+  k.cycle_fn[1] = cycle_fn_t<Model, F, 2, 256, 3>();
+  k.cycle_fn[2] = cycle_fn_t<Model, F, 4, 256, 2>();
+  k.cycle_fn[3] = cycle_fn_t<Model, F, 2, 512, 2>();
+  k.cycle_fn[4] = cycle_fn_t<Model, F, 1, 1024, 1>();
+  k.move_thr = &launch_move_thr_t<F>;
   k.liquid = &launch_liquid_t<Model, F>;
   k.plan = &launch_plan_t<Model, F>;
   k.divide = &launch_divide_t<Model, F>;
@@ -829,7 +921,6 @@ const KernelSet* kernel_set(int model, int f64) {
   return nullptr;
 }
 
-void launch_move_thr(int n_scen, cudaStream_t st, ScenDev* sc) { k_move_thr<<<dim3(4, n_scen), 256, 0, st>>>(sc); }
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {
   k_repartition<<<grid, 256, 0, st>>>(sc, counts);
 }

@@ -14,7 +14,13 @@ using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int);
 using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
                             double*);
 
-using LiquidLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*, int);
+using LiquidLaunch = void (*)(int, unsigned, cudaStream_t, ScenDev*, BatchCtl*, int);
+using MoveThrLaunch = void (*)(int, cudaStream_t, ScenDev*);
+
+// Cycle launch variants: {threads per block, particles per thread}.
+constexpr int kCycleVariants = 5;
+constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024};
+constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1};
 using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*);
 
 struct KernelSet {
@@ -25,8 +31,9 @@ struct KernelSet {
   int n_ctb;
   LiquidLaunch liquid;
   PlanLaunch plan;
-  CycleLaunch cycle[3];      // particles per thread 1, 2, 4
-  const void* cycle_fn[3];   // for occupancy queries / attributes
+  CycleLaunch cycle[kCycleVariants];
+  const void* cycle_fn[kCycleVariants];  // for occupancy queries / attributes
+  MoveThrLaunch move_thr;
   DivideLaunch divide;
   CopyLaunch compact;
   CopyLaunch merge;
@@ -34,7 +41,6 @@ struct KernelSet {
 };
 
 const KernelSet* kernel_set(int model, int f64);
-void launch_move_thr(int n_scen, cudaStream_t st, ScenDev* sc);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);

@@ -171,7 +171,7 @@ def test_repartition_and_force_remove(oracle_mod):
     assert_same_particles(g, o, "force_remove_dead")
 
 
-@pytest.mark.parametrize("shape", [(256, 1, 0), (256, 2, 0), (128, 4, 0), (256, 4, 1)])
+@pytest.mark.parametrize("shape", [(256, 1, 0), (256, 2, 0), (256, 4, 1), (512, 2, 0), (1024, 1, 0)])
 def test_launch_shapes_bit_identical(oracle_mod, shape):
     """Results do not depend on the launch shape: sums are exact."""
     sc = scenarios.workload(2, n_particles=30000, f64=True)
