@@ -76,6 +76,7 @@ SIGNATURES = {
     "bmc_batch_run": [VP, c_dbl, c_u32],
     "bmc_batch_set_shape": [VP, c_u32, c_u32, c_u32],
     "bmc_set_shape": [VP, c_u32, c_u32, c_u32],
+    "bmc_set_step_limit": [VP, c_u32],
     "bmc_batch_synchronize": [VP],
     "bmc_debug_draws": [c_u64, VP, c_u64, c_u32, c_u32, VP],
     "bmc_launch_count": [VP],

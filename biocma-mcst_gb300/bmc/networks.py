@@ -159,7 +159,8 @@ def ring_network(n_c: int = 10, extra_links: int = 2, median_flow: float = 1e-3,
 
 
 def lattice_vortex(n: int = 8, side: float = 1.0, peak_velocity: float = 0.5,
-                   noise: float = 0.1, seed: int = 1) -> Network:
+                   noise: float = 0.1, seed: int = 1, max_courant: float | None = None,
+                   dt: float | None = None) -> Network:
     """``n^3`` cubic lattice in a cube of edge ``side`` (m) with a toroidal
     recirculation: face flows are the discrete curl (Stokes circulation) of
     the vector potential ``A = psi(r, z) e_theta``,
@@ -205,8 +206,8 @@ def lattice_vortex(n: int = 8, side: float = 1.0, peak_velocity: float = 0.5,
     fz = (Ax[:, :-1, :] - Ax[:, 1:, :]) + (Ay[1:, :, :] - Ay[:-1, :, :])  # (n, n, n+1)
     # walls carry no flux (psi = 0 on every boundary edge); drop them
     fx, fy, fz = fx[1:-1], fy[:, 1:-1], fz[:, :, 1:-1]
-    vmax = max(np.abs(fx).max(), np.abs(fy).max(), np.abs(fz).max()) / (h * h)
-    scale = peak_velocity / vmax
+    vmax = max(np.abs(fx).max(initial=0.0), np.abs(fy).max(initial=0.0), np.abs(fz).max(initial=0.0)) / (h * h)
+    scale = peak_velocity / vmax if vmax > 0 else 0.0  # n <= 2: no interior recirculation
     fx, fy, fz = fx * scale, fy * scale, fz * scale
 
     def cid(i, j, k):
@@ -232,8 +233,15 @@ def lattice_vortex(n: int = 8, side: float = 1.0, peak_velocity: float = 0.5,
     volume = np.full(n ** 3, h ** 3)
     net = Network(n ** 3, volume, src, dst, flow,
                   meta={"kind": "lattice_vortex", "n": n, "side": side, "seed": seed,
-                        "peak_velocity": peak_velocity, "noise": noise})
-    return net.finalize()
+                        "peak_velocity": peak_velocity, "noise": noise, "flow_scale": 1.0})
+    net.finalize()
+    if max_courant is not None and dt is not None and len(net.flow):
+        cmax = net.max_courant(dt)
+        if cmax > max_courant:
+            net.flow = net.flow * (max_courant / cmax)
+            net.meta["flow_scale"] = max_courant / cmax
+            net.finalize()
+    return net
 
 
 def single_compartment(volume: float = 1e-3) -> Network:

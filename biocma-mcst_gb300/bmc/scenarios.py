@@ -174,6 +174,36 @@ def workload(index: int, n_particles: int | None = None, n_steps: int | None = N
     raise ValueError(f"unknown workload {index}")
 
 
+def batch_scenario(k: int, seed: int = 1234, n_lo: float = 1e4, n_hi: float = 5e6,
+                   nc_lo: float = 10, nc_hi: float = 2000, steps: int = 1000,
+                   steps_lo: int | None = None, steps_hi: int | None = None,
+                   particle_scale: float = 1.0) -> Scenario:
+    """Scenario k of the batched workload: compartment count log-uniform on
+    [10, 2000] (cubic lattice with a recirculation or a ring, chosen by the
+    seed), particles log-uniform on [1e4, 5e6], mu_max uniform on
+    [0.3, 1.0]/h, initial glucose uniform on [1, 20] g/L, FP32 Monod,
+    dt 0.1 s, closed reactor.  With steps_lo/steps_hi the step count is
+    log-uniform on that range (the served workload)."""
+    rng = np.random.default_rng(seed * 100003 + k)
+    n_c = int(round(math.exp(rng.uniform(math.log(nc_lo), math.log(nc_hi)))))
+    n_p = int(round(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi))) * particle_scale))
+    mu = rng.uniform(0.3, 1.0) / 3600.0
+    glc = rng.uniform(1.0, 20.0)
+    dt = 0.1
+    if rng.random() < 0.5:
+        n = max(3, int(round(n_c ** (1.0 / 3.0))))
+        net = lattice_vortex(n, side=1.0, peak_velocity=0.5, noise=0.1, seed=int(rng.integers(1 << 30)),
+                             max_courant=0.5, dt=dt)
+    else:
+        net = ring_network(max(n_c, 3), 2, 1e-3, 0.5, 0.5e-3, 2e-3, seed=int(rng.integers(1 << 30)),
+                           max_courant=0.5, dt=dt)
+    if steps_lo is not None:
+        steps = int(round(math.exp(rng.uniform(math.log(steps_lo), math.log(steps_hi)))))
+    c0 = np.full((net.n_c, 1), glc)
+    return Scenario(f"batch{k}", net, monod(f64=False, mu_max=mu), max(n_p, 1024), 1, c0, [],
+                    dt=dt, n_steps=steps, seed=seed * 7919 + k)
+
+
 def small_ring(n_particles: int = 4096, n_c: int = 10, seed: int = 3, f64: bool = True,
                model: ModelSpec | None = None, n_steps: int = 20, dt: float = 0.1,
                feeds: bool = False) -> Scenario:

@@ -108,6 +108,10 @@ class GpuScenario:
     def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
         call("bmc_set_shape", self.handle, threads, ppt, blocks_per_sm)
 
+    def set_step_limit(self, limit: int):
+        """Steps become no-ops once the step counter reaches `limit` (0: none)."""
+        call("bmc_set_step_limit", self.handle, limit)
+
     def set_particles(self, parts: dict, next_id: int):
         m = self.scen.model
         ft = np.float64 if m.f64 else np.float32

@@ -196,14 +196,20 @@ int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, 
 }
 
 // Enqueue one step (liquid step optional) for a table of scenarios.
-int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned max_nc,
+// Blocks along x of the liquid step: 256 / n_species compartments per block.
+unsigned liquid_grid(const ScenDev& h) {
+  const unsigned cb = 256u / std::max(1u, h.n_s);
+  return std::max(1u, (h.n_c + cb - 1) / cb);
+}
+
+int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned liq_grid,
                  BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count) {
-  ks->liquid(n_scen, max_nc, st, d_table, d_bctl, do_scalar);
+  ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
   ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl);
-  ks->plan(n_scen, st, d_table);
+  ks->plan(n_scen, st, d_table, d_bctl);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
-  ks->compact(dim3(sm_count * 2), st, d_table, n_scen);
-  ks->merge(dim3(sm_count * 2), st, d_table, n_scen);
+  ks->compact(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
+  ks->merge(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
   g_launches += 6;
   BMC_CUDA(cudaGetLastError());
   return BMC_OK;
@@ -373,7 +379,7 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   e = cudaMallocHost(&s->h_ctl, sizeof(Control));
   if (e == cudaSuccess) e = cudaMemsetAsync(s->parena, 0, cv.off, s->stream);
   if (e == cudaSuccess) {
-    BatchCtl b{0u, n_tiles};
+    BatchCtl b{0u, n_tiles, 0u, 0u};
     e = counted_memcpy_async(s->d_bctl, &b, sizeof(b), cudaMemcpyHostToDevice, s->stream);
   }
   if (e == cudaSuccess) e = counted_memcpy_async(s->d_desc, &h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream);
@@ -673,7 +679,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   cudaGraph_t g = nullptr;
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
-  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->h.n_c, s->d_bctl, 1, s->variant, grid, smem,
+  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, s->variant, grid, smem,
                         s->sm_count);
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
@@ -709,7 +715,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
     return BMC_OK;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
-    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, s->h.n_c, s->d_bctl, do_scalar, s->variant, grid, smem,
+    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, s->variant, grid, smem,
                       s->sm_count);
     if (rc) return rc;
   }
@@ -945,6 +951,15 @@ int bmc_batch_destroy(bmc_batch* b) {
   return BMC_OK;
 }
 
+int bmc_set_step_limit(bmc_scenario* s, uint32_t step_limit) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  s->h.step_limit = step_limit;
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   const unsigned th = threads ? threads : bmc::kVariantThreads[s->variant];
@@ -985,7 +1000,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     ScenDev d = s->h;
     d.tile_base = tiles;
     tiles += d.n_tiles;
-    max_nc = std::max(max_nc, d.n_c);
+    max_nc = std::max(max_nc, liquid_grid(d));
     smem = std::max(smem, cycle_smem(d));
     if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
     b->table[i] = d;
@@ -993,7 +1008,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   if (table_changed || b->dt != dt) {
     BMC_CUDA(cudaStreamSynchronize(b->stream));
     BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
-    BatchCtl bc{0u, tiles};
+    BatchCtl bc{0u, tiles, 0u, 0u};
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
     b->ks->move_thr(n, b->stream, b->d_table);
     g_launches++;
@@ -1054,17 +1069,17 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   cudaStream_t st = s->stream;
   const unsigned variant = s->variant;
   BMC_CUDA(cudaEventRecord(ev[0], st));
-  s->ks->liquid(1, s->h.n_c, st, s->d_desc, s->d_bctl, 1);
+  s->ks->liquid(1, liquid_grid(s->h), st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
   s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[2], st));
-  s->ks->plan(1, st, s->d_desc);
+  s->ks->plan(1, st, s->d_desc, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));
   s->ks->divide(dim3(s->sm_count * 4), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[4], st));
-  s->ks->compact(dim3(s->sm_count * 2), st, s->d_desc, 1);
+  s->ks->compact(dim3(s->sm_count * 2), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[5], st));
-  s->ks->merge(dim3(s->sm_count * 2), st, s->d_desc, 1);
+  s->ks->merge(dim3(s->sm_count * 2), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[6], st));
   g_launches += 6;
   BMC_CUDA(cudaGetLastError());

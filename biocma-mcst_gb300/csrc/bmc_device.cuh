@@ -138,8 +138,13 @@ struct ScenDev {
   unsigned long long min_removal;
   Control* ctl;
   int32_t f64;
-  int32_t pad0;
+  uint32_t step_limit;  // 0: none; otherwise steps stop (no-op) once ctl->step reaches it
 };
+
+// A scenario whose step counter has reached its limit is left untouched.
+__device__ __forceinline__ bool scen_finished(const ScenDev& S, const Control* ctl) {
+  return S.step_limit != 0u && ctl->step >= S.step_limit;
+}
 
 // ---------------------------------------------------------------------------
 // Draw source: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), keyed by

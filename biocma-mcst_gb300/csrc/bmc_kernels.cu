@@ -20,113 +20,92 @@
 namespace bmc {
 
 // ---------------------------------------------------------------------------
-// k_liquid: one thread per compartment j (grid x over compartments, grid y
-// over scenarios).  Feeds into sources and sink, explicit Euler step of the
-// liquid scalars of j
-//   M(j,:) += dt (sum_i C(i,:) T(i,j) - C(j,:) sink(j) + src(j,:)),
-//   C'(j,:) = M(j,:) / V(j),
-// then Model::rates of j from C'(j,:) into the compartment record.  C is
-// double-buffered by step parity (C' goes to the other buffer), so no block
-// waits for another.  With do_scalar == 0 only the rates (and C carried to
-// the next buffer).  Block (0, s) resets the step counters of scenario s;
-// block (0, 0) resets the tile scheduler.
+// k_liquid: one thread per (compartment j, species s) entry; a block holds
+// 256 / n_species whole compartments (grid x over compartment chunks, grid
+// y over scenarios).  Feeds into sources and sink, explicit Euler step
+//   M(j,s) += dt (sum_i C(i,s) T(i,j) - C(j,s) sink(j) + src(j,s)),
+//   C'(j,s) = M(j,s) / V(j),
+// then Model::rates of each compartment of the block from C'(j,:) into its
+// compartment record.  C is double-buffered by step parity (C' goes to the
+// other buffer), so no block waits for another.  With do_scalar == 0 only
+// the rates (and C carried to the next buffer).  Block (0, s) resets the
+// step counters of scenario s; block (0, 0) the tile scheduler and flags.
 template <class Model, class F>
 __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
   const ScenDev& S = sc[blockIdx.y];
   Control* ctl = S.ctl;
+  __shared__ double cs[256];
+  __shared__ double red[2][kMaxSpecies];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (blockIdx.y == 0) bctl->ticket = 0u;
+    if (blockIdx.y == 0) {
+      bctl->ticket = 0u;
+      bctl->flags = 0u;
+    }
     ctl->req_div = 0ull;
     ctl->exits = 0ull;
     ctl->moves = 0ull;
   }
-  const unsigned j = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned nsp = S.n_s;
+  const unsigned cb = 256u / nsp;  // compartments per block
+  const unsigned j0 = blockIdx.x * cb;
+  if (j0 >= S.n_c || scen_finished(S, ctl)) return;
+  const unsigned t = threadIdx.x;
+  const unsigned jl = t / nsp;
+  const unsigned sp = t - jl * nsp;
+  const unsigned j = j0 + jl;
+  const bool active = jl < cb && j < S.n_c;
   const size_t ne = (size_t)S.n_c * nsp;
   const unsigned parity = ctl->step & 1u;
   const double* __restrict__ Cold = S.C + parity * ne;
   double* __restrict__ Cnew = S.C + (parity ^ 1u) * ne;
-  double cn[kMaxSpecies];
-  double mn[kMaxSpecies], mx[kMaxSpecies];
-#pragma unroll
-  for (int k = 0; k < kMaxSpecies; ++k) mn[k] = mx[k] = 0.0;
-  if (j < S.n_c) {
+  if (t < 2 * kMaxSpecies) red[t / kMaxSpecies][t % kMaxSpecies] = 0.0;
+  __syncthreads();
+  if (active) {
+    const size_t e = (size_t)j * nsp + sp;
+    double cn;
     if (!do_scalar) {
-      for (unsigned sp = 0; sp < nsp; ++sp) {
-        cn[sp] = Cold[(size_t)j * nsp + sp];
-        Cnew[(size_t)j * nsp + sp] = cn[sp];
-      }
+      cn = Cold[e];
     } else {
       const double dt = S.dt;
+      double srcv = S.src[e];
       double sinkj = 0.0;
-      for (unsigned f = 0; f < S.n_feeds; ++f)
+      for (unsigned f = 0; f < S.n_feeds; ++f) {
+        if (S.feed_in[f] == j) {
+          const double cf = S.feed_conc[f * kMaxSpecies + sp];
+          if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
+        }
         if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
-      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
-      const double vinv = S.vinv[j], dg = S.diag[j];
-      for (unsigned sp = 0; sp < nsp; ++sp) {
-        const size_t e = (size_t)j * nsp + sp;
-        double srcv = S.src[e];
-        for (unsigned f = 0; f < S.n_feeds; ++f) {
-          if (S.feed_in[f] == j) {
-            const double cf = S.feed_conc[f * kMaxSpecies + sp];
-            if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
-          }
-        }
-        S.src[e] = srcv;
-        double acc = 0.0;
-        for (unsigned q = e0; q < e1; ++q)
-          acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
-        const double cj = Cold[e];
-        acc = __dadd_rn(acc, __dmul_rn(cj, dg));
-        const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
-        const double mold = S.M[e];
-        const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
-        S.M[e] = mnew;
-        cn[sp] = __dmul_rn(mnew, vinv);
-        Cnew[e] = cn[sp];
-#pragma unroll
-        for (int k = 0; k < kMaxSpecies; ++k) {
-          if ((unsigned)k == sp) {
-            mn[k] = mnew;
-            mx[k] = mold + dt * (srcv - cj * sinkj);
-          }
-        }
       }
+      S.src[e] = srcv;
+      double acc = 0.0;
+      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
+      for (unsigned q = e0; q < e1; ++q)
+        acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
+      const double cj = Cold[e];
+      acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
+      const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
+      const double mold = S.M[e];
+      const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
+      S.M[e] = mnew;
+      cn = __dmul_rn(mnew, S.vinv[j]);
+      // mass-balance sums (diagnostic): new mass, expected mass
+      atomicAdd(&red[0][sp], mnew);
+      atomicAdd(&red[1][sp], mold + dt * (srcv - cj * sinkj));
     }
+    Cnew[e] = cn;
+    cs[t] = cn;
+  }
+  __syncthreads();
+  if (t < cb && j0 + t < S.n_c) {
     F r[kMaxRates];
-    Model::rates(cn, S.params, r);
-    F* rec = reinterpret_cast<F*>(S.crec) + (size_t)j * 8;
+    Model::rates(cs + t * nsp, S.params, r);
+    F* rec = reinterpret_cast<F*>(S.crec) + (size_t)(j0 + t) * 8;
 #pragma unroll
     for (int k = 0; k < Model::n_rates; ++k) rec[k] = r[k];
   }
-  if (do_scalar) {
-    // mass-balance sums (diagnostic): block reduction, one atomic per species
-    __shared__ double red[2][8];
-#pragma unroll
-    for (int k = 0; k < kMaxSpecies; ++k) {
-      if ((unsigned)k >= nsp) break;
-      double a = mn[k], b = mx[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-      }
-      if ((threadIdx.x & 31) == 0) {
-        red[0][threadIdx.x >> 5] = a;
-        red[1][threadIdx.x >> 5] = b;
-      }
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double ta = 0.0, tb = 0.0;
-        for (unsigned w = 0; w < blockDim.x / 32; ++w) {
-          ta += red[0][w];
-          tb += red[1][w];
-        }
-        atomicAdd(&ctl->mb_new[k], ta);
-        atomicAdd(&ctl->mb_exp[k], tb);
-      }
-      __syncthreads();
-    }
+  if (do_scalar && t < nsp) {
+    atomicAdd(&ctl->mb_new[t], red[0][t]);
+    atomicAdd(&ctl->mb_exp[t], red[1][t]);
   }
 }
 
@@ -309,7 +288,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const unsigned t = g - S.tile_base;
     const unsigned long long n_used = S.ctl->n_used;
     const unsigned long long base = (unsigned long long)t * kTile;
-    if (base >= n_used) continue;
+    if (base >= n_used || scen_finished(S, S.ctl)) continue;
     since_flush += kTile;
 
     const unsigned long long cap = S.cap;
@@ -478,13 +457,26 @@ __global__ void __launch_bounds__(THREADS, MINB)
 //     source ranks from the end);
 //  4. control block advanced to the state after the step.
 template <class Model, class F>
-__global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
+__global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCtl* __restrict__ bctl) {
   const ScenDev& S = sc[blockIdx.x];
   Control* ctl = S.ctl;
   const int tid = threadIdx.x;
   __shared__ unsigned long long sh64[33];
   __shared__ unsigned long long p_n, p_req, p_rm, p_after;
   __shared__ int p_compact;
+  if (scen_finished(S, ctl)) {
+    // nothing ran for this scenario: leave its state and a no-op plan
+    if (tid == 0) {
+      ctl->plan_births = 0ull;
+      ctl->plan_overflow = 0ull;
+      ctl->plan_compact = 0u;
+      ctl->plan_to_remove = 0ull;
+      ctl->plan_gaps = 0ull;
+      ctl->plan_n_old = ctl->n_used;
+      ctl->plan_n_after = ctl->n_used;
+    }
+    return;
+  }
 
   const unsigned nsp = S.n_s;
   const unsigned n_e = S.n_c * nsp;
@@ -564,6 +556,11 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc) {
     ctl->last_overflow = req - births;
     ctl->last_req_div = req;
     ctl->last_compacted = (unsigned)compact;
+    unsigned fl = 0u;
+    if (req > 0ull) fl |= kFlagDivide;
+    if (compact && after > 0ull && rm < n) fl |= kFlagCompact;
+    if (births > 0ull) fl |= kFlagMerge;
+    if (fl) atomicOr(&bctl->flags, fl);
   }
   __syncthreads();
   const unsigned long long n = p_n;
@@ -622,6 +619,7 @@ __global__ void __launch_bounds__(256) k_divide(const ScenDev* __restrict__ sc, 
                                                const BatchCtl* __restrict__ bctl) {
   constexpr int NV = Model::n_var;
   __shared__ unsigned sh[33];
+  if (!(bctl->flags & (kFlagDivide | kFlagCompact))) return;
   const unsigned total_tiles = bctl->total_tiles;
   const int tid = threadIdx.x;
   int s = -1;
@@ -707,7 +705,9 @@ __global__ void __launch_bounds__(256) k_divide(const ScenDev* __restrict__ sc, 
 // k_merge: append the children after the live particles with ages 0 and
 // fresh ids (InsertFunctor, particles_container.hpp L403-L447).
 template <int NV, class F>
-__global__ void __launch_bounds__(256) k_compact(const ScenDev* __restrict__ sc, int n_scen) {
+__global__ void __launch_bounds__(256) k_compact(const ScenDev* __restrict__ sc, int n_scen,
+                                                const BatchCtl* __restrict__ bctl) {
+  if (!(bctl->flags & kFlagCompact)) return;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (int s = 0; s < n_scen; ++s) {
     const ScenDev& S = sc[s];
@@ -735,7 +735,9 @@ __global__ void __launch_bounds__(256) k_compact(const ScenDev* __restrict__ sc,
 }
 
 template <int NV, class F>
-__global__ void __launch_bounds__(256) k_merge(const ScenDev* __restrict__ sc, int n_scen) {
+__global__ void __launch_bounds__(256) k_merge(const ScenDev* __restrict__ sc, int n_scen,
+                                              const BatchCtl* __restrict__ bctl) {
+  if (!(bctl->flags & kFlagMerge)) return;
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (int s = 0; s < n_scen; ++s) {
     const ScenDev& S = sc[s];
@@ -847,24 +849,24 @@ void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const S
   k_cycle<Model, F, PPT, THREADS, MINB><<<grid, THREADS, smem, st>>>(sc, n, b);
 }
 template <class Model, class F>
-void launch_liquid_t(int n_scen, unsigned max_nc, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
-  k_liquid<Model, F><<<dim3((max_nc + 255) / 256, n_scen), 256, 0, st>>>(sc, b, do_scalar);
+void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
+  k_liquid<Model, F><<<dim3(grid_x, n_scen), 256, 0, st>>>(sc, b, do_scalar);
 }
 template <class Model, class F>
-void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc) {
-  k_plan<Model, F><<<n_scen, 1024, 0, st>>>(sc);
+void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b) {
+  k_plan<Model, F><<<n_scen, 1024, 0, st>>>(sc, b);
 }
 template <class Model, class F>
 void launch_divide_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
   k_divide<Model, F><<<grid, 256, 0, st>>>(sc, n, b);
 }
 template <class Model, class F>
-void launch_compact_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n) {
-  k_compact<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n);
+void launch_compact_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
+  k_compact<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n, b);
 }
 template <class Model, class F>
-void launch_merge_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n) {
-  k_merge<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n);
+void launch_merge_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
+  k_merge<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n, b);
 }
 template <class Model, class F>
 void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long long n, uint32_t lo,

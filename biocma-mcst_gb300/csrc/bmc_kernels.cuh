@@ -24,7 +24,12 @@ constexpr int kTile = 1024;  // particles per tile (scheduling and scan unit)
 struct BatchCtl {
   unsigned int ticket;      // next tile handed out by k_cycle
   unsigned int total_tiles; // tiles over all scenarios
+  unsigned int flags;       // work of this step after the cycle (kFlag*)
+  unsigned int pad;
 };
+constexpr unsigned kFlagDivide = 1u;   // some scenario asked for divisions
+constexpr unsigned kFlagCompact = 2u;  // some scenario compacts
+constexpr unsigned kFlagMerge = 4u;    // some scenario appends children
 
 // ------------------------------------------------------------------------
 // Vector loads / stores of PPT consecutive elements (streaming hints: the

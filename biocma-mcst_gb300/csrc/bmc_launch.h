@@ -10,7 +10,7 @@ namespace bmc {
 
 using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
-using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int);
+using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
                             double*);
 
@@ -21,7 +21,7 @@ using MoveThrLaunch = void (*)(int, cudaStream_t, ScenDev*);
 constexpr int kCycleVariants = 5;
 constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024};
 constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1};
-using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*);
+using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*);
 
 struct KernelSet {
   int model;

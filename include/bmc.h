@@ -202,6 +202,11 @@ int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats)
  * (0 = as many as fit); 0 keeps the current value. */
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 
+/* Step budget: once the scenario's step counter reaches step_limit its
+ * steps are no-ops (0 removes the limit).  Lets a batch hold scenarios that
+ * need different numbers of steps (serving). */
+int bmc_set_step_limit(bmc_scenario* s, uint32_t step_limit);
+
 /* Enqueue n_steps iterations without waiting (bmc_synchronize waits). */
 int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps);
 int bmc_synchronize(bmc_scenario* s);

@@ -1,0 +1,92 @@
+"""Batched form: many uneven scenarios advanced by one set of launches per
+step give, for each scenario, exactly the result it gives alone (and the CPU
+restatement's): draws are keyed by particle, sums are exact."""
+import numpy as np
+import pytest
+
+from bmc import scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def same_bits(a, b):
+    ui = {8: np.uint64, 4: np.uint32}[a.dtype.itemsize]
+    return a.shape == b.shape and bool(np.all((a.view(ui) == b.view(ui)) | (np.isnan(a) & np.isnan(b))))
+
+
+def assert_same(g1, g2, where):
+    p1, p2 = g1.particles(), g2.particles()
+    for k in ("pos", "status", "id"):
+        assert np.array_equal(p1[k], p2[k]), f"{where}: {k}"
+    for k in ("age_h", "age_d", "state"):
+        assert same_bits(p1[k], p2[k]), f"{where}: {k}"
+    l1, l2 = g1.liquid(), g2.liquid()
+    for k in ("C", "M", "src"):
+        assert same_bits(l1[k], l2[k]), f"{where}: {k}"
+
+
+def _mix(n=7, scale=0.02):
+    return [scenarios.batch_scenario(k, seed=77, particle_scale=scale) for k in range(n)]
+
+
+@pytest.mark.parametrize("shape", [(256, 2, 0), (1024, 1, 0)])
+def test_batch_equals_alone(shape):
+    from bmc.sim import GpuBatch, GpuScenario
+
+    scens = _mix()
+    batch_members = [GpuScenario(s) for s in scens]
+    alone = [GpuScenario(s) for s in scens]
+    b = GpuBatch(batch_members)
+    b.set_shape(*shape)
+    steps = 9
+    b.run(steps, 0.1)
+    b.synchronize()
+    for g in alone:
+        g.run(steps)
+    for k, (gb, ga) in enumerate(zip(batch_members, alone)):
+        st = gb.stats()
+        assert st["step"] == steps and st["error"] == 0
+        assert_same(gb, ga, f"scenario {k} ({scens[k].net.n_c} compartments, {scens[k].n_particles} particles)")
+    b.close()
+
+
+def test_batch_member_matches_oracle(oracle_mod):
+    from bmc.sim import GpuBatch, GpuScenario
+
+    scens = _mix(5, 0.01)
+    members = [GpuScenario(s) for s in scens]
+    b = GpuBatch(members)
+    b.run(6, 0.1)
+    b.synchronize()
+    k = int(np.argmax([s.net.n_c for s in scens]))
+    o = oracle_mod.Oracle(scens[k], phys_capacity=members[k].cap)
+    o.init_particles()
+    o.set_weight(members[k].weight)
+    o.run(6)
+    pg, po = members[k].particles(), o.particles()
+    for key in ("pos", "status", "id"):
+        assert np.array_equal(pg[key], po[key]), key
+    assert same_bits(pg["state"], po["state"])
+    assert same_bits(members[k].liquid()["C"], o.C)
+    b.close()
+
+
+def test_batch_then_alone_continues_consistently():
+    """A scenario can leave a batch and continue alone (serving retires and
+    re-forms batches between chunks)."""
+    from bmc.sim import GpuBatch, GpuScenario
+
+    scens = _mix(4, 0.01)
+    mixed = [GpuScenario(s) for s in scens]
+    ref = GpuScenario(scens[2])
+    b = GpuBatch(mixed)
+    b.run(4, 0.1)
+    b.synchronize()
+    b.close()
+    b2 = GpuBatch([mixed[0], mixed[2]])
+    b2.run(3, 0.1)
+    b2.synchronize()
+    mixed[2].run(2)
+    ref.run(9)
+    assert_same(mixed[2], ref, "regrouped")
+    b2.close()
