@@ -44,6 +44,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=50)
     ap.add_argument("--shape", default=None,
                     help="threads,particles_per_thread,blocks_per_sm (skips the autotuner)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the precision / batched / served measurements")
+    ap.add_argument("--forms-steps", type=int, default=100)
+    ap.add_argument("--serve-window", type=float, default=10.0)
     return ap.parse_args()
 
 
@@ -332,6 +336,13 @@ def run_gpu(args):
                "sample": f"{scen.n_particles} particles x {csteps} steps of the same workload "
                          f"({cel:.1f} s), C/OpenMP restatement of the reference path"}
 
+    g.close()
+    forms = None
+    if rank == 0 and world == 1 and not args.no_forms:
+        forms = {"precision": precision_form(args.forms_steps),
+                 "batched": batched_form(args.forms_steps),
+                 "served": served_form(args.serve_window)}
+
     if rank == 0:
         cfg = workload_config(scen)
         cfg["parallelism"] = f"replicas x{world}" if world > 1 else "single GPU"
@@ -345,12 +356,127 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": cfg["state_dtype"], "data": "synthetic", "config": cfg,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
-            "gpu_launches": launches,
+            "gpu_launches": launches, "forms": forms,
         }
         print(json.dumps(line), flush=True)
-    g.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def precision_form(steps: int):
+    """FP32 particle state and model arithmetic (exact contribution sums,
+    FP64 liquid step) on the 4096-compartment workload, timed; the same
+    scenario in FP64 (the GPU FP64 path is bit-identical to the FP64 CPU
+    restatement) gives the reference for the error per species."""
+    import numpy as np
+
+    from bmc import autotune, scenarios, sim
+
+    out = {"workload": "lattice4096_overflow", "n_particles": 50_000_000, "steps": steps}
+    res = {}
+    for f64 in (False, True):
+        scen = scenarios.workload(3, f64=f64)
+        g = sim.GpuScenario(scen)
+        shape, _ = autotune.tune_scenario(g)
+        g.run(3)
+        s0 = g.stats()
+        st, ms = g.run_timed(steps)
+        alive = 0.5 * ((s0["n_used"] - s0["inactive"]) + (st["n_used"] - st["inactive"]))
+        res[f64] = {"value": alive * steps / (ms / 1e3), "ms_per_step": ms / steps,
+                    "C": g.liquid()["C"], "step": st["step"], "mass_balance": st["mass_balance"][:4],
+                    "shape": shape}
+        if not f64:
+            kms = [g.step_timed()[1][1] for _ in range(10)]
+            cyc = statistics.mean(kms)
+            ach = scen.algorithmic_bytes() * alive / (cyc / 1e3) / 1e9
+            out["roofline_frac"] = ach / measured_peak()[0]
+            out["kernel_ms"] = cyc
+        g.close()
+    c32, c64 = res[False]["C"], res[True]["C"]
+    names = ["glucose", "O2", "acetate", "CO2"]
+    err = {}
+    for sp, nm in enumerate(names):
+        ref = np.abs(c64[:, sp])
+        scale = max(float(ref.max()), 1e-300)
+        err[nm] = {"max_abs_err": float(np.abs(c32[:, sp] - c64[:, sp]).max()),
+                   "max_rel_err_vs_field_max": float(np.abs(c32[:, sp] - c64[:, sp]).max() / scale)}
+    out.update({"value_f32": res[False]["value"], "value_f64": res[True]["value"],
+                "ms_per_step_f32": res[False]["ms_per_step"], "ms_per_step_f64": res[True]["ms_per_step"],
+                "after_steps": res[False]["step"], "error_vs_fp64_per_species": err,
+                "mass_balance_f32": res[False]["mass_balance"], "unit": METRIC})
+    return out
+
+
+def batched_form(steps: int, n_scen: int = 256):
+    """256 uneven scenarios advanced by one batched launch sequence per step
+    (one captured graph) against the plain path: each scenario advanced by
+    its own graph on its own stream, all streams in flight together."""
+    from bmc import autotune, scenarios, sim
+
+    scens = [scenarios.batch_scenario(k, seed=1234) for k in range(n_scen)]
+    t0 = time.perf_counter()
+    gs = [sim.GpuScenario(s) for s in scens]
+    setup = time.perf_counter() - t0
+    b = sim.GpuBatch(gs)
+    shape, tune_ms = autotune.tune_batch(b, 0.1)
+    b.run(3, 0.1)
+    b.synchronize()
+    n_alive = sum(s.n_particles for s in scens)
+    t0 = time.perf_counter()
+    b.run(steps, 0.1)
+    b.synchronize()
+    tb = time.perf_counter() - t0
+    b.close()
+    for g in gs:  # plain path: warm its graphs
+        g.run(1)
+    # plain, one scenario after another, each step through bmc_step (the
+    # reference's loop reads its counters back after every cycle)
+    t0 = time.perf_counter()
+    for g in gs:
+        for _ in range(steps):
+            g.step()
+    t_sync = time.perf_counter() - t0
+    # plain, one scenario after another, each as one captured graph of `steps` steps
+    t0 = time.perf_counter()
+    for g in gs:
+        g.run(steps)
+    t_seq = time.perf_counter() - t0
+    # plain, every scenario's graph on its own stream, all in flight together
+    t0 = time.perf_counter()
+    for g in gs:
+        g.run_async(steps)
+    for g in gs:
+        g.synchronize()
+    tp = time.perf_counter() - t0
+    n_small = sum(1 for s in scens if s.n_particles < 1e5)
+    for g in gs:
+        g.close()
+    ps = n_alive * steps
+    return {"scenarios": n_scen, "total_particles": n_alive, "steps": steps,
+            "n_compartments_range": [min(s.net.n_c for s in scens), max(s.net.n_c for s in scens)],
+            "particles_range": [min(s.n_particles for s in scens), max(s.n_particles for s in scens)],
+            "scenarios_below_1e5_particles": n_small,
+            "batched_value": ps / tb,
+            "plain_step_sync_value": ps / t_sync, "plain_graph_sequential_value": ps / t_seq,
+            "plain_graph_concurrent_streams_value": ps / tp,
+            "batched_over_plain_step_sync": t_sync / tb, "batched_over_plain_graph_sequential": t_seq / tb,
+            "batched_over_plain_concurrent_streams": tp / tb, "unit": METRIC, "setup_s": setup,
+            "shape": shape, "accuracy": "bit-identical results batched and plain (tests/test_gpu_batch.py)"}
+
+
+def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):
+    """Poisson arrivals for `window_s` seconds, sizes as the batched workload,
+    steps log-uniform on [100, 10000]; all requests are served to completion."""
+    from bmc import serve
+
+    reqs = serve.poisson_requests(rate, window_s, seed=2027)
+    srv = serve.Server(hbm_budget=budget)
+    out = srv.serve(reqs)
+    out.update({"arrival_rate_per_s": rate, "arrival_window_s": window_s, "hbm_budget_gb": budget / 1e9,
+                "unit": METRIC,
+                "demand_particle_steps_per_s": sum(r.particle_steps for r in reqs) / window_s,
+                "accuracy": "each result bit-identical to the request run alone (tests/test_gpu_serve.py)"})
+    return out
 
 
 def main():

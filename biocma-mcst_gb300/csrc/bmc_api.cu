@@ -115,6 +115,7 @@ struct bmc_batch {
   cudaStream_t stream = nullptr;
   ScenDev* d_table = nullptr;
   BatchCtl* d_bctl = nullptr;
+  unsigned* d_live = nullptr;  // [n + 1] live-tile prefix
   std::vector<ScenDev> table;
   unsigned total_tiles = 0;
   unsigned variant = 0, blocks_per_sm = 0;  // cycle launch variant (bmc_launch.h)
@@ -356,6 +357,8 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   cv.add(&desc_tmp, 1);
   BatchCtl* bctl_tmp = nullptr;
   cv.add(&bctl_tmp, 1);
+  unsigned* live_tmp = nullptr;
+  cv.add(&live_tmp, 2);
   e = cudaMalloc(&s->parena, cv.off);
   if (e != cudaSuccess) {
     cudaStreamDestroy(s->stream);
@@ -379,7 +382,7 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   e = cudaMallocHost(&s->h_ctl, sizeof(Control));
   if (e == cudaSuccess) e = cudaMemsetAsync(s->parena, 0, cv.off, s->stream);
   if (e == cudaSuccess) {
-    BatchCtl b{0u, n_tiles, 0u, 0u};
+    BatchCtl b{0u, n_tiles, 0u, 0u, live_tmp};
     e = counted_memcpy_async(s->d_bctl, &b, sizeof(b), cudaMemcpyHostToDevice, s->stream);
   }
   if (e == cudaSuccess) e = counted_memcpy_async(s->d_desc, &h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream);
@@ -930,6 +933,7 @@ int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(ScenDev) * n);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_bctl, sizeof(BatchCtl));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_live, sizeof(unsigned) * (n + 1));
   if (e != cudaSuccess) {
     if (b->d_table) cudaFree(b->d_table);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -946,6 +950,7 @@ int bmc_batch_destroy(bmc_batch* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->d_table);
   cudaFree(b->d_bctl);
+  cudaFree(b->d_live);
   cudaStreamDestroy(b->stream);
   delete b;
   return BMC_OK;
@@ -1008,7 +1013,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   if (table_changed || b->dt != dt) {
     BMC_CUDA(cudaStreamSynchronize(b->stream));
     BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
-    BatchCtl bc{0u, tiles, 0u, 0u};
+    BatchCtl bc{0u, tiles, 0u, 0u, b->d_live};
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
     b->ks->move_thr(n, b->stream, b->d_table);
     g_launches++;

@@ -36,14 +36,48 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
   Control* ctl = S.ctl;
   __shared__ double cs[256];
   __shared__ double red[2][kMaxSpecies];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    if (blockIdx.y == 0) {
+  if (blockIdx.x == 0 && blockIdx.y == 0) {
+    // live tiles of every scenario (ceil(n_used / 1024), none once finished)
+    // and their prefix: the cycle hands out only tiles that hold particles
+    __shared__ unsigned sh[33];
+    const int n_scen = (int)gridDim.y;
+    unsigned run = 0;
+    for (int b0 = 0; b0 < n_scen; b0 += (int)blockDim.x) {
+      const int s2 = b0 + (int)threadIdx.x;
+      unsigned live = 0;
+      if (s2 < n_scen) {
+        const ScenDev& P = sc[s2];
+        if (!scen_finished(P, P.ctl)) {
+          const unsigned long long lt = (P.ctl->n_used + kTile - 1) / kTile;
+          live = (unsigned)(lt < P.n_tiles ? lt : P.n_tiles);
+        }
+      }
+      unsigned tot;
+      const unsigned pre = block_exscan_u32(live, sh, &tot);
+      if (s2 < n_scen) bctl->live_base[s2] = run + pre;
+      run += tot;
+    }
+    if (threadIdx.x == 0) {
+      bctl->live_base[n_scen] = run;
+      bctl->total_live = run;
       bctl->ticket = 0u;
       bctl->flags = 0u;
     }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctl->req_div = 0ull;
     ctl->exits = 0ull;
     ctl->moves = 0ull;
+  }
+  {
+    // per-tile birth / inactive counters of this step start at zero (the
+    // cycle's warps add to them)
+    const unsigned long long lt = (ctl->n_used + kTile - 1) / kTile;
+    const unsigned n_live = (unsigned)(lt < S.n_tiles ? lt : S.n_tiles);
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n_live; t += gridDim.x * blockDim.x) {
+      S.tile_births[t] = 0u;
+      S.tile_inactive[t] = 0u;
+    }
   }
   const unsigned nsp = S.n_s;
   const unsigned cb = 256u / nsp;  // compartments per block
@@ -188,9 +222,10 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
 }
 
 // ---------------------------------------------------------------------------
-// k_cycle: the fused per-particle hot path.  A persistent grid takes tiles
-// of 1024 slots from a ticket counter (tiles are ordered scenario after
-// scenario).  For each Idle particle (draws: one Philox block, integers
+// k_cycle: the fused per-particle hot path.  Each block of a persistent
+// grid streams a contiguous run of the live tiles (1024-slot tiles that hold
+// particles, ordered scenario after scenario; k_liquid lists them).  For
+// each Idle particle (draws: one Philox block, integers
 // x_k = (r_k >> 8) | 1 with u_k = x_k 2^-24):
 //   ages(i,1) += dt; Model::update(dt, x, rates(pos))
 //   contribution basis (or contributions) -> shared-memory fixed-point
@@ -209,87 +244,80 @@ template <class Model, class F, int PPT, int THREADS, int MINB>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_cycle(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   extern __shared__ unsigned long long sacc[];
-  __shared__ unsigned s_tile;
-  __shared__ unsigned s_tile_births, s_tile_inactive;
   __shared__ unsigned long long s_cnt[5];
   __shared__ F s_pf[16];  // parameters of the current scenario, as F
   constexpr int NV = Model::n_var;
   constexpr int NC = Model::n_ctb;
   constexpr int NA = Model::separable ? 1 : NC;  // accumulator columns
+  constexpr unsigned CH = 32u * PPT;             // slots per warp chunk
+  constexpr unsigned NW = THREADS / 32;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
-  const unsigned total_tiles = bctl->total_tiles;
-  constexpr int passes = kTile / (THREADS * PPT);
+  const unsigned warp = (unsigned)tid >> 5;
+  const unsigned total = bctl->total_live;
+  const unsigned* live_base = bctl->live_base;
   int cur = -1;
-  unsigned since_flush = 0;
+  unsigned long long since_flush = 0;
   unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
   unsigned my_err = 0;
 
-  for (;;) {
-    if (tid == 0) {
-      s_tile = atomicAdd(&bctl->ticket, 1u);
-      s_tile_births = 0u;
-      s_tile_inactive = 0u;
+  // flush the accumulator and the counters of scenario `cur` (whole block)
+  auto flush = [&]() {
+    __syncthreads();
+    const ScenDev& P = sc[cur];
+    const unsigned n_ent = P.n_c * NA;
+    for (unsigned e = tid; e < n_ent; e += THREADS) {
+      const long long p = (long long)sacc[e];
+      if (p != 0) {
+        atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
+        atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
+      }
+    }
+    if (tid < 5) s_cnt[tid] = 0ull;
+    __syncthreads();
+    const unsigned long long r0 = warp_sum_u64(my_req), r1 = warp_sum_u64(my_exit);
+    const unsigned long long r2 = warp_sum_u64(my_move), r3 = warp_sum_u64(my_clamp);
+    unsigned e4 = my_err;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e4 |= __shfl_xor_sync(0xffffffffu, e4, o);
+    if (lane == 0) {
+      atomicAdd(&s_cnt[0], r0);
+      atomicAdd(&s_cnt[1], r1);
+      atomicAdd(&s_cnt[2], r2);
+      atomicAdd(&s_cnt[3], r3);
+      atomicOr(reinterpret_cast<unsigned*>(&s_cnt[4]), e4);
     }
     __syncthreads();
-    const unsigned g = s_tile;
-    __syncthreads();  // every thread has read the ticket before thread 0 takes the next
-    const bool done = g >= total_tiles;
-    const int s = done ? -1 : scen_of_tile(sc, n_scen, g, cur);
-    if (s != cur || since_flush + kTile > kFlushParticles) {
-      if (cur >= 0) {
-        // flush the accumulator and the counters of scenario `cur`
-        const ScenDev& P = sc[cur];
-        const unsigned n_ent = P.n_c * NA;
-        for (unsigned e = tid; e < n_ent; e += blockDim.x) {
-          const long long p = (long long)sacc[e];
-          if (p != 0) {
-            atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
-            atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
-          }
-        }
-        if (tid < 5) s_cnt[tid] = 0ull;
-        __syncthreads();
-        const unsigned long long r0 = warp_sum_u64(my_req), r1 = warp_sum_u64(my_exit);
-        const unsigned long long r2 = warp_sum_u64(my_move), r3 = warp_sum_u64(my_clamp);
-        unsigned e4 = my_err;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) e4 |= __shfl_xor_sync(0xffffffffu, e4, o);
-        if (lane == 0) {
-          atomicAdd(&s_cnt[0], r0);
-          atomicAdd(&s_cnt[1], r1);
-          atomicAdd(&s_cnt[2], r2);
-          atomicAdd(&s_cnt[3], r3);
-          atomicOr(reinterpret_cast<unsigned*>(&s_cnt[4]), e4);
-        }
-        __syncthreads();
-        if (tid == 0) {
-          Control* c = P.ctl;
-          if (s_cnt[0]) atomicAdd(&c->req_div, s_cnt[0]);
-          if (s_cnt[1]) atomicAdd(&c->exits, s_cnt[1]);
-          if (s_cnt[2]) atomicAdd(&c->moves, s_cnt[2]);
-          if (s_cnt[3]) atomicAdd(&c->clamped, s_cnt[3]);
-          const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
-          if (ev) atomicOr(&c->error, ev);
-        }
-        my_req = my_exit = my_move = my_clamp = 0ull;
-        my_err = 0u;
-      }
-      if (done) break;
-      const unsigned n_ent = sc[s].n_c * NA;
-      for (unsigned e = tid; e < n_ent; e += blockDim.x) sacc[e] = 0ull;
-      if (tid < 16) s_pf[tid] = (F)sc[s].params[tid];
-      cur = s;
-      since_flush = 0;
-      __syncthreads();
+    if (tid == 0) {
+      Control* c = P.ctl;
+      if (s_cnt[0]) atomicAdd(&c->req_div, s_cnt[0]);
+      if (s_cnt[1]) atomicAdd(&c->exits, s_cnt[1]);
+      if (s_cnt[2]) atomicAdd(&c->moves, s_cnt[2]);
+      if (s_cnt[3]) atomicAdd(&c->clamped, s_cnt[3]);
+      const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
+      if (ev) atomicOr(&c->error, ev);
     }
-    if (done) break;  // a block that never received a tile (cur == -1) ends here
+    my_req = my_exit = my_move = my_clamp = 0ull;
+    my_err = 0u;
+  };
+
+  // static partition: block b streams the live tiles [g_begin, g_end), a
+  // contiguous run, scenario segment after scenario segment; inside a
+  // segment every warp streams its own 32*PPT-slot chunks with no block
+  // barrier, so warps drift apart and hide each other's latency
+  const unsigned g_begin = (unsigned)(((unsigned long long)total * blockIdx.x) / gridDim.x);
+  const unsigned g_end = (unsigned)(((unsigned long long)total * (blockIdx.x + 1)) / gridDim.x);
+  unsigned g = g_begin;
+  while (g < g_end) {
+    const int s = scen_of_live(live_base, n_scen, g, cur);
+    const unsigned sb = __ldg(live_base + s), se = __ldg(live_base + s + 1);
+    const unsigned ge = se < g_end ? se : g_end;
     const ScenDev& S = sc[s];
-    const unsigned t = g - S.tile_base;
     const unsigned long long n_used = S.ctl->n_used;
-    const unsigned long long base = (unsigned long long)t * kTile;
-    if (base >= n_used || scen_finished(S, S.ctl)) continue;
-    since_flush += kTile;
+    const unsigned long long p_lo = (unsigned long long)(g - sb) * kTile;
+    unsigned long long p_hi = (unsigned long long)(ge - sb) * kTile;
+    if (p_hi > n_used) p_hi = n_used;
+    g = ge;
 
     const unsigned long long cap = S.cap;
     const unsigned n_c = S.n_c, K = S.K;
@@ -300,148 +328,166 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const float dtf = (float)dt;
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
+    const int qe0 = S.q_exp[0];
     const F* __restrict__ crec = reinterpret_cast<const F*>(S.crec);
     const int2* __restrict__ mrow = S.mrow;
     F* __restrict__ state = reinterpret_cast<F*>(S.state);
 
-#pragma unroll 1
-    for (int pass = 0; pass < passes; ++pass) {
-      const unsigned long long first = base + ((unsigned long long)pass * THREADS + tid) * PPT;
-      uint8_t stv[PPT];
-      ld_stream<uint8_t, PPT>(S.status + first, stv);
-      bool idle[PPT];
-      bool any = false, all = true;
-#pragma unroll
-      for (int k = 0; k < PPT; ++k) {
-        idle[k] = (first + k < n_used) && stv[k] == kIdle;
-        any |= idle[k];
-        all &= idle[k];
+    for (unsigned long long q0 = p_lo; q0 < p_hi; q0 += kFlushParticles) {
+      const unsigned long long q1 = q0 + kFlushParticles < p_hi ? q0 + kFlushParticles : p_hi;
+      if (s != cur || since_flush + (q1 - q0) > kFlushParticles) {
+        if (cur >= 0) flush();
+        __syncthreads();
+        const unsigned n_ent = S.n_c * NA;
+        for (unsigned e = tid; e < n_ent; e += THREADS) sacc[e] = 0ull;
+        if (tid < 16) s_pf[tid] = (F)S.params[tid];
+        cur = s;
+        since_flush = 0;
+        __syncthreads();
       }
-      unsigned bits = 0u;
-      unsigned n_inact = 0u;
-      if (any) {
+      since_flush += q1 - q0;
+
+#pragma unroll 1
+      for (unsigned long long c = q0 + (unsigned long long)warp * CH; c < q1; c += (unsigned long long)NW * CH) {
+        const unsigned long long first = c + (unsigned long long)lane * PPT;
+        // every load of the chunk is issued before any result is needed
+        uint8_t stv[PPT];
         uint32_t pv[PPT], idv[PPT];
         float ah[PPT], ad[PPT];
         F x[NV][PPT];
+        ld_stream<uint8_t, PPT>(S.status + first, stv);
         ld_stream<uint32_t, PPT>(S.pos + first, pv);
         ld_stream<uint32_t, PPT>(S.id + first, idv);
         if (n_out > 0) ld_stream<float, PPT>(S.age_h + first, ah);
         ld_stream<float, PPT>(S.age_d + first, ad);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          // variables the update only writes are read back solely when some
-          // slot of the vector keeps its old value
-          if (((Model::read_mask >> v) & 1u) || !all) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
-        }
-        bool st_changed = false;
+        for (int v = 0; v < NV; ++v)
+          if ((Model::read_mask >> v) & 1u) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        bool idle[PPT];
+        bool any = false, all = true;
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
-          if (!idle[k]) continue;
-          const uint32_t p0 = pv[k];
-          if (p0 >= n_c) {
-            my_err |= 1u;
-            continue;
-          }
-          uint32_t r[4];
-          philox_raw(seed, idv[k], step, 0u, r);
-          ad[k] = __fadd_rn(ad[k], dtf);
-          F rr[(Model::n_upd + 1) & ~1];
-          const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
-          F xx[NV];
+          idle[k] = (first + k < n_used) && stv[k] == kIdle;
+          any |= idle[k];
+          all &= idle[k];
+        }
+        // variables the update only writes are read solely when some slot of
+        // the vector keeps its old value
+        if (any && !all) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
-          int st;
-          if constexpr (Model::separable) {
-            F basis;
-            st = Model::update(dtF, xx, rr, basis, s_pf);
-            const long long q = quantize(basis, S.q_exp[0], my_clamp, my_err);
-            atomicAdd(&sacc[p0], (unsigned long long)q);
-          } else {
-            F ctb[NC];
-            st = Model::update_general(dtF, xx, rr, ctb, s_pf);
+          for (int v = 0; v < NV; ++v)
+            if (!((Model::read_mask >> v) & 1u)) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        }
+        unsigned bits = 0u;
+        unsigned n_inact = 0u;
+        if (any) {
+          bool st_changed = false;
 #pragma unroll
-            for (int j = 0; j < NC; ++j) {
-              const double val = __dmul_rn(S.weight, (double)ctb[j]);
-              const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
-              atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
+          for (int k = 0; k < PPT; ++k) {
+            if (!idle[k]) continue;
+            const uint32_t p0 = pv[k];
+            if (p0 >= n_c) {
+              my_err |= 1u;
+              continue;
             }
-          }
+            uint32_t r[4];
+            philox_raw(seed, idv[k], step, 0u, r);
+            ad[k] = __fadd_rn(ad[k], dtf);
+            F rr[(Model::n_upd + 1) & ~1];
+            const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
+            F xx[NV];
 #pragma unroll
-          for (int v = 0; v < NV; ++v) x[v][k] = xx[v];
-          if (st == kDivision) {
-            bits |= 1u << k;
-            S.bpos[first + k] = p0;
-            ++my_req;
-          }
-          uint32_t p = p0;
-          if (do_move) {
-            if (draw_int(r[0]) < mthr) {
-              // the reference's bisection (move_kernel.hpp L89-L101) over the
-              // {threshold, neighbour} pairs of the row; the neighbour of the
-              // answer comes with the probe that set `right`, or with the
-              // last pair, loaded ahead
-              const int x1 = (int)draw_int(r[1]);
-              const int2* row = mrow + (size_t)p0 * K;
-              int nb = __ldg(row + (K - 1)).y;
-              int left = 0, right = (int)K - 1;
-              while (left < right) {
-                const int mid = (left + right) >> 1;
-                const int2 pm = __ldg(row + mid);
-                if (x1 > pm.x) {
-                  left = mid + 1;
-                } else {
-                  right = mid;
-                  nb = pm.y;
-                }
-              }
-              p = (uint32_t)nb;
-              ++my_move;
-            }
-            pv[k] = p;
-          }
-          if (n_out > 0) {
-            ah[k] = __fadd_rn(ah[k], dtf);
-            for (unsigned o = 0; o < n_out; ++o) {
-              if (S.outlet_idx[o] == p) {
-                if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
-                  stv[k] = kExit;
-                  ah[k] = 0.0f;
-                  ++my_exit;
-                  st_changed = true;
-                }
-                break;
+            for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
+            int st;
+            if constexpr (Model::separable) {
+              F basis;
+              st = Model::update(dtF, xx, rr, basis, s_pf);
+              const long long q = quantize(basis, qe0, my_clamp, my_err);
+              atomicAdd(&sacc[p0], (unsigned long long)q);
+            } else {
+              F ctb[NC];
+              st = Model::update_general(dtF, xx, rr, ctb, s_pf);
+#pragma unroll
+              for (int j = 0; j < NC; ++j) {
+                const double val = __dmul_rn(S.weight, (double)ctb[j]);
+                const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
+                atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
               }
             }
+#pragma unroll
+            for (int v = 0; v < NV; ++v) x[v][k] = xx[v];
+            if (st == kDivision) {
+              bits |= 1u << k;
+              S.bpos[first + k] = p0;
+              ++my_req;
+            }
+            uint32_t p = p0;
+            if (do_move) {
+              if (draw_int(r[0]) < mthr) {
+                // the reference's bisection (move_kernel.hpp L89-L101) over the
+                // {threshold, neighbour} pairs of the row; the neighbour of the
+                // answer comes with the probe that set `right`, or with the
+                // last pair, loaded ahead
+                const int x1 = (int)draw_int(r[1]);
+                const int2* row = mrow + (size_t)p0 * K;
+                int nb = __ldg(row + (K - 1)).y;
+                int left = 0, right = (int)K - 1;
+                while (left < right) {
+                  const int mid = (left + right) >> 1;
+                  const int2 pm = __ldg(row + mid);
+                  if (x1 > pm.x) {
+                    left = mid + 1;
+                  } else {
+                    right = mid;
+                    nb = pm.y;
+                  }
+                }
+                p = (uint32_t)nb;
+                ++my_move;
+              }
+              pv[k] = p;
+            }
+            if (n_out > 0) {
+              ah[k] = __fadd_rn(ah[k], dtf);
+              for (unsigned o = 0; o < n_out; ++o) {
+                if (S.outlet_idx[o] == p) {
+                  if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
+                    stv[k] = kExit;
+                    ah[k] = 0.0f;
+                    ++my_exit;
+                    st_changed = true;
+                  }
+                  break;
+                }
+              }
+            }
           }
+#pragma unroll
+          for (int v = 0; v < NV; ++v) st_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+          if (do_move) st_stream<uint32_t, PPT>(S.pos + first, pv);
+          if (n_out > 0) st_stream<float, PPT>(S.age_h + first, ah);
+          st_stream<float, PPT>(S.age_d + first, ad);
+          if (st_changed) st_stream<uint8_t, PPT>(S.status + first, stv);
         }
 #pragma unroll
-        for (int v = 0; v < NV; ++v) st_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
-        if (do_move) st_stream<uint32_t, PPT>(S.pos + first, pv);
-        if (n_out > 0) st_stream<float, PPT>(S.age_h + first, ah);
-        st_stream<float, PPT>(S.age_d + first, ad);
-        if (st_changed) st_stream<uint8_t, PPT>(S.status + first, stv);
-      }
+        for (int k = 0; k < PPT; ++k) n_inact += (first + k < n_used && stv[k] != kIdle) ? 1u : 0u;
+        // birth-request bits: slot first+k -> bit (first+k) % 32 of word (first+k) / 32
+        constexpr int lanes_per_word = 32 / PPT;
+        unsigned w = bits << ((lane % lanes_per_word) * PPT);
 #pragma unroll
-      for (int k = 0; k < PPT; ++k) n_inact += (first + k < n_used && stv[k] != kIdle) ? 1u : 0u;
-      // birth-request bits: slot first+k -> bit (first+k) % 32 of word (first+k) / 32
-      constexpr int lanes_per_word = 32 / PPT;
-      unsigned w = bits << ((lane % lanes_per_word) * PPT);
-#pragma unroll
-      for (int o = 1; o < lanes_per_word; o <<= 1) w |= __shfl_xor_sync(0xffffffffu, w, o);
-      if (lane % lanes_per_word == 0) S.bmask[first >> 5] = w;
-      const unsigned nb = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));
-      const unsigned ni = __reduce_add_sync(0xffffffffu, n_inact);
-      if (lane == 0) {
-        if (nb) atomicAdd(&s_tile_births, nb);
-        if (ni) atomicAdd(&s_tile_inactive, ni);
+        for (int o = 1; o < lanes_per_word; o <<= 1) w |= __shfl_xor_sync(0xffffffffu, w, o);
+        if (lane % lanes_per_word == 0) S.bmask[first >> 5] = w;
+        const unsigned nb = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));
+        const unsigned ni = __reduce_add_sync(0xffffffffu, n_inact);
+        if (lane == 0) {
+          const unsigned t = (unsigned)(c / kTile);  // a chunk lies inside one tile
+          if (nb) atomicAdd(S.tile_births + t, nb);
+          if (ni) atomicAdd(S.tile_inactive + t, ni);
+        }
       }
-    }
-    __syncthreads();
-    if (tid == 0) {
-      S.tile_births[t] = s_tile_births;
-      S.tile_inactive[t] = s_tile_inactive;
     }
   }
+  if (cur >= 0) flush();
 }
 
 // ---------------------------------------------------------------------------

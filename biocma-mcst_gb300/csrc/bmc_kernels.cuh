@@ -22,10 +22,11 @@ constexpr int kTile = 1024;  // particles per tile (scheduling and scan unit)
 
 // Batch-wide scheduling state (device memory).
 struct BatchCtl {
-  unsigned int ticket;      // next tile handed out by k_cycle
-  unsigned int total_tiles; // tiles over all scenarios
+  unsigned int ticket;      // unused (tiles are partitioned statically)
+  unsigned int total_tiles; // allocated tiles over all scenarios
   unsigned int flags;       // work of this step after the cycle (kFlag*)
-  unsigned int pad;
+  unsigned int total_live;  // tiles holding particles this step, all scenarios
+  unsigned int* live_base;  // [n_scen]: first live tile of each scenario
 };
 constexpr unsigned kFlagDivide = 1u;   // some scenario asked for divisions
 constexpr unsigned kFlagCompact = 2u;  // some scenario compacts
@@ -171,6 +172,29 @@ __device__ __forceinline__ double fixed_to_double(long long hi, unsigned long lo
   const unsigned long long lo2 = lo & 0xffffffffull;
   const double d = __dadd_rn(__dmul_rn((double)hi2, 4294967296.0), (double)lo2);
   return __dmul_rn(d, scale_up);
+}
+
+// ------------------------------------------------------------------------
+// Scenario owning live tile g: the largest s with live_base[s] <= g (a
+// scenario without live tiles shares its base with the next one).  `hint`
+// is a scenario not after the answer (tickets grow within a block).
+__device__ __forceinline__ int scen_of_live(const unsigned* live_base, int n_scen, unsigned g, int hint) {
+  int s = hint < 0 ? 0 : hint;
+  if (s + 1 < n_scen && g >= __ldg(live_base + s + 1)) {
+    if (n_scen - s > 8) {
+      int lo = s + 1, hi = n_scen - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(live_base + mid) <= g)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+      return lo;
+    }
+    while (s + 1 < n_scen && g >= __ldg(live_base + s + 1)) ++s;
+  }
+  return s;
 }
 
 // ------------------------------------------------------------------------
