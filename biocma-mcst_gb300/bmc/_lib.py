@@ -39,6 +39,27 @@ class StepStats(ct.Structure):
         return d
 
 
+class UdfInfo(ct.Structure):
+    _fields_ = [("n_var", c_u32), ("n_ctb", c_u32), ("separable", c_i32), ("has_f32", c_i32),
+                ("has_f64", c_i32), ("n_names", c_u32), ("n_species", c_u32), ("pad", c_u32),
+                ("names", ct.c_char_p * 16), ("species", ct.c_char_p * 8)]
+
+
+RATES_FN = ct.CFUNCTYPE(None, VP, VP, VP)
+UPDATE_FN = ct.CFUNCTYPE(c_i32, c_dbl, VP, VP, VP, VP)
+COEF_FN = ct.CFUNCTYPE(c_dbl, VP, c_i32)
+DIVISION_FN = ct.CFUNCTYPE(None, VP, VP, VP, VP)
+INIT_FN = ct.CFUNCTYPE(None, VP, VP, VP)
+MASS_FN = ct.CFUNCTYPE(c_dbl, VP, VP)
+
+
+class UdfHostModel(ct.Structure):
+    """bmc_udf_host_model: the model's functions compiled for the CPU."""
+    _fields_ = [("n_var", c_u32), ("n_ctb", c_u32), ("n_rates", c_u32), ("separable", c_i32),
+                ("rates", VP), ("update", VP), ("coef", VP), ("division", VP), ("init", VP),
+                ("mass", VP)]
+
+
 class BmcError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"libbmc error {code}: {msg}")
@@ -84,6 +105,9 @@ SIGNATURES = {
     "bmc_run_timed": [VP, c_dbl, c_u32, VP, VP],
     "bmc_set_device": [c_i32],
     "bmc_transfer_bytes": [VP, VP],
+    "bmc_udf_load": [ct.c_char_p, VP],
+    "bmc_udf_get_info": [c_i32, VP],
+    "bmc_udf_get_host_model": [c_i32, c_i32, VP],
 }
 
 

@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libbmc.so")
 SOURCES = ["bmc_kernels.cu", "bmc_api.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-O3"]
+         "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:
@@ -58,7 +58,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB + ".tmp"
-    cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    cmd = [nv, *ARCH, "--cudart", "shared", "-shared", "-o", tmp, *objs, "-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -36,6 +36,7 @@ class ModelSpec:
     value_bound: np.ndarray
     separable: bool = True
     read_vars: int = 2  # state variables the update reads (the others are outputs)
+    udf_path: str | None = None  # model library (runtime-loaded model) it comes from
 
     @property
     def itemsize(self) -> int:

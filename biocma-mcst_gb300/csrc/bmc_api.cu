@@ -6,6 +6,7 @@
 // probabilities on the device, outlet thresholds exp(-dt F / V) on the
 // host), the step sequence and its CUDA graph, readback.
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <algorithm>
 #include <array>
@@ -13,6 +14,7 @@
 #include <mutex>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -81,6 +83,15 @@ int ceil_log2(double v) {
   int ex = 0;
   const double m = std::frexp(v, &ex);
   return m == 0.5 ? ex - 1 : ex;
+}
+
+// Launch status of the kernels a set just enqueued: this module's runtime
+// error state and that of the module owning the kernels (a plugin may carry
+// its own copy of the runtime).
+cudaError_t launch_status(const bmc::KernelSet* ks) {
+  const cudaError_t own = cudaGetLastError();
+  const cudaError_t mod = (cudaError_t)ks->last_error();
+  return own != cudaSuccess ? own : mod;
 }
 
 }  // namespace
@@ -174,7 +185,7 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
   if (launch_pmove) {
     s->ks->move_thr(1, s->stream, s->d_desc);
     g_launches++;
-    BMC_CUDA(cudaGetLastError());
+    BMC_CUDA(launch_status(s->ks));
   }
   return BMC_OK;
 }
@@ -183,13 +194,10 @@ size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(un
 
 int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t smem, int sm_count,
                   unsigned* grid_out) {
-  const void* fn = ks->cycle_fn[variant];
-  const unsigned threads = bmc::kVariantThreads[variant];
   if (smem > 227 * 1024)
     return fail(BMC_E_UNSUPPORTED, "n_compartments * n_contributions too large for the shared accumulator");
-  BMC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int bps = 0;
-  BMC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, fn, (int)threads, smem));
+  BMC_CUDA((cudaError_t)ks->cycle_setup[variant](smem, &bps));
   if (bps < 1) return fail(BMC_E_UNSUPPORTED, "cycle kernel cannot be resident with this shape");
   if (bps_req > 0) bps = std::min<int>(bps, (int)bps_req);
   *grid_out = (unsigned)(sm_count * bps);
@@ -212,7 +220,7 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
   ks->merge(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
   g_launches += 6;
-  BMC_CUDA(cudaGetLastError());
+  BMC_CUDA(launch_status(ks));
   return BMC_OK;
 }
 
@@ -637,7 +645,7 @@ int bmc_init_particles(bmc_scenario* s, uint64_t n, int32_t uniform_init, double
   s->ks->init(dim3(s->sm_count * 8), s->stream, s->d_desc, n, 0u, span, d_mass);
   g_launches++;
   std::vector<double> mass(n);
-  cudaError_t e = cudaGetLastError();
+  cudaError_t e = launch_status(s->ks);
   if (e == cudaSuccess) e = counted_memcpy_async(mass.data(), d_mass, n * 8, cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   cudaFree(d_mass);
@@ -1017,7 +1025,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
     b->ks->move_thr(n, b->stream, b->d_table);
     g_launches++;
-    BMC_CUDA(cudaGetLastError());
+    BMC_CUDA(launch_status(b->ks));
     b->dt = dt;
     b->total_tiles = tiles;
   }
@@ -1087,7 +1095,7 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   s->ks->merge(dim3(s->sm_count * 2), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[6], st));
   g_launches += 6;
-  BMC_CUDA(cudaGetLastError());
+  BMC_CUDA(launch_status(s->ks));
   rc = read_ctl(s, stats);
   for (int k = 0; k < 6 && kernel_ms; ++k) cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]);
   for (auto& e : ev) cudaEventDestroy(e);
@@ -1110,6 +1118,153 @@ int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t ste
   cudaFree(d_ids);
   if (d_out) cudaFree(d_out);
   if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug draws: ") + cudaGetErrorString(e));
+  return BMC_OK;
+}
+
+}  // extern "C"
+
+// ---- runtime-loaded cell models ------------------------------------------------
+// Reference: UnsafeUDF::Loader::init_lib (apps/libs/models/ext/udf_includes.cpp
+// L58-L78) binds a module's init/update/division/mass/names/... symbols;
+// Unsafe::load_udf (apps/api/src/udf_handle.cpp L22-L38) takes the path from
+// BIOMC_LIB_UDF.  Here a plugin exports its kernel sets (one per precision)
+// and host entry points; a set is copied into the registry under the id the
+// plugin receives.  Plugins stay loaded until exit: scenarios and graphs
+// hold their launch functions.
+
+namespace {
+
+struct UdfEntry {
+  int32_t id = 0;
+  std::string path;
+  void* handle = nullptr;
+  bmc::KernelSet sets[2]{};  // [f64]
+  bool has[2] = {false, false};
+  bmc_udf_info info{};
+  int (*host_model)(int32_t, bmc_udf_host_model*) = nullptr;
+};
+
+std::mutex g_udf_mu;
+std::vector<UdfEntry*> g_udfs;  // never freed (see above)
+
+UdfEntry* find_udf(int32_t id) {
+  for (UdfEntry* e : g_udfs)
+    if (e->id == id) return e;
+  return nullptr;
+}
+
+}  // namespace
+
+namespace bmc {
+const KernelSet* udf_kernel_set(int model, int f64) {
+  std::lock_guard<std::mutex> lk(g_udf_mu);
+  UdfEntry* e = find_udf(model);
+  if (!e || !e->has[f64 ? 1 : 0]) return nullptr;
+  return &e->sets[f64 ? 1 : 0];
+}
+}  // namespace bmc
+
+extern "C" {
+
+int bmc_udf_load(const char* path, int32_t* model_id) {
+  if (!model_id) return fail(BMC_E_INVALID, "model_id is null");
+  std::string p;
+  if (path) {
+    p = path;
+  } else {
+    const char* env = std::getenv("BIOMC_LIB_UDF");
+    if (!env) return fail(BMC_E_INVALID, "var BIOMC_LIB_UDF not found");
+    p = env;
+  }
+  std::lock_guard<std::mutex> lk(g_udf_mu);
+  for (UdfEntry* e : g_udfs)
+    if (e->path == p) {
+      *model_id = e->id;
+      return BMC_OK;
+    }
+  void* h = dlopen(p.c_str(), RTLD_NOW | RTLD_LOCAL);
+  if (!h) {
+    const char* why = dlerror();
+    return fail(BMC_E_INVALID, std::string("cannot load model library: ") + (why ? why : p));
+  }
+  using AbiFn = int (*)();
+  using SetFn = const void* (*)(int32_t);
+  using SizeFn = size_t (*)();
+  using IntFn = int32_t (*)();
+  using NamesFn = const char* const* (*)(uint32_t*);
+  using HostFn = int (*)(int32_t, bmc_udf_host_model*);
+  auto abi = reinterpret_cast<AbiFn>(dlsym(h, "bmc_udf_abi"));
+  auto kset = reinterpret_cast<SetFn>(dlsym(h, "bmc_udf_kernel_set"));
+  auto nvar = reinterpret_cast<SizeFn>(dlsym(h, "set_nvar_udf"));
+  auto nc = reinterpret_cast<SizeFn>(dlsym(h, "set_nc_udf"));
+  auto sep = reinterpret_cast<IntFn>(dlsym(h, "separable_udf"));
+  auto names = reinterpret_cast<NamesFn>(dlsym(h, "names_udf"));
+  auto species = reinterpret_cast<NamesFn>(dlsym(h, "species_udf"));
+  auto host = reinterpret_cast<HostFn>(dlsym(h, "host_model_udf"));
+  if (!abi || !kset || !nvar || !nc || !sep || !names || !host) {
+    dlclose(h);
+    return fail(BMC_E_INVALID, "not a model library (missing bmc_udf_* / *_udf symbols): " + p);
+  }
+  if (abi() != bmc::kKernelSetAbi) {
+    dlclose(h);
+    return fail(BMC_E_UNSUPPORTED, "model library built against another KernelSet layout: " + p);
+  }
+  auto* e = new UdfEntry();
+  e->id = BMC_MODEL_UDF_FIRST + (int32_t)g_udfs.size();
+  e->path = p;
+  e->handle = h;
+  e->host_model = host;
+  for (int f = 0; f < 2; ++f) {
+    const auto* ks = static_cast<const bmc::KernelSet*>(kset(f));
+    if (!ks) continue;
+    if (ks->abi != bmc::kKernelSetAbi || ks->f64 != (f == 1) || ks->n_var != (int)nvar() ||
+        ks->n_ctb != (int)nc()) {
+      delete e;
+      dlclose(h);
+      return fail(BMC_E_UNSUPPORTED, "inconsistent kernel set in model library: " + p);
+    }
+    e->sets[f] = *ks;
+    e->sets[f].model = e->id;
+    e->has[f] = true;
+  }
+  if (!e->has[0] && !e->has[1]) {
+    delete e;
+    dlclose(h);
+    return fail(BMC_E_UNSUPPORTED, "model library has no kernel set: " + p);
+  }
+  bmc_udf_info& in = e->info;
+  in.n_var = (uint32_t)nvar();
+  in.n_ctb = (uint32_t)nc();
+  in.separable = sep();
+  in.has_f32 = e->has[0] ? 1 : 0;
+  in.has_f64 = e->has[1] ? 1 : 0;
+  uint32_t n = 0;
+  const char* const* v = names(&n);
+  in.n_names = std::min<uint32_t>(n, 16);
+  for (uint32_t k = 0; k < in.n_names; ++k) in.names[k] = v[k];
+  v = species(&n);
+  in.n_species = std::min<uint32_t>(n, 8);
+  for (uint32_t k = 0; k < in.n_species; ++k) in.species[k] = v[k];
+  g_udfs.push_back(e);
+  *model_id = e->id;
+  return BMC_OK;
+}
+
+int bmc_udf_get_info(int32_t model_id, bmc_udf_info* info) {
+  if (!info) return fail(BMC_E_INVALID, "info is null");
+  std::lock_guard<std::mutex> lk(g_udf_mu);
+  UdfEntry* e = find_udf(model_id);
+  if (!e) return fail(BMC_E_INVALID, "no model library loaded under this id");
+  *info = e->info;
+  return BMC_OK;
+}
+
+int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* out) {
+  if (!out) return fail(BMC_E_INVALID, "out is null");
+  std::lock_guard<std::mutex> lk(g_udf_mu);
+  UdfEntry* e = find_udf(model_id);
+  if (!e) return fail(BMC_E_INVALID, "no model library loaded under this id");
+  if (e->host_model(f64 ? 1 : 0, out) != 0) return fail(BMC_E_UNSUPPORTED, "precision not compiled in the model library");
   return BMC_OK;
 }
 

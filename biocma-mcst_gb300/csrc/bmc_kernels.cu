@@ -1,868 +1,11 @@
-// bmc_kernels.cu -- kernels of the Monte Carlo cycle and their launchers.
-//
-// Reference behaviour (BioCMA-MCST paths):
-//   model + division request   apps/libs/simulation/public/simulation/kernels/
-//                              model_kernel.hpp L164-L268
-//   contribution scatter       contribution_kernel.hpp L146-L186
-//   move                       move_kernel.hpp L62-L103, L393-L437
-//   exit                       move_kernel.hpp L348-L359, L588-L648
-//   leave tests                apps/libs/simulation/public/simulation/
-//                              probability_leaving.hpp L18-L35
-//   division / compaction /    apps/libs/mc/public/mc/particles_container.hpp
-//   merge                      L541-L600, L737-L795
-//   liquid step                apps/libs/simulation/src/implScalar.cpp L251
-//   feeds                      apps/libs/simulation/src/simulation.model.cpp L73
+// bmc_kernels.cu -- the built-in model plugins' kernel sets and the
+// model-independent kernels (repartition, draw dump).
 #include <cstdio>
 
-#include "bmc_kernels.cuh"
-#include "bmc_launch.h"
+#include "bmc_kernel_templates.cuh"
 
 namespace bmc {
 
-// ---------------------------------------------------------------------------
-// k_liquid: one thread per (compartment j, species s) entry; a block holds
-// 256 / n_species whole compartments (grid x over compartment chunks, grid
-// y over scenarios).  Feeds into sources and sink, explicit Euler step
-//   M(j,s) += dt (sum_i C(i,s) T(i,j) - C(j,s) sink(j) + src(j,s)),
-//   C'(j,s) = M(j,s) / V(j),
-// then Model::rates of each compartment of the block from C'(j,:) into its
-// compartment record.  C is double-buffered by step parity (C' goes to the
-// other buffer), so no block waits for another.  With do_scalar == 0 only
-// the rates (and C carried to the next buffer).  Block (0, s) resets the
-// step counters of scenario s; block (0, 0) the tile scheduler and flags.
-template <class Model, class F>
-__global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
-  const ScenDev& S = sc[blockIdx.y];
-  Control* ctl = S.ctl;
-  __shared__ double cs[256];
-  __shared__ double red[2][kMaxSpecies];
-  if (blockIdx.x == 0 && blockIdx.y == 0) {
-    // live tiles of every scenario (ceil(n_used / 1024), none once finished)
-    // and their prefix: the cycle hands out only tiles that hold particles
-    __shared__ unsigned sh[33];
-    const int n_scen = (int)gridDim.y;
-    unsigned run = 0;
-    for (int b0 = 0; b0 < n_scen; b0 += (int)blockDim.x) {
-      const int s2 = b0 + (int)threadIdx.x;
-      unsigned live = 0;
-      if (s2 < n_scen) {
-        const ScenDev& P = sc[s2];
-        if (!scen_finished(P, P.ctl)) {
-          const unsigned long long lt = (P.ctl->n_used + kTile - 1) / kTile;
-          live = (unsigned)(lt < P.n_tiles ? lt : P.n_tiles);
-        }
-      }
-      unsigned tot;
-      const unsigned pre = block_exscan_u32(live, sh, &tot);
-      if (s2 < n_scen) bctl->live_base[s2] = run + pre;
-      run += tot;
-    }
-    if (threadIdx.x == 0) {
-      bctl->live_base[n_scen] = run;
-      bctl->total_live = run;
-      bctl->ticket = 0u;
-      bctl->flags = 0u;
-    }
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctl->req_div = 0ull;
-    ctl->exits = 0ull;
-    ctl->moves = 0ull;
-  }
-  {
-    // per-tile birth / inactive counters of this step start at zero (the
-    // cycle's warps add to them)
-    const unsigned long long lt = (ctl->n_used + kTile - 1) / kTile;
-    const unsigned n_live = (unsigned)(lt < S.n_tiles ? lt : S.n_tiles);
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n_live; t += gridDim.x * blockDim.x) {
-      S.tile_births[t] = 0u;
-      S.tile_inactive[t] = 0u;
-    }
-  }
-  const unsigned nsp = S.n_s;
-  const unsigned cb = 256u / nsp;  // compartments per block
-  const unsigned j0 = blockIdx.x * cb;
-  if (j0 >= S.n_c || scen_finished(S, ctl)) return;
-  const unsigned t = threadIdx.x;
-  const unsigned jl = t / nsp;
-  const unsigned sp = t - jl * nsp;
-  const unsigned j = j0 + jl;
-  const bool active = jl < cb && j < S.n_c;
-  const size_t ne = (size_t)S.n_c * nsp;
-  const unsigned parity = ctl->step & 1u;
-  const double* __restrict__ Cold = S.C + parity * ne;
-  double* __restrict__ Cnew = S.C + (parity ^ 1u) * ne;
-  if (t < 2 * kMaxSpecies) red[t / kMaxSpecies][t % kMaxSpecies] = 0.0;
-  __syncthreads();
-  if (active) {
-    const size_t e = (size_t)j * nsp + sp;
-    double cn;
-    if (!do_scalar) {
-      cn = Cold[e];
-    } else {
-      const double dt = S.dt;
-      double srcv = S.src[e];
-      double sinkj = 0.0;
-      for (unsigned f = 0; f < S.n_feeds; ++f) {
-        if (S.feed_in[f] == j) {
-          const double cf = S.feed_conc[f * kMaxSpecies + sp];
-          if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
-        }
-        if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
-      }
-      S.src[e] = srcv;
-      double acc = 0.0;
-      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
-      for (unsigned q = e0; q < e1; ++q)
-        acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
-      const double cj = Cold[e];
-      acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
-      const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
-      const double mold = S.M[e];
-      const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
-      S.M[e] = mnew;
-      cn = __dmul_rn(mnew, S.vinv[j]);
-      // mass-balance sums (diagnostic): new mass, expected mass
-      atomicAdd(&red[0][sp], mnew);
-      atomicAdd(&red[1][sp], mold + dt * (srcv - cj * sinkj));
-    }
-    Cnew[e] = cn;
-    cs[t] = cn;
-  }
-  __syncthreads();
-  if (t < cb && j0 + t < S.n_c) {
-    F r[kMaxRates];
-    Model::rates(cs + t * nsp, S.params, r);
-    F* rec = reinterpret_cast<F*>(S.crec) + (size_t)(j0 + t) * 8;
-#pragma unroll
-    for (int k = 0; k < Model::n_rates; ++k) rec[k] = r[k];
-  }
-  if (do_scalar && t < nsp) {
-    atomicAdd(&ctl->mb_new[t], red[0][t]);
-    atomicAdd(&ctl->mb_exp[t], red[1][t]);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Quantisation of a value to the accumulator's fixed point: the nearest
-// integer multiple of 2^e (ties to even), clamped to |q| <= 2^42.  Done on
-// the integer pipe from the IEEE fields of v, so no FP64 instruction is
-// spent per particle; the result equals rint(v * 2^-e) evaluated in double.
-template <int MBITS, int EBITS, int BIAS, class U>
-__device__ __forceinline__ long long quantize_bits(U bits, int e, unsigned long long& clamped, unsigned& err) {
-  const bool neg = (bits >> (MBITS + EBITS)) & 1u;
-  const int ex = (int)((bits >> MBITS) & (((U)1 << EBITS) - 1));
-  const unsigned long long mant = (unsigned long long)(bits & (((U)1 << MBITS) - 1));
-  long long q;
-  if (ex == 0) {
-    q = 0;  // zero or subnormal: far below any quantum in use
-  } else if (ex == (1 << EBITS) - 1) {
-    q = kQMax;  // inf / nan
-    ++clamped;
-    err |= 2u;
-  } else {
-    const unsigned long long m = mant | (1ull << MBITS);  // value = m * 2^(ex - BIAS - MBITS)
-    const int sh = ex - BIAS - MBITS - e;                  // value / 2^e = m * 2^sh
-    if (sh >= 0) {
-      q = sh > 62 - MBITS ? kQMax + 1 : (long long)(m << sh);
-    } else {
-      const int r = -sh;
-      if (r > MBITS + 1) {
-        q = 0;  // below half a quantum
-      } else {
-        const unsigned long long t = m >> r;
-        const unsigned long long rem = m & ((1ull << r) - 1ull);
-        const unsigned long long half = 1ull << (r - 1);
-        q = (long long)(t + ((rem > half || (rem == half && (t & 1ull))) ? 1ull : 0ull));
-      }
-    }
-    if (q > kQMax) {
-      q = kQMax;
-      ++clamped;
-      err |= 2u;
-    }
-  }
-  return neg ? -q : q;
-}
-
-__device__ __forceinline__ long long quantize(double v, int e, unsigned long long& clamped, unsigned& err) {
-  return quantize_bits<52, 11, 1023>((unsigned long long)__double_as_longlong(v), e, clamped, err);
-}
-__device__ __forceinline__ long long quantize(float v, int e, unsigned long long& clamped, unsigned& err) {
-  return quantize_bits<23, 8, 127>((unsigned)__float_as_uint(v), e, clamped, err);
-}
-
-// Move threshold stored in slot 7 of a compartment record.
-__device__ __forceinline__ uint32_t rec_move_thr(float v) { return __float_as_uint(v); }
-__device__ __forceinline__ uint32_t rec_move_thr(double v) { return (uint32_t)__double_as_longlong(v); }
-
-// Loads the first NU slots of a compartment record (vector loads through
-// the read-only path) and its move threshold (slot 7, same 32-byte sector
-// for float records).
-template <int NU, class F>
-__device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
-  if constexpr (sizeof(F) == 4) {
-    if constexpr (NU > 2) {
-      const float4 a = __ldg(reinterpret_cast<const float4*>(p));
-      out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
-    } else {
-      const float2 a = __ldg(reinterpret_cast<const float2*>(p));
-      out[0] = a.x; out[1] = a.y;
-    }
-    static_assert(NU <= 4, "float records: update may read at most 4 rates");
-  } else {
-#pragma unroll
-    for (int k = 0; k < (NU + 1) / 2; ++k) {
-      const double2 a = __ldg(reinterpret_cast<const double2*>(p) + k);
-      out[2 * k] = a.x;
-      out[2 * k + 1] = a.y;
-    }
-  }
-  return rec_move_thr(__ldg(p + 7));
-}
-
-// ---------------------------------------------------------------------------
-// k_cycle: the fused per-particle hot path.  Each block of a persistent
-// grid streams a contiguous run of the live tiles (1024-slot tiles that hold
-// particles, ordered scenario after scenario; k_liquid lists them).  For
-// each Idle particle (draws: one Philox block, integers
-// x_k = (r_k >> 8) | 1 with u_k = x_k 2^-24):
-//   ages(i,1) += dt; Model::update(dt, x, rates(pos))
-//   contribution basis (or contributions) -> shared-memory fixed-point
-//     accumulator of the pre-move compartment (exact integer sums)
-//   move:  leave iff x_0 < ceil(2^24 dt Q/V)       (<=> dt Q / V > u_0)
-//          next = first k with x_1 <= floor(2^24 CDF(pos,k))
-//                                                  (<=> u_1 <= CDF(pos,k))
-//   exit:  ages(i,0) += dt; leave the reactor iff x_2 > floor(2^24 e^{-dt F/V})
-//                                                  (<=> dt F > -ln(u_2) V)
-// A division request sets a bit of the tile's birth mask; the division
-// itself runs in k_divide once the slot-order ranks are known.
-// Launch variants: THREADS per block, PPT consecutive particles per thread
-// (THREADS * PPT divides the 1024-slot tile) and MINB resident blocks per SM
-// the register budget is cut for.
-template <class Model, class F, int PPT, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB)
-    k_cycle(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
-  extern __shared__ unsigned long long sacc[];
-  __shared__ unsigned long long s_cnt[5];
-  __shared__ F s_pf[16];  // parameters of the current scenario, as F
-  constexpr int NV = Model::n_var;
-  constexpr int NC = Model::n_ctb;
-  constexpr int NA = Model::separable ? 1 : NC;  // accumulator columns
-  constexpr unsigned CH = 32u * PPT;             // slots per warp chunk
-  constexpr unsigned NW = THREADS / 32;
-  const int tid = threadIdx.x;
-  const int lane = tid & 31;
-  const unsigned warp = (unsigned)tid >> 5;
-  const unsigned total = bctl->total_live;
-  const unsigned* live_base = bctl->live_base;
-  int cur = -1;
-  unsigned long long since_flush = 0;
-  unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
-  unsigned my_err = 0;
-
-  // flush the accumulator and the counters of scenario `cur` (whole block)
-  auto flush = [&]() {
-    __syncthreads();
-    const ScenDev& P = sc[cur];
-    const unsigned n_ent = P.n_c * NA;
-    for (unsigned e = tid; e < n_ent; e += THREADS) {
-      const long long p = (long long)sacc[e];
-      if (p != 0) {
-        atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
-        atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
-      }
-    }
-    if (tid < 5) s_cnt[tid] = 0ull;
-    __syncthreads();
-    const unsigned long long r0 = warp_sum_u64(my_req), r1 = warp_sum_u64(my_exit);
-    const unsigned long long r2 = warp_sum_u64(my_move), r3 = warp_sum_u64(my_clamp);
-    unsigned e4 = my_err;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) e4 |= __shfl_xor_sync(0xffffffffu, e4, o);
-    if (lane == 0) {
-      atomicAdd(&s_cnt[0], r0);
-      atomicAdd(&s_cnt[1], r1);
-      atomicAdd(&s_cnt[2], r2);
-      atomicAdd(&s_cnt[3], r3);
-      atomicOr(reinterpret_cast<unsigned*>(&s_cnt[4]), e4);
-    }
-    __syncthreads();
-    if (tid == 0) {
-      Control* c = P.ctl;
-      if (s_cnt[0]) atomicAdd(&c->req_div, s_cnt[0]);
-      if (s_cnt[1]) atomicAdd(&c->exits, s_cnt[1]);
-      if (s_cnt[2]) atomicAdd(&c->moves, s_cnt[2]);
-      if (s_cnt[3]) atomicAdd(&c->clamped, s_cnt[3]);
-      const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
-      if (ev) atomicOr(&c->error, ev);
-    }
-    my_req = my_exit = my_move = my_clamp = 0ull;
-    my_err = 0u;
-  };
-
-  // static partition: block b streams the live tiles [g_begin, g_end), a
-  // contiguous run, scenario segment after scenario segment; inside a
-  // segment every warp streams its own 32*PPT-slot chunks with no block
-  // barrier, so warps drift apart and hide each other's latency
-  const unsigned g_begin = (unsigned)(((unsigned long long)total * blockIdx.x) / gridDim.x);
-  const unsigned g_end = (unsigned)(((unsigned long long)total * (blockIdx.x + 1)) / gridDim.x);
-  unsigned g = g_begin;
-  while (g < g_end) {
-    const int s = scen_of_live(live_base, n_scen, g, cur);
-    const unsigned sb = __ldg(live_base + s), se = __ldg(live_base + s + 1);
-    const unsigned ge = se < g_end ? se : g_end;
-    const ScenDev& S = sc[s];
-    const unsigned long long n_used = S.ctl->n_used;
-    const unsigned long long p_lo = (unsigned long long)(g - sb) * kTile;
-    unsigned long long p_hi = (unsigned long long)(ge - sb) * kTile;
-    if (p_hi > n_used) p_hi = n_used;
-    g = ge;
-
-    const unsigned long long cap = S.cap;
-    const unsigned n_c = S.n_c, K = S.K;
-    const unsigned step = S.ctl->step;
-    const unsigned long long seed = S.seed;
-    const double dt = S.dt;
-    const F dtF = (F)dt;
-    const float dtf = (float)dt;
-    const bool do_move = n_c > 1;
-    const unsigned n_out = S.n_outlets;
-    const int qe0 = S.q_exp[0];
-    const F* __restrict__ crec = reinterpret_cast<const F*>(S.crec);
-    const int2* __restrict__ mrow = S.mrow;
-    F* __restrict__ state = reinterpret_cast<F*>(S.state);
-
-    for (unsigned long long q0 = p_lo; q0 < p_hi; q0 += kFlushParticles) {
-      const unsigned long long q1 = q0 + kFlushParticles < p_hi ? q0 + kFlushParticles : p_hi;
-      if (s != cur || since_flush + (q1 - q0) > kFlushParticles) {
-        if (cur >= 0) flush();
-        __syncthreads();
-        const unsigned n_ent = S.n_c * NA;
-        for (unsigned e = tid; e < n_ent; e += THREADS) sacc[e] = 0ull;
-        if (tid < 16) s_pf[tid] = (F)S.params[tid];
-        cur = s;
-        since_flush = 0;
-        __syncthreads();
-      }
-      since_flush += q1 - q0;
-
-#pragma unroll 1
-      for (unsigned long long c = q0 + (unsigned long long)warp * CH; c < q1; c += (unsigned long long)NW * CH) {
-        const unsigned long long first = c + (unsigned long long)lane * PPT;
-        // every load of the chunk is issued before any result is needed
-        uint8_t stv[PPT];
-        uint32_t pv[PPT], idv[PPT];
-        float ah[PPT], ad[PPT];
-        F x[NV][PPT];
-        ld_stream<uint8_t, PPT>(S.status + first, stv);
-        ld_stream<uint32_t, PPT>(S.pos + first, pv);
-        ld_stream<uint32_t, PPT>(S.id + first, idv);
-        if (n_out > 0) ld_stream<float, PPT>(S.age_h + first, ah);
-        ld_stream<float, PPT>(S.age_d + first, ad);
-#pragma unroll
-        for (int v = 0; v < NV; ++v)
-          if ((Model::read_mask >> v) & 1u) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
-        bool idle[PPT];
-        bool any = false, all = true;
-#pragma unroll
-        for (int k = 0; k < PPT; ++k) {
-          idle[k] = (first + k < n_used) && stv[k] == kIdle;
-          any |= idle[k];
-          all &= idle[k];
-        }
-        // variables the update only writes are read solely when some slot of
-        // the vector keeps its old value
-        if (any && !all) {
-#pragma unroll
-          for (int v = 0; v < NV; ++v)
-            if (!((Model::read_mask >> v) & 1u)) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
-        }
-        unsigned bits = 0u;
-        unsigned n_inact = 0u;
-        if (any) {
-          bool st_changed = false;
-#pragma unroll
-          for (int k = 0; k < PPT; ++k) {
-            if (!idle[k]) continue;
-            const uint32_t p0 = pv[k];
-            if (p0 >= n_c) {
-              my_err |= 1u;
-              continue;
-            }
-            uint32_t r[4];
-            philox_raw(seed, idv[k], step, 0u, r);
-            ad[k] = __fadd_rn(ad[k], dtf);
-            F rr[(Model::n_upd + 1) & ~1];
-            const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
-            F xx[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) xx[v] = x[v][k];
-            int st;
-            if constexpr (Model::separable) {
-              F basis;
-              st = Model::update(dtF, xx, rr, basis, s_pf);
-              const long long q = quantize(basis, qe0, my_clamp, my_err);
-              atomicAdd(&sacc[p0], (unsigned long long)q);
-            } else {
-              F ctb[NC];
-              st = Model::update_general(dtF, xx, rr, ctb, s_pf);
-#pragma unroll
-              for (int j = 0; j < NC; ++j) {
-                const double val = __dmul_rn(S.weight, (double)ctb[j]);
-                const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
-                atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
-              }
-            }
-#pragma unroll
-            for (int v = 0; v < NV; ++v) x[v][k] = xx[v];
-            if (st == kDivision) {
-              bits |= 1u << k;
-              S.bpos[first + k] = p0;
-              ++my_req;
-            }
-            uint32_t p = p0;
-            if (do_move) {
-              if (draw_int(r[0]) < mthr) {
-                // the reference's bisection (move_kernel.hpp L89-L101) over the
-                // {threshold, neighbour} pairs of the row; the neighbour of the
-                // answer comes with the probe that set `right`, or with the
-                // last pair, loaded ahead
-                const int x1 = (int)draw_int(r[1]);
-                const int2* row = mrow + (size_t)p0 * K;
-                int nb = __ldg(row + (K - 1)).y;
-                int left = 0, right = (int)K - 1;
-                while (left < right) {
-                  const int mid = (left + right) >> 1;
-                  const int2 pm = __ldg(row + mid);
-                  if (x1 > pm.x) {
-                    left = mid + 1;
-                  } else {
-                    right = mid;
-                    nb = pm.y;
-                  }
-                }
-                p = (uint32_t)nb;
-                ++my_move;
-              }
-              pv[k] = p;
-            }
-            if (n_out > 0) {
-              ah[k] = __fadd_rn(ah[k], dtf);
-              for (unsigned o = 0; o < n_out; ++o) {
-                if (S.outlet_idx[o] == p) {
-                  if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
-                    stv[k] = kExit;
-                    ah[k] = 0.0f;
-                    ++my_exit;
-                    st_changed = true;
-                  }
-                  break;
-                }
-              }
-            }
-          }
-#pragma unroll
-          for (int v = 0; v < NV; ++v) st_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
-          if (do_move) st_stream<uint32_t, PPT>(S.pos + first, pv);
-          if (n_out > 0) st_stream<float, PPT>(S.age_h + first, ah);
-          st_stream<float, PPT>(S.age_d + first, ad);
-          if (st_changed) st_stream<uint8_t, PPT>(S.status + first, stv);
-        }
-#pragma unroll
-        for (int k = 0; k < PPT; ++k) n_inact += (first + k < n_used && stv[k] != kIdle) ? 1u : 0u;
-        // birth-request bits: slot first+k -> bit (first+k) % 32 of word (first+k) / 32
-        constexpr int lanes_per_word = 32 / PPT;
-        unsigned w = bits << ((lane % lanes_per_word) * PPT);
-#pragma unroll
-        for (int o = 1; o < lanes_per_word; o <<= 1) w |= __shfl_xor_sync(0xffffffffu, w, o);
-        if (lane % lanes_per_word == 0) S.bmask[first >> 5] = w;
-        const unsigned nb = __reduce_add_sync(0xffffffffu, (unsigned)__popc(bits));
-        const unsigned ni = __reduce_add_sync(0xffffffffu, n_inact);
-        if (lane == 0) {
-          const unsigned t = (unsigned)(c / kTile);  // a chunk lies inside one tile
-          if (nb) atomicAdd(S.tile_births + t, nb);
-          if (ni) atomicAdd(S.tile_inactive + t, ni);
-        }
-      }
-    }
-  }
-  if (cur >= 0) flush();
-}
-
-// ---------------------------------------------------------------------------
-// k_plan: per scenario (one block of 1024 threads):
-//  1. exact accumulator totals -> sources: for a separable model
-//     src(j, s) = (w * coef_s(rates_j)) * B_j with B_j the basis total of
-//     compartment j; for a general model src(j, s) = total of w * ctb_s;
-//     accumulators cleared;
-//  2. post_cycle decisions: inactive += exits; compaction iff inactive >
-//     max(min_removal, n * ratio) (update_and_remove_inactive); room for
-//     births = capacity - live particles after compaction;
-//  3. scans of the per-tile counters (birth ranks, gap ranks ascending,
-//     source ranks from the end);
-//  4. control block advanced to the state after the step.
-template <class Model, class F>
-__global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCtl* __restrict__ bctl) {
-  const ScenDev& S = sc[blockIdx.x];
-  Control* ctl = S.ctl;
-  const int tid = threadIdx.x;
-  __shared__ unsigned long long sh64[33];
-  __shared__ unsigned long long p_n, p_req, p_rm, p_after;
-  __shared__ int p_compact;
-  if (scen_finished(S, ctl)) {
-    // nothing ran for this scenario: leave its state and a no-op plan
-    if (tid == 0) {
-      ctl->plan_births = 0ull;
-      ctl->plan_overflow = 0ull;
-      ctl->plan_compact = 0u;
-      ctl->plan_to_remove = 0ull;
-      ctl->plan_gaps = 0ull;
-      ctl->plan_n_old = ctl->n_used;
-      ctl->plan_n_after = ctl->n_used;
-    }
-    return;
-  }
-
-  const unsigned nsp = S.n_s;
-  const unsigned n_e = S.n_c * nsp;
-  const F* rates = reinterpret_cast<const F*>(S.crec);
-  if (tid < (int)nsp && tid < kMaxSpecies) {
-    const double a = ctl->mb_new[tid], b = ctl->mb_exp[tid];
-    const double den = fabs(a) > 1e-300 ? fabs(a) : 1e-300;
-    ctl->mass_balance[tid] = fabs(a - b) / den;
-    ctl->mb_new[tid] = 0.0;
-    ctl->mb_exp[tid] = 0.0;
-  }
-  if constexpr (Model::separable) {
-    for (unsigned j = tid; j < S.n_c; j += blockDim.x) {
-      const double B = fixed_to_double(S.acc_hi[j], S.acc_lo[j], S.q_scale_up[0]);
-      S.acc_hi[j] = 0;
-      S.acc_lo[j] = 0ull;
-      const F* rr = rates + (size_t)j * 8;
-      for (unsigned sp = 0; sp < nsp; ++sp) {
-        double v = 0.0;
-        if (sp < (unsigned)Model::n_ctb) v = __dmul_rn(__dmul_rn(S.weight, (double)Model::coef(rr, (int)sp)), B);
-        S.src[(size_t)j * nsp + sp] = v;
-      }
-    }
-  } else {
-    const unsigned nc = Model::n_ctb;
-    for (unsigned e = tid; e < n_e; e += blockDim.x) {
-      const unsigned j = e / nsp;
-      const unsigned sp = e - j * nsp;
-      double v = 0.0;
-      if (sp < nc) {
-        const unsigned idx = j * nc + sp;
-        v = fixed_to_double(S.acc_hi[idx], S.acc_lo[idx], S.q_scale_up[sp]);
-        S.acc_hi[idx] = 0;
-        S.acc_lo[idx] = 0ull;
-      }
-      S.src[e] = v;
-    }
-  }
-  if (tid == 0) {
-    const unsigned long long n = ctl->n_used;
-    const unsigned long long req = ctl->req_div;
-    const unsigned long long inactive_after = ctl->inactive + ctl->exits;
-    const unsigned long long ratio_thr = (unsigned long long)((double)n * S.dead_ratio);
-    const unsigned long long thr = S.min_removal > ratio_thr ? S.min_removal : ratio_thr;
-    int compact = inactive_after > thr ? 1 : 0;
-    unsigned long long rm = compact ? inactive_after : 0ull;
-    if (rm > n) {
-      ctl->error |= 8u;
-      rm = 0ull;
-      compact = 0;
-    }
-    const unsigned long long after = n - rm;
-    const unsigned long long room = S.cap > after ? S.cap - after : 0ull;
-    const unsigned long long births = req < room ? req : room;
-    p_n = n;
-    p_req = req;
-    p_rm = rm;
-    p_after = after;
-    p_compact = compact;
-    ctl->plan_n_old = n;
-    ctl->plan_to_remove = rm;
-    ctl->plan_n_after = after;
-    ctl->plan_births = births;
-    ctl->plan_overflow = req - births;
-    ctl->plan_next_id = ctl->next_id;
-    ctl->plan_step = ctl->step;
-    ctl->plan_compact = (unsigned)compact;
-    ctl->plan_gaps = 0ull;
-    if (ctl->next_id + births > 0x100000000ull) ctl->error |= 4u;
-    ctl->n_used = after + births;
-    ctl->inactive = compact ? 0ull : inactive_after;
-    ctl->next_id += births;
-    ctl->step += 1u;
-    ctl->last_births = births;
-    ctl->last_exits = ctl->exits;
-    ctl->last_moves = ctl->moves;
-    ctl->last_overflow = req - births;
-    ctl->last_req_div = req;
-    ctl->last_compacted = (unsigned)compact;
-    unsigned fl = 0u;
-    if (req > 0ull) fl |= kFlagDivide;
-    if (compact && after > 0ull && rm < n) fl |= kFlagCompact;
-    if (births > 0ull) fl |= kFlagMerge;
-    if (fl) atomicOr(&bctl->flags, fl);
-  }
-  __syncthreads();
-  const unsigned long long n = p_n;
-  const unsigned n_t = (unsigned)((n + kTile - 1) / kTile);
-  const unsigned chunk = (n_t + blockDim.x - 1) / blockDim.x;
-  const unsigned t0 = tid * chunk;
-  const unsigned t1 = min(t0 + chunk, n_t);
-  unsigned long long tot;
-  if (p_req > 0) {
-    unsigned long long local = 0;
-    for (unsigned t = t0; t < t1; ++t) local += S.tile_births[t];
-    unsigned long long off = block_exscan_u64(local, sh64, &tot);
-    for (unsigned t = t0; t < t1; ++t) {
-      S.tile_boff[t] = (unsigned)off;
-      off += S.tile_births[t];
-    }
-  }
-  if (p_compact && p_after > 0 && p_rm < n) {
-    const unsigned long long after = p_after;
-    // gap offsets for tiles t <= after / kTile (ascending prefix of inactive)
-    const unsigned tg_end = min((unsigned)(after / kTile) + 1u, n_t);
-    unsigned long long local = 0;
-    for (unsigned t = t0; t < t1 && t < tg_end; ++t) local += S.tile_inactive[t];
-    unsigned long long off = block_exscan_u64(local, sh64, &tot);
-    for (unsigned t = t0; t < t1 && t < tg_end; ++t) {
-      S.tile_goff[t] = (unsigned)off;
-      off += S.tile_inactive[t];
-    }
-    // source offsets for tiles t >= after / kTile: idle slots in later tiles
-    const unsigned ts_begin = (unsigned)(after / kTile);
-    unsigned long long local2 = 0;
-    for (unsigned t = t0; t < t1; ++t) {
-      if (t < ts_begin) continue;
-      const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
-      local2 += valid - S.tile_inactive[t];
-    }
-    unsigned long long tot2;
-    unsigned long long pre = block_exscan_u64(local2, sh64, &tot2);
-    for (unsigned t = t0; t < t1; ++t) {
-      if (t < ts_begin) continue;
-      const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
-      pre += valid - S.tile_inactive[t];
-      S.tile_soff[t] = (unsigned)(tot2 - pre);  // idle slots in tiles after t
-    }
-  }
-}
-
-// k_divide: (a) Model::division for the requests of this step, in slot
-// order, the first `plan_births` succeeding (handle_division,
-// particles_container.hpp L561-L575: mother updated in place, child into the
-// buffer, ages(mother,1) = 0); (b) the compaction lists: j-th non-Idle slot
-// of [0, n_after) and j-th Idle slot of [n_after, n) counted from the end
-// (CompactParticlesFunctor run in slot order).  256 threads x 4 slots.
-template <class Model, class F>
-__global__ void __launch_bounds__(256) k_divide(const ScenDev* __restrict__ sc, int n_scen,
-                                               const BatchCtl* __restrict__ bctl) {
-  constexpr int NV = Model::n_var;
-  __shared__ unsigned sh[33];
-  if (!(bctl->flags & (kFlagDivide | kFlagCompact))) return;
-  const unsigned total_tiles = bctl->total_tiles;
-  const int tid = threadIdx.x;
-  int s = -1;
-  for (unsigned g = blockIdx.x; g < total_tiles; g += gridDim.x) {
-    s = scen_of_tile(sc, n_scen, g, s);
-    const ScenDev& S = sc[s];
-    const Control* ctl = S.ctl;
-    const unsigned long long n_old = ctl->plan_n_old;
-    const unsigned t = g - S.tile_base;
-    const unsigned long long base = (unsigned long long)t * kTile;
-    if (base >= n_old) continue;
-    const unsigned long long req = ctl->plan_births + ctl->plan_overflow;
-    const bool cmp = ctl->plan_compact != 0u && ctl->plan_n_after > 0ull && ctl->plan_to_remove < n_old;
-    if (req == 0ull && !cmp) continue;
-    const unsigned long long first = base + (unsigned long long)tid * 4ull;
-    const unsigned long long cap = S.cap;
-    if (req > 0ull && S.tile_births[t] > 0u) {
-      const unsigned word = S.bmask[first >> 5];
-      const unsigned bits = (word >> (first & 31ull)) & 0xFu;
-      unsigned tot;
-      unsigned rank = S.tile_boff[t] + block_exscan_u32((unsigned)__popc(bits), sh, &tot);
-      const unsigned long long births = ctl->plan_births;
-      F* state = reinterpret_cast<F*>(S.state);
-      F* child_state = reinterpret_cast<F*>(S.child_state);
-      for (int k = 0; k < 4; ++k) {
-        if (!((bits >> k) & 1u)) continue;
-        const unsigned long long slot = first + k;
-        if (rank < births) {
-          F x[NV], y[NV];
-#pragma unroll
-          for (int v = 0; v < NV; ++v) x[v] = state[(size_t)v * cap + slot];
-          const Draws d = philox_draws(S.seed, S.id[slot], ctl->plan_step, 1u);
-          Model::division(x, y, d.u, S.params);
-#pragma unroll
-          for (int v = 0; v < NV; ++v) {
-            state[(size_t)v * cap + slot] = x[v];
-            child_state[(size_t)v * cap + rank] = y[v];
-          }
-          S.child_pos[rank] = S.bpos[slot];
-          S.age_d[slot] = 0.0f;
-        }
-        ++rank;
-      }
-    }
-    if (cmp) {
-      const unsigned long long after = ctl->plan_n_after;
-      unsigned gbits = 0u, sbits = 0u;
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const unsigned long long slot = first + k;
-        if (slot >= n_old) continue;
-        const bool idle = S.status[slot] == kIdle;
-        if (slot < after && !idle) gbits |= 1u << k;
-        if (slot >= after && idle) sbits |= 1u << k;
-      }
-      unsigned gtot, stot;
-      const unsigned gpre = block_exscan_u32((unsigned)__popc(gbits), sh, &gtot);
-      const unsigned spre = block_exscan_u32((unsigned)__popc(sbits), sh, &stot);
-      if (gbits) {
-        unsigned r = S.tile_goff[t] + gpre;
-        for (int k = 0; k < 4; ++k)
-          if ((gbits >> k) & 1u) S.gap_slot[r++] = (uint32_t)(first + k);
-      }
-      if (sbits) {
-        unsigned i_loc = 0;
-        for (int k = 0; k < 4; ++k) {
-          if (!((sbits >> k) & 1u)) continue;
-          const unsigned larger = stot - spre - i_loc - 1u;  // sources after this slot in the tile
-          S.src_slot[S.tile_soff[t] + larger] = (uint32_t)(first + k);
-          ++i_loc;
-        }
-      }
-      if (t == (unsigned)(after / kTile) && tid == 0) {
-        Control* c = const_cast<Control*>(ctl);
-        c->plan_gaps = (unsigned long long)S.tile_goff[t] + gtot;
-      }
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// k_compact: copy the j-th source particle into the j-th gap (all fields);
-// k_merge: append the children after the live particles with ages 0 and
-// fresh ids (InsertFunctor, particles_container.hpp L403-L447).
-template <int NV, class F>
-__global__ void __launch_bounds__(256) k_compact(const ScenDev* __restrict__ sc, int n_scen,
-                                                const BatchCtl* __restrict__ bctl) {
-  if (!(bctl->flags & kFlagCompact)) return;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (int s = 0; s < n_scen; ++s) {
-    const ScenDev& S = sc[s];
-    const Control* ctl = S.ctl;
-    if (!ctl->plan_compact) continue;
-    const unsigned long long gaps = ctl->plan_gaps;
-    const unsigned long long cap = S.cap;
-    const unsigned long long after = ctl->plan_n_after, n_old = ctl->plan_n_old;
-    F* state = reinterpret_cast<F*>(S.state);
-    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < gaps; j += stride) {
-      const unsigned long long dst = S.gap_slot[j], src = S.src_slot[j];
-      if (dst >= after || src < after || src >= n_old) {  // lists inconsistent: record, skip
-        atomicOr(&S.ctl->error, 8u);
-        continue;
-      }
-#pragma unroll
-      for (int v = 0; v < NV; ++v) state[(size_t)v * cap + dst] = state[(size_t)v * cap + src];
-      S.pos[dst] = S.pos[src];
-      S.status[dst] = kIdle;
-      S.age_h[dst] = S.age_h[src];
-      S.age_d[dst] = S.age_d[src];
-      S.id[dst] = S.id[src];
-    }
-  }
-}
-
-template <int NV, class F>
-__global__ void __launch_bounds__(256) k_merge(const ScenDev* __restrict__ sc, int n_scen,
-                                              const BatchCtl* __restrict__ bctl) {
-  if (!(bctl->flags & kFlagMerge)) return;
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (int s = 0; s < n_scen; ++s) {
-    const ScenDev& S = sc[s];
-    const Control* ctl = S.ctl;
-    const unsigned long long births = ctl->plan_births;
-    if (births == 0ull) continue;
-    const unsigned long long after = ctl->plan_n_after;
-    const unsigned long long id0 = ctl->plan_next_id;
-    const unsigned long long cap = S.cap;
-    F* state = reinterpret_cast<F*>(S.state);
-    const F* child = reinterpret_cast<const F*>(S.child_state);
-    for (unsigned long long j = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; j < births; j += stride) {
-      const unsigned long long dst = after + j;
-#pragma unroll
-      for (int v = 0; v < NV; ++v) state[(size_t)v * cap + dst] = child[(size_t)v * cap + j];
-      S.pos[dst] = S.child_pos[j];
-      S.status[dst] = kIdle;
-      S.age_h[dst] = 0.0f;
-      S.age_d[dst] = 0.0f;
-      S.id[dst] = (uint32_t)(id0 + j);
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Set-up and diagnostics.
-
-// InitFunctor (apps/libs/mc/src/unit.cpp L102-L137): model init from the
-// particle's draws, position = lo + floor(u32 * span / 2^32), mass out.
-template <class Model, class F>
-__global__ void k_init(const ScenDev* __restrict__ sc, unsigned long long n, uint32_t lo, uint32_t span,
-                       double* __restrict__ mass_out) {
-  const ScenDev& S = *sc;
-  constexpr int NV = Model::n_var;
-  F* state = reinterpret_cast<F*>(S.state);
-  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
-  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    uint32_t r[4];
-    philox_raw(S.seed, (uint32_t)i, 0xFFFFFFFFu, 2u, r);
-    float d[4];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) d[k] = (float)draw_int(r[k]) * 0x1p-24f;
-    F x[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) x[v] = (F)0;
-    Model::init(x, d, S.params);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) state[(size_t)v * S.cap + i] = x[v];
-    S.pos[i] = lo + __umulhi(r[0], span);
-    S.status[i] = kIdle;
-    S.age_h[i] = 0.0f;
-    S.age_d[i] = 0.0f;
-    S.id[i] = (uint32_t)i;
-    mass_out[i] = Model::mass(x, S.params);
-  }
-}
-
-// Move thresholds of every compartment for the current dt, into slot 7 of
-// the compartment record: leave iff u < p = dt*Q/V, i.e. x < ceil(2^24 p)
-// for the integer draw x.
-template <class F>
-__global__ void k_move_thr(ScenDev* __restrict__ sc) {
-  const ScenDev& S = sc[blockIdx.y];
-  F* rec = reinterpret_cast<F*>(S.crec);
-  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x) {
-    const double p = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
-    uint32_t t;
-    if (p >= 1.0)
-      t = (1u << 24) + 1u;
-    else if (!(p > 0.0))
-      t = 0u;
-    else
-      t = (uint32_t)ceil(__dmul_rn(p, 16777216.0));
-    if constexpr (sizeof(F) == 4)
-      rec[(size_t)c * 8 + 7] = __uint_as_float(t);
-    else
-      rec[(size_t)c * 8 + 7] = __longlong_as_double((long long)t);
-  }
-}
 
 __global__ void k_repartition(const ScenDev* __restrict__ sc, unsigned long long* __restrict__ counts) {
   const ScenDev& S = *sc;
@@ -884,89 +27,19 @@ __global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restric
   }
 }
 
-// ---------------------------------------------------------------------------
-// Launchers and the per-model dispatch table.
-
 namespace {
-template <class Model, class F, int PPT, int THREADS, int MINB>
-void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
-                    BatchCtl* b) {
-  (void)block;
-  k_cycle<Model, F, PPT, THREADS, MINB><<<grid, THREADS, smem, st>>>(sc, n, b);
-}
-template <class Model, class F>
-void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
-  k_liquid<Model, F><<<dim3(grid_x, n_scen), 256, 0, st>>>(sc, b, do_scalar);
-}
-template <class Model, class F>
-void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b) {
-  k_plan<Model, F><<<n_scen, 1024, 0, st>>>(sc, b);
-}
-template <class Model, class F>
-void launch_divide_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
-  k_divide<Model, F><<<grid, 256, 0, st>>>(sc, n, b);
-}
-template <class Model, class F>
-void launch_compact_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
-  k_compact<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n, b);
-}
-template <class Model, class F>
-void launch_merge_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {
-  k_merge<Model::n_var, F><<<grid, 256, 0, st>>>(sc, n, b);
-}
-template <class Model, class F>
-void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long long n, uint32_t lo,
-                   uint32_t span, double* mass) {
-  k_init<Model, F><<<grid, 256, 0, st>>>(sc, n, lo, span, mass);
-}
-template <class Model, class F, int PPT, int THREADS, int MINB>
-const void* cycle_fn_t() {
-  return reinterpret_cast<const void*>(&k_cycle<Model, F, PPT, THREADS, MINB>);
-}
-template <class F>
-void launch_move_thr_t(int n_scen, cudaStream_t st, ScenDev* sc) {
-  k_move_thr<F><<<dim3(4, n_scen), 256, 0, st>>>(sc);
-}
-
-template <class Model, class F>
-KernelSet make_set() {
-  KernelSet k{};
-  k.n_var = Model::n_var;
-  k.n_ctb = Model::n_ctb;
-  k.model = Model::model_id;
-  k.f64 = sizeof(F) == 8;
-  k.separable = Model::separable;
-  k.cycle[0] = &launch_cycle_t<Model, F, 1, 256, 4>;
-  k.cycle[1] = &launch_cycle_t<Model, F, 2, 256, 3>;
-  k.cycle[2] = &launch_cycle_t<Model, F, 4, 256, 2>;
-  k.cycle[3] = &launch_cycle_t<Model, F, 2, 512, 2>;
-  k.cycle[4] = &launch_cycle_t<Model, F, 1, 1024, 1>;
-  k.cycle_fn[0] = cycle_fn_t<Model, F, 1, 256, 4>();
-  k.cycle_fn[1] = cycle_fn_t<Model, F, 2, 256, 3>();
-  k.cycle_fn[2] = cycle_fn_t<Model, F, 4, 256, 2>();
-  k.cycle_fn[3] = cycle_fn_t<Model, F, 2, 512, 2>();
-  k.cycle_fn[4] = cycle_fn_t<Model, F, 1, 1024, 1>();
-  k.move_thr = &launch_move_thr_t<F>;
-  k.liquid = &launch_liquid_t<Model, F>;
-  k.plan = &launch_plan_t<Model, F>;
-  k.divide = &launch_divide_t<Model, F>;
-  k.compact = &launch_compact_t<Model, F>;
-  k.merge = &launch_merge_t<Model, F>;
-  k.init = &launch_init_t<Model, F>;
-  return k;
-}
-
+using kset::make_set;
 const KernelSet g_sets[] = {
-    make_set<MonodModel<double>, double>(),    make_set<MonodModel<float>, float>(),
-    make_set<OverflowModel<double>, double>(), make_set<OverflowModel<float>, float>(),
-    make_set<FixedLengthModelT<true>, float>(), make_set<FixedLengthModelT<false>, float>(),
+    make_set<MonodModel<double>, double>(1),       make_set<MonodModel<float>, float>(1),
+    make_set<OverflowModel<double>, double>(2),    make_set<OverflowModel<float>, float>(2),
+    make_set<FixedLengthModelT<true>, float>(3),   make_set<FixedLengthModelT<false>, float>(4),
 };
 }  // namespace
 
 const KernelSet* kernel_set(int model, int f64) {
   for (const KernelSet& k : g_sets)
     if (k.model == model && k.f64 == (f64 != 0)) return &k;
-  return nullptr;
+  return udf_kernel_set(model, f64);
 }
 
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {

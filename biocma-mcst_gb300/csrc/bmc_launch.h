@@ -1,5 +1,10 @@
 // bmc_launch.h -- host-side view of the kernels: one KernelSet per compiled
 // model plugin and precision, plus the model-independent launchers.
+//
+// A KernelSet holds host launch functions only (no kernel handles), so a
+// set built into a separately compiled plugin library (bmc_udf.cuh) is
+// driven by libbmc exactly like a built-in one: every launch, attribute
+// and occupancy query runs inside the module that owns the kernels.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -7,6 +12,10 @@
 #include "bmc_kernels.cuh"
 
 namespace bmc {
+
+// Layout version of KernelSet; a plugin built against another layout is
+// refused at load time.
+constexpr int kKernelSetAbi = 2;
 
 using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
@@ -16,6 +25,9 @@ using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long lo
 
 using LiquidLaunch = void (*)(int, unsigned, cudaStream_t, ScenDev*, BatchCtl*, int);
 using MoveThrLaunch = void (*)(int, cudaStream_t, ScenDev*);
+// Sets the cycle kernel's dynamic shared-memory limit to `smem` and returns
+// (cudaError_t) with the resident blocks per SM in *blocks_per_sm.
+using CycleSetup = int (*)(size_t smem, int* blocks_per_sm);
 
 // Cycle launch variants: {threads per block, particles per thread}.
 constexpr int kCycleVariants = 5;
@@ -24,6 +36,7 @@ constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1};
 using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*);
 
 struct KernelSet {
+  int abi;
   int model;
   bool f64;
   bool separable;
@@ -32,15 +45,18 @@ struct KernelSet {
   LiquidLaunch liquid;
   PlanLaunch plan;
   CycleLaunch cycle[kCycleVariants];
-  const void* cycle_fn[kCycleVariants];  // for occupancy queries / attributes
+  CycleSetup cycle_setup[kCycleVariants];
   MoveThrLaunch move_thr;
   DivideLaunch divide;
   CopyLaunch compact;
   CopyLaunch merge;
   InitLaunch init;
+  int (*last_error)();  // cudaGetLastError of the module owning the kernels
 };
 
+// Built-in sets first, then the sets of loaded plugins (bmc_udf_load).
 const KernelSet* kernel_set(int model, int f64);
+const KernelSet* udf_kernel_set(int model, int f64);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);

@@ -254,6 +254,58 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps);
 int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 int bmc_batch_synchronize(bmc_batch* b);
 
+/* ---- runtime-loaded cell models ("udf_model") ----------------------------- */
+/* A user model is a CUDA source file that defines a model struct and
+ * expands BMC_DEFINE_UDF (biocma-mcst_gb300/csrc/bmc_udf.cuh); compiled with
+ * nvcc into a shared library (bmc/udf.py build_udf), it carries the cycle's
+ * kernels instantiated for that model.  bmc_udf_load opens it and returns
+ * the model id (>= BMC_MODEL_UDF_FIRST) to put in bmc_model_desc.model.
+ * Reference: UnsafeUDF::Loader::init_lib (apps/libs/models/ext/
+ * udf_includes.cpp L58-L78) with the module symbols of udf_includes.hpp
+ * L111-L122; path == NULL reads the library path from BIOMC_LIB_UDF as
+ * Unsafe::load_udf does (apps/api/src/udf_handle.cpp L22-L38).  Loading the
+ * same path again returns the same id; libraries stay loaded until exit. */
+#define BMC_MODEL_UDF_FIRST 64
+int bmc_udf_load(const char* path, int32_t* model_id);
+
+/* Metadata of a loaded model: set_nvar_udf / set_nc_udf / names_udf /
+ * species_udf of the reference's module (udf_includes.hpp L29-L65). */
+typedef struct bmc_udf_info {
+  uint32_t n_var;
+  uint32_t n_ctb;
+  int32_t separable;
+  int32_t has_f32;    /* compiled for float state */
+  int32_t has_f64;    /* compiled for double state */
+  uint32_t n_names;   /* entries of names (state variables) */
+  uint32_t n_species; /* entries of species */
+  uint32_t pad;
+  const char* names[16];  /* owned by the library */
+  const char* species[8];
+} bmc_udf_info;
+int bmc_udf_get_info(int32_t model_id, bmc_udf_info* info);
+
+/* Host (CPU) entry points of a loaded model, compiled from the same source
+ * as its kernels, for CPU callers (initial conditions, post-processing,
+ * reference computations).  x, child and r point to the model's float type
+ * (float or double per f64); rates(c, params, r) fills the compartment
+ * factors from one compartment's concentrations; update advances one
+ * particle and writes its contribution basis (separable models) or its
+ * n_ctb contributions (general models) to out; coef(r, j) is the
+ * contribution of species j per unit basis. */
+typedef struct bmc_udf_host_model {
+  uint32_t n_var;
+  uint32_t n_ctb;
+  uint32_t n_rates;
+  int32_t separable;
+  void (*rates)(const double* c, const double* params, void* r);
+  int32_t (*update)(double dt, void* x, const void* r, void* out, const double* params);
+  double (*coef)(const void* r, int32_t j);
+  void (*division)(void* x, void* child, const float* draws, const double* params);
+  void (*init)(void* x, const float* draws, const double* params);
+  double (*mass)(const void* x, const double* params);
+} bmc_udf_host_model;
+int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* out);
+
 /* ---- diagnostics ---------------------------------------------------------- */
 /* Fill out[4*n] with the four uniform draws of (seed, id[k], step, purpose)
  * computed on the device (checks the draw source against the oracle). */

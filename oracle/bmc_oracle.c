@@ -141,6 +141,10 @@ static int is_fixed_length(const orc_state* s) {
 
 /* Rates of compartment c into r[8] (element type of the model's float). */
 static void model_rates(const orc_state* s, const double* c, void* r) {
+  if (s->udf) {
+    s->udf->rates(c, s->params, r);
+    return;
+  }
   if (s->f64) {
     double* rr = (double*)r;
     if (s->model == ORC_MODEL_MONOD) monod_rates_f64(c, s->params, rr);
@@ -155,6 +159,7 @@ static void model_rates(const orc_state* s, const double* c, void* r) {
 
 /* Contribution coefficient j of a compartment (as double). */
 static double model_coef(const orc_state* s, const void* r, int j) {
+  if (s->udf) return s->udf->coef(r, j);
   if (s->f64) {
     const double* rr = (const double*)r;
     if (s->model == ORC_MODEL_MONOD) return monod_coef_f64(rr, j);
@@ -171,6 +176,26 @@ static double model_coef(const orc_state* s, const void* r, int j) {
  * writes its contribution w-free into ctb[0]. */
 static int model_update(const orc_state* s, double dt, uint64_t i, const void* r, double* basis, double* ctb) {
   const uint64_t cap = s->phys_capacity;
+  if (s->udf && s->f64) {
+    double* st = (double*)s->state;
+    double x[8], out[8] = {0};
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    const int res = s->udf->update(dt, x, r, out, s->params);
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+    *basis = out[0];
+    for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = out[j];
+    return res;
+  }
+  if (s->udf) {
+    float* st = (float*)s->state;
+    float x[8], out[8] = {0};
+    for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
+    const int res = s->udf->update((double)(float)dt, x, r, out, s->params);
+    for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
+    *basis = (double)out[0];
+    for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = (double)out[j];
+    return res;
+  }
   if (s->f64) {
     double* st = (double*)s->state;
     double x[8];
@@ -205,6 +230,20 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
   const uint64_t cap = s->phys_capacity;
   float d[4];
   draws_for(s, s->id[i], 1u, d);
+  if (s->udf) {
+    const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
+    char* st = (char*)s->state;
+    char* ch = (char*)s->child_state;
+    double xb[8], yb[8]; /* storage for up to 8 values of either type */
+    memset(yb, 0, sizeof(yb));
+    for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)xb + v * fs, st + (v * cap + i) * fs, fs);
+    s->udf->division(xb, yb, d, s->params);
+    for (uint32_t v = 0; v < s->n_var; ++v) {
+      memcpy(st + (v * cap + i) * fs, (char*)xb + v * fs, fs);
+      memcpy(ch + (v * cap + child_slot) * fs, (char*)yb + v * fs, fs);
+    }
+    return;
+  }
   if (s->f64) {
     double* st = (double*)s->state;
     double* ch = (double*)s->child_state;
@@ -233,6 +272,14 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
 
 static void model_init(const orc_state* s, uint64_t i, const float* d) {
   const uint64_t cap = s->phys_capacity;
+  if (s->udf) {
+    const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
+    double xb[8];
+    memset(xb, 0, sizeof(xb));
+    s->udf->init(xb, d, s->params);
+    for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)s->state + (v * cap + i) * fs, (char*)xb + v * fs, fs);
+    return;
+  }
   if (s->f64) {
     double* st = (double*)s->state;
     double x[8] = {0};
@@ -250,6 +297,13 @@ static void model_init(const orc_state* s, uint64_t i, const float* d) {
 }
 
 static double model_mass(const orc_state* s, uint64_t i) {
+  if (s->udf) {
+    const uint64_t cap = s->phys_capacity;
+    const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
+    double xb[8];
+    for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)xb + v * fs, (const char*)s->state + (v * cap + i) * fs, fs);
+    return s->udf->mass(xb, s->params);
+  }
   if (s->f64) return ((const double*)s->state)[i];
   if (is_fixed_length(s)) return (double)(((const float*)s->state)[i] * fixed_length_lin_density());
   return (double)((const float*)s->state)[i];

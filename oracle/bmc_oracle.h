@@ -41,6 +41,22 @@ enum { ORC_IDLE = 0, ORC_DIVISION = 1, ORC_EXIT = 2, ORC_DEAD = 3 };
 enum { ORC_MODEL_MONOD = 1, ORC_MODEL_OVERFLOW = 2, ORC_MODEL_FIXED_LENGTH = 3, ORC_MODEL_FIXED_LENGTH_GENERAL = 4 };
 enum { ORC_DRAW_PHILOX = 0, ORC_DRAW_XORSHIFT = 1 };
 
+/* A cell model supplied at run time as host functions (a model library's
+ * bmc_udf_host_model, include/bmc.h; same layout).  x, child and r point to
+ * the model's float type (double when f64 != 0, else float). */
+typedef struct orc_udf_model {
+  uint32_t n_var;
+  uint32_t n_ctb;
+  uint32_t n_rates;
+  int32_t separable;
+  void (*rates)(const double* c, const double* params, void* r);
+  int32_t (*update)(double dt, void* x, const void* r, void* out, const double* params);
+  double (*coef)(const void* r, int32_t j);
+  void (*division)(void* x, void* child, const float* draws, const double* params);
+  void (*init)(void* x, const float* draws, const double* params);
+  double (*mass)(const void* x, const double* params);
+} orc_udf_model;
+
 #define ORC_MAX_OUTLETS 8
 #define ORC_MAX_PARAMS 16
 
@@ -135,6 +151,9 @@ typedef struct orc_state {
   uint64_t requested_divisions;
   int32_t compacted;
   int32_t error;
+
+  /* run-time model: when set, it replaces the compiled-in models */
+  const orc_udf_model* udf;
 } orc_state;
 
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

@@ -48,7 +48,29 @@ class OrcState(ct.Structure):
         ("births", ct.c_uint64), ("exits", ct.c_uint64), ("moves", ct.c_uint64),
         ("overflow", ct.c_uint64), ("requested_divisions", ct.c_uint64),
         ("compacted", ct.c_int32), ("error", ct.c_int32),
+        ("udf", ct.c_void_p),
     ]
+
+
+class OrcUdfModel(ct.Structure):
+    """orc_udf_model: a model library's host functions (bmc_udf_host_model)."""
+    _fields_ = [("n_var", ct.c_uint32), ("n_ctb", ct.c_uint32), ("n_rates", ct.c_uint32),
+                ("separable", ct.c_int32), ("rates", ct.c_void_p), ("update", ct.c_void_p),
+                ("coef", ct.c_void_p), ("division", ct.c_void_p), ("init", ct.c_void_p),
+                ("mass", ct.c_void_p)]
+
+
+def udf_host_model(path: str, f64: bool):
+    """Open a model library and take its host entry points (host_model_udf);
+    the library handle is returned with the table so it stays loaded."""
+    L = ct.CDLL(path)
+    f = L.host_model_udf
+    f.argtypes = [ct.c_int32, ct.c_void_p]
+    f.restype = ct.c_int
+    m = OrcUdfModel()
+    if f(1 if f64 else 0, ct.byref(m)) != 0:
+        raise RuntimeError(f"{path}: precision not compiled in")
+    return L, m
 
 
 _lib = None
@@ -175,6 +197,11 @@ class Oracle:
         s.q_max = 1 << 42
         s.separable = 1 if m.separable else 0
         s.quirk_tag3d = 1 if quirk_tag3d else 0
+        self._udf = None
+        if getattr(m, "udf_path", None):
+            self._udf = udf_host_model(m.udf_path, m.f64)
+            assert self._udf[1].n_var == m.n_var and self._udf[1].n_ctb == m.n_ctb
+            s.udf = ct.addressof(self._udf[1])
         self.s = s
         self.weight = None
 
