@@ -411,6 +411,8 @@ def batched_form(steps: int, n_scen: int = 256):
     """256 uneven scenarios advanced by one batched launch sequence per step
     (one captured graph) against the plain path: each scenario advanced by
     its own graph on its own stream, all streams in flight together."""
+    import numpy as np
+
     from bmc import autotune, scenarios, sim
 
     scens = [scenarios.batch_scenario(k, seed=1234) for k in range(n_scen)]
@@ -426,7 +428,12 @@ def batched_form(steps: int, n_scen: int = 256):
     b.run(steps, 0.1)
     b.synchronize()
     tb = time.perf_counter() - t0
+    # per-kernel device times of single steps (no graph), for the roofline
+    kms = np.median(np.stack([b.step_timed(0.1) for _ in range(10)]), axis=0)
     b.close()
+    bytes_per_particle = scens[0].algorithmic_bytes()
+    cyc_gbs = float(n_alive * bytes_per_particle / (float(kms[1]) * 1e-3) / 1e9)
+    peak = measured_peak()[0]
     for g in gs:  # plain path: warm its graphs
         g.run(1)
     # plain, one scenario after another, each step through bmc_step (the
@@ -461,7 +468,12 @@ def batched_form(steps: int, n_scen: int = 256):
             "plain_graph_concurrent_streams_value": ps / tp,
             "batched_over_plain_step_sync": t_sync / tb, "batched_over_plain_graph_sequential": t_seq / tb,
             "batched_over_plain_concurrent_streams": tp / tb, "unit": METRIC, "setup_s": setup,
-            "shape": shape, "accuracy": "bit-identical results batched and plain (tests/test_gpu_batch.py)"}
+            "shape": shape,
+            "step_breakdown_ms": dict(zip(["liquid", "cycle", "plan", "divide", "compact", "merge"],
+                                          [float(x) for x in kms])),
+            "cycle_roofline": {"achieved": cyc_gbs, "peak": peak, "unit": "GB/s",
+                               "frac": cyc_gbs / peak, "bytes_per_particle": bytes_per_particle},
+            "accuracy": "bit-identical results batched and plain (tests/test_gpu_batch.py)"}
 
 
 def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):

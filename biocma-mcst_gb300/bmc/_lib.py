@@ -103,6 +103,7 @@ SIGNATURES = {
     "bmc_launch_count": [VP],
     "bmc_step_timed": [VP, c_dbl, VP, VP],
     "bmc_run_timed": [VP, c_dbl, c_u32, VP, VP],
+    "bmc_batch_step_timed": [VP, c_dbl, VP],
     "bmc_set_device": [c_i32],
     "bmc_transfer_bytes": [VP, VP],
     "bmc_udf_load": [ct.c_char_p, VP],

@@ -1,8 +1,11 @@
 """Launch-shape autotuner for the cycle kernel.
 
-The cycle kernel has five instantiated shapes per model (256 threads with
-1, 2 or 4 particles per thread, 512 x 2 and 1024 x 1, each compiled for
-its own register budget) and a free choice of resident blocks per SM.  The autotuner times each candidate
+The cycle kernel has seven instantiated shapes per model: five that stream
+particles through registers (256 threads with 1, 2 or 4 particles per
+thread, 512 x 2 and 1024 x 1, each compiled for its own register budget)
+and two that stage 1024-slot tiles in shared memory through the copy
+engine (256 or 512 consumer threads plus a producer warp), with a free
+choice of resident blocks per SM.  The autotuner times each candidate
 on the live scenario (or batch) for a few steps -- every timed step is a
 real step of the simulation, so tuning doubles as warm-up -- and keeps the
 fastest.  Results are remembered per workload key (compartment-count
@@ -14,8 +17,11 @@ from __future__ import annotations
 import math
 import time
 
-# (threads per block, particles per thread, resident blocks per SM; 0 = max)
-CANDIDATES = [(256, 1, 0), (256, 2, 0), (256, 4, 0), (512, 2, 0), (1024, 1, 0)]
+from ._lib import BmcError
+
+# (threads, particles per thread, blocks per SM; 0 = as many as fit).  288 and
+# 544 threads are the tile-staging kernel (256 / 512 consumers + 1 producer warp).
+CANDIDATES = [(256, 1, 0), (256, 2, 0), (256, 4, 0), (512, 2, 0), (1024, 1, 0), (288, 4, 0), (544, 2, 0)]
 
 _cache: dict = {}
 
@@ -36,9 +42,12 @@ def tune_scenario(g, steps: int = 4, candidates=CANDIDATES):
         return _cache[key], {}
     timings = {}
     for shape in candidates:
-        g.set_shape(*shape)
-        g.run(1)  # graph capture for this shape
-        _, ms = g.run_timed(steps)
+        try:
+            g.set_shape(*shape)
+            g.run(1)  # graph capture for this shape
+            _, ms = g.run_timed(steps)
+        except BmcError:  # shape does not fit this scenario (shared memory)
+            continue
         timings[shape] = ms / steps
     best = min(timings, key=timings.get)
     g.set_shape(*best)
@@ -59,12 +68,15 @@ def tune_batch(b, dt: float, steps: int = 3, candidates=CANDIDATES):
         return _cache[key], {}
     timings = {}
     for shape in candidates:
-        b.set_shape(*shape)
-        b.run(1, dt)
-        b.synchronize()
-        t0 = time.perf_counter()
-        b.run(steps, dt)
-        b.synchronize()
+        try:
+            b.set_shape(*shape)
+            b.run(1, dt)
+            b.synchronize()
+            t0 = time.perf_counter()
+            b.run(steps, dt)
+            b.synchronize()
+        except BmcError:  # shape does not fit these scenarios (shared memory)
+            continue
         timings[shape] = (time.perf_counter() - t0) * 1e3 / steps
     best = min(timings, key=timings.get)
     b.set_shape(*best)

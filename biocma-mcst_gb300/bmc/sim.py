@@ -238,6 +238,13 @@ class GpuBatch:
     def run(self, n_steps: int, dt: float):
         call("bmc_batch_run", self.handle, dt, n_steps)
 
+    def step_timed(self, dt: float) -> np.ndarray:
+        """One step with per-kernel device times (ms): liquid, cycle, plan,
+        divide, compact, merge."""
+        ms = np.zeros(6, dtype=np.float32)
+        call("bmc_batch_step_timed", self.handle, dt, _p(ms))
+        return ms
+
     def synchronize(self):
         call("bmc_batch_synchronize", self.handle)
 

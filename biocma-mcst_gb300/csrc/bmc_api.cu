@@ -192,12 +192,16 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
 
 size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(unsigned long long); }
 
-int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t smem, int sm_count,
+// *smem: in, the accumulator bytes; out, the dynamic shared memory of the
+// launch (staged variants append their tile buffers, 128-byte aligned).
+int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t* smem, int sm_count,
                   unsigned* grid_out) {
-  if (smem > 227 * 1024)
-    return fail(BMC_E_UNSUPPORTED, "n_compartments * n_contributions too large for the shared accumulator");
+  if (ks->cycle_extra_smem[variant] > 0) *smem = align_up(*smem, 128) + ks->cycle_extra_smem[variant];
+  if (*smem > 227 * 1024)
+    return fail(BMC_E_UNSUPPORTED, "shared accumulator (n_compartments * n_contributions) and tile buffers "
+                                   "exceed the shared memory of a block for this launch shape");
   int bps = 0;
-  BMC_CUDA((cudaError_t)ks->cycle_setup[variant](smem, &bps));
+  BMC_CUDA((cudaError_t)ks->cycle_setup[variant](*smem, &bps));
   if (bps < 1) return fail(BMC_E_UNSUPPORTED, "cycle kernel cannot be resident with this shape");
   if (bps_req > 0) bps = std::min<int>(bps, (int)bps_req);
   *grid_out = (unsigned)(sm_count * bps);
@@ -221,6 +225,46 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
   ks->merge(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
   g_launches += 6;
   BMC_CUDA(launch_status(ks));
+  return BMC_OK;
+}
+
+// Refresh a batch's descriptor table for dt (uploading it when a member
+// changed) and size the cycle launch.
+int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, size_t* smem_out, unsigned* grid_out) {
+  if (!b) return fail(BMC_E_INVALID, "null batch");
+  const int n = (int)b->scen.size();
+  bool table_changed = b->table.size() != (size_t)n;
+  b->table.resize(n);
+  unsigned tiles = 0, max_nc = 0;
+  size_t smem = 0;
+  for (int i = 0; i < n; ++i) {
+    bmc_scenario* s = b->scen[i];
+    int rc = set_dt(s, dt, false);
+    if (rc) return rc;
+    ScenDev d = s->h;
+    d.tile_base = tiles;
+    tiles += d.n_tiles;
+    max_nc = std::max(max_nc, liquid_grid(d));
+    smem = std::max(smem, cycle_smem(d));
+    if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
+    b->table[i] = d;
+  }
+  if (table_changed || b->dt != dt) {
+    BMC_CUDA(cudaStreamSynchronize(b->stream));
+    BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
+    BatchCtl bc{0u, tiles, 0u, 0u, b->d_live};
+    BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
+    b->ks->move_thr(n, b->stream, b->d_table);
+    g_launches++;
+    BMC_CUDA(launch_status(b->ks));
+    b->dt = dt;
+    b->total_tiles = tiles;
+  }
+  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->scen[0]->sm_count, grid_out);
+  if (rc) return rc;
+  *n_out = n;
+  *max_nc_out = max_nc;
+  *smem_out = smem;
   return BMC_OK;
 }
 
@@ -712,9 +756,9 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   if (rc) return rc;
   rc = set_dt(s, dt, true);
   if (rc) return rc;
-  const size_t smem = cycle_smem(s->h);
+  size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, &grid);
+  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, &smem, s->sm_count, &grid);
   if (rc) return rc;
   if (use_graph && do_scalar) {
     rc = ensure_graph(s, grid, smem);
@@ -1000,37 +1044,10 @@ int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t b
 }
 
 int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
-  if (!b) return fail(BMC_E_INVALID, "null batch");
-  const int n = (int)b->scen.size();
-  bool table_changed = b->table.size() != (size_t)n;
-  b->table.resize(n);
-  unsigned tiles = 0, max_nc = 0;
+  int n = 0;
+  unsigned max_nc = 0, grid = 0;
   size_t smem = 0;
-  for (int i = 0; i < n; ++i) {
-    bmc_scenario* s = b->scen[i];
-    int rc = set_dt(s, dt, false);
-    if (rc) return rc;
-    ScenDev d = s->h;
-    d.tile_base = tiles;
-    tiles += d.n_tiles;
-    max_nc = std::max(max_nc, liquid_grid(d));
-    smem = std::max(smem, cycle_smem(d));
-    if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
-    b->table[i] = d;
-  }
-  if (table_changed || b->dt != dt) {
-    BMC_CUDA(cudaStreamSynchronize(b->stream));
-    BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
-    BatchCtl bc{0u, tiles, 0u, 0u, b->d_live};
-    BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
-    b->ks->move_thr(n, b->stream, b->d_table);
-    g_launches++;
-    BMC_CUDA(launch_status(b->ks));
-    b->dt = dt;
-    b->total_tiles = tiles;
-  }
-  unsigned grid = 0;
-  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, smem, b->scen[0]->sm_count, &grid);
+  int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
   if (!b->graph || b->graph_smem != smem || b->graph_grid != grid) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -1073,9 +1090,9 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   if (rc) return rc;
   rc = set_dt(s, dt, true);
   if (rc) return rc;
-  const size_t smem = cycle_smem(s->h);
+  size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, &grid);
+  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, &smem, s->sm_count, &grid);
   if (rc) return rc;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
@@ -1100,6 +1117,38 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   for (int k = 0; k < 6 && kernel_ms; ++k) cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]);
   for (auto& e : ev) cudaEventDestroy(e);
   return rc;
+}
+
+int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
+  int n = 0;
+  unsigned max_nc = 0, grid = 0;
+  size_t smem = 0;
+  int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
+  if (rc) return rc;
+  const int sm = b->scen[0]->sm_count;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
+  cudaStream_t st = b->stream;
+  const unsigned variant = b->variant;
+  BMC_CUDA(cudaEventRecord(ev[0], st));
+  b->ks->liquid(n, max_nc, st, b->d_table, b->d_bctl, 1);
+  BMC_CUDA(cudaEventRecord(ev[1], st));
+  b->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, b->d_table, n, b->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[2], st));
+  b->ks->plan(n, st, b->d_table, b->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[3], st));
+  b->ks->divide(dim3(sm * 4), st, b->d_table, n, b->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[4], st));
+  b->ks->compact(dim3(sm * 2), st, b->d_table, n, b->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[5], st));
+  b->ks->merge(dim3(sm * 2), st, b->d_table, n, b->d_bctl);
+  BMC_CUDA(cudaEventRecord(ev[6], st));
+  g_launches += 6;
+  BMC_CUDA(launch_status(b->ks));
+  BMC_CUDA(cudaStreamSynchronize(st));
+  for (int k = 0; k < 6 && kernel_ms; ++k) cudaEventElapsedTime(&kernel_ms[k], ev[k], ev[k + 1]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  return BMC_OK;
 }
 
 int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, uint32_t purpose, float* out) {

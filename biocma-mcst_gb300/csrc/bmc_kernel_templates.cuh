@@ -496,6 +496,337 @@ __global__ void __launch_bounds__(THREADS, MINB)
 }
 
 // ---------------------------------------------------------------------------
+// k_cycle_tma: the same per-particle work as k_cycle, with the particle
+// arrays of each 1024-slot tile staged in shared memory by the copy engine.
+// A producer warp (one thread) issues bulk copies (cp.async.bulk, completion
+// on a "full" mbarrier per stage) of the tile's read state variables,
+// compartments, ids, ages and statuses, STAGES tiles ahead; THREADS
+// consumer threads wait on the stage, process slots r*THREADS + tid from
+// shared memory, write results straight to global memory (streaming
+// stores), and release the stage on its "empty" mbarrier.  The loads in
+// flight no longer live in registers, so the memory pipeline stays full at
+// any occupancy.  Tiles map to scenarios exactly as in k_cycle (static
+// contiguous partition of the live tiles).  Every consumer derives the
+// tile -> scenario map itself, so all consumers run the same sequence of
+// flushes and barriers even if a wait gives up (BMC_ERR_TIMEOUT): then
+// processing stops, the producer issues nothing more and drains its
+// copies in flight.
+
+__host__ __device__ constexpr unsigned popcount_c(unsigned v) { return v == 0u ? 0u : (v & 1u) + popcount_c(v >> 1); }
+
+template <class Model, class F>
+struct TileStage {
+  static constexpr unsigned NV = Model::n_var;
+  static constexpr unsigned RV = popcount_c(Model::read_mask & ((1u << NV) - 1u));
+  static constexpr unsigned off_x = 0;
+  static constexpr unsigned off_pos = RV * kTile * (unsigned)sizeof(F);
+  static constexpr unsigned off_id = off_pos + kTile * 4u;
+  static constexpr unsigned off_ad = off_id + kTile * 4u;
+  static constexpr unsigned off_ah = off_ad + kTile * 4u;
+  static constexpr unsigned off_st = off_ah + kTile * 4u;
+  static constexpr unsigned bytes = (off_st + kTile + 127u) & ~127u;
+  // rank of state variable v among the read ones
+  __host__ __device__ static constexpr unsigned rank(unsigned v) { return popcount_c(Model::read_mask & ((1u << v) - 1u)); }
+};
+
+template <class Model, class F, int THREADS, int MINB, int STAGES>
+__global__ void __launch_bounds__(THREADS + 32, MINB)
+    k_cycle_tma(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
+  using TS = TileStage<Model, F>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  unsigned long long* sacc = reinterpret_cast<unsigned long long*>(smem_raw);
+  __shared__ unsigned long long s_full[STAGES], s_empty[STAGES];
+  __shared__ unsigned long long s_cnt[5];
+  __shared__ F s_pf[16];
+  __shared__ unsigned s_abort;
+  constexpr int NV = Model::n_var;
+  constexpr int NC = Model::n_ctb;
+  constexpr int NA = Model::separable ? 1 : NC;
+  constexpr unsigned PPT = kTile / THREADS;
+  static_assert(kTile % THREADS == 0 && THREADS % 32 == 0, "tile must split evenly");
+  unsigned char* const stages = smem_raw + (dynamic_smem_bytes() - (unsigned)STAGES * TS::bytes);
+  const int tid = threadIdx.x;
+  const unsigned total = bctl->total_live;
+  const unsigned* live_base = bctl->live_base;
+  const unsigned g_begin = (unsigned)(((unsigned long long)total * blockIdx.x) / gridDim.x);
+  const unsigned g_end = (unsigned)(((unsigned long long)total * (blockIdx.x + 1)) / gridDim.x);
+  const unsigned n_tiles = g_end - g_begin;
+  if (tid == 0) {
+    for (int k = 0; k < STAGES; ++k) {
+      mbar_init(&s_full[k], 1u);
+      mbar_init(&s_empty[k], (unsigned)THREADS);
+    }
+    s_abort = 0u;
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (n_tiles == 0) return;
+
+  if (tid >= THREADS) {
+    // ---- producer -------------------------------------------------------
+    if (tid != THREADS) return;
+    int hint = -1;
+    unsigned issued = 0;
+    bool ok = true;
+    for (unsigned k = 0; k < n_tiles; ++k) {
+      const unsigned stg = k % STAGES, use = k / STAGES;
+      if (use > 0 && !mbar_wait_bounded(&s_empty[stg], (use - 1u) & 1u, &s_abort)) {
+        ok = false;
+        break;
+      }
+      if (s_abort) {
+        ok = false;
+        break;
+      }
+      const unsigned g = g_begin + k;
+      const int s = scen_of_live(live_base, n_scen, g, hint);
+      hint = s;
+      const ScenDev& S = sc[s];
+      const unsigned long long base = (unsigned long long)(g - __ldg(live_base + s)) * kTile;
+      const unsigned long long n_used = S.ctl->n_used;
+      const unsigned n_in = (unsigned)(n_used - base < kTile ? n_used - base : kTile);
+      // whole 16-slot groups: every copy is a multiple of 16 bytes and stays
+      // inside the tile (capacity is a whole number of tiles)
+      const unsigned n16 = (n_in + 15u) & ~15u;
+      const bool with_ah = S.n_outlets > 0;
+      const unsigned tx = TS::RV * n16 * (unsigned)sizeof(F) + n16 * 13u + (with_ah ? n16 * 4u : 0u);
+      unsigned char* buf = stages + stg * TS::bytes;
+      fence_proxy_async();
+      mbar_arrive_expect_tx(&s_full[stg], tx);
+      const F* state = reinterpret_cast<const F*>(S.state);
+#pragma unroll
+      for (int v = 0; v < NV; ++v)
+        if ((Model::read_mask >> v) & 1u)
+          bulk_g2s(buf + TS::off_x + TS::rank((unsigned)v) * kTile * sizeof(F), state + (size_t)v * S.cap + base,
+                   n16 * (unsigned)sizeof(F), &s_full[stg]);
+      bulk_g2s(buf + TS::off_pos, S.pos + base, n16 * 4u, &s_full[stg]);
+      bulk_g2s(buf + TS::off_id, S.id + base, n16 * 4u, &s_full[stg]);
+      bulk_g2s(buf + TS::off_ad, S.age_d + base, n16 * 4u, &s_full[stg]);
+      if (with_ah) bulk_g2s(buf + TS::off_ah, S.age_h + base, n16 * 4u, &s_full[stg]);
+      bulk_g2s(buf + TS::off_st, S.status + base, n16, &s_full[stg]);
+      issued = k + 1;
+    }
+    if (!ok) {
+      s_abort = 1u;
+      // copies of the last (up to STAGES) issued tiles may still be landing
+      unsigned zero = 0u;
+      const unsigned first = issued > (unsigned)STAGES ? issued - (unsigned)STAGES : 0u;
+      for (unsigned j = first; j < issued; ++j)
+        (void)mbar_wait_bounded(&s_full[j % STAGES], (j / STAGES) & 1u, &zero);
+    }
+    return;
+  }
+
+  // ---- consumers ----------------------------------------------------------
+  const int lane = tid & 31;
+  const unsigned warp = (unsigned)tid >> 5;
+  int cur = -1;
+  bool aborted = false;
+  unsigned long long since_flush = 0;
+  unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
+  unsigned my_err = 0;
+
+  auto flush = [&]() {
+    consumer_sync(THREADS);
+    const ScenDev& P = sc[cur];
+    const unsigned n_ent = P.n_c * NA;
+    if (!aborted)
+      for (unsigned e = tid; e < n_ent; e += THREADS) {
+        const long long p = (long long)sacc[e];
+        if (p != 0) {
+          atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
+          atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
+        }
+      }
+    if (tid < 5) s_cnt[tid] = 0ull;
+    consumer_sync(THREADS);
+    const unsigned long long r0 = warp_sum_u64(my_req), r1 = warp_sum_u64(my_exit);
+    const unsigned long long r2 = warp_sum_u64(my_move), r3 = warp_sum_u64(my_clamp);
+    unsigned e4 = my_err;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) e4 |= __shfl_xor_sync(0xffffffffu, e4, o);
+    if (lane == 0) {
+      atomicAdd(&s_cnt[0], r0);
+      atomicAdd(&s_cnt[1], r1);
+      atomicAdd(&s_cnt[2], r2);
+      atomicAdd(&s_cnt[3], r3);
+      atomicOr(reinterpret_cast<unsigned*>(&s_cnt[4]), e4);
+    }
+    consumer_sync(THREADS);
+    if (tid == 0) {
+      Control* c = P.ctl;
+      if (s_cnt[0]) atomicAdd(&c->req_div, s_cnt[0]);
+      if (s_cnt[1]) atomicAdd(&c->exits, s_cnt[1]);
+      if (s_cnt[2]) atomicAdd(&c->moves, s_cnt[2]);
+      if (s_cnt[3]) atomicAdd(&c->clamped, s_cnt[3]);
+      const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
+      if (ev) atomicOr(&c->error, ev);
+    }
+    my_req = my_exit = my_move = my_clamp = 0ull;
+    my_err = 0u;
+  };
+
+  // scenario fields, loaded when the scenario changes
+  unsigned n_c = 0, K = 0, step = 0, n_out = 0;
+  unsigned long long seed = 0, cap = 0, n_used = 0;
+  F dtF = (F)0;
+  float dtf = 0.0f;
+  int qe0 = 0;
+  bool do_move = false;
+  const F* crec = nullptr;
+  const int2* mrow = nullptr;
+  F* state = nullptr;
+  int hint = -1;
+
+  for (unsigned k = 0; k < n_tiles; ++k) {
+    const unsigned stg = k % STAGES, use = k / STAGES;
+    const unsigned g = g_begin + k;
+    const int s = scen_of_live(live_base, n_scen, g, hint);
+    hint = s;
+    const ScenDev& S = sc[s];
+    const unsigned long long base = (unsigned long long)(g - __ldg(live_base + s)) * kTile;
+    if (s != cur) n_used = S.ctl->n_used;
+    const unsigned n_in = (unsigned)(n_used - base < kTile ? n_used - base : kTile);
+    if (s != cur || since_flush + n_in > kFlushParticles) {
+      if (cur >= 0) flush();
+      const unsigned n_ent = S.n_c * NA;
+      for (unsigned e = tid; e < n_ent; e += THREADS) sacc[e] = 0ull;
+      if (tid < 16) s_pf[tid] = (F)S.params[tid];
+      cur = s;
+      since_flush = 0;
+      n_c = S.n_c;
+      K = S.K;
+      step = S.ctl->step;
+      seed = S.seed;
+      cap = S.cap;
+      dtF = (F)S.dt;
+      dtf = (float)S.dt;
+      do_move = n_c > 1;
+      n_out = S.n_outlets;
+      qe0 = S.q_exp[0];
+      crec = reinterpret_cast<const F*>(S.crec);
+      mrow = S.mrow;
+      state = reinterpret_cast<F*>(S.state);
+      consumer_sync(THREADS);
+    }
+    since_flush += n_in;
+    if (!aborted && !mbar_wait_bounded(&s_full[stg], use & 1u, &s_abort)) {
+      aborted = true;
+      s_abort = 1u;
+      my_err |= 16u;
+    }
+    const unsigned char* buf = stages + stg * TS::bytes;
+    const F* bx = reinterpret_cast<const F*>(buf + TS::off_x);
+    const uint32_t* bpos = reinterpret_cast<const uint32_t*>(buf + TS::off_pos);
+    const uint32_t* bid = reinterpret_cast<const uint32_t*>(buf + TS::off_id);
+    const float* bad = reinterpret_cast<const float*>(buf + TS::off_ad);
+    const float* bah = reinterpret_cast<const float*>(buf + TS::off_ah);
+    const uint8_t* bst = buf + TS::off_st;
+    unsigned nb_t = 0u, ni_t = 0u;
+#pragma unroll 2
+    for (unsigned r = 0; r < PPT; ++r) {
+      const unsigned slot = r * THREADS + (unsigned)tid;
+      const bool act = !aborted && slot < n_in;
+      uint8_t stv = act ? bst[slot] : (uint8_t)kIdle;
+      const bool idle = act && stv == kIdle;
+      bool div = false;
+      if (idle) {
+        const unsigned long long gi = base + slot;
+        const uint32_t p0 = bpos[slot];
+        if (p0 >= n_c) {
+          my_err |= 1u;
+        } else {
+          uint32_t rd[4];
+          philox_raw(seed, bid[slot], step, 0u, rd);
+          const float ad = __fadd_rn(bad[slot], dtf);
+          F rr[(Model::n_upd + 1) & ~1];
+          const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
+          F xx[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            if ((Model::read_mask >> v) & 1u) xx[v] = bx[TS::rank((unsigned)v) * kTile + slot];
+          int st;
+          if constexpr (Model::separable) {
+            F basis;
+            st = Model::update(dtF, xx, rr, basis, s_pf);
+            const long long q = quantize(basis, qe0, my_clamp, my_err);
+            atomicAdd(&sacc[p0], (unsigned long long)q);
+          } else {
+            F ctb[NC];
+            st = Model::update_general(dtF, xx, rr, ctb, s_pf);
+#pragma unroll
+            for (int j = 0; j < NC; ++j) {
+              const double val = __dmul_rn(S.weight, (double)ctb[j]);
+              const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
+              atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
+            }
+          }
+#pragma unroll
+          for (int v = 0; v < NV; ++v) __stcs(state + (size_t)v * cap + gi, xx[v]);
+          if (st == kDivision) {
+            div = true;
+            S.bpos[gi] = p0;
+            ++my_req;
+          }
+          uint32_t p = p0;
+          if (do_move) {
+            if (draw_int(rd[0]) < mthr) {
+              // bisection of move_kernel.hpp L89-L101 over {threshold, neighbour}
+              const int x1 = (int)draw_int(rd[1]);
+              const int2* row = mrow + (size_t)p0 * K;
+              int nb = __ldg(row + (K - 1)).y;
+              int left = 0, right = (int)K - 1;
+              while (left < right) {
+                const int mid = (left + right) >> 1;
+                const int2 pm = __ldg(row + mid);
+                if (x1 > pm.x) {
+                  left = mid + 1;
+                } else {
+                  right = mid;
+                  nb = pm.y;
+                }
+              }
+              p = (uint32_t)nb;
+              ++my_move;
+            }
+            __stcs(S.pos + gi, p);
+          }
+          if (n_out > 0) {
+            float ah = __fadd_rn(bah[slot], dtf);
+            for (unsigned o = 0; o < n_out; ++o) {
+              if (S.outlet_idx[o] == p) {
+                if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {
+                  stv = kExit;
+                  ah = 0.0f;
+                  ++my_exit;
+                  S.status[gi] = kExit;
+                }
+                break;
+              }
+            }
+            __stcs(S.age_h + gi, ah);
+          }
+          __stcs(S.age_d + gi, ad);
+        }
+      }
+      // birth-request word of the 32 slots this warp covers in round r
+      const unsigned bits = __ballot_sync(0xffffffffu, div);
+      const unsigned w0 = r * THREADS + warp * 32u;
+      if (lane == 0 && w0 < n_in) S.bmask[(base + w0) >> 5] = bits;
+      nb_t += (unsigned)__popc(bits);
+      ni_t += __popc(__ballot_sync(0xffffffffu, act && stv != kIdle));
+    }
+    if (lane == 0) {
+      const unsigned t = (unsigned)(base / kTile);
+      if (nb_t) atomicAdd(S.tile_births + t, nb_t);
+      if (ni_t) atomicAdd(S.tile_inactive + t, ni_t);
+    }
+    mbar_arrive(&s_empty[stg]);
+  }
+  if (cur >= 0) flush();
+}
+
+// ---------------------------------------------------------------------------
 // k_plan: per scenario (one block of 1024 threads):
 //  1. exact accumulator totals -> sources: for a separable model
 //     src(j, s) = (w * coef_s(rates_j)) * B_j with B_j the basis total of
@@ -879,6 +1210,12 @@ void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const S
   (void)block;
   k_cycle<Model, F, PPT, THREADS, MINB><<<grid, THREADS, smem, st>>>(sc, n, b);
 }
+template <class Model, class F, int THREADS, int MINB, int STAGES>
+void launch_cycle_tma_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
+                        BatchCtl* b) {
+  (void)block;
+  k_cycle_tma<Model, F, THREADS, MINB, STAGES><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+}
 template <class Model, class F>
 void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
   k_liquid<Model, F><<<dim3(grid_x, n_scen), 256, 0, st>>>(sc, b, do_scalar);
@@ -911,6 +1248,13 @@ int setup_cycle_t(size_t smem, int* blocks_per_sm) {
   if (e != cudaSuccess) return (int)e;
   return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, THREADS, smem);
 }
+template <class Model, class F, int THREADS, int MINB, int STAGES>
+int setup_cycle_tma_t(size_t smem, int* blocks_per_sm) {
+  const void* fn = reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES>);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return (int)e;
+  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, THREADS + 32, smem);
+}
 inline int last_error_t() { return (int)cudaGetLastError(); }
 template <class F>
 void launch_move_thr_t(int n_scen, cudaStream_t st, ScenDev* sc) {
@@ -936,6 +1280,14 @@ KernelSet make_set(int model_id) {
   k.cycle_setup[2] = &setup_cycle_t<Model, F, 4, 256, 2>;
   k.cycle_setup[3] = &setup_cycle_t<Model, F, 2, 512, 2>;
   k.cycle_setup[4] = &setup_cycle_t<Model, F, 1, 1024, 1>;
+  // staged (TMA) variants: 256 consumers with 3 stages, 512 consumers with 2
+  k.cycle[5] = &launch_cycle_tma_t<Model, F, 256, 2, 3>;
+  k.cycle[6] = &launch_cycle_tma_t<Model, F, 512, 2, 2>;
+  k.cycle_setup[5] = &setup_cycle_tma_t<Model, F, 256, 2, 3>;
+  k.cycle_setup[6] = &setup_cycle_tma_t<Model, F, 512, 2, 2>;
+  for (int v = 0; v < kCycleVariants; ++v) k.cycle_extra_smem[v] = 0u;
+  k.cycle_extra_smem[5] = 3u * TileStage<Model, F>::bytes;
+  k.cycle_extra_smem[6] = 2u * TileStage<Model, F>::bytes;
   k.move_thr = &launch_move_thr_t<F>;
   k.liquid = &launch_liquid_t<Model, F>;
   k.plan = &launch_plan_t<Model, F>;

@@ -15,7 +15,7 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 2;
+constexpr int kKernelSetAbi = 3;
 
 using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
@@ -29,10 +29,13 @@ using MoveThrLaunch = void (*)(int, cudaStream_t, ScenDev*);
 // (cudaError_t) with the resident blocks per SM in *blocks_per_sm.
 using CycleSetup = int (*)(size_t smem, int* blocks_per_sm);
 
-// Cycle launch variants: {threads per block, particles per thread}.
-constexpr int kCycleVariants = 5;
-constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024};
-constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1};
+// Cycle launch variants: {threads per block, particles per thread}.  0-4
+// stream particles through registers (k_cycle); 5-6 stage tiles in shared
+// memory through the copy engine (k_cycle_tma: consumer threads plus one
+// producer warp, slots per consumer thread per tile).
+constexpr int kCycleVariants = 7;
+constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024, 288, 544};
+constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1, 4, 2};
 using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*);
 
 struct KernelSet {
@@ -46,6 +49,7 @@ struct KernelSet {
   PlanLaunch plan;
   CycleLaunch cycle[kCycleVariants];
   CycleSetup cycle_setup[kCycleVariants];
+  unsigned cycle_extra_smem[kCycleVariants];  // stage buffers after the accumulator
   MoveThrLaunch move_thr;
   DivideLaunch divide;
   CopyLaunch compact;

@@ -14,7 +14,8 @@
 //   static constexpr int n_rates (<= 7);      factors per compartment
 //   static constexpr int n_upd (<= n_rates);  leading factors update() reads
 //   static constexpr bool separable;          contribution j = coef_j * basis
-//   static constexpr unsigned read_mask;      state variables update() reads
+//   static constexpr unsigned read_mask;      state variables update() reads (it
+//                                             must write every other one)
 //   BMC_UDF_FN static void rates(const double* c, const double* params, F* r);
 //   separable:  BMC_UDF_FN static int update(F dt, F* x, const F* r, F& basis, const F* pf);
 //               BMC_UDF_FN static F coef(const F* r, int j);

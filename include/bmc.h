@@ -59,6 +59,7 @@ extern "C" {
 #define BMC_ERR_CLAMP 2u     /* a contribution exceeded its quantum range */
 #define BMC_ERR_IDS 4u       /* particle id space (2^32) exhausted */
 #define BMC_ERR_COMPACT 8u   /* compaction lists disagree (internal) */
+#define BMC_ERR_TIMEOUT 16u  /* a bounded wait inside a kernel gave up (the step is void) */
 
 typedef struct bmc_scenario bmc_scenario;
 typedef struct bmc_batch bmc_batch;
@@ -317,6 +318,11 @@ int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t ste
  * Reference counterpart: the Kokkos-tools region timers of the cycle
  * (tools/benchs/benchmark.py L145-L229). */
 int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* kernel_ms);
+
+/* One batched step like bmc_batch_run(b, dt, 1), launched without a graph
+ * with CUDA events between the six kernels (kernel_ms as in
+ * bmc_step_timed); waits for the step. */
+int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms);
 
 /* bmc_run with CUDA events recorded on the scenario's stream before the
  * first and after the last step; *elapsed_ms receives the device time. */

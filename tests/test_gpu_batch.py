@@ -29,7 +29,7 @@ def _mix(n=7, scale=0.02):
     return [scenarios.batch_scenario(k, seed=77, particle_scale=scale) for k in range(n)]
 
 
-@pytest.mark.parametrize("shape", [(256, 2, 0), (1024, 1, 0)])
+@pytest.mark.parametrize("shape", [(256, 2, 0), (1024, 1, 0), (288, 4, 0), (544, 2, 0)])
 def test_batch_equals_alone(shape):
     from bmc.sim import GpuBatch, GpuScenario
 

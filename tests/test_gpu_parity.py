@@ -94,14 +94,21 @@ def test_cycle_only_uses_given_concentrations(oracle_mod):
     assert np.array_equal(g.liquid()["src"].view(np.uint64), o.src.view(np.uint64))
 
 
+# default launch shape, and the shape that stages tiles through the copy engine
+SHAPES = [None, (288, 4, 0)]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("f64", [True, False])
-def test_lattice_overflow_model(oracle_mod, f64):
+def test_lattice_overflow_model(oracle_mod, f64, shape):
     sc = scenarios.workload(2, n_particles=40000, n_steps=6, f64=f64)
     sc.net = __import__("bmc.networks", fromlist=["x"]).lattice_vortex(4, seed=7)
     sc.c0 = sc.c0[: sc.net.n_c]
     sc.feeds[0].outlet = sc.net.n_c - 1
     sc.feeds[0].flow = 2e-4
     g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
     for k in range(6):
         gs = g.step()
         os_ = o.step(4)
@@ -110,10 +117,13 @@ def test_lattice_overflow_model(oracle_mod, f64):
     assert_same_particles(g, o, "end")
 
 
+@pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("general", [False, True])
-def test_fixed_length_reference_model(oracle_mod, general):
+def test_fixed_length_reference_model(oracle_mod, general, shape):
     sc = scenarios.small_ring(16000, model=scenarios.fixed_length(general=general), feeds=True)
     g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
     births = 0
     for k in range(60):
         gs = g.step()
@@ -126,12 +136,15 @@ def test_fixed_length_reference_model(oracle_mod, general):
     assert_same_liquid(g, o, "end")
 
 
-def test_divisions_overflow_and_compaction(oracle_mod):
+@pytest.mark.parametrize("shape", SHAPES)
+def test_divisions_overflow_and_compaction(oracle_mod, shape):
     # division mass inside the initial range: many births, refusals once full
     m = scenarios.monod(f64=True, m_div=1.0)
     sc = scenarios.zero_d(3000, model=m, outlet=True)
     sc.feeds[0].flow = 1e-3  # strong outlet: exits trigger compaction
     g, o = make_pair(oracle_mod, sc, capacity=4096)
+    if shape:
+        g.set_shape(*shape)
     saw = {"births": 0, "overflow": 0, "compacted": 0}
     for k in range(25):
         gs = g.step()
@@ -171,7 +184,8 @@ def test_repartition_and_force_remove(oracle_mod):
     assert_same_particles(g, o, "force_remove_dead")
 
 
-@pytest.mark.parametrize("shape", [(256, 1, 0), (256, 2, 0), (256, 4, 1), (512, 2, 0), (1024, 1, 0)])
+@pytest.mark.parametrize("shape", [(256, 1, 0), (256, 2, 0), (256, 4, 1), (512, 2, 0), (1024, 1, 0),
+                                   (288, 4, 0), (288, 4, 1), (544, 2, 0)])
 def test_launch_shapes_bit_identical(oracle_mod, shape):
     """Results do not depend on the launch shape: sums are exact."""
     sc = scenarios.workload(2, n_particles=30000, f64=True)

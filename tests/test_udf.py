@@ -142,7 +142,8 @@ def test_gpu_library_matches_builtin_model(f64):
 
 
 @pytest.mark.gpu
-def test_gpu_library_model_matches_oracle(oracle_mod):
+@pytest.mark.parametrize("shape", [None, (288, 4, 0)])
+def test_gpu_library_model_matches_oracle(oracle_mod, shape):
     """A model that is not built into libbmc (the general contribution
     path): GPU kernels from the library against the oracle driving the
     library's host functions, step by step."""
@@ -151,6 +152,8 @@ def test_gpu_library_model_matches_oracle(oracle_mod):
     sc = scenarios.small_ring(16000, f64=False, model=minimal_udf_spec(), feeds=True)
     sc.alloc_factor = 2.0
     g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
     births = 0
     for k in range(40):
         gs, os_ = g.step(), o.step()
