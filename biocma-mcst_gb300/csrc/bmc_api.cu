@@ -468,12 +468,8 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
   if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
   // rows {floor(2^24 CDF(k)), neighbour(k)}: u > CDF <=> x > floor(2^24 CDF)
-  // for the integer draw x = u 2^24; rows must be non-decreasing.  Rows are
-  // padded to an even length Kp with copies of their last entry (16-byte
-  // aligned rows for vector loads); the first entry with x <= threshold,
-  // or else the last one, names the same neighbour either way.
-  const uint32_t Kp = (K + 1u) & ~1u;
-  std::vector<int2> mrow((size_t)n_c * Kp);
+  // for the integer draw x = u 2^24; rows must be non-decreasing
+  std::vector<int2> mrow((size_t)n_c * K);
   for (uint32_t i = 0; i < n_c; ++i) {
     int32_t prev = -2;
     for (uint32_t k = 0; k < K; ++k) {
@@ -490,9 +486,8 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
       }
       if (th < prev) return fail(BMC_E_INVALID, "cumulative probability rows must be non-decreasing");
       prev = th;
-      mrow[(size_t)i * Kp + k] = make_int2(th, (int)nb);
+      mrow[q] = make_int2(th, (int)nb);
     }
-    for (uint32_t k = K; k < Kp; ++k) mrow[(size_t)i * Kp + k] = mrow[(size_t)i * Kp + K - 1];
   }
   std::vector<double> vol(volume, volume + n_c), outf(out_flows, out_flows + n_c), vinv(n_c), diag(n_c);
   for (uint32_t j = 0; j < n_c; ++j) {
@@ -502,7 +497,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     diag[j] = -outf[j];
   }
   ScenDev& h = s->h;
-  const bool resize = !s->has_domain || h.n_c != n_c || h.K != Kp;
+  const bool resize = !s->has_domain || h.n_c != n_c || h.K != K;
   if (resize) {
     cudaStreamSynchronize(s->stream);
     if (s->darena) cudaFree(s->darena);
@@ -510,7 +505,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_acc;
     Carver cv;
     int2* p_mrow = nullptr;
-    cv.add(&p_mrow, (size_t)n_c * Kp);
+    cv.add(&p_mrow, (size_t)n_c * K);
     double* p_vol = nullptr;
     cv.add(&p_vol, n_c);
     double* p_out = nullptr;
@@ -539,7 +534,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     s->has_transition = false;
   }
   h.n_c = n_c;
-  h.K = Kp;
+  h.K = K;
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.volume), vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<int2*>(h.mrow), mrow.data(), mrow.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));

@@ -226,50 +226,6 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
   return rec_move_thr(__ldg(p + 7));
 }
 
-// Destination of a leaving particle: the first entry k of the compartment's
-// row with x1 <= threshold_k, or the last entry when there is none -- the
-// result of the reference's bisection (move_kernel.hpp L89-L101) over a
-// non-decreasing row.  Rows (even length Kp, 16-byte aligned) of up to
-// kRowVec entries are fetched with independent 16-byte loads, one memory
-// round trip, and the answer is the count of thresholds below x1 (a prefix
-// of the row), selected in registers; longer rows are bisected in memory.
-constexpr unsigned kRowVec = 6;
-__device__ __forceinline__ int next_compartment(const int2* __restrict__ row, unsigned Kp, int x1) {
-  if (Kp <= kRowVec) {
-    const int4* r4 = reinterpret_cast<const int4*>(row);
-    int4 v[kRowVec / 2];
-#pragma unroll
-    for (unsigned j = 0; j < kRowVec / 2; ++j)
-      if (2u * j < Kp) v[j] = __ldg(r4 + j);
-    unsigned m = 0;
-#pragma unroll
-    for (unsigned j = 0; j < kRowVec / 2; ++j)
-      if (2u * j < Kp) m += (unsigned)(v[j].x < x1) + (unsigned)(v[j].z < x1);
-    const unsigned idx = m < Kp ? m : Kp - 1u;
-    int nb = v[0].y;
-#pragma unroll
-    for (unsigned j = 0; j < kRowVec / 2; ++j)
-      if (2u * j < Kp) {
-        nb = idx == 2u * j ? v[j].y : nb;
-        nb = idx == 2u * j + 1u ? v[j].w : nb;
-      }
-    return nb;
-  }
-  int nb = __ldg(row + (Kp - 1)).y;
-  int left = 0, right = (int)Kp - 1;
-  while (left < right) {
-    const int mid = (left + right) >> 1;
-    const int2 pm = __ldg(row + mid);
-    if (x1 > pm.x) {
-      left = mid + 1;
-    } else {
-      right = mid;
-      nb = pm.y;
-    }
-  }
-  return nb;
-}
-
 // ---------------------------------------------------------------------------
 // k_cycle: the fused per-particle hot path.  Each block of a persistent
 // grid streams a contiguous run of the live tiles (1024-slot tiles that hold
@@ -473,7 +429,25 @@ __global__ void __launch_bounds__(THREADS, MINB)
             uint32_t p = p0;
             if (do_move) {
               if (draw_int(r[0]) < mthr) {
-                p = (uint32_t)next_compartment(mrow + (size_t)p0 * K, K, (int)draw_int(r[1]));
+                // the reference's bisection (move_kernel.hpp L89-L101) over the
+                // {threshold, neighbour} pairs of the row; the neighbour of the
+                // answer comes with the probe that set `right`, or with the
+                // last pair, loaded ahead
+                const int x1 = (int)draw_int(r[1]);
+                const int2* row = mrow + (size_t)p0 * K;
+                int nb = __ldg(row + (K - 1)).y;
+                int left = 0, right = (int)K - 1;
+                while (left < right) {
+                  const int mid = (left + right) >> 1;
+                  const int2 pm = __ldg(row + mid);
+                  if (x1 > pm.x) {
+                    left = mid + 1;
+                  } else {
+                    right = mid;
+                    nb = pm.y;
+                  }
+                }
+                p = (uint32_t)nb;
                 ++my_move;
               }
               pv[k] = p;
@@ -797,7 +771,22 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           uint32_t p = p0;
           if (do_move) {
             if (draw_int(rd[0]) < mthr) {
-              p = (uint32_t)next_compartment(mrow + (size_t)p0 * K, K, (int)draw_int(rd[1]));
+              // bisection of move_kernel.hpp L89-L101 over {threshold, neighbour}
+              const int x1 = (int)draw_int(rd[1]);
+              const int2* row = mrow + (size_t)p0 * K;
+              int nb = __ldg(row + (K - 1)).y;
+              int left = 0, right = (int)K - 1;
+              while (left < right) {
+                const int mid = (left + right) >> 1;
+                const int2 pm = __ldg(row + mid);
+                if (x1 > pm.x) {
+                  left = mid + 1;
+                } else {
+                  right = mid;
+                  nb = pm.y;
+                }
+              }
+              p = (uint32_t)nb;
               ++my_move;
             }
             __stcs(S.pos + gi, p);
