@@ -106,6 +106,9 @@ SIGNATURES = {
     "bmc_batch_step_timed": [VP, c_dbl, VP],
     "bmc_set_device": [c_i32],
     "bmc_transfer_bytes": [VP, VP],
+    "bmc_flowmap_add": [VP, VP, VP, VP, VP, c_u64, VP, VP, VP],
+    "bmc_flowmap_period": [VP, c_dbl],
+    "bmc_flowmap_clear": [VP],
     "bmc_udf_load": [ct.c_char_p, VP],
     "bmc_udf_get_info": [c_i32, VP],
     "bmc_udf_get_host_model": [c_i32, c_i32, VP],

@@ -102,6 +102,17 @@ class Scenario:
     dead_ratio_threshold: float = 0.01
     min_removal: int = 0
     uniform_init: bool = True
+    # flow-map cycle: states of the same mesh replayed in turn (flowmaps[0]
+    # is `net`, the state the run starts on); empty: fixed domain
+    flowmaps: list = field(default_factory=list)
+    t_per_flowmap: float = 0.0
+
+    @property
+    def n_per_flowmap(self) -> int:
+        """compute_n_per_flowmap (apps/core/src/global_initaliser.cpp L104-L114)."""
+        if self.t_per_flowmap == 0 or len(self.flowmaps) <= 1:
+            return 1
+        return int(self.t_per_flowmap / self.dt) + 1
 
     @property
     def capacity(self) -> int:

@@ -77,6 +77,10 @@ class GpuScenario:
                 for sp in range(len(fd.conc)):
                     arr[k].conc[sp] = float(fd.conc[sp])
             call("bmc_set_feeds", self.handle, len(scen.feeds), arr)
+        for fm in scen.flowmaps:
+            self.add_flowmap(fm)
+        if scen.flowmaps:
+            call("bmc_flowmap_period", self.handle, scen.t_per_flowmap)
         self.weight = None
         if init:
             self.init_particles(n_particles)
@@ -104,6 +108,15 @@ class GpuScenario:
     def set_weight(self, w: float):
         call("bmc_set_weight", self.handle, w)
         self.weight = w
+
+    def add_flowmap(self, net):
+        """Append a flow-map state of the same mesh (bmc_flowmap_add)."""
+        vol = np.ascontiguousarray(net.volume, dtype=np.float64)
+        nbr = np.ascontiguousarray(net.neighbors, dtype=np.uint64)
+        outf = np.ascontiguousarray(net.out_flow, dtype=np.float64)
+        cdf = np.ascontiguousarray(net.cdf, dtype=np.float64)
+        r, c, v = transition_coo(net)
+        call("bmc_flowmap_add", self.handle, _p(vol), _p(nbr), _p(outf), _p(cdf), len(v), _p(r), _p(c), _p(v))
 
     def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
         call("bmc_set_shape", self.handle, threads, ppt, blocks_per_sm)

@@ -85,6 +85,65 @@ int ceil_log2(double v) {
   return m == 0.5 ? ex - 1 : ex;
 }
 
+// {floor(2^24 CDF(k)), neighbour(k)} rows of a domain; u > CDF <=> x >
+// floor(2^24 CDF) for the integer draw x = u 2^24.  Returns an error text.
+const char* build_rows(uint32_t n_c, uint32_t K, const uint64_t* neighbors, const double* cdf,
+                       std::vector<int2>& mrow) {
+  mrow.assign((size_t)n_c * K, make_int2(0, 0));
+  for (uint32_t i = 0; i < n_c; ++i) {
+    int32_t prev = -2;
+    for (uint32_t k = 0; k < K; ++k) {
+      const size_t q = (size_t)i * K + k;
+      uint32_t nb = i;
+      if (neighbors) {
+        if (neighbors[q] >= n_c) return "neighbor index out of range";
+        nb = (uint32_t)neighbors[q];
+      }
+      int32_t th = 1 << 24;
+      if (cdf) {
+        if (!(cdf[q] == cdf[q])) return "cumulative probability is NaN";
+        th = (int32_t)std::max(-1.0, std::min(16777216.0, std::floor(cdf[q] * 16777216.0)));
+      }
+      if (th < prev) return "cumulative probability rows must be non-decreasing";
+      prev = th;
+      mrow[q] = make_int2(th, (int)nb);
+    }
+  }
+  return nullptr;
+}
+
+// Liquid transition in COO form -> incoming lists by destination column
+// (sources ascending, duplicates summed) and the diagonal.
+const char* build_csr(uint32_t n, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* values,
+                      std::vector<uint32_t>& ptr, std::vector<uint32_t>& idx, std::vector<double>& val,
+                      std::vector<double>& diag) {
+  std::vector<std::pair<std::pair<uint32_t, uint32_t>, double>> off;
+  diag.assign(n, 0.0);
+  off.reserve(nnz);
+  for (uint64_t k = 0; k < nnz; ++k) {
+    if (rows[k] >= n || cols[k] >= n) return "transition index out of range";
+    if (rows[k] == cols[k])
+      diag[rows[k]] += values[k];
+    else
+      off.push_back({{(uint32_t)cols[k], (uint32_t)rows[k]}, values[k]});
+  }
+  std::stable_sort(off.begin(), off.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  ptr.assign(n + 1, 0u);
+  idx.clear();
+  val.clear();
+  for (size_t k = 0; k < off.size(); ++k) {
+    if (!idx.empty() && k > 0 && off[k].first == off[k - 1].first) {
+      val.back() += off[k].second;
+      continue;
+    }
+    idx.push_back(off[k].first.second);
+    val.push_back(off[k].second);
+    ptr[off[k].first.first + 1]++;
+  }
+  for (uint32_t j = 0; j < n; ++j) ptr[j + 1] += ptr[j];
+  return nullptr;
+}
+
 // Launch status of the kernels a set just enqueued: this module's runtime
 // error state and that of the module owning the kernels (a plugin may carry
 // its own copy of the runtime).
@@ -118,9 +177,21 @@ struct bmc_scenario {
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
   unsigned graph_grid = 0;
+  // flow-map cycle (host copies; device copies in marena)
+  struct FlowMap {
+    std::vector<int2> mrow;
+    std::vector<double> vol, vinv, outf, diag;
+    std::vector<uint32_t> ptr, idx;
+    std::vector<double> val;
+  };
+  std::vector<FlowMap> maps;
+  double t_per_map = 0.0;
+  void* marena = nullptr;
+  uint32_t* d_map_exit = nullptr;
 };
 
 struct bmc_batch {
+  bool graph_maps = false;  // the captured graph includes the flow-map switch
   std::vector<bmc_scenario*> scen;
   const bmc::KernelSet* ks = nullptr;
   cudaStream_t stream = nullptr;
@@ -174,13 +245,41 @@ void derive_outlets(bmc_scenario* s) {
   }
 }
 
+// Flow-map tables that depend on dt: steps per map (compute_n_per_flowmap,
+// apps/core/src/global_initaliser.cpp L104-L114) and each map's outlet
+// thresholds (as derive_outlets, with that map's volumes).
+int refresh_map_tables(bmc_scenario* s) {
+  const size_t nm = s->maps.size();
+  s->h.n_maps = (uint32_t)nm;
+  if (nm == 0) {
+    s->h.n_per_map = 1;
+    return BMC_OK;
+  }
+  const double t = s->t_per_map;
+  s->h.n_per_map = (t == 0.0 || nm == 1 || s->dt <= 0.0) ? 1u : (uint32_t)(size_t)(t / s->dt) + 1u;
+  std::vector<uint32_t> thr(nm * bmc::kMaxOutlets, 0u);
+  for (size_t m = 0; m < nm; ++m) {
+    unsigned o = 0;
+    for (const bmc_feed& fd : s->feeds) {
+      if (fd.outlet < 0) continue;
+      const double vol = s->maps[m].vol[(size_t)fd.outlet];
+      const double th = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
+      thr[m * bmc::kMaxOutlets + o++] = (uint32_t)std::min(16777216.0, std::floor(th * 16777216.0));
+    }
+  }
+  BMC_CUDA(counted_memcpy_async(s->d_map_exit, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+  return BMC_OK;
+}
+
 int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
   if (!(dt > 0.0)) return fail(BMC_E_INVALID, "dt must be > 0");
   if (dt == s->dt) return BMC_OK;
   s->dt = dt;
   s->h.dt = dt;
   derive_outlets(s);
-  int rc = upload_desc(s);
+  int rc = refresh_map_tables(s);
+  if (rc) return rc;
+  rc = upload_desc(s);
   if (rc) return rc;
   if (launch_pmove) {
     s->ks->move_thr(1, s->stream, s->d_desc);
@@ -215,8 +314,14 @@ unsigned liquid_grid(const ScenDev& h) {
   return std::max(1u, (h.n_c + cb - 1) / cb);
 }
 
+// With `maps`, the flow-map switch runs first (main-loop steps only).
 int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned liq_grid,
-                 BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count) {
+                 BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count,
+                 bool maps) {
+  if (maps && do_scalar) {
+    ks->flowmap(n_scen, st, d_table);
+    g_launches += 1;
+  }
   ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
   ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl);
   ks->plan(n_scen, st, d_table, d_bctl);
@@ -226,6 +331,12 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
   g_launches += 6;
   BMC_CUDA(launch_status(ks));
   return BMC_OK;
+}
+
+bool batch_has_maps(const bmc_batch* b) {
+  for (const bmc_scenario* m : b->scen)
+    if (m->h.n_maps > 0) return true;
+  return false;
 }
 
 // Refresh a batch's descriptor table for dt (uploading it when a member
@@ -457,6 +568,7 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->parena) cudaFree(s->parena);
   if (s->darena) cudaFree(s->darena);
   if (s->tarena) cudaFree(s->tarena);
+  if (s->marena) cudaFree(s->marena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   cudaStreamDestroy(s->stream);
   delete s;
@@ -467,28 +579,9 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
                       const double* out_flows, const double* cdf) {
   if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
   if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
-  // rows {floor(2^24 CDF(k)), neighbour(k)}: u > CDF <=> x > floor(2^24 CDF)
-  // for the integer draw x = u 2^24; rows must be non-decreasing
-  std::vector<int2> mrow((size_t)n_c * K);
-  for (uint32_t i = 0; i < n_c; ++i) {
-    int32_t prev = -2;
-    for (uint32_t k = 0; k < K; ++k) {
-      const size_t q = (size_t)i * K + k;
-      uint32_t nb = i;
-      if (neighbors) {
-        if (neighbors[q] >= n_c) return fail(BMC_E_INVALID, "neighbor index out of range");
-        nb = (uint32_t)neighbors[q];
-      }
-      int32_t th = 1 << 24;
-      if (cdf) {
-        if (!(cdf[q] == cdf[q])) return fail(BMC_E_INVALID, "cumulative probability is NaN");
-        th = (int32_t)std::max(-1.0, std::min(16777216.0, std::floor(cdf[q] * 16777216.0)));
-      }
-      if (th < prev) return fail(BMC_E_INVALID, "cumulative probability rows must be non-decreasing");
-      prev = th;
-      mrow[q] = make_int2(th, (int)nb);
-    }
-  }
+  if (!s->maps.empty()) return fail(BMC_E_STATE, "the domain follows the flow-map cycle (bmc_flowmap_clear first)");
+  std::vector<int2> mrow;
+  if (const char* why = build_rows(n_c, K, neighbors, cdf, mrow)) return fail(BMC_E_INVALID, why);
   std::vector<double> vol(volume, volume + n_c), outf(out_flows, out_flows + n_c), vinv(n_c), diag(n_c);
   for (uint32_t j = 0; j < n_c; ++j) {
     if (!(vol[j] > 0.0)) return fail(BMC_E_INVALID, "volumes must be > 0");
@@ -562,30 +655,10 @@ int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint
   if (!s || (nnz && (!rows || !cols || !values))) return fail(BMC_E_INVALID, "bad transition arguments");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   if (n != s->h.n_c) return fail(BMC_E_INVALID, "transition size differs from n_compartments");
-  // incoming lists by destination column, sources ascending, duplicates summed
-  std::vector<std::pair<std::pair<uint32_t, uint32_t>, double>> off;
-  std::vector<double> diag(n, 0.0);
-  off.reserve(nnz);
-  for (uint64_t k = 0; k < nnz; ++k) {
-    if (rows[k] >= n || cols[k] >= n) return fail(BMC_E_INVALID, "transition index out of range");
-    if (rows[k] == cols[k])
-      diag[rows[k]] += values[k];
-    else
-      off.push_back({{(uint32_t)cols[k], (uint32_t)rows[k]}, values[k]});
-  }
-  std::stable_sort(off.begin(), off.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
-  std::vector<uint32_t> ptr(n + 1, 0u), idx;
-  std::vector<double> val;
-  for (size_t k = 0; k < off.size(); ++k) {
-    if (!idx.empty() && k > 0 && off[k].first == off[k - 1].first) {
-      val.back() += off[k].second;
-      continue;
-    }
-    idx.push_back(off[k].first.second);
-    val.push_back(off[k].second);
-    ptr[off[k].first.first + 1]++;
-  }
-  for (uint32_t j = 0; j < n; ++j) ptr[j + 1] += ptr[j];
+  if (!s->maps.empty()) return fail(BMC_E_STATE, "the domain follows the flow-map cycle (bmc_flowmap_clear first)");
+  std::vector<uint32_t> ptr, idx;
+  std::vector<double> val, diag;
+  if (const char* why = build_csr(n, nnz, rows, cols, values, ptr, idx, val, diag)) return fail(BMC_E_INVALID, why);
   cudaStreamSynchronize(s->stream);
   if (s->tarena) cudaFree(s->tarena);
   s->tarena = nullptr;
@@ -647,7 +720,9 @@ int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
   }
   s->feeds.assign(feeds, feeds + n_feeds);
   derive_outlets(s);
-  int rc = upload_desc(s);
+  int rc = refresh_map_tables(s);
+  if (rc) return rc;
+  rc = upload_desc(s);
   if (rc) return rc;
   BMC_CUDA(cudaStreamSynchronize(s->stream));
   return BMC_OK;
@@ -735,7 +810,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
   int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, s->variant, grid, smem,
-                        s->sm_count);
+                        s->sm_count, s->h.n_maps > 0);
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc) {
@@ -771,7 +846,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, s->variant, grid, smem,
-                      s->sm_count);
+                      s->sm_count, s->h.n_maps > 0);
     if (rc) return rc;
   }
   return BMC_OK;
@@ -1049,14 +1124,14 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   size_t smem = 0;
   int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
-  if (!b->graph || b->graph_smem != smem || b->graph_grid != grid) {
+  if (!b->graph || b->graph_smem != smem || b->graph_grid != grid || b->graph_maps != batch_has_maps(b)) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
     rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->variant, grid, smem,
-                      b->scen[0]->sm_count);
+                      b->scen[0]->sm_count, batch_has_maps(b));
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -1069,6 +1144,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     b->graph_smem = smem;
     b->graph_grid = grid;
+    b->graph_maps = batch_has_maps(b);
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     BMC_CUDA(cudaGraphLaunch(b->graph, b->stream));
@@ -1082,6 +1158,155 @@ int bmc_batch_synchronize(bmc_batch* b) {
   BMC_CUDA(cudaStreamSynchronize(b->stream));
   return BMC_OK;
 }
+
+// ---- flow-map cycle -----------------------------------------------------------------
+
+namespace {
+
+// Uploads every map of the cycle (one arena) and sizes the current
+// incoming-flow lists for the largest map; map 0 is copied in at the next
+// step (map_cur reset).
+int upload_maps(bmc_scenario* s) {
+  ScenDev& h = s->h;
+  const size_t nm = s->maps.size(), n_c = h.n_c, K = h.K;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->marena) {
+    // the current incoming-flow lists lived in the map arena: a transition
+    // has to be given again (bmc_set_transition_coo) before the next step
+    cudaFree(s->marena);
+    s->marena = nullptr;
+    h.in_ptr = nullptr;
+    h.in_idx = nullptr;
+    h.in_flow = nullptr;
+    s->has_transition = false;
+  }
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  if (nm == 0) {
+    h.n_maps = 0;
+    h.n_per_map = 1;
+    h.map_mrow = nullptr;
+    h.map_volume = h.map_vinv = h.map_out_flow = h.map_diag = h.map_in_flow = nullptr;
+    h.map_in_ptr = h.map_in_idx = h.map_exit_thr = nullptr;
+    s->d_map_exit = nullptr;
+    int rc = upload_desc(s);
+    if (rc) return rc;
+    BMC_CUDA(cudaStreamSynchronize(s->stream));
+    return BMC_OK;
+  }
+  size_t nnz_max = 1;
+  for (const auto& m : s->maps) nnz_max = std::max(nnz_max, m.idx.size());
+  Carver cv;
+  int2* p_mrow = nullptr;
+  double *p_vol = nullptr, *p_vinv = nullptr, *p_out = nullptr, *p_diag = nullptr, *p_flow = nullptr;
+  uint32_t *p_ptr = nullptr, *p_idx = nullptr, *p_exit = nullptr;
+  cv.add(&p_mrow, nm * n_c * K);
+  cv.add(&p_vol, nm * n_c);
+  cv.add(&p_vinv, nm * n_c);
+  cv.add(&p_out, nm * n_c);
+  cv.add(&p_diag, nm * n_c);
+  cv.add(&p_ptr, nm * (n_c + 1));
+  cv.add(&p_idx, nm * nnz_max);
+  cv.add(&p_flow, nm * nnz_max);
+  cv.add(&p_exit, nm * bmc::kMaxOutlets);
+  // current incoming-flow lists, large enough for every map
+  uint32_t *c_ptr = nullptr, *c_idx = nullptr;
+  double* c_flow = nullptr;
+  cv.add(&c_ptr, n_c + 1);
+  cv.add(&c_idx, nnz_max);
+  cv.add(&c_flow, nnz_max);
+  BMC_CUDA(cudaMalloc(&s->marena, cv.off));
+  cv.bind(s->marena);
+  BMC_CUDA(cudaMemsetAsync(s->marena, 0, cv.off, s->stream));
+  for (size_t m = 0; m < nm; ++m) {
+    const auto& f = s->maps[m];
+    BMC_CUDA(counted_memcpy_async(p_mrow + m * n_c * K, f.mrow.data(), n_c * K * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_vol + m * n_c, f.vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_vinv + m * n_c, f.vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_out + m * n_c, f.outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_diag + m * n_c, f.diag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_ptr + m * (n_c + 1), f.ptr.data(), (n_c + 1) * 4, cudaMemcpyHostToDevice, s->stream));
+    if (!f.idx.empty()) {
+      BMC_CUDA(counted_memcpy_async(p_idx + m * nnz_max, f.idx.data(), f.idx.size() * 4, cudaMemcpyHostToDevice, s->stream));
+      BMC_CUDA(counted_memcpy_async(p_flow + m * nnz_max, f.val.data(), f.val.size() * 8, cudaMemcpyHostToDevice, s->stream));
+    }
+  }
+  h.map_mrow = p_mrow;
+  h.map_volume = p_vol;
+  h.map_vinv = p_vinv;
+  h.map_out_flow = p_out;
+  h.map_diag = p_diag;
+  h.map_in_ptr = p_ptr;
+  h.map_in_idx = p_idx;
+  h.map_in_flow = p_flow;
+  h.map_exit_thr = p_exit;
+  h.map_nnz_max = (uint32_t)nnz_max;
+  s->d_map_exit = p_exit;
+  h.in_ptr = c_ptr;
+  h.in_idx = c_idx;
+  h.in_flow = c_flow;
+  s->has_transition = true;
+  // the host's view of the volumes (outlet thresholds of the fixed-domain
+  // path) follows map 0 until the device switches
+  s->volume = s->maps[0].vol;
+  derive_outlets(s);
+  int rc = refresh_map_tables(s);
+  if (rc) return rc;
+  const unsigned none = 0xffffffffu;
+  BMC_CUDA(counted_memcpy_async(&s->d_ctl->map_cur, &none, sizeof(none), cudaMemcpyHostToDevice, s->stream));
+  rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neighbors, const double* out_flows,
+                    const double* cdf, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* values) {
+  if (!s || !volume || !out_flows || (nnz && (!rows || !cols || !values)))
+    return fail(BMC_E_INVALID, "bad flow-map arguments");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update fixes n_compartments and K)");
+  const uint32_t n_c = s->h.n_c, K = s->h.K;
+  if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
+  bmc_scenario::FlowMap f;
+  if (const char* why = build_rows(n_c, K, neighbors, cdf, f.mrow)) return fail(BMC_E_INVALID, why);
+  f.vol.assign(volume, volume + n_c);
+  f.outf.assign(out_flows, out_flows + n_c);
+  f.vinv.resize(n_c);
+  for (uint32_t j = 0; j < n_c; ++j) {
+    if (!(f.vol[j] > 0.0)) return fail(BMC_E_INVALID, "volumes must be > 0");
+    if (!(f.outf[j] >= 0.0)) return fail(BMC_E_INVALID, "out flows must be >= 0");
+    f.vinv[j] = 1.0 / f.vol[j];
+  }
+  if (const char* why = build_csr(n_c, nnz, rows, cols, values, f.ptr, f.idx, f.val, f.diag))
+    return fail(BMC_E_INVALID, why);
+  if (nnz == 0)
+    for (uint32_t j = 0; j < n_c; ++j) f.diag[j] = -f.outf[j];
+  s->maps.push_back(std::move(f));
+  return upload_maps(s);
+}
+
+int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap) {
+  if (!s || !(t_per_flowmap >= 0.0)) return fail(BMC_E_INVALID, "t_per_flowmap must be >= 0");
+  s->t_per_map = t_per_flowmap;
+  int rc = refresh_map_tables(s);
+  if (rc) return rc;
+  rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_flowmap_clear(bmc_scenario* s) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  s->maps.clear();
+  return upload_maps(s);
+}
+
+}  // extern "C"
 
 // ---- diagnostics -----------------------------------------------------------------
 
@@ -1098,6 +1323,10 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = s->stream;
   const unsigned variant = s->variant;
+  if (s->h.n_maps > 0) {
+    s->ks->flowmap(1, st, s->d_desc);
+    g_launches++;
+  }
   BMC_CUDA(cudaEventRecord(ev[0], st));
   s->ks->liquid(1, liquid_grid(s->h), st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
@@ -1130,6 +1359,10 @@ int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = b->stream;
   const unsigned variant = b->variant;
+  if (batch_has_maps(b)) {
+    b->ks->flowmap(n, st, b->d_table);
+    g_launches++;
+  }
   BMC_CUDA(cudaEventRecord(ev[0], st));
   b->ks->liquid(n, max_nc, st, b->d_table, b->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));

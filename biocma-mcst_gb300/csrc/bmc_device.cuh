@@ -65,7 +65,7 @@ struct Control {
   unsigned long long last_overflow;
   unsigned long long last_req_div;
   unsigned int last_compacted;
-  unsigned int pad;
+  unsigned int map_cur;  // flow map the domain arrays hold (0xffffffff: none yet)
   double mass_balance[kMaxSpecies];
   // per-species sums of the liquid step (new mass, expected mass)
   double mb_new[kMaxSpecies];
@@ -139,6 +139,21 @@ struct ScenDev {
   Control* ctl;
   int32_t f64;
   uint32_t step_limit;  // 0: none; otherwise steps stop (no-op) once ctl->step reaches it
+  // Flow-map cycle: n_maps domain states stored back to back; step k runs on
+  // map (k / n_per_map) % n_maps, copied into the domain arrays above when
+  // it changes (k_flowmap).  n_maps == 0: the domain is fixed.
+  uint32_t n_maps;
+  uint32_t n_per_map;
+  uint32_t map_nnz_max;  // stride of the incoming-flow lists
+  const int2* map_mrow;          // [n_maps][n_c * K]
+  const double* map_volume;      // [n_maps][n_c]
+  const double* map_vinv;        // [n_maps][n_c]
+  const double* map_out_flow;    // [n_maps][n_c]
+  const double* map_diag;        // [n_maps][n_c]
+  const uint32_t* map_in_ptr;    // [n_maps][n_c + 1]
+  const uint32_t* map_in_idx;    // [n_maps][map_nnz_max]
+  const double* map_in_flow;     // [n_maps][map_nnz_max]
+  const uint32_t* map_exit_thr;  // [n_maps][kMaxOutlets], for the current dt
 };
 
 // A scenario whose step counter has reached its limit is left untouched.

@@ -931,6 +931,7 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     ctl->n_used = after + births;
     ctl->inactive = compact ? 0ull : inactive_after;
     ctl->next_id += births;
+    if (S.n_maps > 0u) ctl->map_cur = (ctl->step / S.n_per_map) % S.n_maps;
     ctl->step += 1u;
     ctl->last_births = births;
     ctl->last_exits = ctl->exits;
@@ -1200,6 +1201,59 @@ __global__ void k_move_thr(ScenDev* __restrict__ sc) {
   }
 }
 
+// k_flowmap: the flow-map cycle of the reference's main loop
+// (host_specific.cpp L255-L266: when the transitioner advances, the next
+// flow-map state replaces the domain -- volumes, neighbours, out-flows,
+// cumulative probabilities, liquid transition).  At the start of step k the
+// state in use is m = (k / n_per_map) % n_maps; when it differs from the one
+// the domain arrays hold (ctl->map_cur, set by k_plan) it is copied in and
+// the move thresholds of the compartment records are recomputed as
+// k_move_thr does.  The outlet thresholds of m (computed on the host for the
+// current dt) are written every step.  Grid: (blocks, scenarios).
+template <class F>
+__global__ void k_flowmap(ScenDev* __restrict__ sc) {
+  ScenDev& S = sc[blockIdx.y];
+  if (S.n_maps == 0u) return;
+  const Control* ctl = S.ctl;
+  if (scen_finished(S, ctl)) return;
+  const unsigned m = (ctl->step / S.n_per_map) % S.n_maps;
+  if (blockIdx.x == 0 && threadIdx.x < kMaxOutlets) S.exit_thr[threadIdx.x] = S.map_exit_thr[m * kMaxOutlets + threadIdx.x];
+  if (m == ctl->map_cur) return;
+  const unsigned n_c = S.n_c, K = S.K;
+  const size_t o = (size_t)m * n_c;
+  const unsigned stride = gridDim.x * blockDim.x;
+  const unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  F* rec = reinterpret_cast<F*>(S.crec);
+  for (unsigned c = t0; c < n_c; c += stride) {
+    const double vol = S.map_volume[o + c], q = S.map_out_flow[o + c];
+    const_cast<double*>(S.volume)[c] = vol;
+    const_cast<double*>(S.vinv)[c] = S.map_vinv[o + c];
+    const_cast<double*>(S.out_flow)[c] = q;
+    const_cast<double*>(S.diag)[c] = S.map_diag[o + c];
+    const double p = __ddiv_rn(__dmul_rn(S.dt, q), vol);
+    uint32_t t;
+    if (p >= 1.0)
+      t = (1u << 24) + 1u;
+    else if (!(p > 0.0))
+      t = 0u;
+    else
+      t = (uint32_t)ceil(__dmul_rn(p, 16777216.0));
+    if constexpr (sizeof(F) == 4)
+      rec[(size_t)c * 8 + 7] = __uint_as_float(t);
+    else
+      rec[(size_t)c * 8 + 7] = __longlong_as_double((long long)t);
+  }
+  for (size_t e = t0; e < (size_t)n_c * K; e += stride) const_cast<int2*>(S.mrow)[e] = S.map_mrow[o * K + e];
+  const uint32_t* ptr = S.map_in_ptr + (size_t)m * (n_c + 1);
+  for (unsigned c = t0; c <= n_c; c += stride) const_cast<uint32_t*>(S.in_ptr)[c] = ptr[c];
+  const unsigned nnz = ptr[n_c];
+  const size_t on = (size_t)m * S.map_nnz_max;
+  for (unsigned e = t0; e < nnz; e += stride) {
+    const_cast<uint32_t*>(S.in_idx)[e] = S.map_in_idx[on + e];
+    const_cast<double*>(S.in_flow)[e] = S.map_in_flow[on + e];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Launchers and the KernelSet factory.
 
@@ -1260,6 +1314,10 @@ template <class F>
 void launch_move_thr_t(int n_scen, cudaStream_t st, ScenDev* sc) {
   k_move_thr<F><<<dim3(4, n_scen), 256, 0, st>>>(sc);
 }
+template <class F>
+void launch_flowmap_t(int n_scen, cudaStream_t st, ScenDev* sc) {
+  k_flowmap<F><<<dim3(8, n_scen), 256, 0, st>>>(sc);
+}
 
 template <class Model, class F>
 KernelSet make_set(int model_id) {
@@ -1289,6 +1347,7 @@ KernelSet make_set(int model_id) {
   k.cycle_extra_smem[5] = 3u * TileStage<Model, F>::bytes;
   k.cycle_extra_smem[6] = 2u * TileStage<Model, F>::bytes;
   k.move_thr = &launch_move_thr_t<F>;
+  k.flowmap = &launch_flowmap_t<F>;
   k.liquid = &launch_liquid_t<Model, F>;
   k.plan = &launch_plan_t<Model, F>;
   k.divide = &launch_divide_t<Model, F>;

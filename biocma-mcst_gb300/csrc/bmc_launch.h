@@ -15,7 +15,7 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 3;
+constexpr int kKernelSetAbi = 4;
 
 using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
@@ -51,6 +51,7 @@ struct KernelSet {
   CycleSetup cycle_setup[kCycleVariants];
   unsigned cycle_extra_smem[kCycleVariants];  // stage buffers after the accumulator
   MoveThrLaunch move_thr;
+  MoveThrLaunch flowmap;  // flow-map switch at the start of a step
   DivideLaunch divide;
   CopyLaunch compact;
   CopyLaunch merge;

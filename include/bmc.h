@@ -243,6 +243,28 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts);
  * force_remove_dead, particles_container.hpp L460-L465). */
 int bmc_force_remove_dead(bmc_scenario* s);
 
+/* ---- flow-map cycle ------------------------------------------------------- */
+/* Several flow-map states of the same mesh (the reference's CMA case with
+ * n_different_maps > 1, replayed by its FlowMapTransitionner): each map
+ * carries its own volumes, neighbours, out-flows, cumulative probabilities
+ * and liquid transition (arguments as bmc_domain_update and
+ * bmc_set_transition_coo; n_compartments and K are the domain's).  All maps
+ * stay on the device; main-loop step k runs on map (k / n_per_flowmap) %
+ * n_maps, switched in on the device at the start of the step (the
+ * UPDATE_HYDRO_STEP of apps/core/src/host_specific.cpp L255-L266, which
+ * replaces volumes, neighbours, out-flows, probabilities and transition,
+ * apps/libs/simulation/src/simulation.cpp L95-L139; concentrations follow
+ * from the unchanged masses).  n_per_flowmap = floor(t_per_flowmap / dt) + 1,
+ * or 1 when t_per_flowmap is 0 or there is one map (compute_n_per_flowmap,
+ * apps/core/src/global_initaliser.cpp L104-L114).  While maps are set,
+ * bmc_domain_update and bmc_set_transition_coo are refused; bmc_cycle
+ * (cycle only) does not switch maps. */
+int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neighbors,
+                    const double* out_flows, const double* cdf, uint64_t nnz, const uint64_t* rows,
+                    const uint64_t* cols, const double* values);
+int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap);
+int bmc_flowmap_clear(bmc_scenario* s);
+
 /* ---- batching: many scenarios advanced by one set of launches ----------- */
 /* All scenarios of a batch share model and precision; each keeps its own
  * domain, liquid state, parameters, seed and step counter. */

@@ -204,6 +204,8 @@ class Oracle:
             s.udf = ct.addressof(self._udf[1])
         self.s = s
         self.weight = None
+        self._map_arrays = {}
+        self._map_cur = 0
 
     # -- set-up --------------------------------------------------------------
     def init_particles(self, n: int | None = None):
@@ -222,12 +224,50 @@ class Oracle:
         for j in range(8):
             self.s.q_exp[j] = int(e[j])
 
+    # -- flow-map cycle -----------------------------------------------------------
+    def _use_map(self, m: int):
+        """Point the domain at flow-map state m: volumes, out-flows,
+        neighbours, cumulative probabilities, incoming flows, outlet
+        volumes; masses are kept, so concentrations follow at the next
+        liquid step (the reference's updateHydro + ScalarSimulation::
+        setVolumes, apps/libs/simulation/src/simulation.cpp L95-L139)."""
+        net = self.scen.flowmaps[m]
+        keep = self._map_arrays.setdefault(m, {
+            "volume": np.ascontiguousarray(net.volume, dtype=np.float64),
+            "vinv": 1.0 / np.ascontiguousarray(net.volume, dtype=np.float64),
+            "out_flow": np.ascontiguousarray(net.out_flow, dtype=np.float64),
+            "neighbors": np.ascontiguousarray(net.neighbors, dtype=np.uint32),
+            "cdf": np.ascontiguousarray(net.cdf, dtype=np.float64),
+            "in_ptr": np.ascontiguousarray(net.in_ptr, dtype=np.uint32),
+            "in_idx": np.ascontiguousarray(net.in_idx, dtype=np.uint32),
+            "in_flow": np.ascontiguousarray(net.in_flow, dtype=np.float64),
+        })
+        for name, arr in keep.items():
+            setattr(self.s, name, _ptr(arr))
+        for o in range(self.s.n_outlets):
+            self.s.outlet_volume[o] = float(keep["volume"][self.s.outlet_index[o]])
+        self.vol, self.vinv = keep["volume"], keep["vinv"]
+        self._map_cur = m
+
+    def _switch_map(self):
+        fm = self.scen.flowmaps
+        if len(fm) <= 1:
+            return
+        m = (int(self.s.step) // self.scen.n_per_flowmap) % len(fm)
+        if m != self._map_cur:
+            self._use_map(m)
+
     # -- stepping -------------------------------------------------------------
     def step(self, n_threads: int = 1):
+        self._switch_map()
         lib().orc_step(ct.byref(self.s), self.scen.dt, n_threads)
         return self.stats()
 
     def run(self, n_steps: int, n_threads: int = 1):
+        if len(self.scen.flowmaps) > 1:
+            for _ in range(n_steps):
+                self.step(n_threads)
+            return
         lib().orc_run(ct.byref(self.s), self.scen.dt, n_steps, n_threads)
 
     def cycle(self, n_threads: int = 1):
