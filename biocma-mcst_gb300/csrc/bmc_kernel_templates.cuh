@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
 // the integer pipe from the IEEE fields of v, so no FP64 instruction is
 // spent per particle; the result equals rint(v * 2^-e) evaluated in double.
 template <int MBITS, int EBITS, int BIAS, class U>
-__device__ __forceinline__ long long quantize_bits(U bits, int e, unsigned long long& clamped, unsigned& err) {
+__device__ __forceinline__ long long quantize_bits(U bits, int e, unsigned& clamped, unsigned& err) {
   const bool neg = (bits >> (MBITS + EBITS)) & 1u;
   const int ex = (int)((bits >> MBITS) & (((U)1 << EBITS) - 1));
   const unsigned long long mant = (unsigned long long)(bits & (((U)1 << MBITS) - 1));
@@ -190,10 +190,10 @@ __device__ __forceinline__ long long quantize_bits(U bits, int e, unsigned long 
   return neg ? -q : q;
 }
 
-__device__ __forceinline__ long long quantize(double v, int e, unsigned long long& clamped, unsigned& err) {
+__device__ __forceinline__ long long quantize(double v, int e, unsigned& clamped, unsigned& err) {
   return quantize_bits<52, 11, 1023>((unsigned long long)__double_as_longlong(v), e, clamped, err);
 }
-__device__ __forceinline__ long long quantize(float v, int e, unsigned long long& clamped, unsigned& err) {
+__device__ __forceinline__ long long quantize(float v, int e, unsigned& clamped, unsigned& err) {
   return quantize_bits<23, 8, 127>((unsigned)__float_as_uint(v), e, clamped, err);
 }
 
@@ -263,7 +263,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const unsigned* live_base = bctl->live_base;
   int cur = -1;
   unsigned long long since_flush = 0;
-  unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
+  // per-thread counts between flushes (at most kFlushParticles slots)
+  unsigned my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
   unsigned my_err = 0;
 
   // flush the accumulator and the counters of scenario `cur` (whole block)
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
       const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
       if (ev) atomicOr(&c->error, ev);
     }
-    my_req = my_exit = my_move = my_clamp = 0ull;
+    my_req = my_exit = my_move = my_clamp = 0u;
     my_err = 0u;
   };
 
@@ -514,6 +515,19 @@ __global__ void __launch_bounds__(THREADS, MINB)
 
 __host__ __device__ constexpr unsigned popcount_c(unsigned v) { return v == 0u ? 0u : (v & 1u) + popcount_c(v >> 1); }
 
+// Fields of the scenario a k_cycle_tma block is working on.
+template <class F>
+struct CycleScen {
+  unsigned long long seed, cap;
+  const F* crec;
+  const int2* mrow;
+  F* state;
+  unsigned n_c, K, step, n_out;
+  F dtF;
+  float dtf;
+  int qe0;
+};
+
 template <class Model, class F>
 struct TileStage {
   static constexpr unsigned NV = Model::n_var;
@@ -623,7 +637,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
   int cur = -1;
   bool aborted = false;
   unsigned long long since_flush = 0;
-  unsigned long long my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
+  // per-thread counts between flushes (at most kFlushParticles slots)
+  unsigned my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
   unsigned my_err = 0;
 
   auto flush = [&]() {
@@ -662,20 +677,14 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       const unsigned ev = *reinterpret_cast<unsigned*>(&s_cnt[4]);
       if (ev) atomicOr(&c->error, ev);
     }
-    my_req = my_exit = my_move = my_clamp = 0ull;
+    my_req = my_exit = my_move = my_clamp = 0u;
     my_err = 0u;
   };
 
-  // scenario fields, loaded when the scenario changes
-  unsigned n_c = 0, K = 0, step = 0, n_out = 0;
-  unsigned long long seed = 0, cap = 0, n_used = 0;
-  F dtF = (F)0;
-  float dtf = 0.0f;
-  int qe0 = 0;
-  bool do_move = false;
-  const F* crec = nullptr;
-  const int2* mrow = nullptr;
-  F* state = nullptr;
+  // fields of the current scenario, kept in shared memory (written by
+  // thread 0 when the scenario changes) rather than in registers
+  __shared__ CycleScen<F> sr;
+  unsigned long long n_used = 0;
   int hint = -1;
 
   for (unsigned k = 0; k < n_tiles; ++k) {
@@ -694,19 +703,20 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       if (tid < 16) s_pf[tid] = (F)S.params[tid];
       cur = s;
       since_flush = 0;
-      n_c = S.n_c;
-      K = S.K;
-      step = S.ctl->step;
-      seed = S.seed;
-      cap = S.cap;
-      dtF = (F)S.dt;
-      dtf = (float)S.dt;
-      do_move = n_c > 1;
-      n_out = S.n_outlets;
-      qe0 = S.q_exp[0];
-      crec = reinterpret_cast<const F*>(S.crec);
-      mrow = S.mrow;
-      state = reinterpret_cast<F*>(S.state);
+      if (tid == 0) {
+        sr.n_c = S.n_c;
+        sr.K = S.K;
+        sr.step = S.ctl->step;
+        sr.seed = S.seed;
+        sr.cap = S.cap;
+        sr.dtF = (F)S.dt;
+        sr.dtf = (float)S.dt;
+        sr.n_out = S.n_outlets;
+        sr.qe0 = S.q_exp[0];
+        sr.crec = reinterpret_cast<const F*>(S.crec);
+        sr.mrow = S.mrow;
+        sr.state = reinterpret_cast<F*>(S.state);
+      }
       consumer_sync(THREADS);
     }
     since_flush += n_in;
@@ -733,14 +743,14 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       if (idle) {
         const unsigned long long gi = base + slot;
         const uint32_t p0 = bpos[slot];
-        if (p0 >= n_c) {
+        if (p0 >= sr.n_c) {
           my_err |= 1u;
         } else {
           uint32_t rd[4];
-          philox_raw(seed, bid[slot], step, 0u, rd);
-          const float ad = __fadd_rn(bad[slot], dtf);
+          philox_raw(sr.seed, bid[slot], sr.step, 0u, rd);
+          const float ad = __fadd_rn(bad[slot], sr.dtf);
           F rr[(Model::n_upd + 1) & ~1];
-          const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
+          const uint32_t mthr = load_rec<Model::n_upd>(sr.crec + (size_t)p0 * 8, rr);
           F xx[NV];
 #pragma unroll
           for (int v = 0; v < NV; ++v)
@@ -748,12 +758,12 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           int st;
           if constexpr (Model::separable) {
             F basis;
-            st = Model::update(dtF, xx, rr, basis, s_pf);
-            const long long q = quantize(basis, qe0, my_clamp, my_err);
+            st = Model::update(sr.dtF, xx, rr, basis, s_pf);
+            const long long q = quantize(basis, sr.qe0, my_clamp, my_err);
             atomicAdd(&sacc[p0], (unsigned long long)q);
           } else {
             F ctb[NC];
-            st = Model::update_general(dtF, xx, rr, ctb, s_pf);
+            st = Model::update_general(sr.dtF, xx, rr, ctb, s_pf);
 #pragma unroll
             for (int j = 0; j < NC; ++j) {
               const double val = __dmul_rn(S.weight, (double)ctb[j]);
@@ -762,20 +772,20 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             }
           }
 #pragma unroll
-          for (int v = 0; v < NV; ++v) __stcs(state + (size_t)v * cap + gi, xx[v]);
+          for (int v = 0; v < NV; ++v) __stcs(sr.state + (size_t)v * sr.cap + gi, xx[v]);
           if (st == kDivision) {
             div = true;
             S.bpos[gi] = p0;
             ++my_req;
           }
           uint32_t p = p0;
-          if (do_move) {
+          if ((sr.n_c > 1u)) {
             if (draw_int(rd[0]) < mthr) {
               // bisection of move_kernel.hpp L89-L101 over {threshold, neighbour}
               const int x1 = (int)draw_int(rd[1]);
-              const int2* row = mrow + (size_t)p0 * K;
-              int nb = __ldg(row + (K - 1)).y;
-              int left = 0, right = (int)K - 1;
+              const int2* row = sr.mrow + (size_t)p0 * sr.K;
+              int nb = __ldg(row + (sr.K - 1)).y;
+              int left = 0, right = (int)sr.K - 1;
               while (left < right) {
                 const int mid = (left + right) >> 1;
                 const int2 pm = __ldg(row + mid);
@@ -791,9 +801,9 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             }
             __stcs(S.pos + gi, p);
           }
-          if (n_out > 0) {
-            float ah = __fadd_rn(bah[slot], dtf);
-            for (unsigned o = 0; o < n_out; ++o) {
+          if (sr.n_out > 0) {
+            float ah = __fadd_rn(bah[slot], sr.dtf);
+            for (unsigned o = 0; o < sr.n_out; ++o) {
               if (S.outlet_idx[o] == p) {
                 if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {
                   stv = kExit;

@@ -103,8 +103,8 @@ def test_gpu_flowmap_graph_run_and_batch_equal_steps(oracle_mod):
     o.run(14)
     assert_same_particles(g, o, "graph run")
     assert_same_liquid(g, o, "graph run")
-    # in a batch with a fixed-domain scenario
-    other = scenarios.small_ring(3000, f64=True, feeds=True)
+    # in a batch with a fixed-domain scenario of the same model
+    other = dataclasses.replace(sc, flowmaps=[], seed=99, n_particles=3000)
     m1, m2 = GpuScenario(sc), GpuScenario(other)
     b = GpuBatch([m1, m2])
     b.run(14, sc.dt)
