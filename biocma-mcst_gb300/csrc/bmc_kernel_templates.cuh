@@ -24,6 +24,15 @@
 namespace bmc {
 
 
+// Slot of rate k in a compartment record: the NU = Model::n_upd rates the
+// per-particle update reads sit just below the move threshold (slot 7), so
+// that the fewest vector loads fetch both; the other rates (read once per
+// compartment by k_plan) fill the record from slot 0.
+template <class Model>
+__host__ __device__ constexpr int rate_slot(int k) {
+  return k < Model::n_upd ? 7 - Model::n_upd + k : k - Model::n_upd;
+}
+
 // ---------------------------------------------------------------------------
 // k_liquid: one thread per (compartment j, species s) entry; a block holds
 // 256 / n_species whole compartments (grid x over compartment chunks, grid
@@ -140,7 +149,7 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
     Model::rates(cs + t * nsp, S.params, r);
     F* rec = reinterpret_cast<F*>(S.crec) + (size_t)(j0 + t) * 8;
 #pragma unroll
-    for (int k = 0; k < Model::n_rates; ++k) rec[k] = r[k];
+    for (int k = 0; k < Model::n_rates; ++k) rec[rate_slot<Model>(k)] = r[k];
   }
   if (do_scalar && t < nsp) {
     atomicAdd(&ctl->mb_new[t], red[0][t]);
@@ -201,29 +210,51 @@ __device__ __forceinline__ long long quantize(float v, int e, unsigned& clamped,
 __device__ __forceinline__ uint32_t rec_move_thr(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ uint32_t rec_move_thr(double v) { return (uint32_t)__double_as_longlong(v); }
 
-// Loads the first NU slots of a compartment record (vector loads through
-// the read-only path) and its move threshold (slot 7, same 32-byte sector
-// for float records).
+// Loads the NU update rates and the move threshold of a compartment record
+// (slots 7 - NU .. 7) through the read-only path with the widest aligned
+// vector loads.
 template <int NU, class F>
 __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
+  static_assert(NU >= 0 && NU <= 7, "at most 7 update rates");
+  constexpr int s0 = 7 - NU;
   if constexpr (sizeof(F) == 4) {
-    if constexpr (NU > 2) {
-      const float4 a = __ldg(reinterpret_cast<const float4*>(p));
-      out[0] = a.x; out[1] = a.y; out[2] = a.z; out[3] = a.w;
+    // scalars up to slot 3, then one float4 (slots 4..7) or a float2 (6, 7)
+    if constexpr (NU <= 1) {
+      const float2 a = __ldg(reinterpret_cast<const float2*>(p + 6));
+      if constexpr (NU == 1) out[0] = a.x;
+      return rec_move_thr(a.y);
+    } else if constexpr (NU == 2) {
+      out[0] = __ldg(p + 5);
+      const float2 a = __ldg(reinterpret_cast<const float2*>(p + 6));
+      out[1] = a.x;
+      return rec_move_thr(a.y);
     } else {
-      const float2 a = __ldg(reinterpret_cast<const float2*>(p));
-      out[0] = a.x; out[1] = a.y;
-    }
-    static_assert(NU <= 4, "float records: update may read at most 4 rates");
-  } else {
 #pragma unroll
-    for (int k = 0; k < (NU + 1) / 2; ++k) {
-      const double2 a = __ldg(reinterpret_cast<const double2*>(p) + k);
-      out[2 * k] = a.x;
-      out[2 * k + 1] = a.y;
+      for (int q = s0; q < 4; ++q) out[q - s0] = __ldg(p + q);
+      const float4 a = __ldg(reinterpret_cast<const float4*>(p + 4));
+      out[4 - s0] = a.x;
+      out[5 - s0] = a.y;
+      out[6 - s0] = a.z;
+      return rec_move_thr(a.w);
     }
+  } else if constexpr (NU == 0) {
+    return rec_move_thr(__ldg(p + 7));
+  } else {
+    // a scalar when the first slot is odd, then aligned pairs up to slot 7
+    if constexpr ((s0 & 1) != 0) out[0] = __ldg(p + s0);
+    constexpr int q0 = (s0 & 1) != 0 ? s0 + 1 : s0;
+    uint32_t thr = 0u;
+#pragma unroll
+    for (int q = q0; q < 8; q += 2) {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(p + q));
+      out[q - s0] = a.x;
+      if (q + 1 < 7)
+        out[q + 1 - s0] = a.y;
+      else
+        thr = rec_move_thr(a.y);
+    }
+    return thr;
   }
-  return rec_move_thr(__ldg(p + 7));
 }
 
 // ---------------------------------------------------------------------------
@@ -885,7 +916,9 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
       const double B = fixed_to_double(S.acc_hi[j], S.acc_lo[j], S.q_scale_up[0]);
       S.acc_hi[j] = 0;
       S.acc_lo[j] = 0ull;
-      const F* rr = rates + (size_t)j * 8;
+      F rr[kMaxRates];
+#pragma unroll
+      for (int k = 0; k < Model::n_rates; ++k) rr[k] = rates[(size_t)j * 8 + rate_slot<Model>(k)];
       for (unsigned sp = 0; sp < nsp; ++sp) {
         double v = 0.0;
         if (sp < (unsigned)Model::n_ctb) v = __dmul_rn(__dmul_rn(S.weight, (double)Model::coef(rr, (int)sp)), B);
