@@ -48,6 +48,9 @@ def parse():
                     help="skip the precision / batched / served measurements")
     ap.add_argument("--forms-steps", type=int, default=100)
     ap.add_argument("--serve-window", type=float, default=10.0)
+    ap.add_argument("--batched-only", type=float, default=None, metavar="SCALE",
+                    help="run only the batched form, particle counts scaled by SCALE, without the "
+                         "plain-path comparisons (with --shape: no autotuner); for profiling")
     return ap.parse_args()
 
 
@@ -140,10 +143,12 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(scen):
+def profiled_traffic(scen, staged: bool):
     """DRAM bytes per particle of the cycle kernel from the committed ncu
-    summary (profiles/k_cycle_<workload>.txt, line 'dram_bytes_per_particle:')."""
-    p = os.path.join(ROOT, "profiles", f"k_cycle_{scen.name}.txt")
+    summary (profiles/k_cycle[_tma]_<workload>.txt, line
+    'dram_bytes_per_particle:'); `staged` selects the tile-staging kernel."""
+    kernel = "k_cycle_tma" if staged else "k_cycle"
+    p = os.path.join(ROOT, "profiles", f"{kernel}_{scen.name}.txt")
     if not os.path.exists(p):
         return None
     m = re.search(r"dram_bytes_per_particle:\s*([0-9.eE+-]+)", open(p).read())
@@ -274,11 +279,12 @@ def run_gpu(args):
     B = scen.algorithmic_bytes()
     achieved = B * statistics.mean(alive_k) / (cyc_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
-    tpp = profiled_traffic(scen)
+    staged = shape[0] in (288, 544)  # launch shapes of the tile-staging kernel
+    tpp = profiled_traffic(scen, staged)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs",
                 "traffic": (tpp * statistics.mean(alive_k)) if tpp else None,
-                "kernel": "k_cycle", "algorithmic_bytes_per_particle": B,
+                "kernel": "k_cycle_tma" if staged else "k_cycle", "algorithmic_bytes_per_particle": B,
                 "kernel_ms": cyc_ms, "step_kernels_ms": step_ms,
                 "step_breakdown_ms": dict(zip(["liquid", "cycle", "plan", "divide", "compact", "merge"],
                                               [round(statistics.mean(k[i] for k in kms), 5)
@@ -407,7 +413,7 @@ def precision_form(steps: int):
     return out
 
 
-def batched_form(steps: int, n_scen: int = 256):
+def batched_form(steps: int, n_scen: int = 256, scale: float = 1.0, shape=None, compare_plain: bool = True):
     """256 uneven scenarios advanced by one batched launch sequence per step
     (one captured graph) against the plain path: each scenario advanced by
     its own graph on its own stream, all streams in flight together."""
@@ -415,12 +421,15 @@ def batched_form(steps: int, n_scen: int = 256):
 
     from bmc import autotune, scenarios, sim
 
-    scens = [scenarios.batch_scenario(k, seed=1234) for k in range(n_scen)]
+    scens = [scenarios.batch_scenario(k, seed=1234, particle_scale=scale) for k in range(n_scen)]
     t0 = time.perf_counter()
     gs = [sim.GpuScenario(s) for s in scens]
     setup = time.perf_counter() - t0
     b = sim.GpuBatch(gs)
-    shape, tune_ms = autotune.tune_batch(b, 0.1)
+    if shape:
+        b.set_shape(*shape)
+    else:
+        shape, tune_ms = autotune.tune_batch(b, 0.1)
     b.run(3, 0.1)
     b.synchronize()
     n_alive = sum(s.n_particles for s in scens)
@@ -434,6 +443,16 @@ def batched_form(steps: int, n_scen: int = 256):
     bytes_per_particle = scens[0].algorithmic_bytes()
     cyc_gbs = float(n_alive * bytes_per_particle / (float(kms[1]) * 1e-3) / 1e9)
     peak = measured_peak()[0]
+    if not compare_plain:
+        for g in gs:
+            g.close()
+        return {"scenarios": n_scen, "total_particles": n_alive, "steps": steps,
+                "batched_value": n_alive * steps / tb, "shape": list(shape),
+                "step_breakdown_ms": dict(zip(["liquid", "cycle", "plan", "divide", "compact", "merge"],
+                                              [float(x) for x in kms])),
+                "cycle_roofline": {"achieved": cyc_gbs, "peak": peak, "unit": "GB/s",
+                                   "frac": cyc_gbs / peak, "bytes_per_particle": bytes_per_particle},
+                "unit": METRIC}
     for g in gs:  # plain path: warm its graphs
         g.run(1)
     # plain, one scenario after another, each step through bmc_step (the
@@ -493,6 +512,11 @@ def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):
 
 def main():
     args = parse()
+    if args.batched_only is not None:
+        shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
+        print(json.dumps(batched_form(args.forms_steps, scale=args.batched_only, shape=shape,
+                                      compare_plain=False)))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
