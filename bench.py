@@ -212,6 +212,27 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def aggregate_replicas(dist, t: float, psteps: float, device: str = "cuda"):
+    """Whole-job figures of N independent replicas: the slowest rank's time
+    and the particle-steps of all ranks (no collective on the data path;
+    this runs once, after the timed region)."""
+    if dist is None:
+        return t, psteps
+    import torch
+
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    pp = torch.tensor([psteps], dtype=torch.float64, device=device)
+    dist.all_reduce(pp, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(pp.item())
+
+
+def replica_seed(world: int, rank: int):
+    """Seed of a replica's scenario: the workload's own seed on one GPU,
+    a distinct seed per rank otherwise."""
+    return None if world == 1 else 2024 + rank
+
+
 def run_gpu(args):
     world, rank, local = dist_env()
     import torch
@@ -225,8 +246,7 @@ def run_gpu(args):
     from bmc import scenarios, sim
 
     sim.set_device(local)
-    scen = scenarios.workload(args.workload, n_particles=args.particles,
-                              seed=None if world == 1 else 2024 + rank)
+    scen = scenarios.workload(args.workload, n_particles=args.particles, seed=replica_seed(world, rank))
     g = sim.GpuScenario(scen)
 
     def barrier():
@@ -258,13 +278,7 @@ def run_gpu(args):
     alive0 = st0["n_used"] - st0["inactive"]
     alive1 = st1["n_used"] - st1["inactive"]
     psteps = 0.5 * (alive0 + alive1) * args.steps
-    t = ms / 1e3
-    if dist is not None:
-        tt = torch.tensor([t], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        pp = torch.tensor([psteps], dtype=torch.float64, device="cuda")
-        dist.all_reduce(pp, op=dist.ReduceOp.SUM)
-        t, psteps = float(tt.item()), float(pp.item())
+    t, psteps = aggregate_replicas(dist, ms / 1e3, psteps)
     value = psteps / t
 
     # per-kernel durations (events between the six kernels of a step)
@@ -320,13 +334,8 @@ def run_gpu(args):
         barrier()
         te = time.perf_counter() - t0
         h1, d1 = sim.transfer_bytes()
+        te, ps = aggregate_replicas(dist, te, ps)
         ev = ps / te
-        if dist is not None:
-            tt = torch.tensor([te], dtype=torch.float64, device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            pp = torch.tensor([ps], dtype=torch.float64, device="cuda")
-            dist.all_reduce(pp, op=dist.ReduceOp.SUM)
-            ev = float(pp.item()) / float(tt.item())
         e2e = {"value": ev, "unit": METRIC,
                "h2d_bytes_per_step": (h1 - h0) / args.e2e_steps,
                "d2h_bytes_per_step": (d1 - d0) / args.e2e_steps,
