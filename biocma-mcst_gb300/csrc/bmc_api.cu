@@ -317,13 +317,13 @@ unsigned liquid_grid(const ScenDev& h) {
 // With `maps`, the flow-map switch runs first (main-loop steps only).
 int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned liq_grid,
                  BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count,
-                 bool maps) {
+                 bool maps, bool tiny) {
   if (maps && do_scalar) {
     ks->flowmap(n_scen, st, d_table);
     g_launches += 1;
   }
   ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
-  ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl);
+  ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl, tiny);
   ks->plan(n_scen, st, d_table, d_bctl);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
@@ -331,6 +331,15 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
   g_launches += 6;
   BMC_CUDA(launch_status(ks));
   return BMC_OK;
+}
+
+// Launches whose domains all have at most kAggregateMaxCompartments
+// compartments use the cycle kernels with the warp-aggregated scatter.
+bool tiny_domain(const ScenDev& h) { return h.n_c <= bmc::kAggregateMaxCompartments; }
+bool batch_tiny(const bmc_batch* b) {
+  for (const bmc_scenario* m : b->scen)
+    if (!tiny_domain(m->h)) return false;
+  return true;
 }
 
 bool batch_has_maps(const bmc_batch* b) {
@@ -595,6 +604,9 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     cudaStreamSynchronize(s->stream);
     if (s->darena) cudaFree(s->darena);
     s->darena = nullptr;
+    // the step graph's launch choices depend on the domain's size
+    if (s->graph) cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
     const size_t ne = (size_t)n_c * h.n_s, na = (size_t)n_c * h.n_acc;
     Carver cv;
     int2* p_mrow = nullptr;
@@ -810,7 +822,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
   int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, s->variant, grid, smem,
-                        s->sm_count, s->h.n_maps > 0);
+                        s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc) {
@@ -846,7 +858,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, s->variant, grid, smem,
-                      s->sm_count, s->h.n_maps > 0);
+                      s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
     if (rc) return rc;
   }
   return BMC_OK;
@@ -1131,7 +1143,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
     rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->variant, grid, smem,
-                      b->scen[0]->sm_count, batch_has_maps(b));
+                      b->scen[0]->sm_count, batch_has_maps(b), batch_tiny(b));
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -1330,7 +1342,8 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   BMC_CUDA(cudaEventRecord(ev[0], st));
   s->ks->liquid(1, liquid_grid(s->h), st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
-  s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl);
+  s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl,
+                        tiny_domain(s->h));
   BMC_CUDA(cudaEventRecord(ev[2], st));
   s->ks->plan(1, st, s->d_desc, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));
@@ -1366,7 +1379,8 @@ int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   BMC_CUDA(cudaEventRecord(ev[0], st));
   b->ks->liquid(n, max_nc, st, b->d_table, b->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
-  b->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, b->d_table, n, b->d_bctl);
+  b->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, b->d_table, n, b->d_bctl,
+                        batch_tiny(b));
   BMC_CUDA(cudaEventRecord(ev[2], st));
   b->ks->plan(n, st, b->d_table, b->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));

@@ -276,7 +276,7 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
 // Launch variants: THREADS per block, PPT consecutive particles per thread
 // (THREADS * PPT divides the 1024-slot tile) and MINB resident blocks per SM
 // the register budget is cut for.
-template <class Model, class F, int PPT, int THREADS, int MINB>
+template <class Model, class F, int PPT, int THREADS, int MINB, bool AGG>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_cycle(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   extern __shared__ unsigned long long sacc[];
@@ -400,6 +400,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
 #pragma unroll
         for (int v = 0; v < NV; ++v)
           if ((Model::read_mask >> v) & 1u) ld_stream<F, PPT>(state + (size_t)v * cap + first, x[v]);
+        uint32_t p0s[PPT];  // compartments before the move
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) p0s[k] = pv[k];
         bool idle[PPT];
         bool any = false, all = true;
 #pragma unroll
@@ -417,6 +420,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
         }
         unsigned bits = 0u;
         unsigned n_inact = 0u;
+        bool has_q[PPT];  // tiny domains: quantised basis, scattered warp-aggregated
+        long long qv[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          has_q[k] = false;
+          qv[k] = 0;
+        }
         if (any) {
           bool st_changed = false;
 #pragma unroll
@@ -440,7 +450,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
               F basis;
               st = Model::update(dtF, xx, rr, basis, s_pf);
               const long long q = quantize(basis, qe0, my_clamp, my_err);
-              atomicAdd(&sacc[p0], (unsigned long long)q);
+              if constexpr (AGG) {
+                qv[k] = q;
+                has_q[k] = true;
+              } else {
+                atomicAdd(&sacc[p0], (unsigned long long)q);
+              }
             } else {
               F ctb[NC];
               st = Model::update_general(dtF, xx, rr, ctb, s_pf);
@@ -505,6 +520,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
           if (n_out > 0) st_stream<float, PPT>(S.age_h + first, ah);
           st_stream<float, PPT>(S.age_d + first, ad);
           if (st_changed) st_stream<uint8_t, PPT>(S.status + first, stv);
+        }
+        if constexpr (Model::separable && AGG) {
+          // tiny domains: contributions (to the compartment before the move,
+          // p0s) summed per compartment across the warp first
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) warp_aggregated_add(sacc, p0s[k], qv[k], has_q[k]);
         }
 #pragma unroll
         for (int k = 0; k < PPT; ++k) n_inact += (first + k < n_used && stv[k] != kIdle) ? 1u : 0u;
@@ -574,7 +595,7 @@ struct TileStage {
   __host__ __device__ static constexpr unsigned rank(unsigned v) { return popcount_c(Model::read_mask & ((1u << v) - 1u)); }
 };
 
-template <class Model, class F, int THREADS, int MINB, int STAGES>
+template <class Model, class F, int THREADS, int MINB, int STAGES, bool AGG>
 __global__ void __launch_bounds__(THREADS + 32, MINB)
     k_cycle_tma(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   using TS = TileStage<Model, F>;
@@ -771,6 +792,9 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       uint8_t stv = act ? bst[slot] : (uint8_t)kIdle;
       const bool idle = act && stv == kIdle;
       bool div = false;
+      bool has_q = false;  // tiny domains: quantised basis, scattered warp-aggregated
+      long long qv = 0;
+      uint32_t qkey = 0u;
       if (idle) {
         const unsigned long long gi = base + slot;
         const uint32_t p0 = bpos[slot];
@@ -791,7 +815,13 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             F basis;
             st = Model::update(sr.dtF, xx, rr, basis, s_pf);
             const long long q = quantize(basis, sr.qe0, my_clamp, my_err);
-            atomicAdd(&sacc[p0], (unsigned long long)q);
+            if constexpr (AGG) {
+              qv = q;
+              qkey = p0;
+              has_q = true;
+            } else {
+              atomicAdd(&sacc[p0], (unsigned long long)q);
+            }
           } else {
             F ctb[NC];
             st = Model::update_general(sr.dtF, xx, rr, ctb, s_pf);
@@ -850,6 +880,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           __stcs(S.age_d + gi, ad);
         }
       }
+      if constexpr (Model::separable && AGG) warp_aggregated_add(sacc, qkey, qv, has_q);
       // birth-request word of the 32 slots this warp covers in round r
       const unsigned bits = __ballot_sync(0xffffffffu, div);
       const unsigned w0 = r * THREADS + warp * 32u;
@@ -1303,15 +1334,21 @@ __global__ void k_flowmap(ScenDev* __restrict__ sc) {
 namespace kset {
 template <class Model, class F, int PPT, int THREADS, int MINB>
 void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
-                    BatchCtl* b) {
+                    BatchCtl* b, bool tiny) {
   (void)block;
-  k_cycle<Model, F, PPT, THREADS, MINB><<<grid, THREADS, smem, st>>>(sc, n, b);
+  if (tiny)
+    k_cycle<Model, F, PPT, THREADS, MINB, true><<<grid, THREADS, smem, st>>>(sc, n, b);
+  else
+    k_cycle<Model, F, PPT, THREADS, MINB, false><<<grid, THREADS, smem, st>>>(sc, n, b);
 }
 template <class Model, class F, int THREADS, int MINB, int STAGES>
 void launch_cycle_tma_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
-                        BatchCtl* b) {
+                        BatchCtl* b, bool tiny) {
   (void)block;
-  k_cycle_tma<Model, F, THREADS, MINB, STAGES><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+  if (tiny)
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, true><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+  else
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, false><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
 }
 template <class Model, class F>
 void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
@@ -1338,19 +1375,32 @@ void launch_init_t(dim3 grid, cudaStream_t st, const ScenDev* sc, unsigned long 
                    uint32_t span, double* mass) {
   k_init<Model, F><<<grid, 256, 0, st>>>(sc, n, lo, span, mass);
 }
-template <class Model, class F, int PPT, int THREADS, int MINB>
-int setup_cycle_t(size_t smem, int* blocks_per_sm) {
-  const void* fn = reinterpret_cast<const void*>(&k_cycle<Model, F, PPT, THREADS, MINB>);
+// Shared-memory limit and occupancy of both instantiations of a shape (the
+// launch picks one per step); the occupancy reported is the smaller.
+inline int setup_fn(const void* fn, int threads, size_t smem, int* blocks_per_sm) {
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return (int)e;
-  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, THREADS, smem);
+  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, threads, smem);
+}
+inline int setup_pair(const void* f0, const void* f1, int threads, size_t smem, int* blocks_per_sm) {
+  int b0 = 0, b1 = 0;
+  int e = setup_fn(f0, threads, smem, &b0);
+  if (e) return e;
+  e = setup_fn(f1, threads, smem, &b1);
+  *blocks_per_sm = b0 < b1 ? b0 : b1;
+  return e;
+}
+template <class Model, class F, int PPT, int THREADS, int MINB>
+int setup_cycle_t(size_t smem, int* blocks_per_sm) {
+  return setup_pair(reinterpret_cast<const void*>(&k_cycle<Model, F, PPT, THREADS, MINB, false>),
+                    reinterpret_cast<const void*>(&k_cycle<Model, F, PPT, THREADS, MINB, true>), THREADS, smem,
+                    blocks_per_sm);
 }
 template <class Model, class F, int THREADS, int MINB, int STAGES>
 int setup_cycle_tma_t(size_t smem, int* blocks_per_sm) {
-  const void* fn = reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES>);
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return (int)e;
-  return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, THREADS + 32, smem);
+  return setup_pair(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, false>),
+                    reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, true>),
+                    THREADS + 32, smem, blocks_per_sm);
 }
 inline int last_error_t() { return (int)cudaGetLastError(); }
 template <class F>

@@ -1,5 +1,5 @@
-// bmc_kernels.cu -- the built-in model plugins' kernel sets and the
-// model-independent kernels (repartition, draw dump).
+// bmc_kernels.cu -- the table of the built-in model plugins' kernel sets and
+// the model-independent kernels (repartition, draw dump).
 #include <cstdio>
 
 #include "bmc_kernel_templates.cuh"
@@ -27,19 +27,20 @@ __global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restric
   }
 }
 
-namespace {
-using kset::make_set;
-const KernelSet g_sets[] = {
-    make_set<MonodModel<double>, double>(1),       make_set<MonodModel<float>, float>(1),
-    make_set<OverflowModel<double>, double>(2),    make_set<OverflowModel<float>, float>(2),
-    make_set<FixedLengthModelT<true>, float>(3),   make_set<FixedLengthModelT<false>, float>(4),
-};
-}  // namespace
-
+// Built-in kernel sets, one translation unit per model (compiled in
+// parallel): bmc_sets_monod.cu, bmc_sets_overflow.cu, bmc_sets_fixed.cu.
 const KernelSet* kernel_set(int model, int f64) {
-  for (const KernelSet& k : g_sets)
-    if (k.model == model && k.f64 == (f64 != 0)) return &k;
-  return udf_kernel_set(model, f64);
+  switch (model) {
+    case 1:
+      return set_monod(f64);
+    case 2:
+      return set_overflow(f64);
+    case 3:
+    case 4:
+      return f64 ? nullptr : set_fixed_length(model == 3);
+    default:
+      return udf_kernel_set(model, f64);
+  }
 }
 
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {

@@ -15,9 +15,12 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 4;
+constexpr int kKernelSetAbi = 5;
 
-using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*);
+// The last argument selects the instantiation with the warp-aggregated
+// scatter, for launches whose domains all have at most
+// kAggregateMaxCompartments compartments.
+using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*, bool);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
@@ -61,6 +64,9 @@ struct KernelSet {
 
 // Built-in sets first, then the sets of loaded plugins (bmc_udf_load).
 const KernelSet* kernel_set(int model, int f64);
+const KernelSet* set_monod(int f64);
+const KernelSet* set_overflow(int f64);
+const KernelSet* set_fixed_length(bool separable);
 const KernelSet* udf_kernel_set(int model, int f64);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,

@@ -82,6 +82,25 @@ def test_ring_monod_steps(oracle_mod, f64):
     assert_same_particles(g, o, "end")
 
 
+@pytest.mark.parametrize("shape", [None, (256, 2, 0), (544, 2, 0)])
+@pytest.mark.parametrize("n_c", [1, 3])
+def test_tiny_domains_warp_aggregated_scatter(oracle_mod, n_c, shape):
+    """Domains of at most 4 compartments sum the contributions of a warp per
+    compartment before the shared-memory atomic: sums stay exact."""
+    if n_c == 1:
+        sc = scenarios.zero_d(20000, model=scenarios.monod(f64=False), outlet=True)
+    else:
+        sc = scenarios.small_ring(20000, n_c=n_c, f64=False, feeds=True)
+    g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
+    for k in range(8):
+        gs, os_ = g.step(), o.step()
+        assert_same_stats(gs, os_, f"step {k}")
+        assert_same_liquid(g, o, f"step {k}")
+    assert_same_particles(g, o, "end")
+
+
 def test_cycle_only_uses_given_concentrations(oracle_mod):
     sc = scenarios.small_ring(3000, feeds=False)
     g, o = make_pair(oracle_mod, sc)
