@@ -177,6 +177,10 @@ struct bmc_scenario {
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
   unsigned graph_grid = 0;
+  bool ctl_fresh = false;  // h_ctl mirrors the device control block (no work enqueued since)
+  // last cycle-launch sizing (prepare_cycle), reused while its inputs stay
+  unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u;
+  size_t prep_in = 0, prep_out = 0;
   // flow-map cycle (host copies; device copies in marena)
   struct FlowMap {
     std::vector<int2> mrow;
@@ -391,6 +395,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
 int read_ctl(bmc_scenario* s, bmc_step_stats* out) {
   BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
   BMC_CUDA(cudaStreamSynchronize(s->stream));
+  s->ctl_fresh = true;
   if (out) {
     const Control& c = *s->h_ctl;
     std::memset(out, 0, sizeof(*out));
@@ -734,10 +739,9 @@ int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
   derive_outlets(s);
   int rc = refresh_map_tables(s);
   if (rc) return rc;
-  rc = upload_desc(s);
-  if (rc) return rc;
-  BMC_CUDA(cudaStreamSynchronize(s->stream));
-  return BMC_OK;
+  // stream-ordered: the descriptor copy is staged at once, later work on
+  // this stream sees it; no wait for the device
+  return upload_desc(s);
 }
 
 int bmc_set_weight(bmc_scenario* s, double weight) {
@@ -762,6 +766,7 @@ static int write_ctl_fresh(bmc_scenario* s, unsigned long long n, unsigned long 
   c.inactive = inactive;
   BMC_CUDA(counted_memcpy_async(s->d_ctl, &c, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(cudaStreamSynchronize(s->stream));
+  s->ctl_fresh = false;
   return BMC_OK;
 }
 
@@ -838,14 +843,35 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   return BMC_OK;
 }
 
+// prepare_cycle for a scenario, reusing the last answer while the launch
+// shape and the accumulator size are unchanged (no attribute or occupancy
+// query per step).
+static int scenario_prepare(bmc_scenario* s, size_t* smem, unsigned* grid) {
+  if (s->prep_variant == s->variant && s->prep_bps == s->blocks_per_sm && s->prep_in == *smem) {
+    *smem = s->prep_out;
+    *grid = s->prep_grid;
+    return BMC_OK;
+  }
+  const size_t in = *smem;
+  int rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, grid);
+  if (rc) return rc;
+  s->prep_variant = s->variant;
+  s->prep_bps = s->blocks_per_sm;
+  s->prep_in = in;
+  s->prep_out = *smem;
+  s->prep_grid = *grid;
+  return BMC_OK;
+}
+
 static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_scalar, bool use_graph) {
   int rc = check_ready(s, do_scalar != 0);
   if (rc) return rc;
   rc = set_dt(s, dt, true);
   if (rc) return rc;
+  s->ctl_fresh = false;
   size_t smem = cycle_smem(s->h);
   unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, &smem, s->sm_count, &grid);
+  rc = scenario_prepare(s, &smem, &grid);
   if (rc) return rc;
   if (use_graph && do_scalar) {
     rc = ensure_graph(s, grid, smem);
@@ -871,7 +897,7 @@ int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats) {
 }
 
 int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
-  int rc = scenario_steps(s, dt, 1, 1, false);
+  int rc = scenario_steps(s, dt, 1, 1, true);
   if (rc) return rc;
   return read_ctl(s, stats);
 }
@@ -942,8 +968,10 @@ int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
-  int rc = read_ctl(s, nullptr);
-  if (rc && rc != BMC_E_DEVICE) return rc;
+  if (!s->ctl_fresh) {  // the step parity names the current concentration buffer
+    int rc = read_ctl(s, nullptr);
+    if (rc && rc != BMC_E_DEVICE) return rc;
+  }
   const double* cur = s->h.C + (s->h_ctl->step & 1u) * ne;
   if (conc) BMC_CUDA(counted_memcpy_async(conc, cur, ne * 8, cudaMemcpyDeviceToHost, s->stream));
   if (mass) BMC_CUDA(counted_memcpy_async(mass, s->h.M, ne * 8, cudaMemcpyDeviceToHost, s->stream));
@@ -1131,6 +1159,8 @@ int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t b
 }
 
 int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
+  if (b)
+    for (bmc_scenario* m : b->scen) m->ctl_fresh = false;
   int n = 0;
   unsigned max_nc = 0, grid = 0;
   size_t smem = 0;
@@ -1266,6 +1296,7 @@ int upload_maps(bmc_scenario* s) {
   if (rc) return rc;
   const unsigned none = 0xffffffffu;
   BMC_CUDA(counted_memcpy_async(&s->d_ctl->map_cur, &none, sizeof(none), cudaMemcpyHostToDevice, s->stream));
+  s->ctl_fresh = false;
   rc = upload_desc(s);
   if (rc) return rc;
   BMC_CUDA(cudaStreamSynchronize(s->stream));
@@ -1362,6 +1393,8 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
 }
 
 int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
+  if (b)
+    for (bmc_scenario* m : b->scen) m->ctl_fresh = false;
   int n = 0;
   unsigned max_nc = 0, grid = 0;
   size_t smem = 0;
