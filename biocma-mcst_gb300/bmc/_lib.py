@@ -82,6 +82,7 @@ SIGNATURES = {
     "bmc_set_weight": [VP, c_dbl],
     "bmc_set_particles": [VP, c_u64, VP, VP, VP, VP, VP, VP, c_u64],
     "bmc_cycle": [VP, c_dbl, VP],
+    "bmc_cycle_external": [VP, c_dbl, VP, VP, c_i32, VP],
     "bmc_step": [VP, c_dbl, VP],
     "bmc_run": [VP, c_dbl, c_u32, VP],
     "bmc_run_async": [VP, c_dbl, c_u32],
@@ -106,6 +107,10 @@ SIGNATURES = {
     "bmc_batch_step_timed": [VP, c_dbl, VP],
     "bmc_set_device": [c_i32],
     "bmc_transfer_bytes": [VP, VP],
+    "bmc_gas_set": [VP, VP, c_u64, VP, VP, VP, VP, VP],
+    "bmc_gas_set_concentrations": [VP, VP],
+    "bmc_gas_set_feeds": [VP, c_u32, VP],
+    "bmc_gas_read": [VP, VP, VP, VP],
     "bmc_flowmap_add": [VP, VP, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_flowmap_period": [VP, c_dbl],
     "bmc_flowmap_clear": [VP],

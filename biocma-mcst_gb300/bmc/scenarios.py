@@ -86,6 +86,19 @@ class Feed:
 
 
 @dataclass
+class GasPhase:
+    """Gas phase of a two-phase scenario on the same mesh: gas flows and
+    volumes (a Network), Henry constants per species, transfer coefficients
+    kla [n_c, n_species] (1/s), initial concentrations and gas feeds."""
+
+    net: Network
+    henry: np.ndarray
+    kla: np.ndarray
+    c0: np.ndarray
+    feeds: list = field(default_factory=list)
+
+
+@dataclass
 class Scenario:
     name: str
     net: Network
@@ -106,6 +119,7 @@ class Scenario:
     # is `net`, the state the run starts on); empty: fixed domain
     flowmaps: list = field(default_factory=list)
     t_per_flowmap: float = 0.0
+    gas: GasPhase | None = None  # two-phase flow
 
     @property
     def n_per_flowmap(self) -> int:
@@ -214,6 +228,39 @@ def batch_scenario(k: int, seed: int = 1234, n_lo: float = 1e4, n_hi: float = 5e
     c0 = np.full((net.n_c, 1), glc)
     return Scenario(f"batch{k}", net, monod(f64=False, mu_max=mu), max(n_p, 1024), 1, c0, [],
                     dt=dt, n_steps=steps, seed=seed * 7919 + k)
+
+
+def with_gas(scen: Scenario, kla: float = 0.05, henry: float = 0.03, gas_fraction: float = 0.1,
+             gas_flow: float | None = None, seed: int = 17) -> Scenario:
+    """Adds a gas phase to a scenario: a gas ring through the compartments
+    (gas volume = gas_fraction x liquid volume), species 1 (O2 when present,
+    else 0) transferred with the given kla and Henry constant, air-like gas
+    inlet at compartment 0 and outlet at the last one."""
+    import dataclasses
+
+    n_c, ns = scen.net.n_c, scen.n_species
+    rng = np.random.default_rng(seed)
+    src = np.arange(n_c, dtype=np.int64)
+    dst = (src + 1) % n_c
+    # gas Courant number dt Q / V_gas of about 0.2 by default
+    q = gas_flow if gas_flow is not None else 0.2 * float(np.min(scen.net.volume * gas_fraction)) / scen.dt
+    flow = q * rng.uniform(0.8, 1.2, size=n_c) if n_c > 1 else np.zeros(0)
+    if n_c > 1:
+        gnet = Network(n_c, scen.net.volume * gas_fraction, src, dst, flow).finalize()
+    else:
+        gnet = Network(1, scen.net.volume * gas_fraction, np.zeros(0, np.int64), np.zeros(0, np.int64),
+                       np.zeros(0)).finalize()
+    o2 = 1 if ns > 1 else 0
+    k = np.zeros((n_c, ns))
+    k[:, o2] = kla
+    h = np.zeros(ns)
+    h[o2] = henry
+    cg = np.zeros((n_c, ns))
+    cg[:, o2] = 0.28  # kg/m3 of O2 in air
+    conc = np.zeros(ns)
+    conc[o2] = 0.28
+    feeds = [Feed(0, n_c - 1, q, conc)]
+    return dataclasses.replace(scen, gas=GasPhase(gnet, h, k, cg, feeds))
 
 
 def small_ring(n_particles: int = 4096, n_c: int = 10, seed: int = 3, f64: bool = True,

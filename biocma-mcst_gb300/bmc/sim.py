@@ -77,6 +77,8 @@ class GpuScenario:
                 for sp in range(len(fd.conc)):
                     arr[k].conc[sp] = float(fd.conc[sp])
             call("bmc_set_feeds", self.handle, len(scen.feeds), arr)
+        if scen.gas is not None:
+            self.set_gas(scen.gas)
         for fm in scen.flowmaps:
             self.add_flowmap(fm)
         if scen.flowmaps:
@@ -109,6 +111,32 @@ class GpuScenario:
         call("bmc_set_weight", self.handle, w)
         self.weight = w
 
+    def set_gas(self, gas):
+        """Two-phase flow: gas volumes, transition, Henry, kla, initial
+        concentrations and feeds (bmc_gas_*)."""
+        vol = np.ascontiguousarray(gas.net.volume, dtype=np.float64)
+        r, c, v = transition_coo(gas.net)
+        henry = np.zeros(8)
+        henry[: len(gas.henry)] = gas.henry
+        kla = np.ascontiguousarray(gas.kla, dtype=np.float64)
+        call("bmc_gas_set", self.handle, _p(vol), len(v), _p(r), _p(c), _p(v), _p(henry), _p(kla))
+        call("bmc_gas_set_concentrations", self.handle, _p(np.ascontiguousarray(gas.c0, dtype=np.float64)))
+        if gas.feeds:
+            arr = (Feed * len(gas.feeds))()
+            for k, fd in enumerate(gas.feeds):
+                arr[k].inlet = fd.inlet
+                arr[k].outlet = fd.outlet
+                arr[k].flow = fd.flow
+                for sp in range(len(fd.conc)):
+                    arr[k].conc[sp] = float(fd.conc[sp])
+            call("bmc_gas_set_feeds", self.handle, len(gas.feeds), arr)
+
+    def gas(self) -> dict:
+        n, ns = self.scen.net.n_c, self.scen.n_species
+        out = {k: np.zeros((n, ns)) for k in ("Cg", "Mg", "mtr")}
+        call("bmc_gas_read", self.handle, _p(out["Cg"]), _p(out["Mg"]), _p(out["mtr"]))
+        return out
+
     def add_flowmap(self, net):
         """Append a flow-map state of the same mesh (bmc_flowmap_add)."""
         vol = np.ascontiguousarray(net.volume, dtype=np.float64)
@@ -140,6 +168,21 @@ class GpuScenario:
         st = StepStats()
         call("bmc_cycle", self.handle, dt or self.scen.dt, ct.byref(st))
         return st.as_dict()
+
+    def cycle_external(self, conc, sources=None, dt: float | None = None) -> tuple:
+        """bmc_cycle_external: concentrations in, contributions out.  numpy
+        arrays use host pointers; objects with a `data_ptr()` (device
+        tensors) are passed as device pointers."""
+        dt = self.scen.dt if dt is None else dt
+        st = StepStats()
+        if hasattr(conc, "data_ptr"):
+            call("bmc_cycle_external", self.handle, dt, ct.c_void_p(conc.data_ptr()),
+                 ct.c_void_p(sources.data_ptr()), 1, ct.byref(st))
+            return sources, st.as_dict()
+        c = np.ascontiguousarray(conc, dtype=np.float64)
+        out = np.zeros_like(c) if sources is None else sources
+        call("bmc_cycle_external", self.handle, dt, _p(c), _p(out), 0, ct.byref(st))
+        return out, st.as_dict()
 
     def step(self, dt: float | None = None) -> dict:
         st = StepStats()

@@ -192,6 +192,9 @@ struct bmc_scenario {
   double t_per_map = 0.0;
   void* marena = nullptr;
   uint32_t* d_map_exit = nullptr;
+  // gas phase of a two-phase flow (device arrays in garena)
+  void* garena = nullptr;
+  std::vector<double> gvol;
 };
 
 struct bmc_batch {
@@ -583,6 +586,7 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->darena) cudaFree(s->darena);
   if (s->tarena) cudaFree(s->tarena);
   if (s->marena) cudaFree(s->marena);
+  if (s->garena) cudaFree(s->garena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   cudaStreamDestroy(s->stream);
   delete s;
@@ -896,6 +900,24 @@ int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats) {
   return read_ctl(s, stats);
 }
 
+int bmc_cycle_external(bmc_scenario* s, double dt, const double* conc, double* sources, int32_t on_device,
+                       bmc_step_stats* stats) {
+  if (!s || !conc || !sources) return fail(BMC_E_INVALID, "null argument");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  const cudaMemcpyKind kin = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  const cudaMemcpyKind kout = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  // the cycle reads the concentrations from the buffer of the step's parity:
+  // both buffers get them
+  BMC_CUDA(counted_memcpy_async(s->h.C, conc, ne * 8, kin, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.C + ne, conc, ne * 8, kin, s->stream));
+  s->has_conc = true;
+  int rc = scenario_steps(s, dt, 1, 0, false);
+  if (rc) return rc;
+  BMC_CUDA(counted_memcpy_async(sources, s->h.src, ne * 8, kout, s->stream));
+  return read_ctl(s, stats);
+}
+
 int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
   int rc = scenario_steps(s, dt, 1, 1, true);
   if (rc) return rc;
@@ -1200,6 +1222,129 @@ int bmc_batch_synchronize(bmc_batch* b) {
   BMC_CUDA(cudaStreamSynchronize(b->stream));
   return BMC_OK;
 }
+
+// ---- two-phase flow: gas phase -------------------------------------------------------
+// Reference: SimulationUnit with is_two_phase_flow (gas ScalarSimulation,
+// apps/libs/simulation/src/simulation.cpp L47-L81, L133-L139), ode_step
+// (simulation.model.cpp L132-L150: transfer, gas step, liquid step,
+// clearNegs), gas feeds (simulation.model.cpp L112-L119) and the FixedKla
+// transfer (hydro/impl_mtr.cpp L150-L166).
+
+extern "C" {
+
+int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
+                const double* values, const double* henry, const double* kla) {
+  if (!s || !gas_volume || !henry || !kla || (nnz && (!rows || !cols || !values)))
+    return fail(BMC_E_INVALID, "bad gas arguments");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update fixes n_compartments)");
+  ScenDev& h = s->h;
+  const uint32_t n_c = h.n_c;
+  const size_t ne = (size_t)n_c * h.n_s;
+  std::vector<double> gv(gas_volume, gas_volume + n_c), gvinv(n_c);
+  for (uint32_t j = 0; j < n_c; ++j) {
+    if (!(gv[j] > 0.0)) return fail(BMC_E_INVALID, "gas volumes must be > 0");
+    gvinv[j] = 1.0 / gv[j];
+  }
+  for (size_t e = 0; e < ne; ++e)
+    if (!(kla[e] >= 0.0)) return fail(BMC_E_INVALID, "kla must be >= 0");
+  std::vector<uint32_t> ptr, idx;
+  std::vector<double> val, diag;
+  if (const char* why = build_csr(n_c, nnz, rows, cols, values, ptr, idx, val, diag)) return fail(BMC_E_INVALID, why);
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->garena) cudaFree(s->garena);
+  s->garena = nullptr;
+  Carver cv;
+  double *p_gvinv = nullptr, *p_flow = nullptr, *p_diag = nullptr, *p_kla = nullptr;
+  uint32_t *p_ptr = nullptr, *p_idx = nullptr;
+  cv.add(&p_gvinv, n_c);
+  cv.add(&p_ptr, n_c + 1);
+  cv.add(&p_idx, idx.size());
+  cv.add(&p_flow, val.size());
+  cv.add(&p_diag, n_c);
+  cv.add(&p_kla, ne);
+  cv.add(&h.Cg, 2 * ne);
+  cv.add(&h.Mg, ne);
+  cv.add(&h.mtr, ne);
+  BMC_CUDA(cudaMalloc(&s->garena, cv.off));
+  cv.bind(s->garena);
+  BMC_CUDA(cudaMemsetAsync(s->garena, 0, cv.off, s->stream));
+  BMC_CUDA(counted_memcpy_async(p_gvinv, gvinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(p_ptr, ptr.data(), ptr.size() * 4, cudaMemcpyHostToDevice, s->stream));
+  if (!idx.empty()) {
+    BMC_CUDA(counted_memcpy_async(p_idx, idx.data(), idx.size() * 4, cudaMemcpyHostToDevice, s->stream));
+    BMC_CUDA(counted_memcpy_async(p_flow, val.data(), val.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  }
+  BMC_CUDA(counted_memcpy_async(p_diag, diag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(p_kla, kla, ne * 8, cudaMemcpyHostToDevice, s->stream));
+  h.gvinv = p_gvinv;
+  h.g_in_ptr = p_ptr;
+  h.g_in_idx = p_idx;
+  h.g_in_flow = p_flow;
+  h.g_diag = p_diag;
+  h.kla = p_kla;
+  for (int k = 0; k < bmc::kMaxSpecies; ++k) h.henry[k] = k < (int)h.n_s ? henry[k] : 0.0;
+  h.gas = 1;
+  s->gvol = gv;
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_gas_set_concentrations(bmc_scenario* s, const double* conc) {
+  if (!s || !conc) return fail(BMC_E_INVALID, "null argument");
+  if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
+  const size_t n_c = s->h.n_c, ns = s->h.n_s;
+  std::vector<double> C(conc, conc + n_c * ns), M(n_c * ns);
+  for (size_t j = 0; j < n_c; ++j)
+    for (size_t sp = 0; sp < ns; ++sp) {
+      if (!(C[j * ns + sp] >= 0.0)) return fail(BMC_E_INVALID, "concentrations must be >= 0");
+      M[j * ns + sp] = C[j * ns + sp] * s->gvol[j];
+    }
+  BMC_CUDA(counted_memcpy_async(s->h.Cg, C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.Cg + C.size(), C.data(), C.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h.Mg, M.data(), M.size() * 8, cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+int bmc_gas_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
+  if (!s || (n_feeds && !feeds)) return fail(BMC_E_INVALID, "null argument");
+  if (n_feeds > (uint32_t)bmc::kMaxOutlets) return fail(BMC_E_INVALID, "at most 8 gas feeds");
+  if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
+  ScenDev& h = s->h;
+  for (uint32_t f = 0; f < n_feeds; ++f) {
+    if (feeds[f].inlet >= h.n_c || feeds[f].outlet >= (int32_t)h.n_c || feeds[f].outlet < -1)
+      return fail(BMC_E_INVALID, "gas feed position out of range");
+    if (!(feeds[f].flow >= 0.0)) return fail(BMC_E_INVALID, "gas feed flow must be >= 0");
+  }
+  h.n_gfeeds = n_feeds;
+  for (uint32_t f = 0; f < n_feeds; ++f) {
+    h.gfeed_in[f] = feeds[f].inlet;
+    h.gfeed_out[f] = feeds[f].outlet;
+    h.gfeed_flow[f] = feeds[f].flow;
+    for (int sp = 0; sp < bmc::kMaxSpecies; ++sp) h.gfeed_conc[f * bmc::kMaxSpecies + sp] = feeds[f].conc[sp];
+  }
+  return upload_desc(s);
+}
+
+int bmc_gas_read(bmc_scenario* s, double* conc, double* mass, double* transfer) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  if (!s->ctl_fresh) {
+    int rc = read_ctl(s, nullptr);
+    if (rc && rc != BMC_E_DEVICE) return rc;
+  }
+  const double* cur = s->h.Cg + (s->h_ctl->step & 1u) * ne;
+  if (conc) BMC_CUDA(counted_memcpy_async(conc, cur, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (mass) BMC_CUDA(counted_memcpy_async(mass, s->h.Mg, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  if (transfer) BMC_CUDA(counted_memcpy_async(transfer, s->h.mtr, ne * 8, cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+}  // extern "C"
 
 // ---- flow-map cycle -----------------------------------------------------------------
 

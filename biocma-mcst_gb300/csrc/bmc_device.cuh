@@ -33,6 +33,9 @@ constexpr long long kQMax = 1LL << 42;  // |quantised value| bound
 // A block flushes its shared-memory accumulator before it has summed more
 // than 2^20 particles, so |partial| <= 2^62 and no int64 sum can overflow.
 constexpr unsigned kFlushParticles = 1u << 20;
+// ScalarSimulation::clearNegs threshold: scheme relative error 1e-4 times
+// the species scale 5e-3 (implScalar.cpp L273-L277)
+constexpr double kClearNegTol = 1e-4 * 5e-3;
 
 enum : uint8_t { kIdle = 0, kDivision = 1, kExit = 2, kDead = 3 };
 
@@ -154,6 +157,27 @@ struct ScenDev {
   const uint32_t* map_in_idx;    // [n_maps][map_nnz_max]
   const double* map_in_flow;     // [n_maps][map_nnz_max]
   const uint32_t* map_exit_thr;  // [n_maps][kMaxOutlets], for the current dt
+  // Gas phase of a two-phase flow (gas == 0: liquid only): its own volumes,
+  // transition (incoming lists + diagonal) and feeds, concentrations double
+  // buffered like C, and the gas-liquid transfer
+  //   mtr(j,s) = kla(j,s) (H(s) Cg(j,s) - C(j,s)) V(j)
+  // gained by the liquid and lost by the gas in the same step.
+  uint32_t gas;
+  const double* gvinv;
+  const uint32_t* g_in_ptr;
+  const uint32_t* g_in_idx;
+  const double* g_in_flow;
+  const double* g_diag;
+  double* Cg;              // two buffers of n_c * n_s, current one by step parity
+  double* Mg;
+  const double* kla;       // [n_c][n_s], 1/s
+  double* mtr;             // [n_c][n_s], kg/s, of the last step
+  double henry[kMaxSpecies];
+  uint32_t n_gfeeds;
+  uint32_t gfeed_in[kMaxOutlets];
+  int32_t gfeed_out[kMaxOutlets];
+  double gfeed_flow[kMaxOutlets];
+  double gfeed_conc[kMaxOutlets * kMaxSpecies];
 };
 
 // A scenario whose step counter has reached its limit is left untouched.

@@ -131,16 +131,44 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
         acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
       const double cj = Cold[e];
       acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
-      const double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
+      double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
+      double mt = 0.0;
+      if (S.gas) {
+        // gas-liquid transfer from the old concentrations
+        // (fixed_kla_gas_liquid_mass_transfer, impl_mtr.cpp L150-L166), then
+        // the gas step with the transfer lost (performStepGL, Sign::GasToLiquid)
+        const double* __restrict__ Cgo = S.Cg + parity * ne;
+        const double cg = Cgo[e];
+        mt = __dmul_rn(__dmul_rn(S.kla[e], __dsub_rn(__dmul_rn(cg, S.henry[sp]), cj)), S.volume[j]);
+        S.mtr[e] = mt;
+        double gsrc = 0.0, gsink = 0.0;
+        for (unsigned f = 0; f < S.n_gfeeds; ++f) {
+          if (S.gfeed_in[f] == j) gsrc = __dadd_rn(gsrc, __dmul_rn(S.gfeed_flow[f], S.gfeed_conc[f * kMaxSpecies + sp]));
+          if (S.gfeed_out[f] == (int)j) gsink = __dadd_rn(gsink, S.gfeed_flow[f]);
+        }
+        double gacc = 0.0;
+        for (unsigned q = S.g_in_ptr[j]; q < S.g_in_ptr[j + 1]; ++q)
+          gacc = __dadd_rn(gacc, __dmul_rn(Cgo[(size_t)S.g_in_idx[q] * nsp + sp], S.g_in_flow[q]));
+        gacc = __dadd_rn(gacc, __dmul_rn(cg, S.g_diag[j]));
+        const double gdmdt = __dsub_rn(__dadd_rn(__dsub_rn(gacc, __dmul_rn(cg, gsink)), gsrc), mt);
+        const double mg = __dadd_rn(S.Mg[e], __dmul_rn(dt, gdmdt));
+        S.Mg[e] = mg;
+        S.Cg[(parity ^ 1u) * ne + e] = __dmul_rn(mg, S.gvinv[j]);
+        dmdt = __dadd_rn(dmdt, mt);  // Sign::LiquidToGas
+      }
       const double mold = S.M[e];
       const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
       S.M[e] = mnew;
       cn = __dmul_rn(mnew, S.vinv[j]);
+      // two-phase: tiny negative liquid concentrations are cleared
+      // (ScalarSimulation::clearNegs, implScalar.cpp L266-L293)
+      if (S.gas && cn < 0.0 && fabs(cn) < kClearNegTol) cn = 0.0;
       // mass-balance sums (diagnostic): new mass, expected mass
       atomicAdd(&red[0][sp], mnew);
-      atomicAdd(&red[1][sp], mold + dt * (srcv - cj * sinkj));
+      atomicAdd(&red[1][sp], mold + dt * (srcv + mt - cj * sinkj));
     }
     Cnew[e] = cn;
+    if (!do_scalar && S.gas) S.Cg[(parity ^ 1u) * ne + e] = S.Cg[parity * ne + e];
     cs[t] = cn;
   }
   __syncthreads();

@@ -188,6 +188,16 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
  * concentrations currently on the device; leaves the contributions of this
  * cycle as the sources of the next liquid step. */
 int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats);
+/* cycleProcess for a caller that keeps its own liquid-scalar step (the
+ * reference's host ScalarSimulation, SimulationUnit::cycleProcess with
+ * getter concentrations in, scatter_contribute / synchro_sources out:
+ * apps/libs/simulation/src/simulation.cpp L143-L160, implScalar.cpp L194):
+ * concentrations [n_c][n_species] in, the cycle's contributions (sources,
+ * same layout, kg/s) out; both host pointers, or both device pointers when
+ * on_device != 0 (no host round trip).  Feeds are not applied (they belong
+ * to the caller's liquid step); concentrations are not checked on device. */
+int bmc_cycle_external(bmc_scenario* s, double dt, const double* conc, double* sources, int32_t on_device,
+                       bmc_step_stats* stats);
 
 /* One iteration of the reference main loop (apps/core/src/host_specific.cpp
  * L280-L291): update_feed, ode_step (ScalarSimulation::performStep,
@@ -264,6 +274,31 @@ int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neigh
                     const uint64_t* cols, const double* values);
 int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap);
 int bmc_flowmap_clear(bmc_scenario* s);
+
+/* ---- two-phase flow: gas phase ------------------------------------------- */
+/* A gas phase on the scenario's mesh (SimulationUnit with
+ * is_two_phase_flow; apps/libs/simulation/src/simulation.cpp L47-L81):
+ * gas volumes [n_c], the gas transition in COO form (as
+ * bmc_set_transition_coo), Henry constants [n_species] and the transfer
+ * coefficients kla [n_c][n_species] (1/s; the reference's FixedKla gives one
+ * value per species, its FlowmapTurbulence correlation one per compartment,
+ * hydro/impl_mtr.cpp L92-L148).  Each main-loop step then computes, from the
+ * step's old concentrations, mtr(j,s) = kla (H Cg - C) V_liquid
+ * (fixed_kla_gas_liquid_mass_transfer, impl_mtr.cpp L150-L166), advances
+ * the gas with -mtr and the liquid with +mtr (ScalarSimulation::
+ * performStepGL, implScalar.cpp L229-L249; SimulationUnit::ode_step,
+ * simulation.model.cpp L132-L150) and clears tiny negative liquid
+ * concentrations (clearNegs, implScalar.cpp L266-L293).  Particles see the
+ * liquid only.  The gas domain stays fixed while flow maps cycle. */
+int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const uint64_t* rows,
+                const uint64_t* cols, const double* values, const double* henry, const double* kla);
+int bmc_gas_set_concentrations(bmc_scenario* s, const double* conc);
+/* Gas feeds (update_feed's gas_feeds, simulation.model.cpp L112-L119):
+ * inlet sources flow x conc, outlet sinks; no particle exit. */
+int bmc_gas_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds);
+/* Gas concentrations, masses and the last step's transfer to the liquid
+ * (kg/s), each [n_c][n_species] (NULL skips). */
+int bmc_gas_read(bmc_scenario* s, double* conc, double* mass, double* transfer);
 
 /* ---- batching: many scenarios advanced by one set of launches ----------- */
 /* All scenarios of a batch share model and precision; each keeps its own

@@ -364,6 +364,38 @@ uint32_t orc_find_next(const orc_state* s, uint32_t c, double u) {
  * with T(i,j) = F(i->j) off the diagonal and T(j,j) = -sum_k F(j->k). */
 void orc_scalar_step(orc_state* s, double dt) {
   const uint32_t ns = s->n_s;
+  const uint64_t ne = (uint64_t)s->n_c * ns;
+  if (s->gas) {
+    /* transfer from the old concentrations, then the gas step with the
+     * transfer lost (Sign::GasToLiquid); the liquid gains it below */
+    for (uint32_t j = 0; j < s->n_c; ++j)
+      for (uint32_t sp = 0; sp < ns; ++sp) {
+        const uint64_t e = (uint64_t)j * ns + sp;
+        s->mtr[e] = (s->kla[e] * (s->Cg[e] * s->henry[sp] - s->C[e])) * s->volume[j];
+      }
+    double* gsrc = (double*)calloc(ne ? ne : 1, sizeof(double));
+    double* gsink = (double*)calloc(s->n_c, sizeof(double));
+    for (uint32_t f = 0; f < s->n_gfeeds; ++f) {
+      for (uint32_t sp = 0; sp < ns; ++sp)
+        gsrc[(uint64_t)s->gfeed_in[f] * ns + sp] += s->gfeed_flow[f] * s->gfeed_conc[f * 8 + sp];
+      if (s->gfeed_out[f] >= 0) gsink[s->gfeed_out[f]] += s->gfeed_flow[f];
+    }
+    for (uint32_t j = 0; j < s->n_c; ++j)
+      for (uint32_t sp = 0; sp < ns; ++sp) {
+        const uint64_t e = (uint64_t)j * ns + sp;
+        double acc = 0.0;
+        for (uint32_t q = s->g_in_ptr[j]; q < s->g_in_ptr[j + 1]; ++q)
+          acc += s->Cg[(uint64_t)s->g_in_idx[q] * ns + sp] * s->g_in_flow[q];
+        const double cg = s->Cg[e];
+        acc += cg * (-s->g_out_flow[j]);
+        const double dmdt = acc - cg * gsink[j] + gsrc[e] + (-1.0) * s->mtr[e];
+        s->Mg[e] += dt * dmdt;
+      }
+    for (uint32_t j = 0; j < s->n_c; ++j)
+      for (uint32_t sp = 0; sp < ns; ++sp) s->Cg[(uint64_t)j * ns + sp] = s->Mg[(uint64_t)j * ns + sp] * s->gvinv[j];
+    free(gsrc);
+    free(gsink);
+  }
   for (uint32_t j = 0; j < s->n_c; ++j) {
     for (uint32_t sp = 0; sp < ns; ++sp) {
       double acc = 0.0;
@@ -371,13 +403,18 @@ void orc_scalar_step(orc_state* s, double dt) {
         acc += s->C[(uint64_t)s->in_idx[e] * ns + sp] * s->in_flow[e];
       const double cj = s->C[(uint64_t)j * ns + sp];
       acc += cj * (-s->out_flow[j]);
-      const double dmdt = acc - cj * s->sink[j] + s->src[(uint64_t)j * ns + sp];
+      double dmdt = acc - cj * s->sink[j] + s->src[(uint64_t)j * ns + sp];
+      if (s->gas) dmdt = dmdt + s->mtr[(uint64_t)j * ns + sp];
       s->M[(uint64_t)j * ns + sp] += dt * dmdt;
     }
   }
+  const double tol = 1e-4 * 5e-3; /* clearNegs */
   for (uint32_t j = 0; j < s->n_c; ++j)
-    for (uint32_t sp = 0; sp < ns; ++sp)
-      s->C[(uint64_t)j * ns + sp] = s->M[(uint64_t)j * ns + sp] * s->vinv[j];
+    for (uint32_t sp = 0; sp < ns; ++sp) {
+      double c = s->M[(uint64_t)j * ns + sp] * s->vinv[j];
+      if (s->gas && c < 0.0 && fabs(c) < tol) c = 0.0;
+      s->C[(uint64_t)j * ns + sp] = c;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -633,24 +670,32 @@ void orc_post_cycle(orc_state* s) {
 
 /* One main-loop iteration, apps/core/src/host_specific.cpp L280-L291:
  * update_feed -> ode_step -> clearContribution -> cycleProcess. */
-void orc_step(orc_state* s, double dt, int n_threads) {
-  const uint32_t ns = s->n_s;
-  for (uint32_t j = 0; j < s->n_c; ++j) s->sink[j] = 0.0;
+/* Leaving flows of the particles from the feeds' outlets, in feed order
+ * (the set_leaving_flow calls of update_feed, simulation.model.cpp L101-L108). */
+void orc_set_outlets(orc_state* s) {
   s->n_outlets = 0;
   for (uint32_t f = 0; f < s->n_feeds; ++f) {
-    for (uint32_t sp = 0; sp < ns; ++sp) {
-      const double cf = s->feed_conc[f * 8 + sp];
-      if (cf != 0.0) s->src[(uint64_t)s->feed_in[f] * ns + sp] += s->feed_flow[f] * cf;
-    }
     if (s->feed_out[f] >= 0) {
       const uint32_t o = (uint32_t)s->feed_out[f];
-      s->sink[o] += s->feed_flow[f];
       s->outlet_index[s->n_outlets] = o;
       s->outlet_flow[s->n_outlets] = s->feed_flow[f];
       s->outlet_volume[s->n_outlets] = s->volume[o];
       s->n_outlets++;
     }
   }
+}
+
+void orc_step(orc_state* s, double dt, int n_threads) {
+  const uint32_t ns = s->n_s;
+  for (uint32_t j = 0; j < s->n_c; ++j) s->sink[j] = 0.0;
+  for (uint32_t f = 0; f < s->n_feeds; ++f) {
+    for (uint32_t sp = 0; sp < ns; ++sp) {
+      const double cf = s->feed_conc[f * 8 + sp];
+      if (cf != 0.0) s->src[(uint64_t)s->feed_in[f] * ns + sp] += s->feed_flow[f] * cf;
+    }
+    if (s->feed_out[f] >= 0) s->sink[(uint32_t)s->feed_out[f]] += s->feed_flow[f];
+  }
+  orc_set_outlets(s);
   orc_scalar_step(s, dt);
   memset(s->src, 0, sizeof(double) * (size_t)s->n_c * ns);
   orc_cycle(s, dt, n_threads);

@@ -154,8 +154,30 @@ typedef struct orc_state {
 
   /* run-time model: when set, it replaces the compiled-in models */
   const orc_udf_model* udf;
+
+  /* gas phase of a two-phase flow (gas == 0: liquid only):
+   * apps/libs/simulation/src/simulation.model.cpp L132-L150 (ode_step),
+   * implScalar.cpp L229-L249 (performStepGL), hydro/impl_mtr.cpp L150-L166
+   * (fixed kla transfer), implScalar.cpp L266-L293 (clearNegs) */
+  int32_t gas;
+  const double* gvinv;
+  const uint32_t* g_in_ptr;
+  const uint32_t* g_in_idx;
+  const double* g_in_flow;
+  const double* g_out_flow; /* gas diagonal = -g_out_flow */
+  double* Cg;
+  double* Mg;
+  const double* kla;        /* [n_c][n_s] */
+  double* mtr;              /* [n_c][n_s], transfer to the liquid of the last step */
+  double henry[8];
+  uint32_t n_gfeeds;
+  uint32_t gfeed_in[ORC_MAX_OUTLETS];
+  int32_t gfeed_out[ORC_MAX_OUTLETS];
+  double gfeed_flow[ORC_MAX_OUTLETS];
+  double gfeed_conc[ORC_MAX_OUTLETS * 8];
 } orc_state;
 
+void orc_set_outlets(orc_state* s);
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 float orc_u01(uint32_t x);
 void orc_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]);

@@ -49,6 +49,12 @@ class OrcState(ct.Structure):
         ("overflow", ct.c_uint64), ("requested_divisions", ct.c_uint64),
         ("compacted", ct.c_int32), ("error", ct.c_int32),
         ("udf", ct.c_void_p),
+        ("gas", ct.c_int32), ("gvinv", ct.c_void_p), ("g_in_ptr", ct.c_void_p),
+        ("g_in_idx", ct.c_void_p), ("g_in_flow", ct.c_void_p), ("g_out_flow", ct.c_void_p),
+        ("Cg", ct.c_void_p), ("Mg", ct.c_void_p), ("kla", ct.c_void_p), ("mtr", ct.c_void_p),
+        ("henry", ct.c_double * 8), ("n_gfeeds", ct.c_uint32), ("gfeed_in", ct.c_uint32 * MAXO),
+        ("gfeed_out", ct.c_int32 * MAXO), ("gfeed_flow", ct.c_double * MAXO),
+        ("gfeed_conc", ct.c_double * (MAXO * 8)),
     ]
 
 
@@ -94,6 +100,7 @@ def lib():
         L.orc_step.argtypes = [P, ct.c_double, ct.c_int]
         L.orc_run.argtypes = [P, ct.c_double, ct.c_uint32, ct.c_int]
         L.orc_cycle.argtypes = [P, ct.c_double, ct.c_int]
+        L.orc_set_outlets.argtypes = [P]
         L.orc_post_cycle.argtypes = [P]
         L.orc_scalar_step.argtypes = [P, ct.c_double]
         L.orc_remove_inactive.argtypes = [P, ct.c_uint64]
@@ -202,10 +209,39 @@ class Oracle:
             self._udf = udf_host_model(m.udf_path, m.f64)
             assert self._udf[1].n_var == m.n_var and self._udf[1].n_ctb == m.n_ctb
             s.udf = ct.addressof(self._udf[1])
+        if scen.gas is not None:
+            self._setup_gas(s, scen.gas)
         self.s = s
         self.weight = None
         self._map_arrays = {}
         self._map_cur = 0
+
+    def _setup_gas(self, s, gas):
+        """Gas phase arrays (kept alive on the object) and feeds."""
+        gn = gas.net
+        ns = self.scen.n_species
+        self.gvol = np.ascontiguousarray(gn.volume, dtype=np.float64)
+        self.gvinv = 1.0 / self.gvol
+        self.g_in_ptr = np.ascontiguousarray(gn.in_ptr, dtype=np.uint32)
+        self.g_in_idx = np.ascontiguousarray(gn.in_idx, dtype=np.uint32)
+        self.g_in_flow = np.ascontiguousarray(gn.in_flow, dtype=np.float64)
+        self.g_out_flow = np.ascontiguousarray(gn.out_flow, dtype=np.float64)
+        self.Cg = np.ascontiguousarray(gas.c0, dtype=np.float64).copy()
+        self.Mg = (self.Cg * self.gvol[:, None]).copy()
+        self.kla = np.ascontiguousarray(gas.kla, dtype=np.float64)
+        self.mtr = np.zeros_like(self.Cg)
+        s.gas = 1
+        for name in ("gvinv", "g_in_ptr", "g_in_idx", "g_in_flow", "g_out_flow", "Cg", "Mg", "kla", "mtr"):
+            setattr(s, name, _ptr(getattr(self, name)))
+        for sp in range(min(ns, 8)):
+            s.henry[sp] = float(gas.henry[sp])
+        s.n_gfeeds = len(gas.feeds)
+        for f, fd in enumerate(gas.feeds):
+            s.gfeed_in[f] = fd.inlet
+            s.gfeed_out[f] = fd.outlet
+            s.gfeed_flow[f] = fd.flow
+            for sp in range(ns):
+                s.gfeed_conc[f * 8 + sp] = float(fd.conc[sp])
 
     # -- set-up --------------------------------------------------------------
     def init_particles(self, n: int | None = None):
@@ -271,6 +307,9 @@ class Oracle:
         lib().orc_run(ct.byref(self.s), self.scen.dt, n_steps, n_threads)
 
     def cycle(self, n_threads: int = 1):
+        """cycleProcess alone: leaving flows from the feeds' outlets, then the
+        cycle (no liquid step, no feed sources)."""
+        lib().orc_set_outlets(ct.byref(self.s))
         lib().orc_cycle(ct.byref(self.s), self.scen.dt, n_threads)
 
     def post_cycle(self):

@@ -117,6 +117,31 @@ def test_cycle_only_uses_given_concentrations(oracle_mod):
 SHAPES = [None, (288, 4, 0)]
 
 
+def test_cycle_external_host_and_device_pointers(oracle_mod):
+    """bmc_cycle_external: the caller's concentrations in, the cycle's
+    contributions out, bit for bit as the restatement's cycle."""
+    sc = scenarios.small_ring(6000, feeds=True)
+    g, o = make_pair(oracle_mod, sc)
+    rng = np.random.default_rng(11)
+    torch = pytest.importorskip("torch")
+    for k in range(4):
+        conc = rng.uniform(0.5, 8.0, size=(sc.net.n_c, sc.n_species))
+        if k % 2 == 0:
+            src, st = g.cycle_external(conc)
+        else:
+            dc = torch.tensor(conc, dtype=torch.float64, device="cuda")
+            out = torch.zeros_like(dc)
+            _, st = g.cycle_external(dc, out)
+            src = out.cpu().numpy()
+        o.C[:] = conc
+        o.cycle()
+        o.post_cycle()
+        o.s.step += 1
+        assert same_bits(src, o.src), f"cycle {k}"
+        assert st["moves"] == o.s.moves and st["exits"] == o.s.exits, f"cycle {k}"
+    assert_same_particles(g, o, "end")
+
+
 @pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("f64", [True, False])
 def test_lattice_overflow_model(oracle_mod, f64, shape):
