@@ -1,0 +1,161 @@
+"""Edge cases of the GPU path against the CPU restatement: an empty
+container, a container that empties, ragged particle counts around tile and
+warp boundaries, rows longer than any benchmark's, exhausted particle ids,
+and malformed inputs that the library must refuse (the scenario stays
+usable afterwards)."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+
+from bmc import networks, scenarios
+
+pytestmark = pytest.mark.gpu
+
+
+def _parity(g, o, steps, where):
+    from test_gpu_parity import assert_same_liquid, assert_same_particles, assert_same_stats
+
+    for k in range(steps):
+        gs, os_ = g.step(), o.step()
+        assert_same_stats(gs, os_, f"{where} step {k}")
+        assert_same_liquid(g, o, f"{where} step {k}")
+    assert_same_particles(g, o, where)
+
+
+def test_empty_container(oracle_mod):
+    from bmc.sim import GpuScenario
+
+    sc = scenarios.small_ring(0, feeds=True)
+    g = GpuScenario(sc, capacity=1024, init=False)
+    empty = dict(state=np.zeros((2, 0)), pos=np.zeros(0, np.uint32), status=np.zeros(0, np.uint8),
+                 age_h=np.zeros(0, np.float32), age_d=np.zeros(0, np.float32), id=np.zeros(0, np.uint32))
+    g.set_particles(empty, 0)
+    g.set_weight(1.0)
+    o = oracle_mod.Oracle(sc, phys_capacity=g.cap)
+    o.set_weight(1.0)
+    _parity(g, o, 6, "empty")
+    assert g.stats()["n_used"] == 0
+
+
+def test_container_that_empties(oracle_mod):
+    """A 0-D reactor with an outlet faster than growth: every particle
+    leaves, the container compacts to nothing and keeps stepping."""
+    from test_gpu_parity import make_pair
+
+    sc = scenarios.zero_d(3000, outlet=True)
+    sc.feeds[0].flow = 1e-2  # dt F / V = 1: 63 % of the particles leave per step
+    g, o = make_pair(oracle_mod, sc)
+    _parity(g, o, 30, "emptying")
+    st = g.stats()
+    assert st["n_used"] - st["inactive"] == 0
+
+
+@pytest.mark.parametrize("shape", [None, (544, 2, 0)])
+@pytest.mark.parametrize("n", [1, 31, 1023, 1025, 2047])
+def test_ragged_particle_counts(oracle_mod, n, shape):
+    from test_gpu_parity import make_pair
+
+    sc = scenarios.small_ring(n, n_c=16, feeds=True)
+    g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
+    _parity(g, o, 4, f"n={n}")
+
+
+def complete_graph(n_c=13, seed=5):
+    rng = np.random.default_rng(seed)
+    src, dst = [], []
+    for i in range(n_c):
+        for j in range(n_c):
+            if i != j:
+                src.append(i)
+                dst.append(j)
+    src, dst = np.array(src), np.array(dst)
+    flow = rng.uniform(0.5e-5, 2e-5, size=len(src))
+    vol = rng.uniform(0.5e-3, 2e-3, size=n_c)
+    return networks.Network(n_c, vol, src, dst, flow).finalize()
+
+
+@pytest.mark.parametrize("shape", [None, (544, 2, 0)])
+def test_long_neighbour_rows(oracle_mod, shape):
+    """Every compartment connected to all others: rows of 12 entries."""
+    from test_gpu_parity import make_pair
+
+    net = complete_graph()
+    assert net.K == 12
+    sc = scenarios.small_ring(8000, feeds=True)
+    sc.net = net
+    sc.c0 = np.full((net.n_c, 1), 5.0)
+    sc.feeds[0].outlet = net.n_c - 1
+    g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
+    _parity(g, o, 6, "K=12")
+
+
+def test_particle_id_space_exhaustion():
+    """Births that would pass 2^32 ids set the error word (never a fault)."""
+    from bmc import _lib
+    from bmc.sim import GpuScenario
+
+    m = scenarios.monod(f64=True, m_div=1.0)  # every particle asks to divide
+    sc = scenarios.zero_d(2000, model=m, outlet=False)
+    g = GpuScenario(sc, capacity=8192)
+    parts = g.particles()
+    g.set_particles(parts, (1 << 32) - 10)
+    with pytest.raises(_lib.BmcError) as e:
+        g.step()
+    assert e.value.code == -5  # BMC_E_DEVICE
+    st = _lib.StepStats()
+    assert _lib.load().bmc_read_stats(g.handle, ct.byref(st)) == -5
+    assert st.error & 4
+
+
+def test_malformed_inputs_are_refused():
+    from bmc import _lib
+    from bmc.sim import GpuScenario
+
+    sc = scenarios.small_ring(2000, feeds=True)
+    g = GpuScenario(sc)
+    net = sc.net
+    L = _lib.load()
+
+    def domain(vol, nbr, outf, cdf):
+        return L.bmc_domain_update(g.handle, net.n_c, net.K, vol.ctypes.data, nbr.ctypes.data,
+                                   outf.ctypes.data, cdf.ctypes.data)
+
+    vol = np.ascontiguousarray(net.volume, dtype=np.float64)
+    nbr = np.ascontiguousarray(net.neighbors, dtype=np.uint64)
+    outf = np.ascontiguousarray(net.out_flow, dtype=np.float64)
+    cdf = np.ascontiguousarray(net.cdf, dtype=np.float64)
+    bad = cdf.copy()
+    bad[0, 0] = np.nan
+    assert domain(vol, nbr, outf, bad) == -1 and b"NaN" in L.bmc_last_error()
+    bad = cdf.copy()
+    bad[0, :] = bad[0, ::-1] * 0.5  # decreasing row
+    if net.K > 1 and bad[0, 0] > bad[0, 1]:
+        assert domain(vol, nbr, outf, bad) == -1 and b"non-decreasing" in L.bmc_last_error()
+    badn = nbr.copy()
+    badn[1, 0] = net.n_c
+    assert domain(vol, badn, outf, cdf) == -1 and b"out of range" in L.bmc_last_error()
+    badv = vol.copy()
+    badv[2] = 0.0
+    assert domain(badv, nbr, outf, cdf) == -1 and b"volumes" in L.bmc_last_error()
+    # feeds outside the domain
+    f = (_lib.Feed * 1)()
+    f[0].inlet = net.n_c
+    f[0].outlet = -1
+    f[0].flow = 1e-5
+    assert L.bmc_set_feeds(g.handle, 1, f) == -1
+    # more particles than the container holds
+    n = g.cap + 1
+    z = np.zeros(n)
+    assert L.bmc_set_particles(g.handle, n, np.zeros((2, n)).ctypes.data, np.zeros(n, np.uint32).ctypes.data,
+                               np.zeros(n, np.uint8).ctypes.data, np.zeros(n, np.float32).ctypes.data,
+                               np.zeros(n, np.float32).ctypes.data, np.zeros(n, np.uint32).ctypes.data,
+                               ct.c_uint64(n)) == -4
+    del z
+    # the scenario still steps after the refusals
+    st = g.step()
+    assert st["error"] == 0 and st["n_used"] > 0
