@@ -94,6 +94,8 @@ SIGNATURES = {
     "bmc_repartition_static": [VP, VP],
     "bmc_force_remove_dead": [VP],
     "bmc_batch_create": [VP, c_u32, VP],
+    "bmc_batch_create_slots": [c_u32, c_i32, c_i32, VP],
+    "bmc_batch_set_slot": [VP, c_u32, VP],
     "bmc_batch_destroy": [VP],
     "bmc_batch_run": [VP, c_dbl, c_u32],
     "bmc_batch_set_shape": [VP, c_u32, c_u32, c_u32],

@@ -2,14 +2,16 @@
 
 Requests arrive over time (each: a scenario and a number of steps).  The
 server admits them in arrival order while their device memory fits the HBM
-budget, keeps every admitted scenario's particle and liquid state resident
-on the device, and advances all admitted scenarios together, chunk after
-chunk, with one batched launch sequence per step (libbmc's batch API).  A
-scenario carries a step limit, so it stops exactly at its requested step
-count inside a chunk; finished scenarios are retired between chunks, which
-frees memory for waiting requests.  While a chunk runs on the GPU the host
-admits new requests (their initialisation uses their own streams), so
-admission overlaps device work.
+budget and a batch slot is free, keeps every admitted scenario's particle
+and liquid state resident on the device, and advances all admitted
+scenarios together, chunk after chunk, with one batched launch sequence per
+step (libbmc's slot batch: built once, its captured step replayed, empty
+slots skipped on the device).  A scenario carries a step limit, so it stops
+exactly at its requested step count inside a chunk; finished scenarios give
+their slot and memory back between chunks.  While a chunk runs on the GPU
+the host admits new requests (their initialisation uses their own streams)
+and they take their slots as soon as the chunk ends, so admission overlaps
+device work.
 
 Latency of a request = completion time - arrival time.
 """
@@ -74,13 +76,19 @@ def poisson_requests(rate: float, duration: float, seed: int = 5, steps_lo: int 
 
 
 class Server:
+    """Continuous batching over a fixed-slot batch (libbmc's
+    bmc_batch_create_slots): an admitted scenario takes a free slot, a
+    finished one gives it back; the batch and its captured step are built
+    once, empty slots cost nothing on the device."""
+
     def __init__(self, hbm_budget: float = 160e9, chunk_steps: int = 32, dt: float = 0.1,
-                 shape: tuple | None = None, max_chunk_ms: float = 60.0):
+                 shape: tuple | None = None, max_chunk_ms: float = 60.0, slots: int = 512):
         self.budget = hbm_budget
         self.chunk_steps = chunk_steps
         self.dt = dt
         self.shape = shape
         self.max_chunk_ms = max_chunk_ms
+        self.n_slots = slots
         self.used = 0
         self.log = []
 
@@ -93,31 +101,34 @@ class Server:
         t0 = clock()
         i = 0
         pending: deque = deque()
-        active: list = []  # [request, GpuScenario, bytes, step]
+        active: list = []  # [request, GpuScenario, bytes, steps done, slot]
+        joining: list = []  # admitted while a chunk ran: slot set after it
+        free = list(range(self.n_slots - 1, -1, -1))
         batch = None
-        dirty = False
         step_ms = 1.0
         busy = 0.0
         steps_done = 0.0
         running = False
-        chunk = self.chunk_steps
 
-        def admit(now):
-            nonlocal dirty
-            while pending:
+        def admit():
+            nonlocal batch
+            while pending and free:
                 r = pending[0]
                 need = scenario_bytes(r.scen)
                 if self.used + need > self.budget:
-                    if not active and not running:
+                    if not active and not joining and not running:
                         raise RuntimeError(f"request {r.rid} needs {need} B, more than the HBM budget")
                     break
                 pending.popleft()
                 g = GpuScenario(r.scen)
                 g.set_step_limit(r.steps)
                 r.admitted = clock() - t0
-                active.append([r, g, need, 0])
+                if batch is None:
+                    batch = GpuBatch.slots(self.n_slots, r.scen.model)
+                    if self.shape:
+                        batch.set_shape(*self.shape)
+                joining.append([r, g, need, 0, free.pop()])
                 self.used += need
-                dirty = True
 
         while True:
             now = clock() - t0
@@ -126,21 +137,17 @@ class Server:
             while i < len(reqs) and reqs[i].arrival <= now:
                 pending.append(reqs[i])
                 i += 1
-            if not running:
-                admit(now)
+            admit()
+            for a in joining:  # the batch is idle here: slots can change
+                batch.set_slot(a[4], a[1])
+                active.append(a)
+            joining.clear()
             if not active:
                 if i >= len(reqs) and not pending:
                     break
                 nxt = reqs[i].arrival if i < len(reqs) else now
                 sleep(max(0.0, min(0.01, nxt - now)))
                 continue
-            if dirty or batch is None:
-                if batch is not None:
-                    batch.close()
-                batch = GpuBatch([a[1] for a in active])
-                if self.shape:
-                    batch.set_shape(*self.shape)
-                dirty = False
             # chunk length: bounded wall time per chunk so arrivals are admitted promptly
             members = list(active)
             remaining = [a[0].steps - a[3] for a in members]
@@ -148,12 +155,13 @@ class Server:
             tc = clock()
             batch.run(chunk, self.dt)
             running = True
-            # admission overlaps the chunk on the GPU (new scenarios join the next batch)
+            # admission overlaps the chunk on the GPU (new scenarios take
+            # their slots once it is done)
             now = clock() - t0
             while i < len(reqs) and reqs[i].arrival <= now:
                 pending.append(reqs[i])
                 i += 1
-            admit(now)
+            admit()
             batch.synchronize()
             running = False
             el = clock() - tc
@@ -162,7 +170,7 @@ class Server:
             done_at = clock() - t0
             retired = set()
             for a in members:
-                r, g, need, st = a
+                r, g, need, st, slot = a
                 adv = min(chunk, r.steps - st)
                 a[3] = st + adv
                 steps_done += float(r.scen.n_particles) * adv
@@ -171,21 +179,24 @@ class Server:
                     r.result = g.stats()
                     if on_finish is not None:
                         on_finish(r, g)
+                    batch.set_slot(slot, None)
                     g.close()
                     self.used -= need
+                    free.append(slot)
                     retired.add(id(a))
-                    dirty = True
             active = [a for a in active if id(a) not in retired]
         wall = clock() - t0
+        for a in active + joining:
+            if batch is not None:
+                batch.set_slot(a[4], None)
+            a[1].close()
         if batch is not None:
             batch.close()
-        for a in active:
-            a[1].close()
         done = [r for r in reqs if r.finished is not None]
         lat = np.array([r.latency for r in done]) if done else np.array([np.nan])
         return {
             "requests": len(reqs), "completed": len(done), "wall_s": wall, "gpu_busy_s": busy,
             "particle_steps": steps_done, "particle_steps_per_s": steps_done / wall if wall > 0 else 0.0,
             "latency_p50_s": float(np.nanpercentile(lat, 50)), "latency_p99_s": float(np.nanpercentile(lat, 99)),
-            "latency_mean_s": float(np.nanmean(lat)),
+            "latency_mean_s": float(np.nanmean(lat)), "slots": self.n_slots,
         }

@@ -288,6 +288,19 @@ class GpuBatch:
         self.handle = ct.c_void_p()
         call("bmc_batch_create", arr, len(scenarios), ct.byref(self.handle))
 
+    @classmethod
+    def slots(cls, capacity: int, model) -> "GpuBatch":
+        """An empty batch of `capacity` slots for `model` (a ModelSpec)."""
+        b = cls.__new__(cls)
+        b.members = [None] * capacity
+        b.handle = ct.c_void_p()
+        call("bmc_batch_create_slots", capacity, model.model_id, 1 if model.f64 else 0, ct.byref(b.handle))
+        return b
+
+    def set_slot(self, slot: int, scenario: GpuScenario | None):
+        call("bmc_batch_set_slot", self.handle, slot, None if scenario is None else scenario.handle)
+        self.members[slot] = scenario
+
     def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
         call("bmc_batch_set_shape", self.handle, threads, ppt, blocks_per_sm)
 

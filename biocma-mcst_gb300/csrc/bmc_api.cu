@@ -199,6 +199,8 @@ struct bmc_scenario {
 
 struct bmc_batch {
   bool graph_maps = false;  // the captured graph includes the flow-map switch
+  int sm_count = 0;
+  Control* d_dummy_ctl = nullptr;  // control block of empty slots (a finished scenario)
   std::vector<bmc_scenario*> scen;
   const bmc::KernelSet* ks = nullptr;
   cudaStream_t stream = nullptr;
@@ -345,13 +347,13 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
 bool tiny_domain(const ScenDev& h) { return h.n_c <= bmc::kAggregateMaxCompartments; }
 bool batch_tiny(const bmc_batch* b) {
   for (const bmc_scenario* m : b->scen)
-    if (!tiny_domain(m->h)) return false;
+    if (m && !tiny_domain(m->h)) return false;
   return true;
 }
 
 bool batch_has_maps(const bmc_batch* b) {
   for (const bmc_scenario* m : b->scen)
-    if (m->h.n_maps > 0) return true;
+    if (m && m->h.n_maps > 0) return true;
   return false;
 }
 
@@ -362,23 +364,38 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
   const int n = (int)b->scen.size();
   bool table_changed = b->table.size() != (size_t)n;
   b->table.resize(n);
+  int lo = table_changed ? 0 : n, hi = table_changed ? n - 1 : -1;  // changed entries
   unsigned tiles = 0, max_nc = 0;
   size_t smem = 0;
   for (int i = 0; i < n; ++i) {
     bmc_scenario* s = b->scen[i];
-    int rc = set_dt(s, dt, false);
-    if (rc) return rc;
-    ScenDev d = s->h;
+    ScenDev d{};
+    if (s) {
+      int rc = set_dt(s, dt, false);
+      if (rc) return rc;
+      d = s->h;
+    } else {
+      // empty slot: a finished scenario without compartments or tiles that
+      // every kernel skips
+      d.ctl = b->d_dummy_ctl;
+      d.step_limit = 1u;
+    }
     d.tile_base = tiles;
     tiles += d.n_tiles;
     max_nc = std::max(max_nc, liquid_grid(d));
     smem = std::max(smem, cycle_smem(d));
-    if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) table_changed = true;
+    if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) {
+      table_changed = true;
+      lo = std::min(lo, i);
+      hi = std::max(hi, i);
+    }
     b->table[i] = d;
   }
   if (table_changed || b->dt != dt) {
     BMC_CUDA(cudaStreamSynchronize(b->stream));
-    BMC_CUDA(counted_memcpy_async(b->d_table, b->table.data(), sizeof(ScenDev) * n, cudaMemcpyHostToDevice, b->stream));
+    if (hi >= lo)  // only the entries that changed (slots filled or emptied)
+      BMC_CUDA(counted_memcpy_async(b->d_table + lo, b->table.data() + lo, sizeof(ScenDev) * (size_t)(hi - lo + 1),
+                                    cudaMemcpyHostToDevice, b->stream));
     BatchCtl bc{0u, tiles, 0u, 0u, b->d_live};
     BMC_CUDA(counted_memcpy_async(b->d_bctl, &bc, sizeof(bc), cudaMemcpyHostToDevice, b->stream));
     b->ks->move_thr(n, b->stream, b->d_table);
@@ -387,7 +404,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
     b->dt = dt;
     b->total_tiles = tiles;
   }
-  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->scen[0]->sm_count, grid_out);
+  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->sm_count, grid_out);
   if (rc) return rc;
   *n_out = n;
   *max_nc_out = max_nc;
@@ -1102,6 +1119,30 @@ int bmc_force_remove_dead(bmc_scenario* s) {
 
 // ---- batching ------------------------------------------------------------------
 
+// Stream, descriptor table, control blocks and live-tile prefix of a batch
+// of n slots; empty slots point at a control block of a finished scenario.
+static int batch_alloc(bmc_batch* b, uint32_t n) {
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(ScenDev) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_bctl, sizeof(BatchCtl));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_live, sizeof(unsigned) * (n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_dummy_ctl, sizeof(Control));
+  if (e == cudaSuccess) {
+    Control c{};
+    c.step = 1u;  // with step_limit 1: finished
+    e = cudaMemcpy(b->d_dummy_ctl, &c, sizeof(Control), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    if (b->d_table) cudaFree(b->d_table);
+    if (b->d_bctl) cudaFree(b->d_bctl);
+    if (b->d_live) cudaFree(b->d_live);
+    if (b->d_dummy_ctl) cudaFree(b->d_dummy_ctl);
+    if (b->stream) cudaStreamDestroy(b->stream);
+    return fail(BMC_E_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+  }
+  return BMC_OK;
+}
+
 int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out) {
   if (!scenarios || n == 0 || !out) return fail(BMC_E_INVALID, "empty batch");
   auto* b = new bmc_batch();
@@ -1119,17 +1160,51 @@ int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out
     }
     cudaStreamSynchronize(scenarios[i]->stream);
   }
-  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_table, sizeof(ScenDev) * n);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_bctl, sizeof(BatchCtl));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_live, sizeof(unsigned) * (n + 1));
-  if (e != cudaSuccess) {
-    if (b->d_table) cudaFree(b->d_table);
-    if (b->stream) cudaStreamDestroy(b->stream);
+  b->sm_count = scenarios[0]->sm_count;
+  int rc = batch_alloc(b, n);
+  if (rc) {
     delete b;
-    return fail(BMC_E_CUDA, std::string("batch set-up: ") + cudaGetErrorString(e));
+    return rc;
   }
   *out = b;
+  return BMC_OK;
+}
+
+int bmc_batch_create_slots(uint32_t capacity, int32_t model, int32_t f64, bmc_batch** out) {
+  if (capacity == 0 || !out) return fail(BMC_E_INVALID, "empty batch");
+  const bmc::KernelSet* ks = bmc::kernel_set(model, f64);
+  if (!ks) return fail(BMC_E_UNSUPPORTED, "model / precision not compiled in");
+  auto* b = new bmc_batch();
+  b->ks = ks;
+  b->scen.assign(capacity, nullptr);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    delete b;
+    return fail(BMC_E_CUDA, "cannot query the device");
+  }
+  int rc = batch_alloc(b, capacity);
+  if (rc) {
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return BMC_OK;
+}
+
+int bmc_batch_set_slot(bmc_batch* b, uint32_t slot, bmc_scenario* s) {
+  if (!b || slot >= b->scen.size()) return fail(BMC_E_INVALID, "no such slot");
+  if (s) {
+    if (s->ks != b->ks) return fail(BMC_E_INVALID, "all scenarios of a batch must share model and precision");
+    for (size_t i = 0; i < b->scen.size(); ++i)
+      if (b->scen[i] == s && i != slot) return fail(BMC_E_INVALID, "scenario already holds another slot");
+    int rc = check_ready(s, true);
+    if (rc) return rc;
+    BMC_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  // the slot's previous scenario may still be in use by queued steps
+  BMC_CUDA(cudaStreamSynchronize(b->stream));
+  b->scen[slot] = s;
   return BMC_OK;
 }
 
@@ -1140,6 +1215,7 @@ int bmc_batch_destroy(bmc_batch* b) {
   cudaFree(b->d_table);
   cudaFree(b->d_bctl);
   cudaFree(b->d_live);
+  if (b->d_dummy_ctl) cudaFree(b->d_dummy_ctl);
   cudaStreamDestroy(b->stream);
   delete b;
   return BMC_OK;
@@ -1182,7 +1258,8 @@ int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t b
 
 int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   if (b)
-    for (bmc_scenario* m : b->scen) m->ctl_fresh = false;
+    for (bmc_scenario* m : b->scen)
+      if (m) m->ctl_fresh = false;
   int n = 0;
   unsigned max_nc = 0, grid = 0;
   size_t smem = 0;
@@ -1195,7 +1272,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
     rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->variant, grid, smem,
-                      b->scen[0]->sm_count, batch_has_maps(b), batch_tiny(b));
+                      b->sm_count, batch_has_maps(b), batch_tiny(b));
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -1539,13 +1616,14 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
 
 int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   if (b)
-    for (bmc_scenario* m : b->scen) m->ctl_fresh = false;
+    for (bmc_scenario* m : b->scen)
+      if (m) m->ctl_fresh = false;
   int n = 0;
   unsigned max_nc = 0, grid = 0;
   size_t smem = 0;
   int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
-  const int sm = b->scen[0]->sm_count;
+  const int sm = b->sm_count;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = b->stream;

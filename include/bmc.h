@@ -304,6 +304,13 @@ int bmc_gas_read(bmc_scenario* s, double* conc, double* mass, double* transfer);
 /* All scenarios of a batch share model and precision; each keeps its own
  * domain, liquid state, parameters, seed and step counter. */
 int bmc_batch_create(bmc_scenario* const* scenarios, uint32_t n, bmc_batch** out);
+/* A batch of `capacity` slots for one model and precision, all empty; a
+ * serving loop fills and empties slots (bmc_batch_set_slot, NULL empties)
+ * between runs without rebuilding the batch or its captured step: empty
+ * slots are skipped by every kernel.  Setting a slot waits for the batch's
+ * queued steps and for the scenario's own stream. */
+int bmc_batch_create_slots(uint32_t capacity, int32_t model, int32_t f64, bmc_batch** out);
+int bmc_batch_set_slot(bmc_batch* b, uint32_t slot, bmc_scenario* s);
 int bmc_batch_destroy(bmc_batch* b);
 /* Advance every scenario of the batch by n_steps (captured graph). */
 int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps);

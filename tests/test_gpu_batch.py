@@ -90,3 +90,34 @@ def test_batch_then_alone_continues_consistently():
     ref.run(9)
     assert_same(mixed[2], ref, "regrouped")
     b2.close()
+
+
+def test_slot_batch_fill_empty_refill_equals_alone():
+    """Scenarios entering and leaving slots between runs advance exactly as
+    they would alone, and empty slots do nothing."""
+    from bmc.sim import GpuBatch, GpuScenario
+
+    scens = _mix(6, 0.02)
+    members = [GpuScenario(s) for s in scens]
+    alone = [GpuScenario(s) for s in scens]
+    b = GpuBatch.slots(8, scens[0].model)
+    for k in range(4):
+        b.set_slot(2 * k, members[k])  # slots 0, 2, 4, 6; 1, 3, 5, 7 empty
+    b.run(5, 0.1)
+    b.synchronize()
+    b.set_slot(2, None)  # members[1] leaves after 5 steps
+    b.set_slot(3, members[4])  # members[4] joins
+    b.run(4, 0.1)
+    b.synchronize()
+    b.set_slot(7, members[5])
+    b.run(3, 0.1)
+    b.synchronize()
+    steps = [12, 5, 12, 12, 7, 3]
+    for g, n in zip(alone, steps):
+        g.run(n)
+    for k, (gm, ga) in enumerate(zip(members, alone)):
+        assert gm.stats()["step"] == steps[k]
+        assert_same(gm, ga, f"scenario {k}")
+    for slot in (0, 3, 4, 6, 7):
+        b.set_slot(slot, None)
+    b.close()

@@ -49,15 +49,24 @@ def make_fakes(world, budget_probe):
             world.live.discard(self)
 
     class FakeBatch:
-        def __init__(self, members):
-            self.members = list(members)
-            world.batches.append(len(self.members))
+        def __init__(self, capacity):
+            self.members = [None] * capacity
+
+        @classmethod
+        def slots(cls, capacity, model):
+            return cls(capacity)
+
+        def set_slot(self, slot, g):
+            assert (g is None) != (self.members[slot] is None)  # fill an empty slot or empty a full one
+            self.members[slot] = g
 
         def set_shape(self, *a):
             pass
 
         def run(self, n, dt):
-            for m in self.members:
+            live = [m for m in self.members if m is not None]
+            world.batches.append(len(live))
+            for m in live:
                 m.steps = min(m.limit, m.steps + n)
             world.clock.t += n * world.step_cost
 
@@ -65,7 +74,7 @@ def make_fakes(world, budget_probe):
             pass
 
         def close(self):
-            pass
+            assert all(m is None for m in self.members)
 
     return FakeScenario, FakeBatch
 
@@ -141,3 +150,16 @@ def test_arrivals_after_start_are_admitted_while_running(monkeypatch):
     # a request admitted before the previous one finished shared its launches
     overlapped = sum(1 for a, b in zip(reqs, reqs[1:]) if b.admitted < a.finished)
     assert overlapped >= 1
+
+
+def test_slots_bound_the_batch(monkeypatch):
+    clock = FakeClock()
+    world = World(clock)
+    FS, FB = make_fakes(world, lambda: None)
+    monkeypatch.setattr(serve, "GpuScenario", FS)
+    monkeypatch.setattr(serve, "GpuBatch", FB)
+    reqs = requests(7, (40, 80))
+    out = serve.Server(hbm_budget=1e12, chunk_steps=16, slots=2).serve(reqs, clock=clock, sleep=clock.sleep)
+    assert out["completed"] == 7 and out["slots"] == 2
+    assert max(world.batches) <= 2
+    assert not world.live
