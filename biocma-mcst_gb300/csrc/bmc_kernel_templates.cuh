@@ -579,21 +579,31 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // ---------------------------------------------------------------------------
 // k_cycle_tma: the same per-particle work as k_cycle, with the particle
 // arrays of each 1024-slot tile staged in shared memory by the copy engine.
-// A producer warp (one thread) issues bulk copies (cp.async.bulk, completion
-// on a "full" mbarrier per stage) of the tile's read state variables,
-// compartments, ids, ages and statuses, STAGES tiles ahead; THREADS
-// consumer threads wait on the stage, process slots r*THREADS + tid from
-// shared memory, write results straight to global memory (streaming
+// A producer warp (one thread) takes live tiles: half of them as an even
+// contiguous share per block, the rest from a global ticket by guided
+// self-scheduling (half of an even share of what is left per grab, taken
+// one run ahead: long runs of one scenario first, single tiles at the end,
+// so uneven scenarios of a batch finish together), and issues bulk copies
+// (cp.async.bulk, completion on a "full" mbarrier per stage) of the tile's
+// read state variables, compartments, ids, ages and statuses, STAGES tiles
+// ahead, with the tile's scenario and extent in the stage's meta record.
+// THREADS consumer threads wait on the stage, process slots r*THREADS + tid
+// from shared memory, write results straight to global memory (streaming
 // stores), and release the stage on its "empty" mbarrier.  The loads in
 // flight no longer live in registers, so the memory pipeline stays full at
-// any occupancy.  Tiles map to scenarios exactly as in k_cycle (static
-// contiguous partition of the live tiles).  Every consumer derives the
-// tile -> scenario map itself, so all consumers run the same sequence of
-// flushes and barriers even if a wait gives up (BMC_ERR_TIMEOUT): then
-// processing stops, the producer issues nothing more and drains its
-// copies in flight.
+// any occupancy.  Every wait is bounded; consumers vote after each wait, so
+// if one gives up (BMC_ERR_TIMEOUT) all stop at the same point with their
+// barriers matched, the producer issues nothing more and drains its copies
+// in flight.
 
 __host__ __device__ constexpr unsigned popcount_c(unsigned v) { return v == 0u ? 0u : (v & 1u) + popcount_c(v >> 1); }
+
+// Tile held by a stage of k_cycle_tma (s < 0: no tile left).
+struct TileMeta {
+  int s;
+  unsigned n_in;
+  unsigned long long base;
+};
 
 // Fields of the scenario a k_cycle_tma block is working on.
 template <class F>
@@ -642,9 +652,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
   const int tid = threadIdx.x;
   const unsigned total = bctl->total_live;
   const unsigned* live_base = bctl->live_base;
-  const unsigned g_begin = (unsigned)(((unsigned long long)total * blockIdx.x) / gridDim.x);
-  const unsigned g_end = (unsigned)(((unsigned long long)total * (blockIdx.x + 1)) / gridDim.x);
-  const unsigned n_tiles = g_end - g_begin;
+  __shared__ TileMeta s_meta[STAGES];  // tile of each stage, written by the producer
   if (tid == 0) {
     for (int k = 0; k < STAGES; ++k) {
       mbar_init(&s_full[k], 1u);
@@ -654,7 +662,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     fence_barrier_init();
   }
   __syncthreads();
-  if (n_tiles == 0) return;
+  if (total == 0) return;
 
   if (tid >= THREADS) {
     // ---- producer -------------------------------------------------------
@@ -662,7 +670,24 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     int hint = -1;
     unsigned issued = 0;
     bool ok = true;
-    for (unsigned k = 0; k < n_tiles; ++k) {
+    // first half of the tiles: an even contiguous share per block, taken
+    // without atomics; the rest from the ticket by guided self-scheduling
+    const unsigned c0 = (total >> 1) / gridDim.x;
+    const unsigned s0 = c0 * gridDim.x;
+    unsigned next = c0 * blockIdx.x, end = next + c0;  // tiles of the current run
+    unsigned pn = 0, pe = 0;                           // run taken ahead
+    bool ahead = false;
+    auto grab = [&]() {
+      // half of an even share of what is left: long runs while much is
+      // left, single tiles at the end
+      const unsigned seen = s0 + atomicAdd(&bctl->ticket, 0u);
+      const unsigned left = seen < total ? total - seen : 0u;
+      const unsigned c = max(1u, left / (2u * gridDim.x));
+      pn = s0 + atomicAdd(&bctl->ticket, c);
+      pe = min(pn + c, total);
+      ahead = true;
+    };
+    for (unsigned k = 0;; ++k) {
       const unsigned stg = k % STAGES, use = k / STAGES;
       if (use > 0 && !mbar_wait_bounded(&s_empty[stg], (use - 1u) & 1u, &s_abort)) {
         ok = false;
@@ -672,13 +697,31 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         ok = false;
         break;
       }
-      const unsigned g = g_begin + k;
+      if (next >= end) {
+        if (!ahead) grab();
+        next = pn;
+        end = pe;
+        ahead = false;
+        hint = -1;
+      }
+      TileMeta& m = s_meta[stg];
+      if (next >= total) {
+        // no tile left: the stage completes without bytes and says so
+        m.s = -1;
+        mbar_arrive(&s_full[stg]);
+        issued = k;
+        break;
+      }
+      const unsigned g = next++;
       const int s = scen_of_live(live_base, n_scen, g, hint);
       hint = s;
       const ScenDev& S = sc[s];
       const unsigned long long base = (unsigned long long)(g - __ldg(live_base + s)) * kTile;
       const unsigned long long n_used = S.ctl->n_used;
       const unsigned n_in = (unsigned)(n_used - base < kTile ? n_used - base : kTile);
+      m.s = s;
+      m.n_in = n_in;
+      m.base = base;
       // whole 16-slot groups: every copy is a multiple of 16 bytes and stays
       // inside the tile (capacity is a whole number of tiles)
       const unsigned n16 = (n_in + 15u) & ~15u;
@@ -699,6 +742,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       if (with_ah) bulk_g2s(buf + TS::off_ah, S.age_h + base, n16 * 4u, &s_full[stg]);
       bulk_g2s(buf + TS::off_st, S.status + base, n16, &s_full[stg]);
       issued = k + 1;
+      // take the next run while this tile's copies land
+      if (next >= end && !ahead) grab();
     }
     if (!ok) {
       s_abort = 1u;
@@ -764,18 +809,26 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
   // fields of the current scenario, kept in shared memory (written by
   // thread 0 when the scenario changes) rather than in registers
   __shared__ CycleScen<F> sr;
-  unsigned long long n_used = 0;
-  int hint = -1;
-
-  for (unsigned k = 0; k < n_tiles; ++k) {
+  for (unsigned k = 0;; ++k) {
     const unsigned stg = k % STAGES, use = k / STAGES;
-    const unsigned g = g_begin + k;
-    const int s = scen_of_live(live_base, n_scen, g, hint);
-    hint = s;
+    // every consumer agrees whether the stage arrived: if one wait gives up,
+    // all stop here together, so their barriers stay matched
+    const bool ok = mbar_wait_bounded(&s_full[stg], use & 1u, &s_abort);
+    if (consumer_any(!ok, THREADS)) {
+      aborted = true;
+      my_err |= 16u;
+      if (tid == 0) {
+        s_abort = 1u;
+        if (cur < 0) atomicOr(&sc[0].ctl->error, 16u);
+      }
+      break;
+    }
+    const TileMeta m = s_meta[stg];
+    if (m.s < 0) break;  // no tile left
+    const int s = m.s;
     const ScenDev& S = sc[s];
-    const unsigned long long base = (unsigned long long)(g - __ldg(live_base + s)) * kTile;
-    if (s != cur) n_used = S.ctl->n_used;
-    const unsigned n_in = (unsigned)(n_used - base < kTile ? n_used - base : kTile);
+    const unsigned long long base = m.base;
+    const unsigned n_in = m.n_in;
     if (s != cur || since_flush + n_in > kFlushParticles) {
       if (cur >= 0) flush();
       const unsigned n_ent = S.n_c * NA;
@@ -800,11 +853,6 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
       consumer_sync(THREADS);
     }
     since_flush += n_in;
-    if (!aborted && !mbar_wait_bounded(&s_full[stg], use & 1u, &s_abort)) {
-      aborted = true;
-      s_abort = 1u;
-      my_err |= 16u;
-    }
     const unsigned char* buf = stages + stg * TS::bytes;
     const F* bx = reinterpret_cast<const F*>(buf + TS::off_x);
     const uint32_t* bpos = reinterpret_cast<const uint32_t*>(buf + TS::off_pos);

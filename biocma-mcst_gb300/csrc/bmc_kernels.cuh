@@ -22,7 +22,7 @@ constexpr int kTile = 1024;  // particles per tile (scheduling and scan unit)
 
 // Batch-wide scheduling state (device memory).
 struct BatchCtl {
-  unsigned int ticket;      // unused (tiles are partitioned statically)
+  unsigned int ticket;      // next live tile to hand out (tile-staging cycle kernel)
   unsigned int total_tiles; // allocated tiles over all scenarios
   unsigned int flags;       // work of this step after the cycle (kFlag*)
   unsigned int total_live;  // tiles holding particles this step, all scenarios
@@ -291,6 +291,16 @@ __device__ __forceinline__ unsigned dynamic_smem_bytes() {
 }
 __device__ __forceinline__ void consumer_sync(unsigned n_threads) {
   asm volatile("bar.sync 1, %0;" ::"r"(n_threads) : "memory");
+}
+// Block-level OR of v over the n_threads threads using named barrier 1.
+__device__ __forceinline__ bool consumer_any(bool v, unsigned n_threads) {
+  unsigned r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.or.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(r)
+      : "r"((unsigned)v), "r"(n_threads)
+      : "memory");
+  return r != 0u;
 }
 
 // ------------------------------------------------------------------------
