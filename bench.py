@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--batched-only", type=float, default=None, metavar="SCALE",
                     help="run only the batched form, particle counts scaled by SCALE, without the "
                          "plain-path comparisons (with --shape: no autotuner); for profiling")
+    ap.add_argument("--served-only", action="store_true",
+                    help="run only the served form (Poisson arrivals over --serve-window seconds)")
     return ap.parse_args()
 
 
@@ -525,6 +527,9 @@ def main():
         shape = tuple(int(v) for v in args.shape.split(",")) if args.shape else None
         print(json.dumps(batched_form(args.forms_steps, scale=args.batched_only, shape=shape,
                                       compare_plain=False)))
+        return
+    if args.served_only:
+        print(json.dumps(served_form(args.serve_window)))
         return
     if args.impl == "reference":
         run_reference(args)

@@ -173,13 +173,13 @@ struct bmc_scenario {
   std::vector<bmc_feed> feeds;
   double dt = -1.0;
   // launch shape of the cycle kernel
-  unsigned variant = 0, blocks_per_sm = 0;  // cycle launch variant (bmc_launch.h)
+  unsigned variant = bmc::kVariantAuto, blocks_per_sm = 0;  // requested cycle launch variant (bmc_launch.h)
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
-  unsigned graph_grid = 0;
+  unsigned graph_grid = 0, graph_variant = 0;
   bool ctl_fresh = false;  // h_ctl mirrors the device control block (no work enqueued since)
   // last cycle-launch sizing (prepare_cycle), reused while its inputs stay
-  unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u;
+  unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u, prep_run = 0u;
   size_t prep_in = 0, prep_out = 0;
   // flow-map cycle (host copies; device copies in marena)
   struct FlowMap {
@@ -209,10 +209,11 @@ struct bmc_batch {
   unsigned* d_live = nullptr;  // [n + 1] live-tile prefix
   std::vector<ScenDev> table;
   unsigned total_tiles = 0;
-  unsigned variant = 0, blocks_per_sm = 0;  // cycle launch variant (bmc_launch.h)
+  unsigned variant = bmc::kVariantAuto, blocks_per_sm = 0;  // requested cycle launch variant (bmc_launch.h)
   cudaGraphExec_t graph = nullptr;
   size_t graph_smem = 0;
-  unsigned graph_grid = 0;
+  unsigned graph_grid = 0, graph_variant = 0;
+  unsigned run_variant = 0;  // variant of the last prepared launch
   double dt = -1.0;
 };
 
@@ -302,8 +303,8 @@ size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(un
 
 // *smem: in, the accumulator bytes; out, the dynamic shared memory of the
 // launch (staged variants append their tile buffers, 128-byte aligned).
-int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t* smem, int sm_count,
-                  unsigned* grid_out) {
+static int size_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t* smem, int sm_count,
+                      unsigned* grid_out, int* fit_out) {
   if (ks->cycle_extra_smem[variant] > 0) *smem = align_up(*smem, 128) + ks->cycle_extra_smem[variant];
   if (*smem > 227 * 1024)
     return fail(BMC_E_UNSUPPORTED, "shared accumulator (n_compartments * n_contributions) and tile buffers "
@@ -311,8 +312,32 @@ int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, 
   int bps = 0;
   BMC_CUDA((cudaError_t)ks->cycle_setup[variant](*smem, &bps));
   if (bps < 1) return fail(BMC_E_UNSUPPORTED, "cycle kernel cannot be resident with this shape");
+  *fit_out = bps;
   if (bps_req > 0) bps = std::min<int>(bps, (int)bps_req);
   *grid_out = (unsigned)(sm_count * bps);
+  return BMC_OK;
+}
+
+// Dynamic shared memory and grid of the cycle launch for the requested
+// variant; resolves kVariantAuto (*run_out: the variant to launch).
+int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t* smem, int sm_count,
+                  unsigned* grid_out, unsigned* run_out) {
+  int fit = 0;
+  if (variant == bmc::kVariantAuto) {
+    size_t m = *smem;
+    unsigned g = 0;
+    if (size_cycle(ks, bmc::kAutoStaged, bps_req, &m, sm_count, &g, &fit) == BMC_OK && fit >= 2) {
+      *smem = m;
+      *grid_out = g;
+      *run_out = bmc::kAutoStaged;
+      return BMC_OK;
+    }
+    (void)cudaGetLastError();  // a refused size is not an error of the step
+    variant = bmc::kAutoStreamed;
+  }
+  int rc = size_cycle(ks, variant, bps_req, smem, sm_count, grid_out, &fit);
+  if (rc) return rc;
+  *run_out = variant;
   return BMC_OK;
 }
 
@@ -404,7 +429,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
     b->dt = dt;
     b->total_tiles = tiles;
   }
-  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->sm_count, grid_out);
+  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->sm_count, grid_out, &b->run_variant);
   if (rc) return rc;
   *n_out = n;
   *max_nc_out = max_nc;
@@ -840,14 +865,14 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
   return write_ctl_fresh(s, n, next_id, inactive);
 }
 
-static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
-  if (s->graph && s->graph_smem == smem && s->graph_grid == grid) return BMC_OK;
+static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned variant) {
+  if (s->graph && s->graph_smem == smem && s->graph_grid == grid && s->graph_variant == variant) return BMC_OK;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
   cudaGraph_t g = nullptr;
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
-  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, s->variant, grid, smem,
+  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, variant, grid, smem,
                         s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
@@ -861,21 +886,24 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem) {
   if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
   s->graph_smem = smem;
   s->graph_grid = grid;
+  s->graph_variant = variant;
   return BMC_OK;
 }
 
 // prepare_cycle for a scenario, reusing the last answer while the launch
 // shape and the accumulator size are unchanged (no attribute or occupancy
 // query per step).
-static int scenario_prepare(bmc_scenario* s, size_t* smem, unsigned* grid) {
+static int scenario_prepare(bmc_scenario* s, size_t* smem, unsigned* grid, unsigned* variant) {
   if (s->prep_variant == s->variant && s->prep_bps == s->blocks_per_sm && s->prep_in == *smem) {
     *smem = s->prep_out;
     *grid = s->prep_grid;
+    *variant = s->prep_run;
     return BMC_OK;
   }
   const size_t in = *smem;
-  int rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, grid);
+  int rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, grid, variant);
   if (rc) return rc;
+  s->prep_run = *variant;
   s->prep_variant = s->variant;
   s->prep_bps = s->blocks_per_sm;
   s->prep_in = in;
@@ -891,11 +919,11 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   if (rc) return rc;
   s->ctl_fresh = false;
   size_t smem = cycle_smem(s->h);
-  unsigned grid = 0;
-  rc = scenario_prepare(s, &smem, &grid);
+  unsigned grid = 0, variant = 0;
+  rc = scenario_prepare(s, &smem, &grid, &variant);
   if (rc) return rc;
   if (use_graph && do_scalar) {
-    rc = ensure_graph(s, grid, smem);
+    rc = ensure_graph(s, grid, smem, variant);
     if (rc) return rc;
     for (uint32_t k = 0; k < n_steps; ++k) {
       BMC_CUDA(cudaGraphLaunch(s->graph, s->stream));
@@ -904,7 +932,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
     return BMC_OK;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
-    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, s->variant, grid, smem,
+    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, variant, grid, smem,
                       s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
     if (rc) return rc;
   }
@@ -1232,11 +1260,14 @@ int bmc_set_step_limit(bmc_scenario* s, uint32_t step_limit) {
 
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!s) return fail(BMC_E_INVALID, "null scenario");
-  const unsigned th = threads ? threads : bmc::kVariantThreads[s->variant];
-  const unsigned pp = ppt ? ppt : bmc::kVariantPPT[s->variant];
-  const int v = variant_of(th, pp);
-  if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
-  s->variant = (unsigned)v;
+  if (threads || ppt) {  // 0 and 0 keep the current variant (the automatic one included)
+    const unsigned cur = s->variant == bmc::kVariantAuto ? bmc::kAutoStaged : s->variant;
+    const unsigned th = threads ? threads : bmc::kVariantThreads[cur];
+    const unsigned pp = ppt ? ppt : bmc::kVariantPPT[cur];
+    const int v = variant_of(th, pp);
+    if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
+    s->variant = (unsigned)v;
+  }
   s->blocks_per_sm = blocks_per_sm;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
@@ -1245,11 +1276,14 @@ int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t bloc
 
 int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
   if (!b) return fail(BMC_E_INVALID, "null batch");
-  const unsigned th = threads ? threads : bmc::kVariantThreads[b->variant];
-  const unsigned pp = ppt ? ppt : bmc::kVariantPPT[b->variant];
-  const int v = variant_of(th, pp);
-  if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
-  b->variant = (unsigned)v;
+  if (threads || ppt) {  // 0 and 0 keep the current variant (the automatic one included)
+    const unsigned cur = b->variant == bmc::kVariantAuto ? bmc::kAutoStaged : b->variant;
+    const unsigned th = threads ? threads : bmc::kVariantThreads[cur];
+    const unsigned pp = ppt ? ppt : bmc::kVariantPPT[cur];
+    const int v = variant_of(th, pp);
+    if (v < 0) return fail(BMC_E_INVALID, "no compiled cycle variant with this threads x ppt");
+    b->variant = (unsigned)v;
+  }
   b->blocks_per_sm = blocks_per_sm;
   if (b->graph) cudaGraphExecDestroy(b->graph);
   b->graph = nullptr;
@@ -1265,13 +1299,14 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   size_t smem = 0;
   int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
-  if (!b->graph || b->graph_smem != smem || b->graph_grid != grid || b->graph_maps != batch_has_maps(b)) {
+  if (!b->graph || b->graph_smem != smem || b->graph_grid != grid || b->graph_variant != b->run_variant ||
+      b->graph_maps != batch_has_maps(b)) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
-    rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->variant, grid, smem,
+    rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->run_variant, grid, smem,
                       b->sm_count, batch_has_maps(b), batch_tiny(b));
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
@@ -1285,6 +1320,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     b->graph_smem = smem;
     b->graph_grid = grid;
+    b->graph_variant = b->run_variant;
     b->graph_maps = batch_has_maps(b);
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
@@ -1581,13 +1617,12 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   rc = set_dt(s, dt, true);
   if (rc) return rc;
   size_t smem = cycle_smem(s->h);
-  unsigned grid = 0;
-  rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, &smem, s->sm_count, &grid);
+  unsigned grid = 0, variant = 0;
+  rc = scenario_prepare(s, &smem, &grid, &variant);
   if (rc) return rc;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = s->stream;
-  const unsigned variant = s->variant;
   if (s->h.n_maps > 0) {
     s->ks->flowmap(1, st, s->d_desc);
     g_launches++;
@@ -1627,7 +1662,7 @@ int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
   cudaStream_t st = b->stream;
-  const unsigned variant = b->variant;
+  const unsigned variant = b->run_variant;
   if (batch_has_maps(b)) {
     b->ks->flowmap(n, st, b->d_table);
     g_launches++;

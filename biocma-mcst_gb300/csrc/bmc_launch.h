@@ -39,6 +39,11 @@ using CycleSetup = int (*)(size_t smem, int* blocks_per_sm);
 constexpr int kCycleVariants = 7;
 constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024, 288, 544};
 constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1, 4, 2};
+// Launch shape a scenario or batch starts with: resolved per launch to the
+// tile-staging 544 x 2 shape when two of its blocks fit on an SM (shared
+// accumulator plus stage buffers), else to register streaming 256 x 2.
+constexpr unsigned kVariantAuto = kCycleVariants;
+constexpr unsigned kAutoStaged = 6, kAutoStreamed = 1;
 using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*);
 
 struct KernelSet {

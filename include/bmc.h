@@ -208,9 +208,14 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
  * CUDA graph replayed).  Statistics are those of the last step. */
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats);
 
-/* Launch shape of the scenario's cycle kernel: threads per block (multiple
- * of 32, <= 256), particles per thread (1, 2, 4), resident blocks per SM
- * (0 = as many as fit); 0 keeps the current value. */
+/* Launch shape of the scenario's cycle kernel: threads per block and
+ * particles per thread of a compiled variant (256 x 1, 256 x 2, 256 x 4,
+ * 512 x 2, 1024 x 1 stream particles through registers; 288 x 4 and 544 x 2
+ * are 256 or 512 consumer threads plus a producer warp staging tiles through
+ * the copy engine), resident blocks per SM (0 = as many as fit); threads and
+ * ppt both 0 keep the current variant.  A new scenario starts in the
+ * automatic shape: 544 x 2 when two of its blocks fit on an SM (shared
+ * accumulator plus stage buffers), else 256 x 2. */
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 
 /* Step budget: once the scenario's step counter reaches step_limit its
@@ -314,8 +319,8 @@ int bmc_batch_set_slot(bmc_batch* b, uint32_t slot, bmc_scenario* s);
 int bmc_batch_destroy(bmc_batch* b);
 /* Advance every scenario of the batch by n_steps (captured graph). */
 int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps);
-/* Kernel shape (threads per block, particles per thread, blocks per SM); 0
- * keeps the default.  Used by the autotuner. */
+/* Kernel shape of the batch, as bmc_set_shape (a new batch starts in the
+ * automatic shape).  Used by the autotuner. */
 int bmc_batch_set_shape(bmc_batch* b, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 int bmc_batch_synchronize(bmc_batch* b);
 

@@ -51,7 +51,7 @@ def test_container_that_empties(oracle_mod):
     assert st["n_used"] - st["inactive"] == 0
 
 
-@pytest.mark.parametrize("shape", [None, (544, 2, 0)])
+@pytest.mark.parametrize("shape", [None, (256, 2, 0)])
 @pytest.mark.parametrize("n", [1, 31, 1023, 1025, 2047])
 def test_ragged_particle_counts(oracle_mod, n, shape):
     from test_gpu_parity import make_pair
@@ -77,7 +77,7 @@ def complete_graph(n_c=13, seed=5):
     return networks.Network(n_c, vol, src, dst, flow).finalize()
 
 
-@pytest.mark.parametrize("shape", [None, (544, 2, 0)])
+@pytest.mark.parametrize("shape", [None, (256, 2, 0)])
 def test_long_neighbour_rows(oracle_mod, shape):
     """Every compartment connected to all others: rows of 12 entries."""
     from test_gpu_parity import make_pair
@@ -92,6 +92,21 @@ def test_long_neighbour_rows(oracle_mod, shape):
     if shape:
         g.set_shape(*shape)
     _parity(g, o, 6, "K=12")
+
+
+def test_automatic_shape_on_a_domain_too_large_for_tile_staging(oracle_mod):
+    """10,648 compartments: the shared accumulator and two blocks of stage
+    buffers do not fit on an SM, so the automatic shape streams particles
+    through registers instead; results stay those of the CPU restatement."""
+    from test_gpu_parity import make_pair
+
+    net = networks.lattice_vortex(22, side=1.0, peak_velocity=0.5, noise=0.1, seed=7, max_courant=0.4, dt=0.05)
+    sc = scenarios.workload(2, n_particles=60000, f64=True)
+    sc.net = net
+    sc.c0 = np.tile(sc.c0[:1], (net.n_c, 1))
+    sc.feeds[0].outlet = net.n_c - 1
+    g, o = make_pair(oracle_mod, sc)
+    _parity(g, o, 3, "n_c=10648")
 
 
 def test_particle_id_space_exhaustion():

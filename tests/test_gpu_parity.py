@@ -19,7 +19,9 @@ def make_pair(oracle_mod, scen, capacity=None):
     g = GpuScenario(scen, capacity=capacity)
     o = oracle_mod.Oracle(scen, phys_capacity=g.cap)
     w = o.init_particles()
-    assert abs(w - g.weight) <= 1e-14 * g.weight
+    # the initial mass and volume totals are summed in different orders
+    # (tree reduction on the device); the oracle then takes the device weight
+    assert abs(w - g.weight) <= 1e-12 * g.weight
     o.set_weight(g.weight)
     return g, o
 
@@ -114,7 +116,7 @@ def test_cycle_only_uses_given_concentrations(oracle_mod):
 
 
 # default launch shape, and the shape that stages tiles through the copy engine
-SHAPES = [None, (288, 4, 0)]
+SHAPES = [None, (288, 4, 0), (256, 2, 0)]
 
 
 def test_cycle_external_host_and_device_pointers(oracle_mod):
