@@ -113,6 +113,10 @@ SIGNATURES = {
     "bmc_gas_set_concentrations": [VP, VP],
     "bmc_gas_set_feeds": [VP, c_u32, VP],
     "bmc_gas_read": [VP, VP, VP, VP],
+    "bmc_cma_derive": [c_u32, c_u64, VP, VP, VP, VP, c_u32, VP, VP, VP],
+    "bmc_cma_transition": [c_u32, c_u64, VP, VP, VP, VP, c_u64, VP, VP, VP],
+    "bmc_cma_time_step": [c_dbl, c_u32, c_u32, VP, VP, VP],
+    "bmc_cma_read_field": [ct.c_char_p, c_u64, VP, VP],
     "bmc_flowmap_add": [VP, VP, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_flowmap_period": [VP, c_dbl],
     "bmc_flowmap_clear": [VP],

@@ -1,7 +1,7 @@
 """Build libbmc.so in-tree with nvcc for sm_103a (no CMake).
 
 The translation units (one per built-in model, the model-independent kernels,
-the C-ABI) compile in parallel, then link into
+the C-ABI, the host-only CMA ingestion) compile in parallel, then link into
 ``biocma-mcst_gb300/lib/libbmc.so``.  ``--fmad=false`` keeps every multiply
 and add separately rounded, which the bit-exact comparison with the CPU
 restatement relies on.
@@ -18,7 +18,8 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libbmc.so")
-SOURCES = ["bmc_sets_monod.cu", "bmc_sets_overflow.cu", "bmc_sets_fixed.cu", "bmc_kernels.cu", "bmc_api.cu"]
+SOURCES = ["bmc_sets_monod.cu", "bmc_sets_overflow.cu", "bmc_sets_fixed.cu", "bmc_kernels.cu", "bmc_api.cu",
+           "bmc_cma.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off"]
@@ -47,7 +48,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     nv = nvcc()
 
     def compile_one(src):
-        obj = os.path.join(LIBDIR, "obj", src.replace(".cu", ".o"))
+        obj = os.path.join(LIBDIR, "obj", os.path.splitext(src)[0] + ".o")
         cmd = [nv, *ARCH, *FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

@@ -65,7 +65,8 @@ class Network:
                 continue
             d = dst[start:start + c]
             f = flow[start:start + c]
-            acc = np.cumsum(f) / f.sum()
+            run = np.cumsum(f)  # sequential: its last value is the out-flow
+            acc = run / run[-1]
             neighbors[i, :c] = d
             neighbors[i, c:] = d[-1]
             cdf[i, :c] = acc

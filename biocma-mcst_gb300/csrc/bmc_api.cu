@@ -155,6 +155,11 @@ cudaError_t launch_status(const bmc::KernelSet* ks) {
 
 }  // namespace
 
+namespace bmc {
+// Error reporting for the other host translation units of the C-ABI.
+int api_fail(int code, const std::string& msg) { return fail(code, msg); }
+}  // namespace bmc
+
 struct bmc_scenario {
   bmc_scenario_desc desc{};
   const bmc::KernelSet* ks = nullptr;

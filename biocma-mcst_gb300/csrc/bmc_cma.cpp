@@ -1,0 +1,185 @@
+// bmc_cma.cpp -- CMA ingestion on the host (declared in include/bmc.h):
+// the per-compartment quantities the cycle reads, derived from a flow map,
+// the automatic time step of a flow-map set, and the field files of a CMA
+// case.  Pure host code: nothing here touches the device.
+//
+// Derivations (documentation/pages/03_cma.md, "Transition Matrix" and
+// "Cumulative probability"; CmaUtils::get_transition_matrix,
+// get_diag_transition, get_cumulative_probabilities):
+//   T(i, j) = F(i, j) for i != j,  T(i, i) = -sum_{j != i} F(i, j);
+//   P(I_j | L) = F(i, j) / sum_k F(i, k), accumulated over the destinations
+//   of i in ascending order.
+// Self-flows F(i, i) carry no particle and no scalar (the reference's
+// transition test, apps/libs/cma_utils/tests/test_transition_matrix.cpp
+// L7-L25: flows {{1,2},{3,4}} give {{-2,2},{3,-3}}).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/bmc.h"
+
+namespace bmc {
+int api_fail(int code, const std::string& msg);
+}
+
+namespace {
+
+struct Link {
+  uint32_t dst;
+  double flow;
+};
+
+// Out-links of every compartment: entries with i == j or F == 0 dropped,
+// duplicates of one (i, j) summed in input order, destinations ascending.
+const char* gather_links(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
+                         const double* flows, std::vector<uint64_t>& ptr, std::vector<Link>& links) {
+  std::vector<std::pair<std::pair<uint32_t, uint32_t>, double>> e;
+  e.reserve(nnz);
+  for (uint64_t k = 0; k < nnz; ++k) {
+    if (rows[k] >= n_c || cols[k] >= n_c) return "flow index out of range";
+    const double f = flows[k];
+    if (!std::isfinite(f) || f < 0.0) return "flows must be finite and >= 0";
+    if (rows[k] == cols[k] || f == 0.0) continue;
+    e.push_back({{(uint32_t)rows[k], (uint32_t)cols[k]}, f});
+  }
+  std::stable_sort(e.begin(), e.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  ptr.assign((size_t)n_c + 1, 0u);
+  links.clear();
+  for (size_t k = 0; k < e.size(); ++k) {
+    if (k > 0 && e[k].first == e[k - 1].first) {
+      links.back().flow += e[k].second;
+      continue;
+    }
+    links.push_back({e[k].first.second, e[k].second});
+    ptr[e[k].first.first + 1]++;
+  }
+  for (uint32_t i = 0; i < n_c; ++i) ptr[i + 1] += ptr[i];
+  return nullptr;
+}
+
+uint32_t read_u32_le(const unsigned char* b) {
+  return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+}
+
+double read_f64_le(const unsigned char* b) {
+  uint64_t u = 0;
+  for (int k = 7; k >= 0; --k) u = (u << 8) | (uint64_t)b[k];
+  double d;
+  std::memcpy(&d, &u, 8);
+  return d;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bmc_cma_derive(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* flows,
+                   uint32_t* K, uint32_t k_cap, uint64_t* neighbors, double* out_flows, double* cdf) {
+  if (n_c == 0 || !K || (nnz && (!rows || !cols || !flows))) return bmc::api_fail(BMC_E_INVALID, "bad flow map");
+  std::vector<uint64_t> ptr;
+  std::vector<Link> links;
+  if (const char* why = gather_links(n_c, nnz, rows, cols, flows, ptr, links)) return bmc::api_fail(BMC_E_INVALID, why);
+  uint64_t kmax = 1;
+  for (uint32_t i = 0; i < n_c; ++i) kmax = std::max<uint64_t>(kmax, ptr[i + 1] - ptr[i]);
+  *K = (uint32_t)kmax;
+  if (!neighbors && !out_flows && !cdf) return BMC_OK;
+  if (!neighbors || !out_flows || !cdf) return bmc::api_fail(BMC_E_INVALID, "give all three output arrays or none");
+  if (k_cap < kmax) return bmc::api_fail(BMC_E_INVALID, "k_cap is below the largest out-degree (K)");
+  std::vector<double> cum;
+  for (uint32_t i = 0; i < n_c; ++i) {
+    const uint64_t b = ptr[i], deg = ptr[i + 1] - b;
+    uint64_t* nb = neighbors + (size_t)i * kmax;
+    double* cd = cdf + (size_t)i * kmax;
+    // running sum in destination order: its last value is the out-flow,
+    // so the last cumulative probability is exactly 1
+    cum.resize(deg);
+    double s = 0.0;
+    for (uint64_t k = 0; k < deg; ++k) {
+      s += links[b + k].flow;
+      cum[k] = s;
+    }
+    out_flows[i] = s;
+    for (uint64_t k = 0; k < deg; ++k) {
+      nb[k] = links[b + k].dst;
+      cd[k] = cum[k] / s;
+    }
+    const uint64_t pad = deg ? links[b + deg - 1].dst : i;
+    for (uint64_t k = deg; k < kmax; ++k) {
+      nb[k] = pad;
+      cd[k] = 1.0;
+    }
+  }
+  return BMC_OK;
+}
+
+int bmc_cma_transition(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* flows,
+                       uint64_t* t_nnz, uint64_t cap, uint64_t* t_rows, uint64_t* t_cols, double* t_values) {
+  if (n_c == 0 || !t_nnz || (nnz && (!rows || !cols || !flows))) return bmc::api_fail(BMC_E_INVALID, "bad flow map");
+  std::vector<uint64_t> ptr;
+  std::vector<Link> links;
+  if (const char* why = gather_links(n_c, nnz, rows, cols, flows, ptr, links)) return bmc::api_fail(BMC_E_INVALID, why);
+  const uint64_t total = links.size() + n_c;
+  *t_nnz = total;
+  if (!t_rows && !t_cols && !t_values) return BMC_OK;
+  if (!t_rows || !t_cols || !t_values) return bmc::api_fail(BMC_E_INVALID, "give all three output arrays or none");
+  if (cap < total) return bmc::api_fail(BMC_E_INVALID, "cap is below the entry count");
+  uint64_t o = 0;
+  for (uint32_t i = 0; i < n_c; ++i) {
+    double s = 0.0;
+    for (uint64_t k = ptr[i]; k < ptr[i + 1]; ++k) s += links[k].flow;
+    bool diag_done = false;
+    for (uint64_t k = ptr[i]; k < ptr[i + 1]; ++k) {
+      if (!diag_done && links[k].dst > i) {
+        t_rows[o] = i, t_cols[o] = i, t_values[o] = -s, ++o;
+        diag_done = true;
+      }
+      t_rows[o] = i, t_cols[o] = links[k].dst, t_values[o] = links[k].flow, ++o;
+    }
+    if (!diag_done) t_rows[o] = i, t_cols[o] = i, t_values[o] = -s, ++o;
+  }
+  return BMC_OK;
+}
+
+int bmc_cma_time_step(double user_dt, uint32_t n_maps, uint32_t n_c, const double* volumes, const double* out_flows,
+                      double* dt) {
+  if (!dt) return bmc::api_fail(BMC_E_INVALID, "null dt");
+  if (user_dt > 0.0) {
+    *dt = user_dt;
+    return BMC_OK;
+  }
+  if (n_maps == 0 || n_c == 0 || !volumes || !out_flows) return bmc::api_fail(BMC_E_INVALID, "no flow map");
+  double m = std::numeric_limits<double>::max();
+  for (size_t k = 0; k < (size_t)n_maps * n_c; ++k)
+    if (volumes[k] > 0.0) m = std::min(m, out_flows[k] / volumes[k]);
+  if (m == std::numeric_limits<double>::max() || m == 0.0)
+    return bmc::api_fail(BMC_E_INVALID, "no time step given and impossible to estimate it with the given flow maps");
+  *dt = m / 100.;
+  return BMC_OK;
+}
+
+int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t* n) {
+  if (!path || !n) return bmc::api_fail(BMC_E_INVALID, "null argument");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
+  std::vector<unsigned char> buf;
+  unsigned char chunk[65536];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  std::fclose(f);
+  if (buf.size() < 4) return bmc::api_fail(BMC_E_INVALID, "field file shorter than its count");
+  const uint64_t count = read_u32_le(buf.data());
+  if (buf.size() != 4 + 8 * count)
+    return bmc::api_fail(BMC_E_INVALID, "field file size differs from 4 + 8 * count");
+  *n = count;
+  if (!values) return BMC_OK;
+  if (cap < count) return bmc::api_fail(BMC_E_INVALID, "cap is below the value count");
+  for (uint64_t k = 0; k < count; ++k) values[k] = read_f64_le(buf.data() + 4 + 8 * k);
+  return BMC_OK;
+}
+
+}  // extern "C"

@@ -280,6 +280,47 @@ int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neigh
 int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap);
 int bmc_flowmap_clear(bmc_scenario* s);
 
+/* ---- CMA ingestion (host only) ------------------------------------------- */
+/* Derivations of CmaUtils from a flow map F(i, j) (m^3/s, i -> j) in COO
+ * form over n_c compartments (documentation/pages/03_cma.md, "Transition
+ * Matrix" and "Cumulative probability"; the reference computes them in
+ * rcmtool, which is outside its tree).  Self-flows F(i, i) and zero flows
+ * are dropped, duplicate (i, j) entries summed; flows must be finite, >= 0.
+ *
+ * bmc_cma_derive: *K = the largest out-degree (at least 1).  With the three
+ * arrays non-NULL (rows of K entries, k_cap >= K) it writes the arguments of
+ * bmc_domain_update: neighbours [n_c*K] in ascending destination order,
+ * padded with the last destination (the compartment itself when it has
+ * none), out-flows [n_c] = sum_j F(i, j) summed in that order
+ * (get_diag_transition), cumulative probabilities [n_c*K] = running sum /
+ * out-flow (exactly 1 at the last destination and in the padding).
+ *
+ * bmc_cma_transition: *t_nnz = entry count; with the arrays non-NULL (cap >=
+ * count) the liquid transition T(i, j) = F(i, j), T(i, i) = -out-flow(i)
+ * (get_transition_matrix), sorted by (row, col): the arguments of
+ * bmc_set_transition_coo.  Known answers:
+ * apps/libs/cma_utils/tests/test_transition_matrix.cpp L7-L25. */
+int bmc_cma_derive(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* flows,
+                   uint32_t* K, uint32_t k_cap, uint64_t* neighbors, double* out_flows, double* cdf);
+int bmc_cma_transition(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
+                       const double* flows, uint64_t* t_nnz, uint64_t cap, uint64_t* t_rows, uint64_t* t_cols,
+                       double* t_values);
+
+/* Time step of a run (get_time_step, apps/core/src/global_initaliser.cpp
+ * L51-L86, with CmaUtils::get_min_residence_time,
+ * apps/libs/cma_utils/src/utils.cpp L47-L73): user_dt when > 0, else
+ * min over the n_maps flow maps and their compartments of positive volume of
+ * out_flow / volume, divided by 100.  volumes and out_flows: [n_maps*n_c].
+ * BMC_E_INVALID when no compartment gives a positive value. */
+int bmc_cma_time_step(double user_dt, uint32_t n_maps, uint32_t n_c, const double* volumes,
+                      const double* out_flows, double* dt);
+
+/* Field file of a CMA case (vofL.raw, turbE.raw, ...): a little-endian
+ * uint32 count followed by that many little-endian float64 values (the
+ * layout of the fixture apps/api/tests/data/0d/).  *n = count; values are
+ * written when values is non-NULL and cap >= count. */
+int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t* n);
+
 /* ---- two-phase flow: gas phase ------------------------------------------- */
 /* A gas phase on the scenario's mesh (SimulationUnit with
  * is_two_phase_flow; apps/libs/simulation/src/simulation.cpp L47-L81):

@@ -16,6 +16,13 @@ the reference's source code; nothing is computed by this repository's code:
   test (apps/libs/mc/tests/test_container.cpp L14-L127): 1000 particles,
   10 divisions -> 1010 after merge; 10 removed -> 990; capacity =
   n * allocation_factor.
+* cma_cases.json -- the transition matrices of the reference's (disabled)
+  CmaUtils test (apps/libs/cma_utils/tests/test_transition_matrix.cpp
+  L7-L25), the cumulative probabilities of the 3x3 case worked by hand from
+  P(I_j | L) = F(i, j) / sum_k F(i, k) (documentation/pages/03_cma.md), and
+  the bytes of the two field files of the reference's 0-D case fixture
+  (apps/api/tests/data/0d/vofL.raw and turbE.raw.raw, 12 bytes each: uint32
+  count 1, then float64 0.02 and 0.5).
 """
 import json
 import os
@@ -54,8 +61,21 @@ def main():
     }
     container = {"size": 1000, "ndiv": 10, "after_merge": 1010, "to_remove": 10,
                  "after_remove": 990, "allocation_factor_cuda": 1.5, "allocation_factor_cpu": 2.5}
+    cma = {
+        "transition": [
+            {"flows": [[1, 2], [3, 4]], "expected": [[-2, 2], [3, -3]]},
+            {"flows": [[1, 2, 3], [4, 5, 6], [7, 8, 9]], "expected": [[-5, 2, 3], [4, -10, 6], [7, 8, -15]]},
+        ],
+        # 3x3 case: row 0 -> {1: 2, 2: 3}, row 1 -> {0: 4, 2: 6}, row 2 -> {0: 7, 1: 8}
+        "derive_3x3": {"K": 2, "neighbors": [[1, 2], [0, 2], [0, 1]], "out_flow": [5, 10, 15],
+                       "cdf": [[0.4, 1.0], [0.4, 1.0], [7 / 15, 1.0]]},
+        "fields_0d": [
+            {"file": "vofL.raw", "hex": "010000007b14ae47e17a943f", "values": [0.02]},
+            {"file": "turbE.raw.raw", "hex": "01000000000000000000e03f", "values": [0.5]},
+        ],
+    }
     for name, obj in (("philox_kat.json", philox), ("move_cases.json", move),
-                      ("container_counts.json", container)):
+                      ("container_counts.json", container), ("cma_cases.json", cma)):
         with open(os.path.join(HERE, name), "w") as f:
             json.dump(obj, f, indent=1)
 
