@@ -186,6 +186,8 @@ struct bmc_scenario {
   // last cycle-launch sizing (prepare_cycle), reused while its inputs stay
   unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u, prep_run = 0u;
   size_t prep_in = 0, prep_out = 0;
+  unsigned graph_liq = 0, graph_plan = 0;
+  bool graph_tiny = false;
   // flow-map cycle (host copies; device copies in marena)
   struct FlowMap {
     std::vector<int2> mrow;
@@ -219,6 +221,9 @@ struct bmc_batch {
   size_t graph_smem = 0;
   unsigned graph_grid = 0, graph_variant = 0;
   unsigned run_variant = 0;  // variant of the last prepared launch
+  unsigned plan_y = 1;       // k_plan slices of the last prepared launch
+  unsigned graph_liq = 0, graph_plan = 0;
+  bool graph_tiny = false;
   double dt = -1.0;
 };
 
@@ -347,23 +352,27 @@ int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, 
 }
 
 // Enqueue one step (liquid step optional) for a table of scenarios.
-// Blocks along x of the liquid step: 256 / n_species compartments per block.
+// Slices of k_plan (grid y): kPlanSlice compartments each.
+unsigned plan_slices(const ScenDev& h) { return std::max(1u, (h.n_c + bmc::kPlanSlice - 1) / bmc::kPlanSlice); }
+
+// Blocks along x of the liquid step: kLiquidThreads / n_species compartments
+// per block.
 unsigned liquid_grid(const ScenDev& h) {
-  const unsigned cb = 256u / std::max(1u, h.n_s);
+  const unsigned cb = bmc::kLiquidThreads / std::max(1u, h.n_s);
   return std::max(1u, (h.n_c + cb - 1) / cb);
 }
 
 // With `maps`, the flow-map switch runs first (main-loop steps only).
 int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned liq_grid,
-                 BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem, int sm_count,
-                 bool maps, bool tiny) {
+                 unsigned plan_y, BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem,
+                 int sm_count, bool maps, bool tiny) {
   if (maps && do_scalar) {
     ks->flowmap(n_scen, st, d_table);
     g_launches += 1;
   }
   ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
   ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl, tiny);
-  ks->plan(n_scen, st, d_table, d_bctl);
+  ks->plan(n_scen, plan_y, st, d_table, d_bctl);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
   ks->merge(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
@@ -395,7 +404,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
   bool table_changed = b->table.size() != (size_t)n;
   b->table.resize(n);
   int lo = table_changed ? 0 : n, hi = table_changed ? n - 1 : -1;  // changed entries
-  unsigned tiles = 0, max_nc = 0;
+  unsigned tiles = 0, max_nc = 0, max_plan = 1;
   size_t smem = 0;
   for (int i = 0; i < n; ++i) {
     bmc_scenario* s = b->scen[i];
@@ -413,6 +422,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
     d.tile_base = tiles;
     tiles += d.n_tiles;
     max_nc = std::max(max_nc, liquid_grid(d));
+    max_plan = std::max(max_plan, plan_slices(d));
     smem = std::max(smem, cycle_smem(d));
     if (std::memcmp(&d, &b->table[i], sizeof(ScenDev)) != 0) {
       table_changed = true;
@@ -439,6 +449,7 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
   *n_out = n;
   *max_nc_out = max_nc;
   *smem_out = smem;
+  b->plan_y = max_plan;
   return BMC_OK;
 }
 
@@ -871,14 +882,18 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
 }
 
 static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned variant) {
-  if (s->graph && s->graph_smem == smem && s->graph_grid == grid && s->graph_variant == variant) return BMC_OK;
+  const unsigned liq = liquid_grid(s->h), plan = plan_slices(s->h);
+  const bool tiny = tiny_domain(s->h);
+  if (s->graph && s->graph_smem == smem && s->graph_grid == grid && s->graph_variant == variant &&
+      s->graph_liq == liq && s->graph_plan == plan && s->graph_tiny == tiny)
+    return BMC_OK;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
   cudaGraph_t g = nullptr;
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
-  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, 1, variant, grid, smem,
-                        s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
+  int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liq, plan, s->d_bctl, 1, variant, grid, smem, s->sm_count,
+                        s->h.n_maps > 0, tiny);
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc) {
@@ -892,6 +907,9 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned va
   s->graph_smem = smem;
   s->graph_grid = grid;
   s->graph_variant = variant;
+  s->graph_liq = liq;
+  s->graph_plan = plan;
+  s->graph_tiny = tiny;
   return BMC_OK;
 }
 
@@ -937,8 +955,8 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
     return BMC_OK;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
-    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), s->d_bctl, do_scalar, variant, grid, smem,
-                      s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
+    rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), plan_slices(s->h), s->d_bctl, do_scalar,
+                      variant, grid, smem, s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
     if (rc) return rc;
   }
   return BMC_OK;
@@ -1304,15 +1322,17 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   size_t smem = 0;
   int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
+  const bool tiny = batch_tiny(b);
   if (!b->graph || b->graph_smem != smem || b->graph_grid != grid || b->graph_variant != b->run_variant ||
-      b->graph_maps != batch_has_maps(b)) {
+      b->graph_maps != batch_has_maps(b) || b->graph_liq != max_nc || b->graph_plan != b->plan_y ||
+      b->graph_tiny != tiny) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
-    rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->d_bctl, 1, b->run_variant, grid, smem,
-                      b->sm_count, batch_has_maps(b), batch_tiny(b));
+    rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->plan_y, b->d_bctl, 1, b->run_variant, grid,
+                      smem, b->sm_count, batch_has_maps(b), tiny);
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -1327,6 +1347,9 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     b->graph_grid = grid;
     b->graph_variant = b->run_variant;
     b->graph_maps = batch_has_maps(b);
+    b->graph_liq = max_nc;
+    b->graph_plan = b->plan_y;
+    b->graph_tiny = tiny;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     BMC_CUDA(cudaGraphLaunch(b->graph, b->stream));
@@ -1638,7 +1661,7 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl,
                         tiny_domain(s->h));
   BMC_CUDA(cudaEventRecord(ev[2], st));
-  s->ks->plan(1, st, s->d_desc, s->d_bctl);
+  s->ks->plan(1, plan_slices(s->h), st, s->d_desc, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));
   s->ks->divide(dim3(s->sm_count * 4), st, s->d_desc, 1, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[4], st));
@@ -1678,7 +1701,7 @@ int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   b->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, b->d_table, n, b->d_bctl,
                         batch_tiny(b));
   BMC_CUDA(cudaEventRecord(ev[2], st));
-  b->ks->plan(n, st, b->d_table, b->d_bctl);
+  b->ks->plan(n, b->plan_y, st, b->d_table, b->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));
   b->ks->divide(dim3(sm * 4), st, b->d_table, n, b->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[4], st));

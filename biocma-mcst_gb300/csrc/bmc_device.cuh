@@ -73,6 +73,10 @@ struct Control {
   // per-species sums of the liquid step (new mass, expected mass)
   double mb_new[kMaxSpecies];
   double mb_exp[kMaxSpecies];
+  // 1 while the current step runs for this scenario (set by the liquid step
+  // from the step limit, before the plan kernel advances the step counter)
+  unsigned int cycling;
+  unsigned int pad;
 };
 
 // Scenario descriptor as the kernels see it (one per scenario, device memory).

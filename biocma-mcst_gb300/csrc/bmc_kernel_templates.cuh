@@ -35,7 +35,7 @@ __host__ __device__ constexpr int rate_slot(int k) {
 
 // ---------------------------------------------------------------------------
 // k_liquid: one thread per (compartment j, species s) entry; a block holds
-// 256 / n_species whole compartments (grid x over compartment chunks, grid
+// kLiquidThreads / n_species whole compartments (grid x over compartment chunks, grid
 // y over scenarios).  Feeds into sources and sink, explicit Euler step
 //   M(j,s) += dt (sum_i C(i,s) T(i,j) - C(j,s) sink(j) + src(j,s)),
 //   C'(j,s) = M(j,s) / V(j),
@@ -45,10 +45,10 @@ __host__ __device__ constexpr int rate_slot(int k) {
 // the rates (and C carried to the next buffer).  Block (0, s) resets the
 // step counters of scenario s; block (0, 0) the tile scheduler and flags.
 template <class Model, class F>
-__global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
+__global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
   const ScenDev& S = sc[blockIdx.y];
   Control* ctl = S.ctl;
-  __shared__ double cs[256];
+  __shared__ double cs[kLiquidThreads];
   __shared__ double red[2][kMaxSpecies];
   if (blockIdx.x == 0 && blockIdx.y == 0) {
     // live tiles of every scenario (ceil(n_used / 1024), none once finished)
@@ -82,6 +82,7 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
     ctl->req_div = 0ull;
     ctl->exits = 0ull;
     ctl->moves = 0ull;
+    ctl->cycling = scen_finished(S, ctl) ? 0u : 1u;
   }
   {
     // per-tile birth / inactive counters of this step start at zero (the
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(256) k_liquid(ScenDev* __restrict__ sc, BatchC
     }
   }
   const unsigned nsp = S.n_s;
-  const unsigned cb = 256u / nsp;  // compartments per block
+  const unsigned cb = kLiquidThreads / nsp;  // compartments per block
   const unsigned j0 = blockIdx.x * cb;
   if (j0 >= S.n_c || scen_finished(S, ctl)) return;
   const unsigned t = threadIdx.x;
@@ -975,11 +976,13 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
 }
 
 // ---------------------------------------------------------------------------
-// k_plan: per scenario (one block of 1024 threads):
-//  1. exact accumulator totals -> sources: for a separable model
-//     src(j, s) = (w * coef_s(rates_j)) * B_j with B_j the basis total of
-//     compartment j; for a general model src(j, s) = total of w * ctb_s;
-//     accumulators cleared;
+// k_plan: per scenario (grid x), blocks of 1024 threads over slices of
+// kPlanSlice compartments (grid y):
+//  1. every slice: exact accumulator totals -> sources of its compartments:
+//     for a separable model src(j, s) = (w * coef_s(rates_j)) * B_j with B_j
+//     the basis total of compartment j; for a general model src(j, s) =
+//     total of w * ctb_s; accumulators cleared (FP64 work, spread over SMs);
+// slice 0 only:
 //  2. post_cycle decisions: inactive += exits; compaction iff inactive >
 //     max(min_removal, n * ratio) (update_and_remove_inactive); room for
 //     births = capacity - live particles after compaction;
@@ -994,9 +997,11 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
   __shared__ unsigned long long sh64[33];
   __shared__ unsigned long long p_n, p_req, p_rm, p_after;
   __shared__ int p_compact;
-  if (scen_finished(S, ctl)) {
+  // (not scen_finished: slice 0 advances the step counter while the other
+  // slices may still be starting)
+  if (!ctl->cycling) {
     // nothing ran for this scenario: leave its state and a no-op plan
-    if (tid == 0) {
+    if (blockIdx.y == 0 && tid == 0) {
       ctl->plan_births = 0ull;
       ctl->plan_overflow = 0ull;
       ctl->plan_compact = 0u;
@@ -1009,9 +1014,11 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
   }
 
   const unsigned nsp = S.n_s;
-  const unsigned n_e = S.n_c * nsp;
   const F* rates = reinterpret_cast<const F*>(S.crec);
-  if (tid < (int)nsp && tid < kMaxSpecies) {
+  // sources of this block's slice of compartments
+  const unsigned jb = blockIdx.y * kPlanSlice;
+  const unsigned je = min(jb + kPlanSlice, S.n_c);
+  if (blockIdx.y == 0 && tid < (int)nsp && tid < kMaxSpecies) {
     const double a = ctl->mb_new[tid], b = ctl->mb_exp[tid];
     const double den = fabs(a) > 1e-300 ? fabs(a) : 1e-300;
     ctl->mass_balance[tid] = fabs(a - b) / den;
@@ -1019,7 +1026,7 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     ctl->mb_exp[tid] = 0.0;
   }
   if constexpr (Model::separable) {
-    for (unsigned j = tid; j < S.n_c; j += blockDim.x) {
+    for (unsigned j = jb + tid; j < je; j += blockDim.x) {
       const double B = fixed_to_double(S.acc_hi[j], S.acc_lo[j], S.q_scale_up[0]);
       S.acc_hi[j] = 0;
       S.acc_lo[j] = 0ull;
@@ -1034,7 +1041,7 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     }
   } else {
     const unsigned nc = Model::n_ctb;
-    for (unsigned e = tid; e < n_e; e += blockDim.x) {
+    for (unsigned e = jb * nsp + tid; e < je * nsp; e += blockDim.x) {
       const unsigned j = e / nsp;
       const unsigned sp = e - j * nsp;
       double v = 0.0;
@@ -1047,6 +1054,7 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
       S.src[e] = v;
     }
   }
+  if (blockIdx.y != 0) return;
   if (tid == 0) {
     const unsigned long long n = ctl->n_used;
     const unsigned long long req = ctl->req_div;
@@ -1098,46 +1106,34 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
   __syncthreads();
   const unsigned long long n = p_n;
   const unsigned n_t = (unsigned)((n + kTile - 1) / kTile);
-  const unsigned chunk = (n_t + blockDim.x - 1) / blockDim.x;
-  const unsigned t0 = tid * chunk;
-  const unsigned t1 = min(t0 + chunk, n_t);
-  unsigned long long tot;
+  const unsigned* __restrict__ births = S.tile_births;
+  const unsigned* __restrict__ inact = S.tile_inactive;
   if (p_req > 0) {
-    unsigned long long local = 0;
-    for (unsigned t = t0; t < t1; ++t) local += S.tile_births[t];
-    unsigned long long off = block_exscan_u64(local, sh64, &tot);
-    for (unsigned t = t0; t < t1; ++t) {
-      S.tile_boff[t] = (unsigned)off;
-      off += S.tile_births[t];
-    }
+    // birth ranks: births in earlier tiles
+    block_exscan_items(
+        n_t, [&](unsigned t) { return (unsigned long long)births[t]; },
+        [&](unsigned t, unsigned long long pre, unsigned long long) { S.tile_boff[t] = (unsigned)pre; }, sh64);
   }
   if (p_compact && p_after > 0 && p_rm < n) {
     const unsigned long long after = p_after;
     // gap offsets for tiles t <= after / kTile (ascending prefix of inactive)
     const unsigned tg_end = min((unsigned)(after / kTile) + 1u, n_t);
-    unsigned long long local = 0;
-    for (unsigned t = t0; t < t1 && t < tg_end; ++t) local += S.tile_inactive[t];
-    unsigned long long off = block_exscan_u64(local, sh64, &tot);
-    for (unsigned t = t0; t < t1 && t < tg_end; ++t) {
-      S.tile_goff[t] = (unsigned)off;
-      off += S.tile_inactive[t];
-    }
+    block_exscan_items(
+        tg_end, [&](unsigned t) { return (unsigned long long)inact[t]; },
+        [&](unsigned t, unsigned long long pre, unsigned long long) { S.tile_goff[t] = (unsigned)pre; }, sh64);
     // source offsets for tiles t >= after / kTile: idle slots in later tiles
     const unsigned ts_begin = (unsigned)(after / kTile);
-    unsigned long long local2 = 0;
-    for (unsigned t = t0; t < t1; ++t) {
-      if (t < ts_begin) continue;
+    auto idle = [&](unsigned i) {
+      const unsigned t = ts_begin + i;
       const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
-      local2 += valid - S.tile_inactive[t];
-    }
-    unsigned long long tot2;
-    unsigned long long pre = block_exscan_u64(local2, sh64, &tot2);
-    for (unsigned t = t0; t < t1; ++t) {
-      if (t < ts_begin) continue;
-      const unsigned long long valid = min((unsigned long long)kTile, n - (unsigned long long)t * kTile);
-      pre += valid - S.tile_inactive[t];
-      S.tile_soff[t] = (unsigned)(tot2 - pre);  // idle slots in tiles after t
-    }
+      return valid - inact[t];
+    };
+    block_exscan_items(
+        n_t - ts_begin, idle,
+        [&](unsigned i, unsigned long long pre, unsigned long long tot) {
+          S.tile_soff[ts_begin + i] = (unsigned)(tot - pre - idle(i));
+        },
+        sh64);
   }
 }
 
@@ -1428,11 +1424,11 @@ void launch_cycle_tma_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, con
 }
 template <class Model, class F>
 void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
-  k_liquid<Model, F><<<dim3(grid_x, n_scen), 256, 0, st>>>(sc, b, do_scalar);
+  k_liquid<Model, F><<<dim3(grid_x, n_scen), kLiquidThreads, 0, st>>>(sc, b, do_scalar);
 }
 template <class Model, class F>
-void launch_plan_t(int n_scen, cudaStream_t st, ScenDev* sc, BatchCtl* b) {
-  k_plan<Model, F><<<n_scen, 1024, 0, st>>>(sc, b);
+void launch_plan_t(int n_scen, unsigned slices, cudaStream_t st, ScenDev* sc, BatchCtl* b) {
+  k_plan<Model, F><<<dim3(n_scen, slices), 1024, 0, st>>>(sc, b);
 }
 template <class Model, class F>
 void launch_divide_t(dim3 grid, cudaStream_t st, const ScenDev* sc, int n, const BatchCtl* b) {

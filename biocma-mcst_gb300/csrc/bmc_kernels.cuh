@@ -137,32 +137,52 @@ __device__ __forceinline__ unsigned block_exscan_u32(unsigned v, unsigned* sh, u
   return warp_off + x - v;
 }
 
-__device__ __forceinline__ unsigned long long block_exscan_u64(unsigned long long v, unsigned long long* sh,
-                                                               unsigned long long* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  unsigned long long x = v;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
-    if (lane >= o) x += y;
-  }
-  if (lane == 31) sh[wid] = x;
+// Exclusive prefix sums over items [0, n) of a block whose size is a
+// multiple of 32: item i has value v(i) (at most 2^32 / 32 per item), and
+// out(i, prefix, total) receives the sum of v over [0, i) and over [0, n).
+// Each warp takes a contiguous range of whole 32-item rounds and walks it
+// one round at a time (lane l reads item round + l: coalesced), first for
+// its total, then, with the block's warp offsets, for the prefixes.  v is
+// read twice.  sh: 33 words of shared memory.
+template <class V, class O>
+__device__ __forceinline__ unsigned long long block_exscan_items(unsigned n, V v, O out, unsigned long long* sh) {
+  const unsigned lane = threadIdx.x & 31u, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned per = ((n + nw - 1u) / nw + 31u) & ~31u;
+  const unsigned b = min(w * per, n), e = min(b + per, n);
+  unsigned long long mine = 0ull;
+  for (unsigned r = b; r < e; r += 32u)
+    if (r + lane < e) mine += v(r + lane);
+  mine = warp_sum_u64(mine);
+  if (lane == 0) sh[w] = mine;
   __syncthreads();
-  if (wid == 0) {
-    unsigned long long w = lane < nw ? sh[lane] : 0ull;
+  if (w == 0) {
+    const unsigned long long own = lane < nw ? sh[lane] : 0ull;
+    unsigned long long x = own;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
-      if (lane >= o) w += y;
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += y;
     }
-    if (lane < nw) sh[lane] = w;
+    if (lane < nw) sh[lane] = x - own;  // exclusive warp offsets
+    if (lane == 31u) sh[32] = x;        // block total
   }
   __syncthreads();
-  const unsigned long long warp_off = wid > 0 ? sh[wid - 1] : 0ull;
-  const unsigned long long tot = sh[nw - 1];
-  __syncthreads();
-  *total = tot;
-  return warp_off + x - v;
+  const unsigned long long total = sh[32];
+  unsigned long long carry = sh[w];
+  for (unsigned r = b; r < e; r += 32u) {
+    const unsigned i = r + lane;
+    const unsigned x0 = i < e ? (unsigned)v(i) : 0u;  // a round sums to < 2^32
+    unsigned x = x0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((int)lane >= o) x += y;
+    }
+    if (i < e) out(i, carry + (x - x0), total);
+    carry += __shfl_sync(0xffffffffu, x, 31);
+  }
+  __syncthreads();  // sh may be reused
+  return total;
 }
 
 // Exact total of a fixed-point accumulator (hi limb sums p >> 32, lo limb

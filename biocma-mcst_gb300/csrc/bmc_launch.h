@@ -15,7 +15,10 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 5;
+constexpr int kKernelSetAbi = 6;
+// Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
+// whole compartments per block, so a small domain still spreads over many SMs.
+constexpr unsigned kLiquidThreads = 32;
 
 // The last argument selects the instantiation with the warp-aggregated
 // scatter, for launches whose domains all have at most
@@ -44,7 +47,10 @@ constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1, 4, 2};
 // accumulator plus stage buffers), else to register streaming 256 x 2.
 constexpr unsigned kVariantAuto = kCycleVariants;
 constexpr unsigned kAutoStaged = 6, kAutoStreamed = 1;
-using PlanLaunch = void (*)(int, cudaStream_t, ScenDev*, BatchCtl*);
+// Compartments whose sources one k_plan block computes (grid y of k_plan:
+// ceil(n_compartments / kPlanSlice) slices; slice 0 also plans the step).
+constexpr unsigned kPlanSlice = 256;
+using PlanLaunch = void (*)(int n_scen, unsigned slices, cudaStream_t, ScenDev*, BatchCtl*);
 
 struct KernelSet {
   int abi;

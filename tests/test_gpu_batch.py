@@ -121,3 +121,33 @@ def test_slot_batch_fill_empty_refill_equals_alone():
     for slot in (0, 3, 4, 6, 7):
         b.set_slot(slot, None)
     b.close()
+
+
+@pytest.mark.parametrize("n_small,n_large", [(17, 25), (300, 700)])
+def test_slot_batch_recaptures_when_a_larger_domain_joins(n_small, n_large):
+    """A scenario with more compartments joining after the step graph was
+    captured needs more liquid-step blocks (and, past 256 compartments, more
+    plan slices) even when its shared accumulator rounds to the same size:
+    the batch re-captures, and both scenarios advance as they would alone."""
+    from bmc.sim import GpuBatch, GpuScenario
+
+    def ring(n_c, seed):  # 4 species: 8 compartments per liquid-step block
+        return scenarios.small_ring(3000, n_c=n_c, feeds=True, seed=seed, model=scenarios.overflow(f64=True))
+
+    small, large = ring(n_small, 3), ring(n_large, 4)
+    gs, gl = GpuScenario(small), GpuScenario(large)
+    a_s, a_l = GpuScenario(small), GpuScenario(large)
+    b = GpuBatch.slots(4, small.model)
+    b.set_slot(0, gs)
+    b.run(3, small.dt)
+    b.synchronize()
+    b.set_slot(1, gl)
+    b.run(4, small.dt)
+    b.synchronize()
+    a_s.run(7)
+    a_l.run(4)
+    assert_same(gs, a_s, "small")
+    assert_same(gl, a_l, "large")
+    b.set_slot(0, None)
+    b.set_slot(1, None)
+    b.close()
