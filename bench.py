@@ -41,7 +41,7 @@ def parse():
     ap.add_argument("--workload", type=int, default=2)
     ap.add_argument("--particles", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=50)
+    ap.add_argument("--e2e-steps", type=int, default=200)
     ap.add_argument("--shape", default=None,
                     help="threads,particles_per_thread,blocks_per_sm (skips the autotuner)")
     ap.add_argument("--no-forms", action="store_true",
@@ -330,8 +330,7 @@ def run_gpu(args):
         ps = 0.0
         for _ in range(args.e2e_steps):
             call("bmc_set_feeds", g.handle, len(scen.feeds), arr)
-            s_ = g.step()
-            call("bmc_read_liquid", g.handle, ct.c_void_p(conc.ctypes.data), None, None)
+            s_ = g.step_read(conc)
             ps += s_["n_used"] - s_["inactive"]
         barrier()
         te = time.perf_counter() - t0
@@ -341,7 +340,8 @@ def run_gpu(args):
         e2e = {"value": ev, "unit": METRIC,
                "h2d_bytes_per_step": (h1 - h0) / args.e2e_steps,
                "d2h_bytes_per_step": (d1 - d0) / args.e2e_steps,
-               "api": "bmc_set_feeds + bmc_step + bmc_read_liquid per step (C-ABI, host buffers)"}
+               "api": "bmc_set_feeds + bmc_step_read per step (C-ABI, host buffers: feeds in, "
+                      "counters and concentrations out)"}
         del a0
 
     cpu = None

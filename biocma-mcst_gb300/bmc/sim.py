@@ -189,6 +189,16 @@ class GpuScenario:
         call("bmc_step", self.handle, dt or self.scen.dt, ct.byref(st))
         return st.as_dict()
 
+    def step_read(self, conc: np.ndarray, dt: float | None = None) -> dict:
+        """One step; the concentrations after it are written into `conc`
+        (float64 [n_c, n_species], C-contiguous) in the same synchronisation."""
+        n = self.scen.net.n_c * self.scen.n_species
+        if conc.dtype != np.float64 or not conc.flags.c_contiguous or conc.size != n:
+            raise ValueError(f"conc must be a C-contiguous float64 array of {n} values")
+        st = StepStats()
+        call("bmc_step_read", self.handle, dt or self.scen.dt, ct.byref(st), _p(conc))
+        return st.as_dict()
+
     def step_timed(self, dt: float | None = None):
         """One step with per-kernel CUDA-event durations (ms): liquid, cycle,
         plan, divide, compact, merge."""

@@ -173,6 +173,8 @@ struct bmc_scenario {
   Control* d_ctl = nullptr;
   BatchCtl* d_bctl = nullptr;
   Control* h_ctl = nullptr;  // pinned
+  double* h_cstage = nullptr;  // pinned: both concentration buffers (bmc_step_read)
+  size_t cstage_n = 0;
   bool has_domain = false, has_transition = false, has_conc = false, has_weight = false;
   std::vector<double> volume;
   std::vector<bmc_feed> feeds;
@@ -646,6 +648,7 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->marena) cudaFree(s->marena);
   if (s->garena) cudaFree(s->garena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
+  if (s->h_cstage) cudaFreeHost(s->h_cstage);
   cudaStreamDestroy(s->stream);
   delete s;
   return BMC_OK;
@@ -990,6 +993,27 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
   int rc = scenario_steps(s, dt, 1, 1, true);
   if (rc) return rc;
   return read_ctl(s, stats);
+}
+
+int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc) {
+  if (!conc) return fail(BMC_E_INVALID, "null concentrations");
+  int rc = scenario_steps(s, dt, 1, 1, true);
+  if (rc) return rc;
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  if (s->cstage_n < ne) {
+    if (s->h_cstage) cudaFreeHost(s->h_cstage);
+    s->h_cstage = nullptr;
+    s->cstage_n = 0;
+    BMC_CUDA(cudaMallocHost(&s->h_cstage, 2 * ne * sizeof(double)));
+    s->cstage_n = ne;
+  }
+  // both buffers: the step parity, read back with the control block in the
+  // same synchronisation, names the current one
+  BMC_CUDA(counted_memcpy_async(s->h_cstage, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  rc = read_ctl(s, stats);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  std::memcpy(conc, s->h_cstage + (s->h_ctl->step & 1u) * ne, ne * sizeof(double));
+  return rc;
 }
 
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats) {

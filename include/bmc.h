@@ -204,6 +204,12 @@ int bmc_cycle_external(bmc_scenario* s, double dt, const double* conc, double* s
  * implScalar.cpp L251-L264), clearContribution, cycleProcess. */
 int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
 
+/* bmc_step followed by bmc_read_liquid(conc) with a single device
+ * synchronisation: the step, the control block and the concentrations
+ * [n_c][n_s] after the step travel back together (the host loop that reads
+ * the field every iteration). */
+int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc);
+
 /* n_steps iterations on the device without host round trips (one captured
  * CUDA graph replayed).  Statistics are those of the last step. */
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats);

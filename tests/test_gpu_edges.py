@@ -174,3 +174,23 @@ def test_malformed_inputs_are_refused():
     # the scenario still steps after the refusals
     st = g.step()
     assert st["error"] == 0 and st["n_used"] > 0
+
+
+def test_step_read_equals_step_then_read_liquid():
+    """bmc_step_read returns the counters and concentrations bmc_step +
+    bmc_read_liquid return, including after the step limit is reached."""
+    from bmc.sim import GpuScenario
+
+    sc = scenarios.small_ring(5000, feeds=True)
+    g1, g2 = GpuScenario(sc), GpuScenario(sc)
+    g1.set_step_limit(6)
+    g2.set_step_limit(6)
+    conc = np.zeros((sc.net.n_c, sc.n_species))
+    for k in range(8):
+        s1 = g1.step()
+        c1 = g1.liquid()["C"]
+        s2 = g2.step_read(conc)
+        assert s1 == s2, k
+        assert np.array_equal(c1.view(np.uint64), conc.view(np.uint64)), k
+    with pytest.raises(ValueError):
+        g2.step_read(np.zeros(3))
