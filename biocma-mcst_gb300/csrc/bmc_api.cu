@@ -189,7 +189,7 @@ struct bmc_scenario {
   unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u, prep_run = 0u;
   size_t prep_in = 0, prep_out = 0;
   unsigned graph_liq = 0, graph_plan = 0;
-  bool graph_tiny = false;
+  int graph_scatter = 0;
   // flow-map cycle (host copies; device copies in marena)
   struct FlowMap {
     std::vector<int2> mrow;
@@ -225,7 +225,7 @@ struct bmc_batch {
   unsigned run_variant = 0;  // variant of the last prepared launch
   unsigned plan_y = 1;       // k_plan slices of the last prepared launch
   unsigned graph_liq = 0, graph_plan = 0;
-  bool graph_tiny = false;
+  int graph_scatter = 0;
   double dt = -1.0;
 };
 
@@ -311,7 +311,12 @@ int set_dt(bmc_scenario* s, double dt, bool launch_pmove) {
   return BMC_OK;
 }
 
-size_t cycle_smem(const ScenDev& h) { return (size_t)h.n_c * h.n_acc * sizeof(unsigned long long); }
+size_t cycle_smem(const ScenDev& h) {
+  size_t n = (size_t)h.n_c * h.n_acc;
+  if (h.n_acc == 1 && h.n_c <= bmc::kScatterCopyMaxCompartments)  // copies of the accumulator
+    n = std::max(n, (size_t)bmc::kAccCopies * bmc::scatter_stride(h.n_c));
+  return n * sizeof(unsigned long long);
+}
 
 // *smem: in, the accumulator bytes; out, the dynamic shared memory of the
 // launch (staged variants append their tile buffers, 128-byte aligned).
@@ -367,13 +372,13 @@ unsigned liquid_grid(const ScenDev& h) {
 // With `maps`, the flow-map switch runs first (main-loop steps only).
 int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, int n_scen, unsigned liq_grid,
                  unsigned plan_y, BatchCtl* d_bctl, int do_scalar, unsigned variant, unsigned grid, size_t smem,
-                 int sm_count, bool maps, bool tiny) {
+                 int sm_count, bool maps, int scatter) {
   if (maps && do_scalar) {
     ks->flowmap(n_scen, st, d_table);
     g_launches += 1;
   }
   ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
-  ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl, tiny);
+  ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl, scatter);
   ks->plan(n_scen, plan_y, st, d_table, d_bctl);
   ks->divide(dim3(sm_count * 4), st, d_table, n_scen, d_bctl);
   ks->compact(dim3(sm_count * 2), st, d_table, n_scen, d_bctl);
@@ -386,10 +391,23 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
 // Launches whose domains all have at most kAggregateMaxCompartments
 // compartments use the cycle kernels with the warp-aggregated scatter.
 bool tiny_domain(const ScenDev& h) { return h.n_c <= bmc::kAggregateMaxCompartments; }
+// Domains whose separable-model scatter goes to accumulator copies.
+bool copy_domain(const bmc::KernelSet* ks, const ScenDev& h) {
+  return ks->separable && h.n_c <= bmc::kScatterCopyMaxCompartments;
+}
+int scenario_scatter(const bmc::KernelSet* ks, const ScenDev& h) {
+  return tiny_domain(h) ? bmc::kScatterWarp : copy_domain(ks, h) ? bmc::kScatterCopied : bmc::kScatterPlain;
+}
 bool batch_tiny(const bmc_batch* b) {
   for (const bmc_scenario* m : b->scen)
     if (m && !tiny_domain(m->h)) return false;
   return true;
+}
+int batch_scatter(const bmc_batch* b) {
+  if (batch_tiny(b)) return bmc::kScatterWarp;
+  for (const bmc_scenario* m : b->scen)
+    if (m && copy_domain(b->ks, m->h)) return bmc::kScatterCopied;
+  return bmc::kScatterPlain;
 }
 
 bool batch_has_maps(const bmc_batch* b) {
@@ -886,9 +904,9 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
 
 static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned variant) {
   const unsigned liq = liquid_grid(s->h), plan = plan_slices(s->h);
-  const bool tiny = tiny_domain(s->h);
+  const int scatter = scenario_scatter(s->ks, s->h);
   if (s->graph && s->graph_smem == smem && s->graph_grid == grid && s->graph_variant == variant &&
-      s->graph_liq == liq && s->graph_plan == plan && s->graph_tiny == tiny)
+      s->graph_liq == liq && s->graph_plan == plan && s->graph_scatter == scatter)
     return BMC_OK;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
@@ -896,7 +914,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned va
   BMC_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   const unsigned long long before = g_launches.load();
   int rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liq, plan, s->d_bctl, 1, variant, grid, smem, s->sm_count,
-                        s->h.n_maps > 0, tiny);
+                        s->h.n_maps > 0, scatter);
   g_launches = before;
   cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   if (rc) {
@@ -912,7 +930,7 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned va
   s->graph_variant = variant;
   s->graph_liq = liq;
   s->graph_plan = plan;
-  s->graph_tiny = tiny;
+  s->graph_scatter = scatter;
   return BMC_OK;
 }
 
@@ -959,7 +977,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), plan_slices(s->h), s->d_bctl, do_scalar,
-                      variant, grid, smem, s->sm_count, s->h.n_maps > 0, tiny_domain(s->h));
+                      variant, grid, smem, s->sm_count, s->h.n_maps > 0, scenario_scatter(s->ks, s->h));
     if (rc) return rc;
   }
   return BMC_OK;
@@ -1346,17 +1364,17 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
   size_t smem = 0;
   int rc = batch_prepare(b, dt, &n, &max_nc, &smem, &grid);
   if (rc) return rc;
-  const bool tiny = batch_tiny(b);
+  const int scatter = batch_scatter(b);
   if (!b->graph || b->graph_smem != smem || b->graph_grid != grid || b->graph_variant != b->run_variant ||
       b->graph_maps != batch_has_maps(b) || b->graph_liq != max_nc || b->graph_plan != b->plan_y ||
-      b->graph_tiny != tiny) {
+      b->graph_scatter != scatter) {
     if (b->graph) cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
     cudaGraph_t g = nullptr;
     BMC_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     const unsigned long long before = g_launches.load();
     rc = enqueue_step(b->ks, b->stream, b->d_table, n, max_nc, b->plan_y, b->d_bctl, 1, b->run_variant, grid,
-                      smem, b->sm_count, batch_has_maps(b), tiny);
+                      smem, b->sm_count, batch_has_maps(b), scatter);
     g_launches = before;
     cudaError_t e = cudaStreamEndCapture(b->stream, &g);
     if (rc) {
@@ -1373,7 +1391,7 @@ int bmc_batch_run(bmc_batch* b, double dt, uint32_t n_steps) {
     b->graph_maps = batch_has_maps(b);
     b->graph_liq = max_nc;
     b->graph_plan = b->plan_y;
-    b->graph_tiny = tiny;
+    b->graph_scatter = scatter;
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     BMC_CUDA(cudaGraphLaunch(b->graph, b->stream));
@@ -1683,7 +1701,7 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   s->ks->liquid(1, liquid_grid(s->h), st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
   s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl,
-                        tiny_domain(s->h));
+                        scenario_scatter(s->ks, s->h));
   BMC_CUDA(cudaEventRecord(ev[2], st));
   s->ks->plan(1, plan_slices(s->h), st, s->d_desc, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));
@@ -1723,7 +1741,7 @@ int bmc_batch_step_timed(bmc_batch* b, double dt, float* kernel_ms) {
   b->ks->liquid(n, max_nc, st, b->d_table, b->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
   b->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, b->d_table, n, b->d_bctl,
-                        batch_tiny(b));
+                        batch_scatter(b));
   BMC_CUDA(cudaEventRecord(ev[2], st));
   b->ks->plan(n, b->plan_y, st, b->d_table, b->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));

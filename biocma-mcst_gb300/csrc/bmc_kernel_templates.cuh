@@ -617,6 +617,7 @@ struct CycleScen {
   F dtF;
   float dtf;
   int qe0;
+  unsigned rep_mask, rep_stride;  // accumulator copies - 1, copy stride
 };
 
 template <class Model, class F>
@@ -634,9 +635,11 @@ struct TileStage {
   __host__ __device__ static constexpr unsigned rank(unsigned v) { return popcount_c(Model::read_mask & ((1u << v) - 1u)); }
 };
 
-template <class Model, class F, int THREADS, int MINB, int STAGES, bool AGG>
+template <class Model, class F, int THREADS, int MINB, int STAGES, int SCATTER>
 __global__ void __launch_bounds__(THREADS + 32, MINB)
     k_cycle_tma(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
+  constexpr bool AGG = SCATTER == kScatterWarp;
+  constexpr bool COPIES = SCATTER == kScatterCopied;
   using TS = TileStage<Model, F>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned long long* sacc = reinterpret_cast<unsigned long long*>(smem_raw);
@@ -767,13 +770,20 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
   unsigned my_req = 0, my_exit = 0, my_move = 0, my_clamp = 0;
   unsigned my_err = 0;
 
+  // fields of the current scenario, kept in shared memory (written by
+  // thread 0 when the scenario changes) rather than in registers
+  __shared__ CycleScen<F> sr;
+
   auto flush = [&]() {
     consumer_sync(THREADS);
     const ScenDev& P = sc[cur];
     const unsigned n_ent = P.n_c * NA;
+    const unsigned copies = COPIES ? sr.rep_mask + 1u : 1u, cstride = sr.rep_stride;
     if (!aborted)
       for (unsigned e = tid; e < n_ent; e += THREADS) {
-        const long long p = (long long)sacc[e];
+        unsigned long long u = sacc[e];
+        for (unsigned c = 1; c < copies; ++c) u += sacc[e + c * cstride];
+        const long long p = (long long)u;
         if (p != 0) {
           atomicAdd(reinterpret_cast<unsigned long long*>(P.acc_hi + e), (unsigned long long)(p >> 32));
           atomicAdd(P.acc_lo + e, (unsigned long long)p & 0xffffffffull);
@@ -807,9 +817,6 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     my_err = 0u;
   };
 
-  // fields of the current scenario, kept in shared memory (written by
-  // thread 0 when the scenario changes) rather than in registers
-  __shared__ CycleScen<F> sr;
   for (unsigned k = 0;; ++k) {
     const unsigned stg = k % STAGES, use = k / STAGES;
     // every consumer agrees whether the stage arrived: if one wait gives up,
@@ -832,8 +839,17 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     const unsigned n_in = m.n_in;
     if (s != cur || since_flush + n_in > kFlushParticles) {
       if (cur >= 0) flush();
-      const unsigned n_ent = S.n_c * NA;
-      for (unsigned e = tid; e < n_ent; e += THREADS) sacc[e] = 0ull;
+      const bool copied = Model::separable && COPIES && S.n_c <= kScatterCopyMaxCompartments;
+      const unsigned n_zero = copied ? kAccCopies * scatter_stride(S.n_c) : S.n_c * NA;
+      // the copies must end before the stage buffers (a launch sized for one
+      // accumulator would have them overwrite tiles in flight): refuse
+      if constexpr (COPIES)
+        if ((size_t)n_zero * 8u > (size_t)(stages - smem_raw)) {
+          aborted = true;
+          my_err |= 32u;  // BMC_ERR_SMEM
+        }
+      if (!aborted)
+        for (unsigned e = tid; e < n_zero; e += THREADS) sacc[e] = 0ull;
       if (tid < 16) s_pf[tid] = (F)S.params[tid];
       cur = s;
       since_flush = 0;
@@ -850,6 +866,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.crec = reinterpret_cast<const F*>(S.crec);
         sr.mrow = S.mrow;
         sr.state = reinterpret_cast<F*>(S.state);
+        sr.rep_mask = copied ? kAccCopies - 1u : 0u;
+        sr.rep_stride = copied ? scatter_stride(S.n_c) : 0u;
       }
       consumer_sync(THREADS);
     }
@@ -897,7 +915,10 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
               qkey = p0;
               has_q = true;
             } else {
-              atomicAdd(&sacc[p0], (unsigned long long)q);
+              if constexpr (COPIES)
+                atomicAdd(&sacc[p0 + ((unsigned)lane & sr.rep_mask) * sr.rep_stride], (unsigned long long)q);
+              else
+                atomicAdd(&sacc[p0], (unsigned long long)q);
             }
           } else {
             F ctb[NC];
@@ -1406,21 +1427,23 @@ __global__ void k_flowmap(ScenDev* __restrict__ sc) {
 namespace kset {
 template <class Model, class F, int PPT, int THREADS, int MINB>
 void launch_cycle_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
-                    BatchCtl* b, bool tiny) {
+                    BatchCtl* b, int scatter) {
   (void)block;
-  if (tiny)
+  if (scatter == kScatterWarp)
     k_cycle<Model, F, PPT, THREADS, MINB, true><<<grid, THREADS, smem, st>>>(sc, n, b);
   else
     k_cycle<Model, F, PPT, THREADS, MINB, false><<<grid, THREADS, smem, st>>>(sc, n, b);
 }
 template <class Model, class F, int THREADS, int MINB, int STAGES>
 void launch_cycle_tma_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, const ScenDev* sc, int n,
-                        BatchCtl* b, bool tiny) {
+                        BatchCtl* b, int scatter) {
   (void)block;
-  if (tiny)
-    k_cycle_tma<Model, F, THREADS, MINB, STAGES, true><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+  if (scatter == kScatterWarp)
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterWarp><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+  else if (scatter == kScatterCopied)
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterCopied><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
   else
-    k_cycle_tma<Model, F, THREADS, MINB, STAGES, false><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterPlain><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
 }
 template <class Model, class F>
 void launch_liquid_t(int n_scen, unsigned grid_x, cudaStream_t st, ScenDev* sc, BatchCtl* b, int do_scalar) {
@@ -1470,9 +1493,15 @@ int setup_cycle_t(size_t smem, int* blocks_per_sm) {
 }
 template <class Model, class F, int THREADS, int MINB, int STAGES>
 int setup_cycle_tma_t(size_t smem, int* blocks_per_sm) {
-  return setup_pair(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, false>),
-                    reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, true>),
-                    THREADS + 32, smem, blocks_per_sm);
+  int b2 = 0;
+  int e = setup_pair(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterPlain>),
+                     reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterWarp>),
+                     THREADS + 32, smem, blocks_per_sm);
+  if (e) return e;
+  e = setup_fn(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterCopied>),
+               THREADS + 32, smem, &b2);
+  if (b2 < *blocks_per_sm) *blocks_per_sm = b2;
+  return e;
 }
 inline int last_error_t() { return (int)cudaGetLastError(); }
 template <class F>

@@ -15,7 +15,7 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 6;
+constexpr int kKernelSetAbi = 7;
 // Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
 // whole compartments per block, so a small domain still spreads over many SMs.
 constexpr unsigned kLiquidThreads = 32;
@@ -23,7 +23,12 @@ constexpr unsigned kLiquidThreads = 32;
 // The last argument selects the instantiation with the warp-aggregated
 // scatter, for launches whose domains all have at most
 // kAggregateMaxCompartments compartments.
-using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*, bool);
+// Scatter form of a cycle launch: plain shared-memory atomics; warp-aggregated
+// (every domain of the launch at most kAggregateMaxCompartments
+// compartments); accumulator copies (some domain of a separable model at most
+// kScatterCopyMaxCompartments compartments, tile-staging kernel only).
+enum ScatterForm : int { kScatterPlain = 0, kScatterWarp = 1, kScatterCopied = 2 };
+using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*, int scatter);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using InitLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, unsigned long long, uint32_t, uint32_t,
@@ -47,6 +52,19 @@ constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1, 4, 2};
 // accumulator plus stage buffers), else to register streaming 256 x 2.
 constexpr unsigned kVariantAuto = kCycleVariants;
 constexpr unsigned kAutoStaged = 6, kAutoStreamed = 1;
+// Domains of at most kScatterCopyMaxCompartments compartments (separable
+// models) scatter into kAccCopies copies of the shared accumulator in the
+// tile-staging kernel, lane l into copy l % kAccCopies: lanes of a warp
+// that hit the same compartment mostly hit different copies, so their
+// atomics stop serialising.  Copy stride: the compartment count rounded up to
+// 16 plus 16 / kAccCopies, so the copies of one compartment (8 bytes, two
+// banks each) sit in different banks.
+constexpr unsigned kAccCopies = 8;
+constexpr unsigned kScatterCopyMaxCompartments = 256;
+__host__ __device__ constexpr unsigned scatter_stride(unsigned n_c) {
+  return ((n_c + 15u) & ~15u) + 16u / kAccCopies;
+}
+
 // Compartments whose sources one k_plan block computes (grid y of k_plan:
 // ceil(n_compartments / kPlanSlice) slices; slice 0 also plans the step).
 constexpr unsigned kPlanSlice = 256;

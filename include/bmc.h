@@ -60,6 +60,7 @@ extern "C" {
 #define BMC_ERR_IDS 4u       /* particle id space (2^32) exhausted */
 #define BMC_ERR_COMPACT 8u   /* compaction lists disagree (internal) */
 #define BMC_ERR_TIMEOUT 16u  /* a bounded wait inside a kernel gave up (the step is void) */
+#define BMC_ERR_SMEM 32u     /* the launch's shared memory is smaller than the accumulator (internal; the step is void) */
 
 typedef struct bmc_scenario bmc_scenario;
 typedef struct bmc_batch bmc_batch;
