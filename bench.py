@@ -509,8 +509,9 @@ def batched_form(steps: int, n_scen: int = 256, scale: float = 1.0, shape=None, 
 def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):
     """Poisson arrivals for `window_s` seconds, sizes as the batched workload,
     steps log-uniform on [100, 10000]; all requests are served to completion."""
-    from bmc import serve
+    from bmc import _lib, serve
 
+    _lib.load()  # built and loaded before the arrival clock starts
     reqs = serve.poisson_requests(rate, window_s, seed=2027)
     srv = serve.Server(hbm_budget=budget)
     out = srv.serve(reqs)
