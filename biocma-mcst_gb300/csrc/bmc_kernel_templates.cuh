@@ -239,6 +239,18 @@ __device__ __forceinline__ long long quantize(float v, int e, unsigned& clamped,
 __device__ __forceinline__ uint32_t rec_move_thr(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ uint32_t rec_move_thr(double v) { return (uint32_t)__double_as_longlong(v); }
 
+// 32-byte read-only loads (one request per lane instead of two; the address
+// is 32-byte aligned: records start at multiples of 8 slots of an arena
+// aligned to 256 bytes).
+__device__ __forceinline__ void ldg_v8(const float* p, float (&v)[8]) {
+  asm volatile("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+               : "l"(p));
+}
+__device__ __forceinline__ void ldg_v4(const double* p, double (&v)[4]) {
+  asm volatile("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
+}
+
 // Loads the NU update rates and the move threshold of a compartment record
 // (slots 7 - NU .. 7) through the read-only path with the widest aligned
 // vector loads.
@@ -247,42 +259,43 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
   static_assert(NU >= 0 && NU <= 7, "at most 7 update rates");
   constexpr int s0 = 7 - NU;
   if constexpr (sizeof(F) == 4) {
-    // scalars up to slot 3, then one float4 (slots 4..7) or a float2 (6, 7)
     if constexpr (NU <= 1) {
+      // slots 6, 7
       const float2 a = __ldg(reinterpret_cast<const float2*>(p + 6));
       if constexpr (NU == 1) out[0] = a.x;
       return rec_move_thr(a.y);
-    } else if constexpr (NU == 2) {
-      out[0] = __ldg(p + 5);
-      const float2 a = __ldg(reinterpret_cast<const float2*>(p + 6));
-      out[1] = a.x;
-      return rec_move_thr(a.y);
     } else {
+      // the whole 32-byte record
+      float v[8];
+      ldg_v8(p, v);
 #pragma unroll
-      for (int q = s0; q < 4; ++q) out[q - s0] = __ldg(p + q);
-      const float4 a = __ldg(reinterpret_cast<const float4*>(p + 4));
-      out[4 - s0] = a.x;
-      out[5 - s0] = a.y;
-      out[6 - s0] = a.z;
-      return rec_move_thr(a.w);
+      for (int q = s0; q < 7; ++q) out[q - s0] = v[q];
+      return rec_move_thr(v[7]);
     }
   } else if constexpr (NU == 0) {
     return rec_move_thr(__ldg(p + 7));
+  } else if constexpr (NU == 1) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p + 6));
+    out[0] = a.x;
+    return rec_move_thr(a.y);
   } else {
-    // a scalar when the first slot is odd, then aligned pairs up to slot 7
-    if constexpr ((s0 & 1) != 0) out[0] = __ldg(p + s0);
-    constexpr int q0 = (s0 & 1) != 0 ? s0 + 1 : s0;
-    uint32_t thr = 0u;
+    // slots below 4: a scalar when the first is odd, then aligned pairs;
+    // slots 4..7 in one 32-byte load
+    if constexpr (s0 < 4) {
+      if constexpr ((s0 & 1) != 0) out[0] = __ldg(p + s0);
+      constexpr int q0 = (s0 & 1) != 0 ? s0 + 1 : s0;
 #pragma unroll
-    for (int q = q0; q < 8; q += 2) {
-      const double2 a = __ldg(reinterpret_cast<const double2*>(p + q));
-      out[q - s0] = a.x;
-      if (q + 1 < 7)
+      for (int q = q0; q < 4; q += 2) {
+        const double2 a = __ldg(reinterpret_cast<const double2*>(p + q));
+        out[q - s0] = a.x;
         out[q + 1 - s0] = a.y;
-      else
-        thr = rec_move_thr(a.y);
+      }
     }
-    return thr;
+    double v[4];
+    ldg_v4(p + 4, v);
+#pragma unroll
+    for (int q = (s0 > 4 ? s0 : 4); q < 7; ++q) out[q - s0] = v[q - 4];
+    return rec_move_thr(v[3]);
   }
 }
 
