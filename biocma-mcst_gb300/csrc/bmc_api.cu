@@ -699,6 +699,8 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     Carver cv;
     int2* p_mrow = nullptr;
     cv.add(&p_mrow, (size_t)n_c * K);
+    int32_t* p_thr8 = nullptr;
+    cv.add(&p_thr8, (size_t)n_c * 8);
     double* p_vol = nullptr;
     cv.add(&p_vol, n_c);
     double* p_out = nullptr;
@@ -717,6 +719,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     BMC_CUDA(cudaMalloc(&s->darena, cv.off));
     cv.bind(s->darena);
     h.mrow = p_mrow;
+    h.mthr8 = p_thr8;
     h.volume = p_vol;
     h.out_flow = p_out;
     h.diag = p_diag;
@@ -731,6 +734,14 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.volume), vol.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<int2*>(h.mrow), mrow.data(), mrow.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
+  {
+    // the rows' thresholds, 8 slots a compartment, padded with INT32_MAX
+    std::vector<int32_t> thr8((size_t)n_c * 8, INT32_MAX);
+    for (size_t i = 0; i < n_c; ++i)
+      for (size_t k = 0; k < K && k < 8; ++k) thr8[i * 8 + k] = mrow[i * K + k].x;
+    BMC_CUDA(counted_memcpy_async(const_cast<int32_t*>(h.mthr8), thr8.data(), thr8.size() * sizeof(int32_t),
+                                  cudaMemcpyHostToDevice, s->stream));
+  }
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.vinv), vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   if (!s->has_transition)
     BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.diag), diag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));

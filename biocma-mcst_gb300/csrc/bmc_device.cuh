@@ -104,6 +104,9 @@ struct ScenDev {
   uint32_t tile_base;  // first global tile of this scenario in its batch
   // domain
   const int2* mrow;
+  // [n_c][8] the thresholds of mrow's rows (K <= 8), padded with INT32_MAX:
+  // one 32-byte load gives a row's answer as a count
+  const int32_t* mthr8;
   const double* volume;
   const double* out_flow;
   const uint32_t* in_ptr;

@@ -247,6 +247,11 @@ __device__ __forceinline__ void ldg_v8(const float* p, float (&v)[8]) {
                : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
                : "l"(p));
 }
+__device__ __forceinline__ void ldg_v8(const int32_t* p, int (&v)[8]) {
+  asm volatile("ld.global.nc.v8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+               : "l"(p));
+}
 __device__ __forceinline__ void ldg_v4(const double* p, double (&v)[4]) {
   asm volatile("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
 }
@@ -297,6 +302,38 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
     for (int q = (s0 > 4 ? s0 : 4); q < 7; ++q) out[q - s0] = v[q - 4];
     return rec_move_thr(v[3]);
   }
+}
+
+// Next compartment of a leaving particle: the first k of the row with
+// x1 <= floor(2^24 CDF(k)) (K - 1 when none), the answer of the reference's
+// bisection (move_kernel.hpp L89-L101).  Rows of up to 8 entries: one
+// 32-byte load of the padded thresholds, the answer is the count of those
+// below x1 (thresholds are non-decreasing), then the neighbour; longer rows:
+// the bisection over {threshold, neighbour} pairs.
+__device__ __forceinline__ int next_compartment(const int2* __restrict__ mrow, const int32_t* __restrict__ thr8,
+                                                unsigned p0, unsigned K, int x1) {
+  const int2* row = mrow + (size_t)p0 * K;
+  if (K <= 8u) {
+    int t[8];
+    ldg_v8(thr8 + (size_t)p0 * 8, t);
+    unsigned below = 0u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) below += t[k] < x1 ? 1u : 0u;
+    return __ldg(row + min(below, K - 1u)).y;
+  }
+  int nb = __ldg(row + (K - 1)).y;
+  int left = 0, right = (int)K - 1;
+  while (left < right) {
+    const int mid = (left + right) >> 1;
+    const int2 pm = __ldg(row + mid);
+    if (x1 > pm.x) {
+      left = mid + 1;
+    } else {
+      right = mid;
+      nb = pm.y;
+    }
+  }
+  return nb;
 }
 
 // ---------------------------------------------------------------------------
@@ -518,25 +555,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             uint32_t p = p0;
             if (do_move) {
               if (draw_int(r[0]) < mthr) {
-                // the reference's bisection (move_kernel.hpp L89-L101) over the
-                // {threshold, neighbour} pairs of the row; the neighbour of the
-                // answer comes with the probe that set `right`, or with the
-                // last pair, loaded ahead
-                const int x1 = (int)draw_int(r[1]);
-                const int2* row = mrow + (size_t)p0 * K;
-                int nb = __ldg(row + (K - 1)).y;
-                int left = 0, right = (int)K - 1;
-                while (left < right) {
-                  const int mid = (left + right) >> 1;
-                  const int2 pm = __ldg(row + mid);
-                  if (x1 > pm.x) {
-                    left = mid + 1;
-                  } else {
-                    right = mid;
-                    nb = pm.y;
-                  }
-                }
-                p = (uint32_t)nb;
+                p = (uint32_t)next_compartment(mrow, S.mthr8, p0, K, (int)draw_int(r[1]));
                 ++my_move;
               }
               pv[k] = p;
@@ -625,6 +644,7 @@ struct CycleScen {
   unsigned long long seed, cap;
   const F* crec;
   const int2* mrow;
+  const int32_t* mthr8;
   F* state;
   unsigned n_c, K, step, n_out;
   F dtF;
@@ -878,6 +898,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.qe0 = S.q_exp[0];
         sr.crec = reinterpret_cast<const F*>(S.crec);
         sr.mrow = S.mrow;
+        sr.mthr8 = S.mthr8;
         sr.state = reinterpret_cast<F*>(S.state);
         sr.rep_mask = copied ? kAccCopies - 1u : 0u;
         sr.rep_stride = copied ? scatter_stride(S.n_c) : 0u;
@@ -953,22 +974,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           uint32_t p = p0;
           if ((sr.n_c > 1u)) {
             if (draw_int(rd[0]) < mthr) {
-              // bisection of move_kernel.hpp L89-L101 over {threshold, neighbour}
-              const int x1 = (int)draw_int(rd[1]);
-              const int2* row = sr.mrow + (size_t)p0 * sr.K;
-              int nb = __ldg(row + (sr.K - 1)).y;
-              int left = 0, right = (int)sr.K - 1;
-              while (left < right) {
-                const int mid = (left + right) >> 1;
-                const int2 pm = __ldg(row + mid);
-                if (x1 > pm.x) {
-                  left = mid + 1;
-                } else {
-                  right = mid;
-                  nb = pm.y;
-                }
-              }
-              p = (uint32_t)nb;
+              p = (uint32_t)next_compartment(sr.mrow, sr.mthr8, p0, sr.K, (int)draw_int(rd[1]));
               ++my_move;
             }
             __stcs(S.pos + gi, p);
@@ -1424,6 +1430,10 @@ __global__ void k_flowmap(ScenDev* __restrict__ sc) {
       rec[(size_t)c * 8 + 7] = __longlong_as_double((long long)t);
   }
   for (size_t e = t0; e < (size_t)n_c * K; e += stride) const_cast<int2*>(S.mrow)[e] = S.map_mrow[o * K + e];
+  for (size_t e = t0; e < (size_t)n_c * 8; e += stride) {
+    const unsigned k = (unsigned)(e & 7u);
+    const_cast<int32_t*>(S.mthr8)[e] = k < K ? S.map_mrow[o * K + (e >> 3) * K + k].x : INT32_MAX;
+  }
   const uint32_t* ptr = S.map_in_ptr + (size_t)m * (n_c + 1);
   for (unsigned c = t0; c <= n_c; c += stride) const_cast<uint32_t*>(S.in_ptr)[c] = ptr[c];
   const unsigned nnz = ptr[n_c];

@@ -15,7 +15,7 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 7;
+constexpr int kKernelSetAbi = 8;
 // Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
 // whole compartments per block, so a small domain still spreads over many SMs.
 constexpr unsigned kLiquidThreads = 32;
