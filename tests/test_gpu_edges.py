@@ -78,12 +78,14 @@ def complete_graph(n_c=13, seed=5):
 
 
 @pytest.mark.parametrize("shape", [None, (256, 2, 0)])
-def test_long_neighbour_rows(oracle_mod, shape):
-    """Every compartment connected to all others: rows of 12 entries."""
+@pytest.mark.parametrize("n_c", [9, 10, 13])
+def test_long_neighbour_rows(oracle_mod, shape, n_c):
+    """Every compartment connected to all others: rows of 8 entries (the
+    longest the threshold count covers), 9 and 12 (the bisection)."""
     from test_gpu_parity import make_pair
 
-    net = complete_graph()
-    assert net.K == 12
+    net = complete_graph(n_c)
+    assert net.K == n_c - 1
     sc = scenarios.small_ring(8000, feeds=True)
     sc.net = net
     sc.c0 = np.full((net.n_c, 1), 5.0)
@@ -91,7 +93,7 @@ def test_long_neighbour_rows(oracle_mod, shape):
     g, o = make_pair(oracle_mod, sc)
     if shape:
         g.set_shape(*shape)
-    _parity(g, o, 6, "K=12")
+    _parity(g, o, 6, f"K={net.K}")
 
 
 def test_automatic_shape_on_a_domain_too_large_for_tile_staging(oracle_mod):
