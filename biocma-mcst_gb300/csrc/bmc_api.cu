@@ -699,8 +699,8 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     Carver cv;
     int2* p_mrow = nullptr;
     cv.add(&p_mrow, (size_t)n_c * K);
-    int32_t* p_thr8 = nullptr;
-    cv.add(&p_thr8, (size_t)n_c * 8);
+    int32_t* p_row16 = nullptr;
+    cv.add(&p_row16, (size_t)n_c * 16);
     double* p_vol = nullptr;
     cv.add(&p_vol, n_c);
     double* p_out = nullptr;
@@ -719,7 +719,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     BMC_CUDA(cudaMalloc(&s->darena, cv.off));
     cv.bind(s->darena);
     h.mrow = p_mrow;
-    h.mthr8 = p_thr8;
+    h.mrow16 = p_row16;
     h.volume = p_vol;
     h.out_flow = p_out;
     h.diag = p_diag;
@@ -735,11 +735,15 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.out_flow), outf.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
   BMC_CUDA(counted_memcpy_async(const_cast<int2*>(h.mrow), mrow.data(), mrow.size() * sizeof(int2), cudaMemcpyHostToDevice, s->stream));
   {
-    // the rows' thresholds, 8 slots a compartment, padded with INT32_MAX
-    std::vector<int32_t> thr8((size_t)n_c * 8, INT32_MAX);
+    // rows of up to 8 entries: thresholds (padded with INT32_MAX) then
+    // neighbours (padded with the last), 16 slots a compartment
+    std::vector<int32_t> row16((size_t)n_c * 16, INT32_MAX);
     for (size_t i = 0; i < n_c; ++i)
-      for (size_t k = 0; k < K && k < 8; ++k) thr8[i * 8 + k] = mrow[i * K + k].x;
-    BMC_CUDA(counted_memcpy_async(const_cast<int32_t*>(h.mthr8), thr8.data(), thr8.size() * sizeof(int32_t),
+      for (size_t k = 0; k < 8; ++k) {
+        if (k < K) row16[i * 16 + k] = mrow[i * K + k].x;
+        row16[i * 16 + 8 + k] = mrow[i * K + std::min<size_t>(k, K - 1)].y;
+      }
+    BMC_CUDA(counted_memcpy_async(const_cast<int32_t*>(h.mrow16), row16.data(), row16.size() * sizeof(int32_t),
                                   cudaMemcpyHostToDevice, s->stream));
   }
   BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.vinv), vinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));

@@ -104,9 +104,10 @@ struct ScenDev {
   uint32_t tile_base;  // first global tile of this scenario in its batch
   // domain
   const int2* mrow;
-  // [n_c][8] the thresholds of mrow's rows (K <= 8), padded with INT32_MAX:
-  // one 32-byte load gives a row's answer as a count
-  const int32_t* mthr8;
+  // [n_c][16] rows of up to 8 entries: thresholds of mrow in slots 0..7
+  // (padded with INT32_MAX), neighbours in slots 8..15 (padded with the last
+  // one); two independent 32-byte loads give a row's answer
+  const int32_t* mrow16;
   const double* volume;
   const double* out_flow;
   const uint32_t* in_ptr;

@@ -306,20 +306,24 @@ __device__ __forceinline__ uint32_t load_rec(const F* p, F* out) {
 
 // Next compartment of a leaving particle: the first k of the row with
 // x1 <= floor(2^24 CDF(k)) (K - 1 when none), the answer of the reference's
-// bisection (move_kernel.hpp L89-L101).  Rows of up to 8 entries: one
-// 32-byte load of the padded thresholds, the answer is the count of those
-// below x1 (thresholds are non-decreasing), then the neighbour; longer rows:
-// the bisection over {threshold, neighbour} pairs.
-__device__ __forceinline__ int next_compartment(const int2* __restrict__ mrow, const int32_t* __restrict__ thr8,
+// bisection (move_kernel.hpp L89-L101).  Rows of up to 8 entries: two
+// independent 32-byte loads of the padded thresholds and neighbours; the
+// answer is the count of thresholds below x1 (they are non-decreasing);
+// longer rows: the bisection over {threshold, neighbour} pairs.
+__device__ __forceinline__ int next_compartment(const int2* __restrict__ mrow, const int32_t* __restrict__ row16,
                                                 unsigned p0, unsigned K, int x1) {
   const int2* row = mrow + (size_t)p0 * K;
   if (K <= 8u) {
-    int t[8];
-    ldg_v8(thr8 + (size_t)p0 * 8, t);
+    int t[8], n[8];
+    ldg_v8(row16 + (size_t)p0 * 16, t);
+    ldg_v8(row16 + (size_t)p0 * 16 + 8, n);
     unsigned below = 0u;
 #pragma unroll
     for (int k = 0; k < 8; ++k) below += t[k] < x1 ? 1u : 0u;
-    return __ldg(row + min(below, K - 1u)).y;
+    int nb = n[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) nb = below >= (unsigned)k ? n[k] : nb;
+    return nb;
   }
   int nb = __ldg(row + (K - 1)).y;
   int left = 0, right = (int)K - 1;
@@ -555,7 +559,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             uint32_t p = p0;
             if (do_move) {
               if (draw_int(r[0]) < mthr) {
-                p = (uint32_t)next_compartment(mrow, S.mthr8, p0, K, (int)draw_int(r[1]));
+                p = (uint32_t)next_compartment(mrow, S.mrow16, p0, K, (int)draw_int(r[1]));
                 ++my_move;
               }
               pv[k] = p;
@@ -644,7 +648,7 @@ struct CycleScen {
   unsigned long long seed, cap;
   const F* crec;
   const int2* mrow;
-  const int32_t* mthr8;
+  const int32_t* mrow16;
   F* state;
   unsigned n_c, K, step, n_out;
   F dtF;
@@ -898,7 +902,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.qe0 = S.q_exp[0];
         sr.crec = reinterpret_cast<const F*>(S.crec);
         sr.mrow = S.mrow;
-        sr.mthr8 = S.mthr8;
+        sr.mrow16 = S.mrow16;
         sr.state = reinterpret_cast<F*>(S.state);
         sr.rep_mask = copied ? kAccCopies - 1u : 0u;
         sr.rep_stride = copied ? scatter_stride(S.n_c) : 0u;
@@ -974,7 +978,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           uint32_t p = p0;
           if ((sr.n_c > 1u)) {
             if (draw_int(rd[0]) < mthr) {
-              p = (uint32_t)next_compartment(sr.mrow, sr.mthr8, p0, sr.K, (int)draw_int(rd[1]));
+              p = (uint32_t)next_compartment(sr.mrow, sr.mrow16, p0, sr.K, (int)draw_int(rd[1]));
               ++my_move;
             }
             __stcs(S.pos + gi, p);
@@ -1432,7 +1436,11 @@ __global__ void k_flowmap(ScenDev* __restrict__ sc) {
   for (size_t e = t0; e < (size_t)n_c * K; e += stride) const_cast<int2*>(S.mrow)[e] = S.map_mrow[o * K + e];
   for (size_t e = t0; e < (size_t)n_c * 8; e += stride) {
     const unsigned k = (unsigned)(e & 7u);
-    const_cast<int32_t*>(S.mthr8)[e] = k < K ? S.map_mrow[o * K + (e >> 3) * K + k].x : INT32_MAX;
+    const size_t c = e >> 3;
+    const int2* row = S.map_mrow + o * K + c * K;
+    int32_t* r16 = const_cast<int32_t*>(S.mrow16) + c * 16;
+    r16[k] = k < K ? row[k].x : INT32_MAX;
+    r16[8 + k] = row[k < K ? k : K - 1].y;
   }
   const uint32_t* ptr = S.map_in_ptr + (size_t)m * (n_c + 1);
   for (unsigned c = t0; c <= n_c; c += stride) const_cast<uint32_t*>(S.in_ptr)[c] = ptr[c];
