@@ -537,7 +537,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 qv[k] = q;
                 has_q[k] = true;
               } else {
-                atomicAdd(&sacc[p0], (unsigned long long)q);
+                acc_add(&sacc[p0], q);
               }
             } else {
               F ctb[NC];
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
               for (int j = 0; j < NC; ++j) {
                 const double val = __dmul_rn(S.weight, (double)ctb[j]);
                 const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
-                atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
+                acc_add(&sacc[p0 * NC + j], q);
               }
             }
 #pragma unroll
@@ -954,9 +954,9 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
               has_q = true;
             } else {
               if constexpr (COPIES)
-                atomicAdd(&sacc[p0 + ((unsigned)lane & sr.rep_mask) * sr.rep_stride], (unsigned long long)q);
+                acc_add(&sacc[p0 + ((unsigned)lane & sr.rep_mask) * sr.rep_stride], q);
               else
-                atomicAdd(&sacc[p0], (unsigned long long)q);
+                acc_add(&sacc[p0], q);
             }
           } else {
             F ctb[NC];
@@ -965,7 +965,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             for (int j = 0; j < NC; ++j) {
               const double val = __dmul_rn(S.weight, (double)ctb[j]);
               const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
-              atomicAdd(&sacc[p0 * NC + j], (unsigned long long)q);
+              acc_add(&sacc[p0 * NC + j], q);
             }
           }
 #pragma unroll
