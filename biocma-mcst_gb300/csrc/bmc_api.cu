@@ -1793,6 +1793,23 @@ int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t ste
   return BMC_OK;
 }
 
+int bmc_debug_wait(uint64_t limit_ns, int32_t arrive, uint32_t* error_word, uint64_t* waited_ns) {
+  if (!error_word || !waited_ns) return fail(BMC_E_INVALID, "null argument");
+  if (limit_ns > 2000000000ull) return fail(BMC_E_INVALID, "limit above the kernels' own 2 s");
+  unsigned long long* d = nullptr;
+  BMC_CUDA(cudaMalloc(&d, 16));
+  bmc::launch_debug_wait(0, limit_ns, arrive, d);
+  g_launches++;
+  unsigned long long h[2] = {0ull, 0ull};
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = counted_memcpy(h, d, 16, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug wait: ") + cudaGetErrorString(e));
+  *error_word = (uint32_t)h[0];
+  *waited_ns = h[1];
+  return BMC_OK;
+}
+
 }  // extern "C"
 
 // ---- runtime-loaded cell models ------------------------------------------------

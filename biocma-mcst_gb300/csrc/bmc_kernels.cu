@@ -27,6 +27,25 @@ __global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restric
   }
 }
 
+// Self-test of the bounded wait the cycle kernels use on their mbarriers:
+// one thread waits on phase 0 of a barrier expecting one arrival, which it
+// makes first (`arrive` != 0: the wait succeeds) or that nothing makes (the
+// wait gives up after limit_ns).  out[0]: BMC_ERR_TIMEOUT (16) when the wait
+// gave up, else 0; out[1]: nanoseconds waited.
+__global__ void k_debug_wait(unsigned long long limit_ns, int arrive, unsigned long long* out) {
+  __shared__ unsigned long long bar;
+  __shared__ unsigned abort_word;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1u);
+  abort_word = 0u;
+  fence_barrier_init();
+  if (arrive) mbar_arrive(&bar);
+  const unsigned long long t0 = global_ns();
+  const bool ok = mbar_wait_for(&bar, 0u, &abort_word, limit_ns);
+  out[0] = ok ? 0ull : 16ull;
+  out[1] = global_ns() - t0;
+}
+
 // Built-in kernel sets, one translation unit per model (compiled in
 // parallel): bmc_sets_monod.cu, bmc_sets_overflow.cu, bmc_sets_fixed.cu.
 const KernelSet* kernel_set(int model, int f64) {
@@ -45,6 +64,9 @@ const KernelSet* kernel_set(int model, int f64) {
 
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid) {
   k_repartition<<<grid, 256, 0, st>>>(sc, counts);
+}
+void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive, unsigned long long* out) {
+  k_debug_wait<<<1, 32, 0, st>>>(limit_ns, arrive, out);
 }
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out) {

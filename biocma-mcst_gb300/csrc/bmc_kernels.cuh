@@ -281,19 +281,23 @@ __device__ __forceinline__ unsigned long long global_ns() {
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
-// Waits for phase `parity` of the barrier.  Returns false on time-out or
-// when *abort is set (by another thread of the block).
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
-                                                  volatile unsigned* abort) {
+// Waits for phase `parity` of the barrier.  Returns false after limit_ns of
+// wall time or when *abort is set (by another thread of the block).
+__device__ __forceinline__ bool mbar_wait_for(unsigned long long* bar, unsigned parity, volatile unsigned* abort,
+                                              unsigned long long limit_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = global_ns();
   for (unsigned it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 255u) == 0u) {
       if (*abort) return false;
-      if (global_ns() - t0 > kWaitNs) return false;
+      if (global_ns() - t0 > limit_ns) return false;
     }
   }
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  volatile unsigned* abort) {
+  return mbar_wait_for(bar, parity, abort, kWaitNs);
 }
 // Global -> shared bulk copy of `bytes` (a multiple of 16; both addresses
 // 16-byte aligned) completing on `bar` (transaction bytes).

@@ -429,6 +429,13 @@ int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* ou
  * computed on the device (checks the draw source against the oracle). */
 int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step,
                     uint32_t purpose, float* out);
+/* Self-test of the bounded barrier wait of the cycle kernels: one thread
+ * waits on an mbarrier whose single arrival it makes first (arrive != 0) or
+ * that nothing makes; in the second case the wait gives up after limit_ns
+ * (at most 2 s) and *error_word = BMC_ERR_TIMEOUT, the bit a cycle kernel
+ * sets in the step's error word when a tile copy never lands.  *waited_ns:
+ * device time spent in the wait. */
+int bmc_debug_wait(uint64_t limit_ns, int32_t arrive, uint32_t* error_word, uint64_t* waited_ns);
 /* One main-loop iteration like bmc_step, with CUDA events recorded on the
  * scenario's stream between its six kernels; kernel_ms[0..5] receive the
  * durations of: liquid step, cycle, plan, divide, compact, merge.

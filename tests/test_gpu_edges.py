@@ -196,3 +196,23 @@ def test_step_read_equals_step_then_read_liquid():
         assert np.array_equal(c1.view(np.uint64), conc.view(np.uint64)), k
     with pytest.raises(ValueError):
         g2.step_read(np.zeros(3))
+
+
+def test_bounded_wait_gives_up_with_the_timeout_bit():
+    """The bounded mbarrier wait of the cycle kernels, on a barrier nothing
+    completes, returns after its limit with BMC_ERR_TIMEOUT; the context
+    stays usable (a wait that is satisfied returns at once)."""
+    from bmc import _lib
+
+    L = _lib.load()
+    err, ns = ct.c_uint32(), ct.c_uint64()
+    assert L.bmc_debug_wait(ct.c_uint64(50_000_000), 0, ct.byref(err), ct.byref(ns)) == 0
+    assert err.value == 16  # BMC_ERR_TIMEOUT
+    assert 50_000_000 <= ns.value < 1_000_000_000
+    assert L.bmc_debug_wait(ct.c_uint64(50_000_000), 1, ct.byref(err), ct.byref(ns)) == 0
+    assert err.value == 0 and ns.value < 50_000_000
+    # a scenario still steps afterwards
+    from bmc.sim import GpuScenario
+
+    g = GpuScenario(scenarios.small_ring(2000, feeds=True))
+    assert g.step()["error"] == 0
