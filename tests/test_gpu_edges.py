@@ -216,3 +216,14 @@ def test_bounded_wait_gives_up_with_the_timeout_bit():
 
     g = GpuScenario(scenarios.small_ring(2000, feeds=True))
     assert g.step()["error"] == 0
+
+
+@pytest.mark.parametrize("n_c", [4, 5, 256, 257])
+def test_scatter_forms_at_their_boundaries(oracle_mod, n_c):
+    """Domains of 4 compartments (warp-aggregated scatter), 5 and 256
+    (accumulator copies) and 257 (one accumulator): the same sums."""
+    from test_gpu_parity import make_pair
+
+    sc = scenarios.small_ring(6000, n_c=n_c, feeds=True, model=scenarios.overflow(f64=True))
+    g, o = make_pair(oracle_mod, sc)
+    _parity(g, o, 4, f"n_c={n_c}")
