@@ -18,8 +18,8 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 CSRC = os.path.join(PKG, "csrc")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libbmc.so")
-SOURCES = ["bmc_sets_monod.cu", "bmc_sets_overflow.cu", "bmc_sets_fixed.cu", "bmc_kernels.cu", "bmc_api.cu",
-           "bmc_cma.cpp"]
+SOURCES = ["bmc_sets_monod.cu", "bmc_sets_overflow.cu", "bmc_sets_fixed.cu", "bmc_sets_acetate.cu",
+           "bmc_kernels.cu", "bmc_api.cu", "bmc_cma.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off"]

@@ -17,6 +17,7 @@ MODEL_MONOD = 1
 MODEL_OVERFLOW = 2
 MODEL_FIXED_LENGTH = 3
 MODEL_FIXED_LENGTH_GENERAL = 4
+MODEL_SIMPLE_ACETATE = 5
 
 MU_MAX = 0.77 / 3600.0  # 1/s
 
@@ -75,6 +76,21 @@ def fixed_length(general: bool = False) -> ModelSpec:
                          np.array([4.0 * phi]), separable=False)
     # contribution = -phi_s(C) per particle: basis 1
     return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([1.0]))
+
+
+def simple_acetate() -> ModelSpec:
+    """The reference's SimpleAcetate model: float state of 9 variables
+    (length, l_max, a_p, a_max, a_e, a_e_s, a_e_a, phi_s, phi_a), glucose and
+    acetate, two contributions per particle (general path), log-normal and
+    truncated-normal draws at division."""
+    a_max = np.float32(2e-6 / 3600.0)
+    d_m = np.float32(0.6e-6)
+    lin = np.float32(1000) * np.float32(math.pi) * d_m * d_m / np.float32(4.0)
+    # |phi_s| <= a_max * lin * y_s, |phi_a| <= a_max * lin * max(1, y_s / y_a)
+    bound = 4.0 * float(a_max) * float(lin) * 2.0
+    p = np.zeros(16)
+    return ModelSpec("simple_acetate", MODEL_SIMPLE_ACETATE, 9, 2, False, p, np.array([bound, bound]),
+                     separable=False, read_vars=4)
 
 
 @dataclass

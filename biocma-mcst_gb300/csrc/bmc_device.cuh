@@ -27,7 +27,7 @@ namespace bmc {
 
 constexpr int kMaxOutlets = 8;
 constexpr int kMaxSpecies = 8;
-constexpr int kMaxVar = 8;
+constexpr int kMaxVar = 16;
 constexpr int kMaxRates = 8;
 constexpr long long kQMax = 1LL << 42;  // |quantised value| bound
 // A block flushes its shared-memory accumulator before it has summed more
@@ -458,6 +458,217 @@ struct FixedLengthModelT {
     const float l_min_m = l_max_m / (float)2.;
     x[0] = l_min_m + (l_max_m - l_min_m) * d[1];
     x[1] = l_max_m;
+  }
+  __device__ __forceinline__ static double mass(const float* x, const double* p) {
+    (void)p;
+    return (double)(x[0] * lin_density());
+  }
+};
+
+
+// ---------------------------------------------------------------------------
+// Elementary functions for the model draws, written out with IEEE basic
+// operations only (no fused multiply-add under --fmad=false), so the CPU
+// restatement, which writes the same steps in C, rounds identically.
+//   log: x = m 2^e, m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(t),
+//        t = (m - 1) / (m + 1), odd series to t^27 (|t| <= 0.172)
+//   exp: x = k ln2 + r (Cody-Waite split of ln2, |r| <= ln2 / 2), Taylor
+//        series of e^r to r^20, times 2^k
+namespace sa_math {
+constexpr double kLn2Hi = 6.93147180369123816490e-01;  // upper bits of ln 2
+constexpr double kLn2Lo = 1.90821492927058770002e-10;  // ln 2 - kLn2Hi
+constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kSqrt2 = 1.41421356237309504880;
+constexpr double kPi = 3.14159265358979323846;
+
+__device__ __forceinline__ double scale2(double v, int k) {
+  // v * 2^k by exact powers of two (k within [-2044, 2046])
+  while (k > 1000) {
+    v *= 0x1p1000;
+    k -= 1000;
+  }
+  while (k < -1000) {
+    v *= 0x1p-1000;
+    k += 1000;
+  }
+  return v * __longlong_as_double((long long)(1023 + k) << 52);
+}
+
+__device__ __forceinline__ double log_d(double x) {
+  if (x != x || x < 0.0) return __longlong_as_double(0x7ff8000000000000ll);
+  if (x == 0.0) return __longlong_as_double((long long)0xfff0000000000000ull);
+  if (x == __longlong_as_double(0x7ff0000000000000ll)) return x;
+  int e = 0;
+  if (x < 0x1p-1022) {  // subnormal: scale into the normal range
+    x *= 0x1p54;
+    e = -54;
+  }
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  e += (int)((b >> 52) & 0x7ffull) - 1022;
+  double m = __longlong_as_double((long long)((b & 0x000fffffffffffffull) | 0x3fe0000000000000ull));  // [0.5, 1)
+  if (m < 0.70710678118654752440) {
+    m = m * 2.0;
+    e -= 1;
+  }
+  const double t = (m - 1.0) / (m + 1.0);
+  const double t2 = t * t;
+  double sum = 1.0 / 27.0;
+  for (int k = 25; k >= 1; k -= 2) sum = sum * t2 + 1.0 / (double)k;
+  return ((double)e * kLn2Hi + 2.0 * t * sum) + (double)e * kLn2Lo;
+}
+
+__device__ __forceinline__ double exp_d(double x) {
+  if (x != x) return x;
+  if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000ll);
+  if (x < -745.1332191019412) return 0.0;
+  const double k = floor(x / kLn2 + 0.5);
+  const double r = (x - k * kLn2Hi) - k * kLn2Lo;
+  double s = 1.0;
+  for (int n = 20; n >= 1; --n) s = 1.0 + s * r / (double)n;
+  return scale2(s, (int)k);
+}
+
+// Winitzki's approximation of erfinv (a = 0.147), with the reference's
+// type flow (prng_extension.hpp L79-L94): the logarithm in double, the
+// terms and square roots in the distribution's type.
+__device__ __forceinline__ float erfinv_f(float x) {
+  const float a = 0.147f;
+  const float inv_a = (float)(1. / (double)a);
+  const float tmp = (float)(2 / (kPi * (double)a));
+  const double ln1mx2 = log_d((1. - (double)x) * (1. + (double)x));
+  const float term1 = (float)((double)tmp + 0.5 * ln1mx2);
+  const float term2 = (float)((double)inv_a * ln1mx2);
+  return copysignf(sqrtf(sqrtf(term1 * term1 - term2) - term1), x);
+}
+__device__ __forceinline__ double erfinv_d(double x) {
+  const double a = 0.147;
+  const double inv_a = 1. / a;
+  const double tmp = 2 / (kPi * a);
+  const double ln1mx2 = log_d((1. - x) * (1. + x));
+  const double term1 = tmp + 0.5 * ln1mx2;
+  const double term2 = inv_a * ln1mx2;
+  return copysign(sqrt(sqrt(term1 * term1 - term2) - term1), x);
+}
+// norminv (prng_extension.hpp L137-L147): mean + sd sqrt2 clamp(erfinv(2p - 1), -5, 5)
+__device__ __forceinline__ float norminv_f(float p, float mean, float sd) {
+  const float z = fminf(fmaxf(erfinv_f(2.f * p - 1.f), -5.f), 5.f);
+  return (float)((double)mean + (double)sd * kSqrt2 * (double)z);
+}
+__device__ __forceinline__ double norminv_d(double p, double mean, double sd) {
+  const double z = fmin(fmax(erfinv_d(2. * p - 1.), -5.), 5.);
+  return mean + sd * kSqrt2 * z;
+}
+// TruncatedNormal draw (prng_extension.hpp L379-L414) from the uniform u,
+// with the distribution's 0.5 erfc(-z / sqrt2) at its bounds given
+__device__ __forceinline__ float truncnorm_f(float u, float mu, float sd, float pl, float pu) {
+  const float p = u * (pu - pl) + pl;
+  return norminv_f(p, mu, sd);
+}
+}  // namespace sa_math
+
+// The reference's SimpleAcetate model (apps/libs/models/public/models/
+// simple_acetate.hpp L26-L250): float state {length, l_max, a_p, a_max,
+// a_e, a_e_s, a_e_a, phi_s, phi_a}, two species (glucose, acetate), two
+// contributions per particle (general path).  Per compartment: the uptake
+// saturations g_j = c_j / (c_j + k_j), in double, rounded to float once (the
+// reference rounds 1 / (c_j + k_j) to float and multiplies by c_j in double
+// per particle).  Division draws: two log-normal uptake capacities a_p and
+// two truncated-normal l_max; init: length and l_max from the length
+// distribution (the reference's init draws l_max from l_dist too).  The
+// normal draws are inverse-CDF draws with the reference's erfinv (one
+// uniform each; the reference's log-normal draws a Kokkos normal).
+struct SimpleAcetateModel {
+  static constexpr int n_var = 9;
+  static constexpr int n_ctb = 2;
+  static constexpr int n_rates = 2;
+  static constexpr int n_upd = 2;
+  static constexpr int model_id = 5;
+  static constexpr bool separable = false;
+  static constexpr unsigned read_mask = 0xFu;  // length, l_max, a_p, a_max
+  __device__ __forceinline__ static float a_max_m() { return (float)(2e-6 / 3600.); }
+  __device__ __forceinline__ static float l_max_m() { return (float)2e-6; }
+  __device__ __forceinline__ static float lin_density() {
+    const float d_m = (float)0.6e-6;
+    return (float)1000 * (float)3.14159265358979323846 * d_m * d_m / (float)4.;
+  }
+  // r = {g_s, g_a}
+  __device__ __forceinline__ static void rates(const double* c, const double* p, float* r) {
+    (void)p;
+    const double k_s = (double)(float)1e-3, k_a = (double)(float)1e-4;
+    r[0] = (float)(c[0] / (c[0] + k_s));
+    r[1] = (float)(c[1] / (c[1] + k_a));
+  }
+  __device__ __forceinline__ static int update(float dt, float* x, const float* r, float& basis, const float* pf) {
+    float ctb[2];
+    (void)basis;
+    return update_general(dt, x, r, ctb, pf);
+  }
+  __device__ __forceinline__ static int update_general(float dt, float* x, const float* r, float* ctb,
+                                                       const float* pf) {
+    (void)pf;
+    const float y_s = 2.f, y_a = 3.f;
+    const float lin = lin_density();
+    const float adm0 = x[3], adm1 = x[3] / 3.f;
+    const float d0 = adm0 * r[0];
+    const float d1 = adm1 * r[1];
+    float a_e = 0.f;
+    const float u0 = fminf(d0, x[2]);
+    a_e += u0;
+    const float pa = d0 - x[2];
+    const float mask = pa < 0.f ? 1.f : 0.f;
+    const float u1 = mask * fminf(d1, -pa) + (1.f - mask) * 0.f;
+    a_e += u1;
+    x[0] += dt * a_e;
+    x[4] = a_e;
+    x[5] = u0;
+    x[6] = u1;
+    const float phi_s = -1.f * d0 * lin * y_s;
+    const float phi_a = mask * (-u1 * lin * y_a) + (1.f - mask) * (pa * lin * y_s / y_a);
+    x[7] = phi_s;
+    x[8] = phi_a;
+    ctb[0] = phi_s;
+    ctb[1] = phi_a;
+    return x[0] >= x[1] ? kDivision : kIdle;
+  }
+  __device__ __forceinline__ static float coef(const float* r, int j) {
+    (void)r;
+    (void)j;
+    return 0.f;
+  }
+  __device__ __forceinline__ static void division(float* x, float* child, const float* d, const double* p) {
+    (void)p;
+    const float lm = l_max_m();
+    x[0] = x[0] / 2.F;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) child[v] = x[v];
+#pragma unroll
+    for (int v = 4; v < 9; ++v) child[v] = 0.f;
+    const double sigma = 0.2;
+    const double average = sa_math::log_d((double)x[4]) - sigma * sigma / 2;
+    const float gen1 = (float)sa_math::exp_d(sa_math::norminv_d((double)d[0], average, sigma));
+    const float gen2 = (float)sa_math::exp_d(sa_math::norminv_d((double)d[1], average, sigma));
+    // l_max_dist: TruncatedNormal(l_max, l_max / 10, 0.7 l_max, 1.3 l_max):
+    // z = -3, +3, 0.5 erfc(-z / sqrt2) rounded to float
+    const float sd = (float)((double)lm / 10.);
+    const float lmax1 = sa_math::truncnorm_f(d[2], lm, sd, 0x1.61de2p-10f, 0x1.ff4f1p-1f);
+    const float lmax2 = sa_math::truncnorm_f(d[3], lm, sd, 0x1.61de2p-10f, 0x1.ff4f1p-1f);
+    x[2] = gen1;
+    x[1] = lmax1;
+    child[2] = gen2;
+    child[1] = lmax2;
+  }
+  __device__ __forceinline__ static void init(float* x, const float* d, const double* p) {
+    (void)p;
+    const float lm = l_max_m();
+    // l_dist: TruncatedNormal(0.75 l_max, l_max / 10, 0.7 l_min, 1.3 l_max):
+    // z = -4.0000005, +5.4999995
+    const float mu = (float)((double)lm * 0.75), sd = (float)((double)lm / 10.);
+    x[0] = sa_math::truncnorm_f(d[1], mu, sd, 0x1.09ad56p-15f, 1.0f);
+    x[1] = sa_math::truncnorm_f(d[2], mu, sd, 0x1.09ad56p-15f, 1.0f);
+    x[2] = a_max_m() / 2.f;
+    x[3] = a_max_m();  // the mean of a_max_dist, symmetric about a_max
+#pragma unroll
+    for (int v = 4; v < 9; ++v) x[v] = 0.f;
   }
   __device__ __forceinline__ static double mass(const float* x, const double* p) {
     (void)p;

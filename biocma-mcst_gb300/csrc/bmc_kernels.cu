@@ -47,7 +47,8 @@ __global__ void k_debug_wait(unsigned long long limit_ns, int arrive, unsigned l
 }
 
 // Built-in kernel sets, one translation unit per model (compiled in
-// parallel): bmc_sets_monod.cu, bmc_sets_overflow.cu, bmc_sets_fixed.cu.
+// parallel): bmc_sets_monod.cu, bmc_sets_overflow.cu, bmc_sets_fixed.cu,
+// bmc_sets_acetate.cu.
 const KernelSet* kernel_set(int model, int f64) {
   switch (model) {
     case 1:
@@ -57,6 +58,8 @@ const KernelSet* kernel_set(int model, int f64) {
     case 3:
     case 4:
       return f64 ? nullptr : set_fixed_length(model == 3);
+    case 5:
+      return f64 ? nullptr : set_simple_acetate();
     default:
       return udf_kernel_set(model, f64);
   }

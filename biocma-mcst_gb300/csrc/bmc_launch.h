@@ -96,6 +96,7 @@ const KernelSet* kernel_set(int model, int f64);
 const KernelSet* set_monod(int f64);
 const KernelSet* set_overflow(int f64);
 const KernelSet* set_fixed_length(bool separable);
+const KernelSet* set_simple_acetate();
 const KernelSet* udf_kernel_set(int model, int f64);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive, unsigned long long* out);

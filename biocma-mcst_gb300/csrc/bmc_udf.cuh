@@ -101,7 +101,7 @@ template <template <class> class M, int P, class F>
 const KernelSet* kernel_set_for() {
   if constexpr ((P & precision_bit<F>()) != 0) {
     using Model = M<F>;
-    static_assert(Model::n_var >= 1 && Model::n_var <= kMaxVar, "n_var must be in [1, 8]");
+    static_assert(Model::n_var >= 1 && Model::n_var <= kMaxVar, "n_var must be in [1, 16]");
     static_assert(Model::n_ctb >= 1 && Model::n_ctb <= kMaxSpecies, "n_ctb must be in [1, 8]");
     static_assert(Model::n_rates >= 1 && Model::n_rates <= 7, "n_rates must be in [1, 7]");
     static_assert(Model::n_upd >= 0 && Model::n_upd <= Model::n_rates, "n_upd must be <= n_rates");

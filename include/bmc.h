@@ -53,6 +53,11 @@ extern "C" {
 #define BMC_MODEL_FIXED_LENGTH 3
 /* FixedLength through the general per-particle contribution path. */
 #define BMC_MODEL_FIXED_LENGTH_GENERAL 4
+/* The reference's SimpleAcetate model (apps/libs/models/public/models/
+ * simple_acetate.hpp): float state of 9 variables, glucose and acetate
+ * uptake, two contributions per particle, log-normal and truncated-normal
+ * draws at division. */
+#define BMC_MODEL_SIMPLE_ACETATE 5
 
 /* Device error word bits (copied back with the step statistics). */
 #define BMC_ERR_POSITION 1u  /* compartment index out of range */

@@ -154,6 +154,7 @@ static void model_rates(const orc_state* s, const double* c, void* r) {
     if (s->model == ORC_MODEL_MONOD) monod_rates_f32(c, s->params, rr);
     if (s->model == ORC_MODEL_OVERFLOW) overflow_rates_f32(c, s->params, rr);
     if (is_fixed_length(s)) fixed_length_rates(c, s->params, rr);
+    if (s->model == ORC_MODEL_SIMPLE_ACETATE) simple_acetate_rates(c, s->params, rr);
   }
 }
 
@@ -178,7 +179,7 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
   const uint64_t cap = s->phys_capacity;
   if (s->udf && s->f64) {
     double* st = (double*)s->state;
-    double x[8], out[8] = {0};
+    double x[16], out[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
     const int res = s->udf->update(dt, x, r, out, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
@@ -188,7 +189,7 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
   }
   if (s->udf) {
     float* st = (float*)s->state;
-    float x[8], out[8] = {0};
+    float x[16], out[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
     const int res = s->udf->update((double)(float)dt, x, r, out, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
@@ -198,7 +199,7 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
   }
   if (s->f64) {
     double* st = (double*)s->state;
-    double x[8];
+    double x[16];
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
     double b = 0.0;
     int res = ORC_IDLE;
@@ -209,9 +210,9 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
     return res;
   } else {
     float* st = (float*)s->state;
-    float x[8];
+    float x[16];
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    float b = 0.0f, cf[8] = {0};
+    float b = 0.0f, cf[16] = {0};
     int res = ORC_IDLE;
     const float* rr = (const float*)r;
     const float dtf = (float)dt;
@@ -219,6 +220,7 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
     if (s->model == ORC_MODEL_OVERFLOW) res = overflow_update_f32(dtf, x, rr, &b, s->params);
     if (s->model == ORC_MODEL_FIXED_LENGTH) res = fixed_length_update(dtf, x, rr, &b, s->params);
     if (s->model == ORC_MODEL_FIXED_LENGTH_GENERAL) res = fixed_length_update_general(dtf, x, rr, cf, s->params);
+    if (s->model == ORC_MODEL_SIMPLE_ACETATE) res = simple_acetate_update_general(dtf, x, rr, cf, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
     *basis = (double)b;
     for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = (double)cf[j];
@@ -234,7 +236,7 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
     const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
     char* st = (char*)s->state;
     char* ch = (char*)s->child_state;
-    double xb[8], yb[8]; /* storage for up to 8 values of either type */
+    double xb[16], yb[16]; /* storage for up to 16 values of either type */
     memset(yb, 0, sizeof(yb));
     for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)xb + v * fs, st + (v * cap + i) * fs, fs);
     s->udf->division(xb, yb, d, s->params);
@@ -247,7 +249,7 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
   if (s->f64) {
     double* st = (double*)s->state;
     double* ch = (double*)s->child_state;
-    double x[8], y[8] = {0};
+    double x[16], y[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
     if (s->model == ORC_MODEL_MONOD) monod_division_f64(x, y, d, s->params);
     if (s->model == ORC_MODEL_OVERFLOW) overflow_division_f64(x, y, d, s->params);
@@ -258,11 +260,12 @@ static void model_division(const orc_state* s, uint64_t i, uint64_t child_slot) 
   } else {
     float* st = (float*)s->state;
     float* ch = (float*)s->child_state;
-    float x[8], y[8] = {0};
+    float x[16], y[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
     if (s->model == ORC_MODEL_MONOD) monod_division_f32(x, y, d, s->params);
     if (s->model == ORC_MODEL_OVERFLOW) overflow_division_f32(x, y, d, s->params);
     if (is_fixed_length(s)) fixed_length_division(x, y, d, s->params);
+    if (s->model == ORC_MODEL_SIMPLE_ACETATE) simple_acetate_division(x, y, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) {
       st[v * cap + i] = x[v];
       ch[v * cap + child_slot] = y[v];
@@ -274,7 +277,7 @@ static void model_init(const orc_state* s, uint64_t i, const float* d) {
   const uint64_t cap = s->phys_capacity;
   if (s->udf) {
     const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
-    double xb[8];
+    double xb[16];
     memset(xb, 0, sizeof(xb));
     s->udf->init(xb, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)s->state + (v * cap + i) * fs, (char*)xb + v * fs, fs);
@@ -282,16 +285,17 @@ static void model_init(const orc_state* s, uint64_t i, const float* d) {
   }
   if (s->f64) {
     double* st = (double*)s->state;
-    double x[8] = {0};
+    double x[16] = {0};
     if (s->model == ORC_MODEL_MONOD) monod_init_f64(x, d, s->params);
     if (s->model == ORC_MODEL_OVERFLOW) overflow_init_f64(x, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
   } else {
     float* st = (float*)s->state;
-    float x[8] = {0};
+    float x[16] = {0};
     if (s->model == ORC_MODEL_MONOD) monod_init_f32(x, d, s->params);
     if (s->model == ORC_MODEL_OVERFLOW) overflow_init_f32(x, d, s->params);
     if (is_fixed_length(s)) fixed_length_init(x, d, s->params);
+    if (s->model == ORC_MODEL_SIMPLE_ACETATE) simple_acetate_init(x, d, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
   }
 }
@@ -300,14 +304,21 @@ static double model_mass(const orc_state* s, uint64_t i) {
   if (s->udf) {
     const uint64_t cap = s->phys_capacity;
     const size_t fs = s->f64 ? sizeof(double) : sizeof(float);
-    double xb[8];
+    double xb[16];
     for (uint32_t v = 0; v < s->n_var; ++v) memcpy((char*)xb + v * fs, (const char*)s->state + (v * cap + i) * fs, fs);
     return s->udf->mass(xb, s->params);
   }
   if (s->f64) return ((const double*)s->state)[i];
   if (is_fixed_length(s)) return (double)(((const float*)s->state)[i] * fixed_length_lin_density());
+  if (s->model == ORC_MODEL_SIMPLE_ACETATE) return (double)(((const float*)s->state)[i] * sa_lin_density());
   return (double)((const float*)s->state)[i];
 }
+
+/* The SimpleAcetate draw functions, exported for their accuracy tests. */
+double orc_sa_log(double x) { return sa_log(x); }
+double orc_sa_exp(double x) { return sa_exp(x); }
+double orc_sa_erfinv(double x) { return sa_erfinv_d(x); }
+float orc_sa_truncnorm(float u, float mu, float sd, float pl, float pu) { return sa_truncnorm_f(u, mu, sd, pl, pu); }
 
 /* ------------------------------------------------------------------------ */
 /* Initialisation: apps/libs/mc/src/unit.cpp L102-L163 (InitFunctor: model

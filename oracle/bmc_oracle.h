@@ -38,7 +38,13 @@ extern "C" {
 #endif
 
 enum { ORC_IDLE = 0, ORC_DIVISION = 1, ORC_EXIT = 2, ORC_DEAD = 3 };
-enum { ORC_MODEL_MONOD = 1, ORC_MODEL_OVERFLOW = 2, ORC_MODEL_FIXED_LENGTH = 3, ORC_MODEL_FIXED_LENGTH_GENERAL = 4 };
+enum {
+  ORC_MODEL_MONOD = 1,
+  ORC_MODEL_OVERFLOW = 2,
+  ORC_MODEL_FIXED_LENGTH = 3,
+  ORC_MODEL_FIXED_LENGTH_GENERAL = 4,
+  ORC_MODEL_SIMPLE_ACETATE = 5
+};
 enum { ORC_DRAW_PHILOX = 0, ORC_DRAW_XORSHIFT = 1 };
 
 /* A cell model supplied at run time as host functions (a model library's
@@ -196,6 +202,12 @@ int64_t orc_quantize(double v, int32_t e, int64_t qmax, int* clamped);
 double orc_fixed_to_double(__int128 t, int32_t e);
 uint32_t orc_find_next(const orc_state* s, uint32_t c, double u);
 void orc_repartition(const orc_state* s, uint64_t* counts);
+
+/* SimpleAcetate draw functions (for their accuracy tests). */
+double orc_sa_log(double x);
+double orc_sa_exp(double x);
+double orc_sa_erfinv(double x);
+float orc_sa_truncnorm(float u, float mu, float sd, float pl, float pu);
 
 #ifdef __cplusplus
 }

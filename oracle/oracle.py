@@ -113,6 +113,11 @@ def lib():
         L.orc_u01.restype = ct.c_float
         L.orc_quantize.argtypes = [ct.c_double, ct.c_int32, ct.c_int64, ct.c_void_p]
         L.orc_quantize.restype = ct.c_int64
+        for name in ("orc_sa_log", "orc_sa_exp", "orc_sa_erfinv"):
+            getattr(L, name).argtypes = [ct.c_double]
+            getattr(L, name).restype = ct.c_double
+        L.orc_sa_truncnorm.argtypes = [ct.c_float] * 5
+        L.orc_sa_truncnorm.restype = ct.c_float
         _lib = L
     return _lib
 
