@@ -84,3 +84,19 @@ def test_gpu_simple_acetate_matches_oracle(oracle_mod, shape):
         births += gs["births"]
     assert births > 0
     assert_same_particles(g, o, "end")
+
+
+def test_lognormal_division_draw_keeps_the_mean(oracle_mod):
+    """a_p of a daughter ~ LogNormal(log(a_e) - s^2/2, s), s = 0.2
+    (simple_acetate.hpp L226-L233): its mean is the mother's a_e.  The
+    draw is exp(mu + s sqrt2 erfinv(2u - 1)); over a fine grid of u the mean
+    must come out at a_e to within the erfinv approximation."""
+    L = oracle_mod.lib()
+    a_e, s = 3.7e-10, 0.2
+    mu = L.orc_sa_log(a_e) - s * s / 2
+    u = (np.arange(20000) + 0.5) / 20000
+    z = np.array([math.sqrt(2.0) * L.orc_sa_erfinv(2 * x - 1) for x in u])
+    z = np.clip(z, -5 * math.sqrt(2.0), 5 * math.sqrt(2.0))
+    draws = np.array([L.orc_sa_exp(mu + s * v) for v in z])
+    assert abs(draws.mean() / a_e - 1.0) < 5e-3
+    assert abs(np.log(draws).std() - s) < 5e-3
