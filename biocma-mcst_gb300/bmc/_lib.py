@@ -114,6 +114,7 @@ SIGNATURES = {
     "bmc_gas_set_feeds": [VP, c_u32, VP],
     "bmc_gas_read": [VP, VP, VP, VP],
     "bmc_step_read": [VP, c_dbl, VP, VP],
+    "bmc_reserve": [VP, c_u64],
     "bmc_debug_wait": [c_u64, c_i32, VP, VP],
     "bmc_cma_derive": [c_u32, c_u64, VP, VP, VP, VP, c_u32, VP, VP, VP],
     "bmc_cma_transition": [c_u32, c_u64, VP, VP, VP, VP, c_u64, VP, VP, VP],

@@ -189,6 +189,11 @@ class GpuScenario:
         call("bmc_step", self.handle, dt or self.scen.dt, ct.byref(st))
         return st.as_dict()
 
+    def reserve(self, capacity: int):
+        """Grow the container to at least `capacity` slots (bmc_reserve)."""
+        call("bmc_reserve", self.handle, int(capacity))
+        self.cap = max(self.cap, (int(capacity) + 1023) // 1024 * 1024)
+
     def step_read(self, conc: np.ndarray, dt: float | None = None) -> dict:
         """One step; the concentrations after it are written into `conc`
         (float64 [n_c, n_species], C-contiguous) in the same synchronisation."""

@@ -558,6 +558,40 @@ int bmc_transfer_bytes(uint64_t* h2d, uint64_t* d2h) {
   return BMC_OK;
 }
 
+}  // extern "C"
+
+// Particle arena of a scenario: the container arrays for `cap` slots
+// (state of `state_bytes` per slot), the per-step scratch (division buffer,
+// tile counters, request words, compaction lists), then the control block,
+// the descriptor, the tile scheduler and its two-word live prefix.
+static void carve_particles(Carver& cv, ScenDev& h, size_t state_bytes, unsigned long long cap, Control** ctl,
+                            ScenDev** desc, BatchCtl** bctl, unsigned** live) {
+  const unsigned n_tiles = (unsigned)(cap / kTile);
+  cv.add_raw(&h.state, state_bytes * cap);
+  cv.add(&h.pos, cap);
+  cv.add(&h.status, cap);
+  cv.add(&h.age_h, cap);
+  cv.add(&h.age_d, cap);
+  cv.add(&h.id, cap);
+  cv.add_raw(&h.child_state, state_bytes * cap);
+  cv.add(&h.child_pos, cap);
+  cv.add(&h.tile_births, n_tiles);
+  cv.add(&h.tile_inactive, n_tiles);
+  cv.add(&h.tile_boff, n_tiles);
+  cv.add(&h.tile_goff, n_tiles);
+  cv.add(&h.tile_soff, n_tiles);
+  cv.add(&h.bmask, cap / 32);
+  cv.add(&h.bpos, cap);
+  cv.add(&h.gap_slot, cap);
+  cv.add(&h.src_slot, cap);
+  cv.add(ctl, 1);
+  cv.add(desc, 1);
+  cv.add(bctl, 1);
+  cv.add(live, 2);
+}
+
+extern "C" {
+
 int bmc_launch_count(uint64_t* count) {
   if (count) *count = g_launches.load();
   return BMC_OK;
@@ -592,31 +626,11 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   h.n_tiles = n_tiles;
   h.tile_base = 0;
   Carver cv;
-  cv.add_raw(&h.state, fsz * ks->n_var * cap);
-  cv.add(&h.pos, cap);
-  cv.add(&h.status, cap);
-  cv.add(&h.age_h, cap);
-  cv.add(&h.age_d, cap);
-  cv.add(&h.id, cap);
-  cv.add_raw(&h.child_state, fsz * ks->n_var * cap);
-  cv.add(&h.child_pos, cap);
-  cv.add(&h.tile_births, n_tiles);
-  cv.add(&h.tile_inactive, n_tiles);
-  cv.add(&h.tile_boff, n_tiles);
-  cv.add(&h.tile_goff, n_tiles);
-  cv.add(&h.tile_soff, n_tiles);
-  cv.add(&h.bmask, cap / 32);
-  cv.add(&h.bpos, cap);
-  cv.add(&h.gap_slot, cap);
-  cv.add(&h.src_slot, cap);
   Control* ctl_tmp = nullptr;
-  cv.add(&ctl_tmp, 1);
   ScenDev* desc_tmp = nullptr;
-  cv.add(&desc_tmp, 1);
   BatchCtl* bctl_tmp = nullptr;
-  cv.add(&bctl_tmp, 1);
   unsigned* live_tmp = nullptr;
-  cv.add(&live_tmp, 2);
+  carve_particles(cv, h, fsz * ks->n_var, cap, &ctl_tmp, &desc_tmp, &bctl_tmp, &live_tmp);
   e = cudaMalloc(&s->parena, cv.off);
   if (e != cudaSuccess) {
     cudaStreamDestroy(s->stream);
@@ -669,6 +683,66 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->h_cstage) cudaFreeHost(s->h_cstage);
   cudaStreamDestroy(s->stream);
   delete s;
+  return BMC_OK;
+}
+
+int bmc_reserve(bmc_scenario* s, uint64_t capacity) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (capacity == 0 || capacity > 0xFFFFFFFFull - kTile) return fail(BMC_E_INVALID, "capacity must be in [1, 2^32 - 1024]");
+  const unsigned long long cap = align_up(capacity, kTile);
+  if (cap <= s->h.cap) return BMC_OK;  // never shrinks
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  const unsigned long long n = s->h_ctl->n_used;
+  const size_t fsz = s->h.f64 ? 8 : 4;
+  const int nv = (int)s->h.n_var;
+  ScenDev h = s->h;  // old pointers stay in s->h until the copy is done
+  h.cap = cap;
+  h.n_tiles = (unsigned)(cap / kTile);
+  Carver cv;
+  Control* ctl = nullptr;
+  ScenDev* desc = nullptr;
+  BatchCtl* bctl = nullptr;
+  unsigned* live = nullptr;
+  carve_particles(cv, h, fsz * nv, cap, &ctl, &desc, &bctl, &live);
+  void* arena = nullptr;
+  BMC_CUDA(cudaMalloc(&arena, cv.off));
+  cv.bind(arena);
+  cudaError_t e = cudaMemsetAsync(arena, 0, cv.off, s->stream);
+  // the n live slots of every container array, and the control block
+  for (int v = 0; v < nv && e == cudaSuccess; ++v)
+    e = cudaMemcpyAsync(static_cast<char*>(h.state) + (size_t)v * cap * fsz,
+                        static_cast<const char*>(s->h.state) + (size_t)v * s->h.cap * fsz, n * fsz,
+                        cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.pos, s->h.pos, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.status, s->h.status, n, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.age_h, s->h.age_h, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.age_d, s->h.age_d, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.id, s->h.id, n * 4, cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    cudaFree(arena);
+    return fail(BMC_E_CUDA, std::string("reserve: ") + cudaGetErrorString(e));
+  }
+  cudaFree(s->parena);
+  s->parena = arena;
+  h.ctl = ctl;
+  s->h = h;
+  s->d_ctl = ctl;
+  s->d_desc = desc;
+  s->d_bctl = bctl;
+  s->desc.capacity = capacity;
+  // the captured step holds the old descriptor and scheduler addresses
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  s->ctl_fresh = false;
+  BatchCtl b{0u, h.n_tiles, 0u, 0u, live};
+  BMC_CUDA(counted_memcpy_async(s->d_bctl, &b, sizeof(b), cudaMemcpyHostToDevice, s->stream));
+  int rc = upload_desc(s);
+  if (rc) return rc;
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
   return BMC_OK;
 }
 

@@ -150,6 +150,14 @@ int bmc_device_sm_count(int32_t* sm_count);
 int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out);
 int bmc_scenario_destroy(bmc_scenario* s);
 
+/* Grow the particle container to at least `capacity` slots between steps
+ * (ParticlesContainer::_resize on growth, apps/libs/mc/public/mc/
+ * particles_container.hpp L603-L650: the live particles keep their slots;
+ * the reference grows inside merge_buffer, here a caller grows when a step
+ * reports overflow or when n_used nears the capacity).  Never shrinks;
+ * the scenario's captured step is re-captured at its next run. */
+int bmc_reserve(bmc_scenario* s, uint64_t capacity);
+
 /* ReactorDomain::update (apps/libs/mc/src/domain.cpp L44-L74):
  * liquid volumes [n_c], neighbours [n_c*K] (row-major, std::size_t in the
  * reference), total out-flows per compartment (diag_transition) [n_c] and

@@ -248,6 +248,33 @@ class Oracle:
             for sp in range(ns):
                 s.gfeed_conc[f * 8 + sp] = float(fd.conc[sp])
 
+    def reserve(self, capacity: int):
+        """Grow the container to `capacity` slots keeping the live particles
+        in their slots (the restatement of ParticlesContainer::_resize on
+        growth, particles_container.hpp L603-L650)."""
+        if capacity <= self.cap:
+            return
+        n = int(self.s.n_used)
+        m = self.scen.model
+        old_cap, cap = self.cap, capacity
+        st = self.state.reshape(m.n_var, old_cap)
+        new_state = np.zeros(m.n_var * cap, dtype=self.state.dtype)
+        new_state.reshape(m.n_var, cap)[:, :n] = st[:, :n]
+        self.state = new_state
+        for name in ("pos", "status", "age_h", "age_d", "id"):
+            a = getattr(self, name)
+            b = np.zeros(cap, dtype=a.dtype)
+            b[:n] = a[:n]
+            setattr(self, name, b)
+        for name in ("div_flag", "div_pos", "child_pos", "gap_slot", "src_slot"):
+            setattr(self, name, np.zeros(cap, dtype=getattr(self, name).dtype))
+        self.child_state = np.zeros(m.n_var * cap, dtype=self.state.dtype)
+        for name in ("state", "pos", "status", "age_h", "age_d", "id", "div_flag", "div_pos",
+                     "child_state", "child_pos", "gap_slot", "src_slot"):
+            setattr(self.s, name, _ptr(getattr(self, name)))
+        self.s.phys_capacity = cap
+        self.cap = cap
+
     # -- set-up --------------------------------------------------------------
     def init_particles(self, n: int | None = None):
         n = self.scen.n_particles if n is None else n

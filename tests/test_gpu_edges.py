@@ -227,3 +227,27 @@ def test_scatter_forms_at_their_boundaries(oracle_mod, n_c):
     sc = scenarios.small_ring(6000, n_c=n_c, feeds=True, model=scenarios.overflow(f64=True))
     g, o = make_pair(oracle_mod, sc)
     _parity(g, o, 4, f"n_c={n_c}")
+
+
+def test_reserve_grows_the_container_between_steps(oracle_mod):
+    """A container too small for the births overflows; grown with
+    bmc_reserve between steps (the reference's _resize on growth) it keeps
+    its particles in place and stays equal to the CPU restatement grown the
+    same way; the births then fit."""
+    from test_gpu_parity import make_pair
+
+    m = scenarios.monod(f64=True, m_div=1.0)  # every particle asks to divide
+    sc = scenarios.zero_d(3000, model=m, outlet=False)
+    g, o = make_pair(oracle_mod, sc, capacity=4096)
+    assert g.cap == 4096 and o.cap == 4096
+    gs, os_ = g.step(), o.step()
+    assert gs["overflow"] == os_["overflow"] > 0  # 3000 requests, 1096 free slots
+    before = g.particles()
+    g.reserve(3 * 4096)
+    o.reserve(3 * 4096)
+    after = g.particles()
+    for k in ("pos", "status", "id"):
+        assert np.array_equal(before[k], after[k]), k
+    assert np.array_equal(before["state"].view(np.uint64), after["state"].view(np.uint64))
+    _parity(g, o, 3, "after reserve")
+    assert g.stats()["n_used"] > 4096

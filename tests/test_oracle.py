@@ -94,3 +94,17 @@ def test_tag3d_quirk_drops_contributions(oracle_mod):
     b.cycle()
     # slots 6..31 of the first chunk are skipped by the quirk
     assert (np.abs(b.src[:, 0]).sum()) < (np.abs(a.src[:, 0]).sum())
+
+
+def test_reserve_keeps_the_particles(oracle_mod):
+    sc = scenarios.small_ring(3000, feeds=True)
+    o = oracle_mod.Oracle(sc, phys_capacity=4096)
+    o.init_particles()
+    o.run(3)
+    before = o.particles()
+    o.reserve(10240)
+    assert o.cap == 10240
+    after = o.particles()
+    for k in before:
+        assert np.array_equal(np.asarray(before[k]), np.asarray(after[k])), k
+    o.run(3)  # still steps
