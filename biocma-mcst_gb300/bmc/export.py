@@ -1,0 +1,120 @@
+"""Time records of a run, in the dataset layout of the reference's exporters.
+
+The reference writes, every `dump_interval` main-loop iterations, into an
+HDF5 file (apps/core/src/dataexporter/main_exporter.cpp L52-L150,
+partial_exporter.cpp L25-L160, host_export_handler.cpp L70-L115):
+
+  records/time                  [n_export]
+  records/concentration_liquid  [n_export, n_compartments, n_species]
+  records/volume_liquid         [n_export, n_compartments]
+  records/concentration_gas     [n_export, n_compartments, n_species]  (two-phase)
+  records/volume_gas            [n_export, n_compartments]             (two-phase)
+  records/mtr                   [n_export, n_compartments, n_species]  (two-phase)
+  records/number_particle       [n_export, n_compartments]
+  records/tallies               [n_export, n_tallies]
+
+plus `initial_parameters/*` and `final_result/*` scalars.  `Records`
+collects the same arrays from a device scenario (read-backs between graph
+runs) and writes them under the same names: with h5py to an HDF5 file,
+without it (this image) to a NumPy archive whose keys are the dataset paths.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+TALLIES = ("births", "exits", "moves", "overflow", "n_used", "inactive")
+
+
+class Records:
+    """Accumulates the records of one scenario (a GpuScenario, or any object
+    with `liquid()`, `repartition()`, `stats()`, `scen`, and `gas()` for a
+    two-phase scenario)."""
+
+    def __init__(self, g):
+        self.g = g
+        self.rows: dict[str, list] = {}
+        sc = g.scen
+        self.initial = {
+            "initial_parameters/number_compartment": sc.net.n_c,
+            "initial_parameters/delta_time": sc.dt,
+            "initial_parameters/number_particles": sc.n_particles,
+            "initial_parameters/n_map": max(1, len(getattr(sc, "flowmaps", []) or [])),
+            "initial_parameters/t_per_flow_map": getattr(sc, "t_per_flowmap", 0.0),
+        }
+        self.final: dict[str, float] = {}
+
+    def _append(self, name: str, value):
+        self.rows.setdefault(name, []).append(np.asarray(value))
+
+    def record(self, t: float, volume=None):
+        """One export: the time, the liquid field, the volumes (the current
+        flow map's when given), the particle count per compartment and the
+        tallies of the last step."""
+        sc = self.g.scen
+        self._append("records/time", float(t))
+        self._append("records/concentration_liquid", self.g.liquid()["C"])
+        self._append("records/volume_liquid", np.asarray(sc.net.volume if volume is None else volume, dtype=float))
+        if getattr(sc, "gas", None) is not None:
+            gas = self.g.gas()
+            self._append("records/concentration_gas", gas["Cg"])
+            self._append("records/volume_gas", np.asarray(sc.gas.net.volume, dtype=float))
+            self._append("records/mtr", gas["mtr"])
+        self._append("records/number_particle", self.g.repartition().astype(np.uint64))
+        st = self.g.stats()
+        self._append("records/tallies", np.array([st[k] for k in TALLIES], dtype=np.uint64))
+
+    def run(self, n_steps: int, dump_interval: int, t0: float = 0.0):
+        """Advance n_steps in graph-replayed runs of dump_interval steps,
+        recording the first state and after every run (the reference records
+        the first and the last state as well, main_exporter.cpp L58)."""
+        dt = self.g.scen.dt
+        self.record(t0)
+        done = 0
+        while done < n_steps:
+            k = min(dump_interval, n_steps - done)
+            self.g.run(k)
+            done += k
+            self.record(t0 + done * dt)
+        st = self.g.stats()
+        self.final = {
+            "final_result/number_particles": st["n_used"] - st["inactive"],
+            "final_result/events/total_exit": st["exits"],
+        }
+        return self
+
+    def arrays(self) -> dict:
+        out = {k: np.stack(v) for k, v in self.rows.items()}
+        out.update({k: np.asarray(v) for k, v in self.initial.items()})
+        out.update({k: np.asarray(v) for k, v in self.final.items()})
+        return out
+
+    def save(self, path: str) -> str:
+        """Write the records: HDF5 when h5py is importable, else a NumPy
+        archive (`path` gets the .npz suffix) with the dataset paths as keys."""
+        data = self.arrays()
+        try:
+            import h5py  # noqa: F401
+        except ImportError:
+            if not path.endswith(".npz"):
+                path = path + ".npz"
+            np.savez_compressed(path, **data)
+            return path
+        import h5py
+
+        with h5py.File(path, "w") as f:
+            for k, v in data.items():
+                f.create_dataset(k, data=v)
+        return path
+
+
+def load(path: str) -> dict:
+    """Read records written by `Records.save` (either form)."""
+    if path.endswith(".npz"):
+        with np.load(path) as z:
+            return {k: z[k] for k in z.files}
+    import h5py
+
+    out = {}
+    with h5py.File(path, "r") as f:
+        f.visititems(lambda k, v: out.__setitem__(k, v[()]) if hasattr(v, "shape") else None)
+    return out

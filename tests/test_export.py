@@ -1,0 +1,70 @@
+"""Time records in the dataset layout of the reference's exporters
+(records/time, concentration_liquid, volume_liquid, number_particle,
+tallies, gas fields for two-phase runs)."""
+import numpy as np
+import pytest
+
+from bmc import export, scenarios
+
+
+class FakeScenario:
+    """What Records reads from a device scenario, from the CPU restatement."""
+
+    def __init__(self, oracle_mod, sc):
+        self.scen = sc
+        self.o = oracle_mod.Oracle(sc)
+        self.o.init_particles()
+        self.last = {}
+
+    def run(self, n):
+        for _ in range(n):
+            self.last = self.o.step()
+
+    def liquid(self):
+        return {"C": self.o.C.copy()}
+
+    def repartition(self):
+        p = self.o.particles()
+        idle = p["status"] == 0
+        return np.bincount(p["pos"][idle], minlength=self.scen.net.n_c).astype(np.uint64)
+
+    def stats(self):
+        st = {k: 0 for k in ("births", "exits", "moves", "overflow")}
+        st.update(self.last)
+        st["n_used"], st["inactive"] = int(self.o.s.n_used), int(self.o.s.inactive)
+        return st
+
+
+def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
+    sc = scenarios.small_ring(3000, feeds=True)
+    rec = export.Records(FakeScenario(oracle_mod, sc)).run(10, dump_interval=4)
+    a = rec.arrays()
+    n_exp = 1 + 3  # first state, after 4, 8 and 10 steps
+    assert a["records/time"].shape == (n_exp,)
+    assert np.allclose(a["records/time"], [0.0, 4 * sc.dt, 8 * sc.dt, 10 * sc.dt])
+    assert a["records/concentration_liquid"].shape == (n_exp, sc.net.n_c, sc.n_species)
+    assert a["records/volume_liquid"].shape == (n_exp, sc.net.n_c)
+    assert a["records/number_particle"].shape == (n_exp, sc.net.n_c)
+    assert a["records/tallies"].shape == (n_exp, len(export.TALLIES))
+    n_used = a["records/tallies"][:, list(export.TALLIES).index("n_used")]
+    inactive = a["records/tallies"][:, list(export.TALLIES).index("inactive")]
+    assert np.array_equal(a["records/number_particle"].sum(axis=1), n_used - inactive)
+    path = rec.save(str(tmp_path / "run"))
+    back = export.load(path)
+    for k, v in a.items():
+        assert np.array_equal(back[k], v), k
+
+
+@pytest.mark.gpu
+def test_gpu_records_match_the_scenario():
+    from bmc.sim import GpuScenario
+
+    sc = scenarios.with_gas(scenarios.small_ring(5000, n_c=12, feeds=True,
+                                                 model=scenarios.overflow(f64=True)), kla=0.05, henry=0.03)
+    g = GpuScenario(sc)
+    rec = export.Records(g).run(9, dump_interval=3)
+    a = rec.arrays()
+    assert a["records/concentration_gas"].shape == (4, 12, sc.n_species)
+    assert np.array_equal(a["records/concentration_liquid"][-1], g.liquid()["C"])
+    assert np.array_equal(a["records/number_particle"][-1], g.repartition())
+    assert a["final_result/number_particles"] == g.stats()["n_used"] - g.stats()["inactive"]
