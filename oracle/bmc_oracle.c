@@ -1,7 +1,7 @@
 /*
  * bmc_oracle.c -- CPU restatement of the BioCMA-MCST Monte Carlo cycle.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  The product never links this file.
+ * TEST INFRASTRUCTURE ONLY (the oracle).  The product never links this file.
  * Reference citations for every function are in bmc_oracle.h and beside each
  * function below.  Compile with -ffp-contract=off: the GPU path is compiled
  * without multiply-add contraction, so both sides round every operation the

@@ -1,7 +1,7 @@
 /*
  * bmc_oracle.h -- CPU restatement of the BioCMA-MCST Monte Carlo cycle.
  *
- * TEST INFRASTRUCTURE ONLY.  This file and bmc_oracle.c are the checker the
+ * TEST INFRASTRUCTURE ONLY.  This file and bmc_oracle.c are the oracle the
  * GPU path is compared against; the product (libbmc) never links, loads or
  * calls them.  Only tests/, __graft_entry__.smoke() and bench.py's CPU
  * baseline leg use the oracle.
