@@ -385,16 +385,21 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def precision_form(steps: int):
+def precision_form(steps: int, error_steps: int = 2000):
     """FP32 particle state and model arithmetic (exact contribution sums,
-    FP64 liquid step) on the 4096-compartment workload, timed; the same
-    scenario in FP64 (the GPU FP64 path is bit-identical to the FP64 CPU
-    restatement) gives the reference for the error per species."""
+    FP64 liquid step) on the 4096-compartment workload, timed over `steps`
+    steps; then both runs continue to the workload's configured
+    `error_steps` (2000) steps, and the FP64 run (the GPU FP64 path is
+    bit-identical to the FP64 CPU restatement) is the reference for the
+    per-element concentration error per species:
+    |C32 - C64| / max(|C64|, floor), floor = 1e-12 kg/m^3."""
     import numpy as np
 
     from bmc import autotune, scenarios, sim
 
-    out = {"workload": "lattice4096_overflow", "n_particles": 50_000_000, "steps": steps}
+    floor = 1e-12
+    out = {"workload": "lattice4096_overflow", "n_particles": 50_000_000, "steps": steps,
+           "error_after_steps": error_steps, "error_floor_kg_m3": floor}
     res = {}
     for f64 in (False, True):
         scen = scenarios.workload(3, f64=f64)
@@ -404,27 +409,41 @@ def precision_form(steps: int):
         s0 = g.stats()
         st, ms = g.run_timed(steps)
         alive = 0.5 * ((s0["n_used"] - s0["inactive"]) + (st["n_used"] - st["inactive"]))
-        res[f64] = {"value": alive * steps / (ms / 1e3), "ms_per_step": ms / steps,
-                    "C": g.liquid()["C"], "step": st["step"], "mass_balance": st["mass_balance"][:4],
-                    "shape": shape}
+        res[f64] = {"value": alive * steps / (ms / 1e3), "ms_per_step": ms / steps, "shape": shape}
         if not f64:
             kms = [g.step_timed()[1][1] for _ in range(10)]
             cyc = statistics.mean(kms)
             ach = scen.algorithmic_bytes() * alive / (cyc / 1e3) / 1e9
             out["roofline_frac"] = ach / measured_peak()[0]
             out["kernel_ms"] = cyc
+        left = error_steps - g.stats()["step"]
+        if left > 0:
+            st = g.run(left)
+        res[f64].update({"C": g.liquid()["C"], "step": st["step"], "mass_balance": st["mass_balance"][:4],
+                         "alive": st["n_used"] - st["inactive"]})
         g.close()
     c32, c64 = res[False]["C"], res[True]["C"]
     names = ["glucose", "O2", "acetate", "CO2"]
-    err = {}
+    err, above = {}, []
     for sp, nm in enumerate(names):
         ref = np.abs(c64[:, sp])
-        scale = max(float(ref.max()), 1e-300)
-        err[nm] = {"max_abs_err": float(np.abs(c32[:, sp] - c64[:, sp]).max()),
-                   "max_rel_err_vs_field_max": float(np.abs(c32[:, sp] - c64[:, sp]).max() / scale)}
+        diff = np.abs(c32[:, sp] - c64[:, sp])
+        rel = diff / np.maximum(ref, floor)
+        k = int(np.argmax(rel))
+        err[nm] = {"max_per_element_rel_err": float(rel.max()),
+                   "median_per_element_rel_err": float(np.median(rel)),
+                   "elements_above_1e-5": int((rel > 1e-5).sum()),
+                   "worst_element": {"compartment": k, "c64": float(c64[k, sp]), "c32": float(c32[k, sp])},
+                   "max_abs_err": float(diff.max()),
+                   "max_abs_err_vs_field_max": float(diff.max() / max(float(ref.max()), 1e-300))}
+        if rel.max() > 1e-5:
+            above.append(nm)
     out.update({"value_f32": res[False]["value"], "value_f64": res[True]["value"],
                 "ms_per_step_f32": res[False]["ms_per_step"], "ms_per_step_f64": res[True]["ms_per_step"],
-                "after_steps": res[False]["step"], "error_vs_fp64_per_species": err,
+                "after_steps": [res[False]["step"], res[True]["step"]],
+                "alive_after": [res[False]["alive"], res[True]["alive"]],
+                "error_vs_fp64_per_species": err,
+                "species_above_1e-5_per_element": above,
                 "mass_balance_f32": res[False]["mass_balance"], "unit": METRIC})
     return out
 

@@ -164,6 +164,7 @@ struct bmc_scenario {
   bmc_scenario_desc desc{};
   const bmc::KernelSet* ks = nullptr;
   cudaStream_t stream = nullptr;
+  int device = 0;  // CUDA device the scenario's memory and stream belong to
   int sm_count = 0;
   void* parena = nullptr;  // particle container
   void* darena = nullptr;  // domain + liquid
@@ -612,6 +613,7 @@ int bmc_scenario_create(const bmc_scenario_desc* desc, bmc_scenario** out) {
   s->ks = ks;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
+  s->device = dev;
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
@@ -1104,6 +1106,18 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
 
 int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc) {
   if (!conc) return fail(BMC_E_INVALID, "null concentrations");
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  // When the host mirror of the control block is current, the step counter
+  // after this step is known before it runs (it advances by one unless the
+  // step limit holds it), so only the concentration buffer that step writes
+  // is copied back; otherwise both are, and the parity read back with the
+  // control block names the current one.
+  int predicted = -1;
+  if (s->ctl_fresh) {
+    const uint32_t step = s->h_ctl->step;
+    const bool held = s->h.step_limit != 0u && step >= s->h.step_limit;
+    predicted = (int)((held ? step : step + 1u) & 1u);
+  }
   int rc = scenario_steps(s, dt, 1, 1, true);
   if (rc) return rc;
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
@@ -1114,12 +1128,21 @@ int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* con
     BMC_CUDA(cudaMallocHost(&s->h_cstage, 2 * ne * sizeof(double)));
     s->cstage_n = ne;
   }
-  // both buffers: the step parity, read back with the control block in the
-  // same synchronisation, names the current one
-  BMC_CUDA(counted_memcpy_async(s->h_cstage, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  if (predicted >= 0)
+    BMC_CUDA(counted_memcpy_async(s->h_cstage + predicted * ne, s->h.C + predicted * ne, ne * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s->stream));
+  else
+    BMC_CUDA(counted_memcpy_async(s->h_cstage, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s->stream));
   rc = read_ctl(s, stats);
   if (rc && rc != BMC_E_DEVICE) return rc;
-  std::memcpy(conc, s->h_cstage + (s->h_ctl->step & 1u) * ne, ne * sizeof(double));
+  const int cur = (int)(s->h_ctl->step & 1u);
+  if (predicted >= 0 && predicted != cur) {  // not expected: fetch the buffer the counter names
+    BMC_CUDA(counted_memcpy_async(s->h_cstage + cur * ne, s->h.C + cur * ne, ne * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s->stream));
+    BMC_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  std::memcpy(conc, s->h_cstage + cur * ne, ne * sizeof(double));
   return rc;
 }
 
@@ -1220,14 +1243,32 @@ int bmc_repartition(bmc_scenario* s, uint64_t* counts) {
 }
 
 // ---- allocation-free repartition --------------------------------------------------
-// Per-compartment counters of bmc_repartition_static.  The name below is a
-// host-side stand-in in host code: the device address is looked up once per
-// device with cudaGetSymbolAddress and passed to the kernel.
+// Per-compartment counters of bmc_repartition_static: one array in the
+// library's static device memory, present on every GPU that loads the
+// library until the process exits.  In host code the name below only
+// stands in for the array; its device address on a GPU comes from
+// cudaGetSymbolAddress with that GPU current, looked up once per device and
+// passed to the kernel.
 static __device__ __align__(256) unsigned long long g_repartition_scratch[BMC_REPARTITION_STATIC_MAX];
 
 namespace {
 std::mutex g_scratch_mu;
-std::array<unsigned long long*, 64> g_scratch_ptr{};  // by device ordinal
+std::array<unsigned long long*, 64> g_scratch_ptr{};  // device address of the array, by device ordinal
+
+// Makes `dev` the calling thread's current device for one scope and puts the
+// caller's device back at its end.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int dev) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+    else if (err == cudaSuccess) prev = -1;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 }  // namespace
 
 int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
@@ -1237,9 +1278,12 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
     return fail(BMC_E_CAPACITY, "bmc_repartition_static: " + std::to_string(s->h.n_c) +
                                     " compartments exceed the static scratch of " +
                                     std::to_string(BMC_REPARTITION_STATIC_MAX));
-  int dev = 0;
-  BMC_CUDA(cudaGetDevice(&dev));
+  const int dev = s->device;
   if (dev < 0 || dev >= (int)g_scratch_ptr.size()) return fail(BMC_E_INVALID, "device ordinal out of range");
+  // the scenario's device is current for the look-up, the kernel and the copies
+  DeviceScope scope(dev);
+  if (scope.err != cudaSuccess)
+    return fail(BMC_E_CUDA, std::string("bmc_repartition_static: device ") + cudaGetErrorString(scope.err));
   unsigned long long* scratch = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -1251,6 +1295,7 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
     scratch = g_scratch_ptr[dev];
   }
   const size_t bytes = (size_t)s->h.n_c * sizeof(unsigned long long);
+  // the array keeps the previous call's counts: clear this call's range
   BMC_CUDA(cudaMemsetAsync(scratch, 0, bytes, s->stream));
   bmc::launch_repartition(s->stream, s->d_desc, scratch, s->sm_count * 4);
   g_launches++;

@@ -256,21 +256,24 @@ int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* p
 int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources);
 /* MonteCarloUnit::getRepartition (apps/libs/mc/src/unit.cpp L191-L230). */
 int bmc_repartition(bmc_scenario* s, uint64_t* counts);
-/* Allocation-free bmc_repartition, for callers that cannot allocate device
- * memory at this point: code running while its stream is being captured
- * into a CUDA graph, or programs whose device memory is owned by a caching
- * pool allocator (for example PyTorch's) under a fixed cap, where a raw
- * cudaMalloc would synchronize the device or fail.  No counterpart in the
- * reference (MonteCarloUnit::getRepartition allocates its count view on
- * every call).
+/* bmc_repartition without any device allocation.  It has no counterpart in
+ * the reference.  It is for callers that cannot allocate device memory when
+ * they ask for the counts: a program whose device memory is all handed out
+ * in advance (a caching pool allocator such as PyTorch's under a fixed cap,
+ * or a serving loop that admits scenarios against an HBM budget), where a
+ * cudaMalloc outside that budget fails, and a program that cannot afford
+ * the device-wide synchronisation cudaMalloc and cudaFree can cause while
+ * other streams (a batch, another scenario) keep running.
  * The per-compartment counters live in one static device array of
  * BMC_REPARTITION_STATIC_MAX (65536) entries, 512 KiB held on every GPU
  * that loads the library until the process exits; scenarios with more
- * compartments are rejected with BMC_E_CAPACITY.  The first call on a
- * device looks the array up (cudaGetSymbolAddress) and must come before any
- * stream capture.  Calls share the array: the call clears it, and two calls
- * whose work overlaps on the GPU (different streams) race.  counts is a host
- * array of n_compartments entries; the call waits for its result. */
+ * compartments are rejected with BMC_E_CAPACITY.  The call works on the
+ * scenario's own device (made current for the call, the caller's device
+ * restored after it); its first call on a device looks the array up
+ * (cudaGetSymbolAddress).  Every call shares the array and clears the part
+ * it uses; two calls whose work overlaps on the GPU (different streams,
+ * different host threads) race.  counts is a host array of n_compartments
+ * entries; the call waits for its result. */
 #define BMC_REPARTITION_STATIC_MAX 65536
 int bmc_repartition_static(bmc_scenario* s, uint64_t* counts);
 

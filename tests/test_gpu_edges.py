@@ -194,6 +194,22 @@ def test_step_read_equals_step_then_read_liquid():
         s2 = g2.step_read(conc)
         assert s1 == s2, k
         assert np.array_equal(c1.view(np.uint64), conc.view(np.uint64)), k
+    # with the counters current on the host, one concentration buffer (not
+    # both) travels back per step, beside the control block
+    from bmc.sim import transfer_bytes
+
+    g2.set_step_limit(0)
+    g2.step_read(conc)
+    d0 = transfer_bytes()[1]
+    g2.stats()
+    ctl_bytes = transfer_bytes()[1] - d0
+    d0 = transfer_bytes()[1]
+    g2.step_read(conc)
+    assert transfer_bytes()[1] - d0 == ctl_bytes + sc.net.n_c * sc.n_species * 8
+    g1.set_step_limit(0)
+    g1.step()
+    g1.step()
+    assert np.array_equal(g1.liquid()["C"].view(np.uint64), conc.view(np.uint64))
     with pytest.raises(ValueError):
         g2.step_read(np.zeros(3))
 

@@ -1,9 +1,11 @@
 """bmc_repartition_static: the allocation-free repartition entry point.
 
 It serves callers that cannot allocate device memory where they ask for the
-per-compartment particle counts, such as a step loop being captured into a
-CUDA graph or a program whose device memory belongs to a capped caching
-allocator.  Its counters live in a static device array shared by every
+per-compartment particle counts: programs whose device memory is all handed
+out in advance (a capped caching pool allocator, a serving loop admitting
+work against an HBM budget), where an extra cudaMalloc fails, or that cannot
+afford the device-wide synchronisation of cudaMalloc / cudaFree while other
+streams run.  Its counters live in a static device array shared by every
 call.  This test calls it through the C-ABI twice in a row, on scenarios of
 different sizes (so the clearing of the shared array is exercised), and
 checks each result against bmc_repartition, which allocates its counters.
