@@ -3,7 +3,7 @@
 // Host-side responsibilities: device memory of each scenario (one arena for
 // the particle container, one for the domain and liquid state), the
 // scenario descriptor the kernels read, the per-dt quantities (move
-// probabilities on the device, outlet thresholds exp(-dt F / V) on the
+// probabilities on the device, the outlets' exit thresholds on the
 // host), the step sequence and its CUDA graph, readback.
 #include <cuda_runtime.h>
 #include <dlfcn.h>
@@ -244,8 +244,33 @@ int upload_desc(bmc_scenario* s) {
   return BMC_OK;
 }
 
+// Threshold of the reference's exit test on the integer draw x (odd, the
+// draw u = x 2^-24): probability_leaving<precision_tag>
+// (apps/libs/simulation/public/simulation/probability_leaving.hpp L18-L33)
+// exits iff dt*F > -ln(u)*V with the logarithm of the float draw taken in
+// float (CommonMaths::_ln<true>, the C library's logf on the reference's
+// host build) and the product in double.  -logf(u) does not grow with u (the
+// CPU tests check logf over every draw value), so the test holds exactly
+// for x > thr, thr = (smallest exiting draw) - 1, found by bisection over
+// the 2^23 draw values; 2^24 when no draw exits.
+uint32_t exit_threshold(double dt, double flow, double volume) {
+  auto exits = [&](uint32_t k) {
+    const float u = (float)(2u * k + 1u) * 0x1p-24f;
+    return (dt * flow) > ((double)(-logf(u)) * volume);
+  };
+  uint32_t lo = 0, hi = 1u << 23;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) / 2u;
+    if (exits(mid))
+      hi = mid;
+    else
+      lo = mid + 1u;
+  }
+  return lo == (1u << 23) ? (1u << 24) : 2u * lo;
+}
+
 // Outlets follow the feeds in order (SimulationUnit::update_feed assigns the
-// leaving-flow slots in feed order); thresholds exp(-(dt*F)/V).
+// leaving-flow slots in feed order), each with its exit threshold.
 void derive_outlets(bmc_scenario* s) {
   s->h.n_feeds = (uint32_t)s->feeds.size();
   s->h.n_outlets = 0;
@@ -260,10 +285,7 @@ void derive_outlets(bmc_scenario* s) {
       s->h.outlet_idx[o] = (uint32_t)fd.outlet;
       s->h.outlet_flow[o] = fd.flow;
       const double vol = s->volume[(size_t)fd.outlet];
-      // leave the reactor iff dt*F > -ln(u)*V  <=>  u > exp(-(dt*F)/V)
-      // <=>  x > floor(2^24 exp(-(dt*F)/V)) for the integer draw x = u 2^24
-      const double thr = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
-      s->h.exit_thr[o] = (uint32_t)std::min(16777216.0, std::floor(thr * 16777216.0));
+      s->h.exit_thr[o] = s->dt > 0 ? exit_threshold(s->dt, fd.flow, vol) : (1u << 24);
     }
   }
 }
@@ -286,8 +308,7 @@ int refresh_map_tables(bmc_scenario* s) {
     for (const bmc_feed& fd : s->feeds) {
       if (fd.outlet < 0) continue;
       const double vol = s->maps[m].vol[(size_t)fd.outlet];
-      const double th = s->dt > 0 ? std::exp(-(s->dt * fd.flow) / vol) : 1.0;
-      thr[m * bmc::kMaxOutlets + o++] = (uint32_t)std::min(16777216.0, std::floor(th * 16777216.0));
+      thr[m * bmc::kMaxOutlets + o++] = s->dt > 0 ? exit_threshold(s->dt, fd.flow, vol) : (1u << 24);
     }
   }
   BMC_CUDA(counted_memcpy_async(s->d_map_exit, thr.data(), thr.size() * 4, cudaMemcpyHostToDevice, s->stream));

@@ -22,6 +22,7 @@
 //   M, src   f64[n_c][n_s];   acc_hi/acc_lo i64/u64[n_c][n_acc] fixed point
 #pragma once
 #include <cstdint>
+#include <cstring>
 
 namespace bmc {
 
@@ -38,6 +39,99 @@ constexpr unsigned kFlushParticles = 1u << 20;
 constexpr double kClearNegTol = 1e-4 * 5e-3;
 
 enum : uint8_t { kIdle = 0, kDivision = 1, kExit = 2, kDead = 3 };
+
+// ---------------------------------------------------------------------------
+// Age step of the reference: ages are float, the time step a double, and
+// `ages(i, 0) += d_t` (MoveFunctor, move_kernel.hpp L356; and
+// `ages(i, 1) += d_t` of CycleFunctor for models whose FloatType is double,
+// model_kernel.hpp L193, L270) rounds the sum to double, then to float:
+// (float)((double)a + d).  Evaluated here on the integer pipe (the FP64
+// pipe is scarce on this part): the exact sum rounded to 53 bits (nearest,
+// ties to even) from a guard, round and sticky bit, then to 24 bits.
+// Domain: a >= 0 finite, d >= 0 finite, d the same for a whole step.
+struct AgeStep {
+  unsigned long long md;  // d = md * 2^ed, md normalised to bit 52
+  int ed;
+  float d_rounded;  // (float)d: the result for a == 0
+  int zero;         // d == 0: the age does not change
+};
+
+__host__ __device__ inline AgeStep age_step(double d) {
+  unsigned long long b;
+  memcpy(&b, &d, 8);
+  AgeStep k;
+  k.zero = d == 0.0;
+  const int ef = (int)((b >> 52) & 0x7ffu);
+  unsigned long long m = (b & ((1ull << 52) - 1ull)) | (ef ? (1ull << 52) : 0ull);
+  int e = (ef ? ef : 1) - 1075;
+  while (m && !(m >> 52)) {  // subnormal d: normalise
+    m <<= 1;
+    e -= 1;
+  }
+  k.md = m;
+  k.ed = e;
+  k.d_rounded = (float)d;
+  return k;
+}
+
+__host__ __device__ inline float age_add(float a, const AgeStep& k) {
+  if (k.zero) return a;
+  unsigned ab;
+  memcpy(&ab, &a, 4);
+  if ((ab << 1) == 0u) return k.d_rounded;
+  const int ef = (int)((ab >> 23) & 0xffu);
+  unsigned long long ma = (unsigned long long)((ab & 0x7fffffu) | (ef ? 0x800000u : 0u)) << 29;
+  int ea = (ef ? ef : 1) - 150 - 29;  // a = ma * 2^ea
+  while (!(ma >> 52)) {  // subnormal a: normalise
+    ma <<= 1;
+    ea -= 1;
+  }
+  unsigned long long mx = ma, my = k.md;
+  int ex = ea, ey = k.ed;
+  if (ey > ex) {
+    mx = k.md;
+    my = ma;
+    ex = k.ed;
+    ey = ea;
+  }
+  const int sh = ex - ey;
+  const unsigned long long x3 = mx << 3, y3 = my << 3;
+  unsigned long long yal;
+  if (sh == 0)
+    yal = y3;
+  else if (sh < 56)
+    yal = (y3 >> sh) | (unsigned long long)((y3 << (64 - sh)) != 0ull);
+  else
+    yal = 1ull;
+  unsigned long long s = x3 + yal;
+  int e = ex;
+  if (s >> 56) {
+    s = (s >> 1) | (s & 1ull);
+    e += 1;
+  }
+  unsigned long long m = s >> 3;  // round to 53 bits
+  const unsigned g = (unsigned)(s & 7ull);
+  if (g > 4u || (g == 4u && (m & 1ull))) {
+    m += 1ull;
+    if (m >> 53) {
+      m >>= 1;
+      e += 1;
+    }
+  }
+  unsigned long long q = m >> 29;  // round to 24 bits
+  const unsigned long long r = m & ((1ull << 29) - 1ull);
+  if (r > (1ull << 28) || (r == (1ull << 28) && (q & 1ull))) {
+    q += 1ull;
+    if (q >> 24) {
+      q >>= 1;
+      e += 1;
+    }
+  }
+  const unsigned out = ((unsigned)(e + 179) << 23) | (unsigned)(q & 0x7fffffull);
+  float f;
+  memcpy(&f, &out, 4);
+  return f;
+}
 
 // Per-scenario control block, written by the kernels (device memory).
 struct Control {
@@ -569,19 +663,21 @@ __device__ __forceinline__ float truncnorm_f(float u, float mu, float sd, float 
 // The reference's SimpleAcetate model (apps/libs/models/public/models/
 // simple_acetate.hpp L26-L250): float state {length, l_max, a_p, a_max,
 // a_e, a_e_s, a_e_a, phi_s, phi_a}, two species (glucose, acetate), two
-// contributions per particle (general path).  Per compartment: the uptake
-// saturations g_j = c_j / (c_j + k_j), in double, rounded to float once (the
-// reference rounds 1 / (c_j + k_j) to float and multiplies by c_j in double
-// per particle).  Division draws: two log-normal uptake capacities a_p and
-// two truncated-normal l_max; init: length and l_max from the length
-// distribution (the reference's init draws l_max from l_dist too).  The
-// normal draws are inverse-CDF draws with the reference's erfinv (one
-// uniform each; the reference's log-normal draws a Kokkos normal).
+// contributions per particle (general path).  The update follows the
+// reference's type flow (L153-L203): per compartment the concentrations c_j
+// (double) and inv_j = (float)(1. / (c_j + k_j)); per particle
+// D_j = (float)(((double)adm_j * c_j) * inv_j).  Division draws: two
+// log-normal uptake capacities a_p = exp(log(a_e) - sigma^2/2 + sigma z)
+// with log(a_e) in float (the reference's Kokkos::log of the float a_e) and
+// z a standard normal drawn by inverse CDF with the reference's erfinv (the
+// reference draws a Kokkos normal), and two truncated-normal l_max; init:
+// length and l_max from the length distribution (the reference's init draws
+// l_max from l_dist too).
 struct SimpleAcetateModel {
   static constexpr int n_var = 9;
   static constexpr int n_ctb = 2;
-  static constexpr int n_rates = 2;
-  static constexpr int n_upd = 2;
+  static constexpr int n_rates = 6;
+  static constexpr int n_upd = 6;
   static constexpr int model_id = 5;
   static constexpr bool separable = false;
   static constexpr unsigned read_mask = 0xFu;  // length, l_max, a_p, a_max
@@ -591,12 +687,16 @@ struct SimpleAcetateModel {
     const float d_m = (float)0.6e-6;
     return (float)1000 * (float)3.14159265358979323846 * d_m * d_m / (float)4.;
   }
-  // r = {g_s, g_a}
+  // r = {c_s (two words), c_a (two words), inv_s, inv_a}
   __device__ __forceinline__ static void rates(const double* c, const double* p, float* r) {
     (void)p;
-    const double k_s = (double)(float)1e-3, k_a = (double)(float)1e-4;
-    r[0] = (float)(c[0] / (c[0] + k_s));
-    r[1] = (float)(c[1] / (c[1] + k_a));
+    const float k_s = (float)1e-3, k_a = (float)1e-4;
+    r[0] = __int_as_float(__double2loint(c[0]));
+    r[1] = __int_as_float(__double2hiint(c[0]));
+    r[2] = __int_as_float(__double2loint(c[1]));
+    r[3] = __int_as_float(__double2hiint(c[1]));
+    r[4] = __double2float_rn(__ddiv_rn(1., __dadd_rn(c[0], (double)k_s)));
+    r[5] = __double2float_rn(__ddiv_rn(1., __dadd_rn(c[1], (double)k_a)));
   }
   __device__ __forceinline__ static int update(float dt, float* x, const float* r, float& basis, const float* pf) {
     float ctb[2];
@@ -606,17 +706,20 @@ struct SimpleAcetateModel {
   __device__ __forceinline__ static int update_general(float dt, float* x, const float* r, float* ctb,
                                                        const float* pf) {
     (void)pf;
+    const double c0 = __hiloint2double(__float_as_int(r[1]), __float_as_int(r[0]));
+    const double c1 = __hiloint2double(__float_as_int(r[3]), __float_as_int(r[2]));
     const float y_s = 2.f, y_a = 3.f;
     const float lin = lin_density();
     const float adm0 = x[3], adm1 = x[3] / 3.f;
-    const float d0 = adm0 * r[0];
-    const float d1 = adm1 * r[1];
+    const float d0 = __double2float_rn(__dmul_rn(__dmul_rn((double)adm0, c0), (double)r[4]));
+    const float d1 = __double2float_rn(__dmul_rn(__dmul_rn((double)adm1, c1), (double)r[5]));
     float a_e = 0.f;
-    const float u0 = fminf(d0, x[2]);
+    // Kokkos::min(a, b) = (b < a) ? b : a
+    const float u0 = (x[2] < d0) ? x[2] : d0;
     a_e += u0;
     const float pa = d0 - x[2];
     const float mask = pa < 0.f ? 1.f : 0.f;
-    const float u1 = mask * fminf(d1, -pa) + (1.f - mask) * 0.f;
+    const float u1 = mask * ((-pa < d1) ? -pa : d1) + (1.f - mask) * 0.f;
     a_e += u1;
     x[0] += dt * a_e;
     x[4] = a_e;
@@ -644,9 +747,13 @@ struct SimpleAcetateModel {
 #pragma unroll
     for (int v = 4; v < 9; ++v) child[v] = 0.f;
     const double sigma = 0.2;
-    const double average = sa_math::log_d((double)x[4]) - sigma * sigma / 2;
-    const float gen1 = (float)sa_math::exp_d(sa_math::norminv_d((double)d[0], average, sigma));
-    const float gen2 = (float)sa_math::exp_d(sa_math::norminv_d((double)d[1], average, sigma));
+    const float log_ae = __double2float_rn(sa_math::log_d((double)x[4]));
+    const double average = (double)log_ae - sigma * sigma / 2;
+    // Kokkos' normal(mean, sd) = mean + sd * z, z standard normal
+    const double z1 = sa_math::norminv_d((double)d[0], 0.0, 1.0);
+    const double z2 = sa_math::norminv_d((double)d[1], 0.0, 1.0);
+    const float gen1 = (float)sa_math::exp_d(average + sigma * z1);
+    const float gen2 = (float)sa_math::exp_d(average + sigma * z2);
     // l_max_dist: TruncatedNormal(l_max, l_max / 10, 0.7 l_max, 1.3 l_max):
     // z = -3, +3, 0.5 erfc(-z / sqrt2) rounded to float
     const float sd = (float)((double)lm / 10.);

@@ -446,6 +446,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const double dt = S.dt;
     const F dtF = (F)dt;
     const float dtf = (float)dt;
+    const AgeStep ak = age_step(dt);
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
     const int qe0 = S.q_exp[0];
@@ -522,7 +523,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
             }
             uint32_t r[4];
             philox_raw(seed, idv[k], step, 0u, r);
-            ad[k] = __fadd_rn(ad[k], dtf);
+            // ages(i, 1) += d_t in the model's float type
+            if constexpr (sizeof(F) == 8)
+              ad[k] = age_add(ad[k], ak);
+            else
+              ad[k] = __fadd_rn(ad[k], dtf);
             F rr[(Model::n_upd + 1) & ~1];
             const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
             F xx[NV];
@@ -565,7 +570,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
               pv[k] = p;
             }
             if (n_out > 0) {
-              ah[k] = __fadd_rn(ah[k], dtf);
+              ah[k] = age_add(ah[k], ak);  // ages(i, 0) += d_t (double)
               for (unsigned o = 0; o < n_out; ++o) {
                 if (S.outlet_idx[o] == p) {
                   if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
@@ -653,6 +658,7 @@ struct CycleScen {
   unsigned n_c, K, step, n_out;
   F dtF;
   float dtf;
+  AgeStep ak;
   int qe0;
   unsigned rep_mask, rep_stride;  // accumulator copies - 1, copy stride
 };
@@ -898,6 +904,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.cap = S.cap;
         sr.dtF = (F)S.dt;
         sr.dtf = (float)S.dt;
+        sr.ak = age_step(S.dt);
         sr.n_out = S.n_outlets;
         sr.qe0 = S.q_exp[0];
         sr.crec = reinterpret_cast<const F*>(S.crec);
@@ -936,7 +943,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         } else {
           uint32_t rd[4];
           philox_raw(sr.seed, bid[slot], sr.step, 0u, rd);
-          const float ad = __fadd_rn(bad[slot], sr.dtf);
+          // ages(i, 1) += d_t in the model's float type
+          const float ad = sizeof(F) == 8 ? age_add(bad[slot], sr.ak) : __fadd_rn(bad[slot], sr.dtf);
           F rr[(Model::n_upd + 1) & ~1];
           const uint32_t mthr = load_rec<Model::n_upd>(sr.crec + (size_t)p0 * 8, rr);
           F xx[NV];
@@ -984,7 +992,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             __stcs(S.pos + gi, p);
           }
           if (sr.n_out > 0) {
-            float ah = __fadd_rn(bah[slot], sr.dtf);
+            float ah = age_add(bah[slot], sr.ak);  // ages(i, 0) += d_t (double)
             for (unsigned o = 0; o < sr.n_out; ++o) {
               if (S.outlet_idx[o] == p) {
                 if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {

@@ -429,14 +429,59 @@ void orc_scalar_step(orc_state* s, double dt) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Move of one Idle particle at compartment p, MoveFunctor::handle_move
+ * (move_kernel.hpp L393-L437): leave iff probability_leaving<fast_tag>
+ * (probability_leaving.hpp L35-L48), (dt * Q / V) > u1 with the float draw
+ * compared in double, p_move = (dt * Q) / V given; then the bisection of
+ * __find_next_compartment with u2. */
+static inline uint32_t move_one(const orc_state* s, double p_move, uint32_t p, float u1, float u2, int* moved) {
+  if (p_move > (double)u1) {
+    *moved = 1;
+    return orc_find_next(s, p, (double)u2);
+  }
+  *moved = 0;
+  return p;
+}
+
+/* Exit test of probability_leaving<precision_tag> (probability_leaving.hpp
+ * L18-L33): dt * F > -ln(u) * V with the logarithm of the float draw taken
+ * in float (CommonMaths::_ln<true>, apps/libs/common/public/common/
+ * maths.hpp L28-L34, i.e. Kokkos::log(float), the C library's logf on the
+ * reference's host build) and the product in double. */
+static inline int exit_test(double dt, double flow, double volume, float u) {
+  return (dt * flow) > ((double)(-logf(u)) * volume);
+}
+
+/* TagLeave on one Idle particle at compartment p (move_kernel.hpp
+ * L348-L359 and handle_exit L588-L648): age(0) += dt (float); the first
+ * outlet whose index is p decides; with a non-zero flow the draw u is
+ * tested, and on exit the status becomes Exit and age(0) is reset.
+ * Returns 1 on exit. */
+static inline int leave_one(const orc_state* s, double dt, float dtf, uint32_t p, uint8_t* status, float* age_h,
+                            float u) {
+  (void)dtf;
+  *age_h = (float)((double)*age_h + dt); /* ages(idx, 0) += d_t, d_t double */
+  for (uint32_t o = 0; o < s->n_outlets; ++o) {
+    if (s->outlet_index[o] == p) {
+      if (s->outlet_flow[o] != 0.0 && exit_test(dt, s->outlet_flow[o], s->outlet_volume[o], u)) {
+        *status = ORC_EXIT;
+        *age_h = 0.0f;
+        return 1;
+      }
+      return 0;
+    }
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* One cycle over the container (reference CycleFunctors::launch_model then
  * launch_move, kernels.hpp L124-L224).  Per Idle particle:
  *   ages(i,1) += dt; status = Model::update(...)       model_kernel.hpp L193
  *   S(:, pos) += w * contribs                          contribution_kernel.hpp
  *   move: leave iff dt*Q/V > u1, next = CDF search(u2) move_kernel.hpp L393
  *   ages(i,0) += dt; exit iff dt*F > -ln(u3)*V          move_kernel.hpp L588
- * The exit test is evaluated as u3 > exp(-(dt*F)/V), the same inequality
- * after exponentiation, with the threshold computed once per outlet.
+ * with the reference's own expressions (move_one, leave_one above).
  * Division requests are recorded here and carried out in slot order by
  * orc_post_cycle, which is where the reference's buffer order becomes
  * deterministic. */
@@ -454,8 +499,6 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
   double pmove_small[1];
   double* pmove = s->n_c > 1 ? (double*)malloc(sizeof(double) * s->n_c) : pmove_small;
   for (uint32_t c = 0; c < s->n_c && do_move; ++c) pmove[c] = (dt * s->out_flow[c]) / s->volume[c];
-  double thr[ORC_MAX_OUTLETS];
-  for (uint32_t o = 0; o < s->n_outlets; ++o) thr[o] = exp(-(dt * s->outlet_flow[o]) / s->outlet_volume[o]);
   const float dtf = (float)dt;
 
   /* Optional emulation of the reference's Tag3D contribution loop
@@ -495,7 +538,9 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
       if (s->status[i] != ORC_IDLE) continue;
       float d[4];
       draws_for(s, s->id[i], 0u, d);
-      s->age_d[i] = s->age_d[i] + dtf;
+      /* ages(i, 1) += d_t with d_t of the model's float type (model_kernel.hpp
+       * L193, L270) */
+      s->age_d[i] = s->f64 ? (float)((double)s->age_d[i] + dt) : s->age_d[i] + dtf;
       const uint32_t p0 = s->pos[i];
       double basis = 0.0, ctb[8] = {0};
       const int st = model_update(s, dt, i, rates + (size_t)p0 * 8 * rsz, &basis, ctb);
@@ -519,25 +564,12 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
       }
       uint32_t p = p0;
       if (do_move) {
-        if (pmove[p] > (double)d[0]) {
-          p = orc_find_next(s, p, (double)d[1]);
-          moves++;
-        }
+        int moved = 0;
+        p = move_one(s, pmove[p], p, d[0], d[1], &moved);
+        moves += (uint64_t)moved;
         s->pos[i] = p;
       }
-      if (do_leave) {
-        s->age_h[i] = s->age_h[i] + dtf;
-        for (uint32_t o = 0; o < s->n_outlets; ++o) {
-          if (s->outlet_index[o] == p) {
-            if (s->outlet_flow[o] != 0.0 && (double)d[2] > thr[o]) {
-              s->status[i] = ORC_EXIT;
-              s->age_h[i] = 0.0f;
-              exits++;
-            }
-            break;
-          }
-        }
-      }
+      if (do_leave) exits += (uint64_t)leave_one(s, dt, dtf, p, &s->status[i], &s->age_h[i], d[2]);
     }
   }
 #ifndef _OPENMP
@@ -724,4 +756,115 @@ void orc_repartition(const orc_state* s, uint64_t* counts) {
   for (uint32_t c = 0; c < s->n_c; ++c) counts[c] = 0;
   for (uint64_t i = 0; i < s->n_used; ++i)
     if (s->status[i] == ORC_IDLE) counts[s->pos[i]]++;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Pin entry points: one particle through the functions the cycle above
+ * uses, so tests/test_ref_pins.py can hold them against outputs of the
+ * reference's own code compiled from its headers. */
+uint32_t orc_pin_find_next(uint32_t K, const double* cdf_row, const uint32_t* nbr_row, double u) {
+  orc_state t;
+  memset(&t, 0, sizeof(t));
+  t.K = K;
+  t.n_c = 1;
+  t.cdf = (double*)cdf_row;
+  t.neighbors = (uint32_t*)nbr_row;
+  return orc_find_next(&t, 0, u);
+}
+
+uint32_t orc_pin_move(uint32_t n_c, uint32_t K, const double* volume, const double* out_flow, const uint32_t* nbr,
+                      const double* cdf, double dt, uint32_t pos, float u1, float u2, int32_t* moved) {
+  orc_state t;
+  memset(&t, 0, sizeof(t));
+  t.K = K;
+  t.n_c = n_c;
+  t.cdf = (double*)cdf;
+  t.neighbors = (uint32_t*)nbr;
+  const double p_move = (dt * out_flow[pos]) / volume[pos]; /* as orc_cycle's pmove */
+  int m = 0;
+  const uint32_t r = move_one(&t, p_move, pos, u1, u2, &m);
+  *moved = m;
+  return r;
+}
+
+int32_t orc_pin_leave(uint32_t n_outlets, const uint32_t* index, const double* flow, const double* volume, double dt,
+                      uint32_t pos, uint8_t* status, float* age_h, float u) {
+  orc_state t;
+  memset(&t, 0, sizeof(t));
+  t.n_outlets = n_outlets;
+  for (uint32_t o = 0; o < n_outlets && o < ORC_MAX_OUTLETS; ++o) {
+    t.outlet_index[o] = index[o];
+    t.outlet_flow[o] = flow[o];
+    t.outlet_volume[o] = volume[o];
+  }
+  if (*status != ORC_IDLE) return 0; /* TagLeave skips particles that are not Idle */
+  return leave_one(&t, dt, (float)dt, pos, status, age_h, u);
+}
+
+int32_t orc_pin_exit_test(double dt, double flow, double volume, float u) { return exit_test(dt, flow, volume, u); }
+
+/* The float models' update on one particle (state x in place) in a
+ * compartment of concentrations c; the per-particle contributions to ctb. */
+int32_t orc_pin_model_update(int32_t model, double dt, float* x, const double* c, float* ctb) {
+  orc_state t;
+  memset(&t, 0, sizeof(t));
+  t.model = model;
+  t.f64 = 0;
+  float r[8] = {0};
+  model_rates(&t, c, r);
+  const float dtf = (float)dt;
+  if (model == ORC_MODEL_FIXED_LENGTH || model == ORC_MODEL_FIXED_LENGTH_GENERAL)
+    return fixed_length_update_general(dtf, x, r, ctb, t.params);
+  if (model == ORC_MODEL_SIMPLE_ACETATE) return simple_acetate_update_general(dtf, x, r, ctb, t.params);
+  return -1;
+}
+
+void orc_pin_fixed_length_division(float* x, float* child) {
+  const float d[4] = {0};
+  fixed_length_division(x, child, d, NULL);
+}
+
+void orc_pin_simple_acetate_division(float* x, float* child, double z1, double z2, float u3, float u4) {
+  simple_acetate_division_z(x, child, z1, z2, u3, u4);
+}
+
+/* init draws d[1], d[2] are the length and l_max uniforms */
+void orc_pin_simple_acetate_init(float* x, float u_length, float u_lmax) {
+  const float d[4] = {0.f, u_length, u_lmax, 0.f};
+  simple_acetate_init(x, d, NULL);
+}
+
+float orc_pin_erfinv_f(float x) { return sa_erfinv_f(x); }
+double orc_pin_erfinv_d(double x) { return sa_erfinv_d(x); }
+float orc_pin_norminv_f(float p, float mean, float sd) { return sa_norminv_f(p, mean, sd); }
+double orc_pin_std_normal(float u) { return sa_std_normal(u); }
+
+/* TruncatedNormal<float>::draw_from (prng_extension.hpp L379-L414) with
+ * the bounds' probabilities computed as the reference does, 0.5 *
+ * erfc(-z / sqrt2) in double from the float z, rounded to float. */
+float orc_pin_truncnorm_f(double u, float mu, float sd, float lower, float upper) {
+  float zl = (lower - mu) / sd;
+  zl = zl < -5e3f ? -5e3f : (zl > 0.f ? 0.f : zl);
+  float zu = (upper - mu) / sd;
+  zu = zu < 0.f ? 0.f : (zu > 5e3f ? 5e3f : zu);
+  const float pl = (float)(0.5 * erfc((double)(-zl) / SA_SQRT2));
+  const float pu = (float)(0.5 * erfc((double)(-zu) / SA_SQRT2));
+  return sa_truncnorm_f((float)u, mu, sd, pl, pu);
+}
+
+/* 1 when the C library's logf is non-increasing in -logf over the draw
+ * values (2k + 1) / 2^24 (the exit test is then monotone in the draw and a
+ * threshold on the integer draw decides it); the first k that breaks it in
+ * *bad_k otherwise. */
+int32_t orc_logf_monotone_over_draws(uint32_t* bad_k) {
+  float prev = logf(0x1p-24f);
+  for (uint32_t k = 1; k < (1u << 23); ++k) {
+    const float v = logf((float)(2u * k + 1u) * 0x1p-24f);
+    if (v < prev) {
+      if (bad_k) *bad_k = k;
+      return 0;
+    }
+    prev = v;
+  }
+  return 1;
 }

@@ -209,6 +209,25 @@ double orc_sa_exp(double x);
 double orc_sa_erfinv(double x);
 float orc_sa_truncnorm(float u, float mu, float sd, float pl, float pu);
 
+
+/* Pin entry points (one particle through the cycle's own functions). */
+uint32_t orc_pin_find_next(uint32_t K, const double* cdf_row, const uint32_t* nbr_row, double u);
+uint32_t orc_pin_move(uint32_t n_c, uint32_t K, const double* volume, const double* out_flow, const uint32_t* nbr,
+                      const double* cdf, double dt, uint32_t pos, float u1, float u2, int32_t* moved);
+int32_t orc_pin_leave(uint32_t n_outlets, const uint32_t* index, const double* flow, const double* volume, double dt,
+                      uint32_t pos, uint8_t* status, float* age_h, float u);
+int32_t orc_pin_exit_test(double dt, double flow, double volume, float u);
+int32_t orc_pin_model_update(int32_t model, double dt, float* x, const double* c, float* ctb);
+void orc_pin_fixed_length_division(float* x, float* child);
+void orc_pin_simple_acetate_division(float* x, float* child, double z1, double z2, float u3, float u4);
+void orc_pin_simple_acetate_init(float* x, float u_length, float u_lmax);
+float orc_pin_erfinv_f(float x);
+double orc_pin_erfinv_d(double x);
+float orc_pin_norminv_f(float p, float mean, float sd);
+double orc_pin_std_normal(float u);
+float orc_pin_truncnorm_f(double u, float mu, float sd, float lower, float upper);
+int32_t orc_logf_monotone_over_draws(uint32_t* bad_k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,22 +62,6 @@ def test_leave_probability_hand_derived():
         assert ((case["dt"] * case["q"]) / case["v"] > u) == case["leave"]
 
 
-def test_exit_test_forms_agree_on_every_draw():
-    """The exit test dt*F > -ln(u)*V (probability_leaving.hpp L217) is
-    evaluated as u > exp(-(dt*F)/V).  Over every value the draw source can
-    produce (odd 24-bit integers / 2^24) the two forms agree."""
-    k = np.arange(1 << 23, dtype=np.float64)
-    u = (2.0 * k + 1.0) * 2.0 ** -24
-    rng = np.random.default_rng(11)
-    for _ in range(6):
-        dt = 10 ** rng.uniform(-3, 0)
-        F = 10 ** rng.uniform(-6, -2)
-        V = 10 ** rng.uniform(-4, 0)
-        a = (dt * F) > (-np.log(u)) * V
-        b = u > math.exp(-(dt * F) / V)
-        assert int((a != b).sum()) == 0
-
-
 def test_quantize_exact_sums(oracle_mod):
     L = oracle_mod.lib()
     cl = ct.c_int(0)
