@@ -27,6 +27,12 @@ class Feed(ct.Structure):
     _fields_ = [("inlet", c_u32), ("outlet", c_i32), ("flow", c_dbl), ("conc", c_dbl * 8)]
 
 
+class FeedSchedule(ct.Structure):
+    """bmc_feed_schedule: kind 0 constant, 1 linear f0 + t rate, 2
+    exponential f0 + exp(rate t)."""
+    _fields_ = [("kind", c_i32), ("pad", c_i32), ("f0", c_dbl), ("rate", c_dbl)]
+
+
 class StepStats(ct.Structure):
     _fields_ = [("n_used", c_u64), ("inactive", c_u64), ("births", c_u64), ("exits", c_u64),
                 ("moves", c_u64), ("overflow", c_u64), ("requested_divisions", c_u64),
@@ -78,6 +84,8 @@ SIGNATURES = {
     "bmc_set_transition_coo": [VP, c_u32, c_u64, VP, VP, VP],
     "bmc_set_concentrations": [VP, VP],
     "bmc_set_feeds": [VP, c_u32, VP],
+    "bmc_set_feed_schedules": [VP, c_u32, VP],
+    "bmc_feed_time": [VP, VP],
     "bmc_init_particles": [VP, c_u64, c_i32, c_dbl, VP],
     "bmc_set_weight": [VP, c_dbl],
     "bmc_set_particles": [VP, c_u64, VP, VP, VP, VP, VP, VP, c_u64],

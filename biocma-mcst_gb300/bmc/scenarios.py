@@ -93,12 +93,24 @@ def simple_acetate() -> ModelSpec:
                      separable=False, read_vars=4)
 
 
+FEED_CONSTANT = 0
+FEED_LINEAR = 1
+FEED_EXPONENTIAL = 2
+
+
 @dataclass
 class Feed:
+    """A liquid feed (Simulation::Feed::FeedDescriptor): inlet, optional
+    outlet, flow and inlet concentrations; kind selects the flow's time
+    dependence: constant (`flow`), linear f0 + t * rate, or exponential
+    f0 + exp(rate * t) at the relative time t."""
     inlet: int
     outlet: int  # -1 when the feed has no outlet
     flow: float  # m^3/s
     conc: np.ndarray  # kg/m^3 per species
+    kind: int = FEED_CONSTANT
+    f0: float = 0.0
+    rate: float = 0.0
 
 
 @dataclass

@@ -77,6 +77,8 @@ class GpuScenario:
                 for sp in range(len(fd.conc)):
                     arr[k].conc[sp] = float(fd.conc[sp])
             call("bmc_set_feeds", self.handle, len(scen.feeds), arr)
+            if any(fd.kind != 0 for fd in scen.feeds):
+                self.set_feed_schedules(scen.feeds)
         if scen.gas is not None:
             self.set_gas(scen.gas)
         for fm in scen.flowmaps:
@@ -106,6 +108,18 @@ class GpuScenario:
              self.scen.x0, ct.byref(w))
         self.weight = w.value
         return self.weight
+
+    def set_feed_schedules(self, feeds):
+        """bmc_set_feed_schedules from the kind / f0 / rate of each Feed."""
+        arr = (_lib.FeedSchedule * len(feeds))()
+        for k, fd in enumerate(feeds):
+            arr[k].kind, arr[k].f0, arr[k].rate = fd.kind, fd.f0, fd.rate
+        call("bmc_set_feed_schedules", self.handle, len(feeds), arr)
+
+    def feed_time(self) -> float:
+        t = ct.c_double()
+        call("bmc_feed_time", self.handle, ct.byref(t))
+        return t.value
 
     def set_weight(self, w: float):
         call("bmc_set_weight", self.handle, w)

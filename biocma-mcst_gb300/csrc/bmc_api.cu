@@ -283,6 +283,7 @@ void derive_outlets(bmc_scenario* s) {
     if (fd.outlet >= 0) {
       const unsigned o = s->h.n_outlets++;
       s->h.outlet_idx[o] = (uint32_t)fd.outlet;
+      s->h.outlet_feed[o] = (uint32_t)f;
       s->h.outlet_flow[o] = fd.flow;
       const double vol = s->volume[(size_t)fd.outlet];
       s->h.exit_thr[o] = s->dt > 0 ? exit_threshold(s->dt, fd.flow, vol) : (1u << 24);
@@ -808,6 +809,8 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     cv.add(&p_vinv, n_c);
     double* p_rec = nullptr;
     cv.add(&p_rec, (size_t)n_c * 8);
+    uint4* p_age = nullptr;
+    cv.add(&p_age, (size_t)bmc::kAgeTabN);
     cv.add(&h.C, 2 * ne);
     cv.add(&h.M, ne);
     cv.add(&h.src, ne);
@@ -822,6 +825,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     h.diag = p_diag;
     h.vinv = p_vinv;
     h.crec = p_rec;
+    h.age_tab = p_age;
     BMC_CUDA(cudaMemsetAsync(s->darena, 0, cv.off, s->stream));
     s->has_conc = false;
     s->has_transition = false;
@@ -931,6 +935,13 @@ int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
     if (!(feeds[f].flow >= 0.0)) return fail(BMC_E_INVALID, "feed flow must be >= 0");
   }
   s->feeds.assign(feeds, feeds + n_feeds);
+  // new feeds are constant until bmc_set_feed_schedules says otherwise
+  s->h.n_sched = 0u;
+  for (int f = 0; f < bmc::kMaxOutlets; ++f) {
+    s->h.feed_kind[f] = BMC_FEED_CONSTANT;
+    s->h.feed_f0[f] = 0.0;
+    s->h.feed_rate[f] = 0.0;
+  }
   derive_outlets(s);
   int rc = refresh_map_tables(s);
   if (rc) return rc;
@@ -2098,3 +2109,74 @@ int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* ou
 }
 
 }  // extern "C"
+
+// ---- feed schedules ------------------------------------------------------------------
+namespace {
+std::mutex g_nlog_mu;
+std::array<float*, 64> g_nlog{};  // -logf of every draw value, by device ordinal
+}  // namespace
+
+// The table the device's exit thresholds search (exit_threshold_dev):
+// nlog[k] = -logf((2k + 1) 2^-24), from this process's C library, the same
+// logf the host-side thresholds and the CPU restatement use.  32 MiB per
+// device, made once, held until the process exits.
+static int ensure_nlog(bmc_scenario* s) {
+  const int dev = s->device;
+  if (dev < 0 || dev >= (int)g_nlog.size()) return fail(BMC_E_INVALID, "device ordinal out of range");
+  std::lock_guard<std::mutex> lock(g_nlog_mu);
+  if (!g_nlog[dev]) {
+    DeviceScope scope(dev);
+    if (scope.err != cudaSuccess) return fail(BMC_E_CUDA, std::string("feed schedules: ") + cudaGetErrorString(scope.err));
+    const size_t n = (size_t)1 << 23;
+    std::vector<float> h(n);
+    for (size_t k = 0; k < n; ++k) h[k] = -logf((float)(2u * (uint32_t)k + 1u) * 0x1p-24f);
+    float* d = nullptr;
+    BMC_CUDA(cudaMalloc(&d, n * sizeof(float)));
+    const cudaError_t e = cudaMemcpy(d, h.data(), n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(d);
+      return fail(BMC_E_CUDA, std::string("feed schedules: ") + cudaGetErrorString(e));
+    }
+    g_h2d += n * sizeof(float);
+    g_nlog[dev] = d;
+  }
+  s->h.nlog = g_nlog[dev];
+  return BMC_OK;
+}
+
+int bmc_set_feed_schedules(bmc_scenario* s, uint32_t n_feeds, const bmc_feed_schedule* schedules) {
+  if (!s || (n_feeds && !schedules)) return fail(BMC_E_INVALID, "null argument");
+  if (n_feeds != (uint32_t)s->feeds.size())
+    return fail(BMC_E_INVALID, "one schedule per feed of bmc_set_feeds, in the same order");
+  uint32_t n_sched = 0;
+  bool outlet_sched = false;
+  for (uint32_t f = 0; f < n_feeds; ++f) {
+    const bmc_feed_schedule& q = schedules[f];
+    if (q.kind < BMC_FEED_CONSTANT || q.kind > BMC_FEED_EXPONENTIAL) return fail(BMC_E_INVALID, "unknown feed kind");
+    if (!std::isfinite(q.f0) || !std::isfinite(q.rate)) return fail(BMC_E_INVALID, "schedule values must be finite");
+    if (q.kind != BMC_FEED_CONSTANT) {
+      ++n_sched;
+      if (s->feeds[f].outlet >= 0) outlet_sched = true;
+    }
+  }
+  if (outlet_sched) {
+    const int rc = ensure_nlog(s);
+    if (rc) return rc;
+  }
+  for (uint32_t f = 0; f < n_feeds; ++f) {
+    s->h.feed_kind[f] = schedules[f].kind;
+    s->h.feed_f0[f] = schedules[f].f0;
+    s->h.feed_rate[f] = schedules[f].rate;
+  }
+  s->h.n_sched = n_sched;
+  return upload_desc(s);
+}
+
+int bmc_feed_time(bmc_scenario* s, double* t) {
+  if (!s || !t) return fail(BMC_E_INVALID, "null argument");
+  const int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  *t = s->h_ctl->t_rel;
+  return BMC_OK;
+}
+

@@ -133,6 +133,19 @@ __host__ __device__ inline float age_add(float a, const AgeStep& k) {
   return f;
 }
 
+// Table of the age step by binade of the age, for a fast exact path.  For a
+// in [2^e, 2^(e+1)) with ulp u = 2^(e-23), write d = Q u + rho (Q integer,
+// 0 <= rho < u).  While A = a + Q u stays below 2^(e+1) (a < lim =
+// 2^(e+1) - Q u), the sum A + rho lies in the same binade: rounding it to 53
+// bits rounds rho alone (A has no bits below u), and rounding that to 24
+// bits adds 0 or u to A, the choice depending only on rho and on the parity
+// of a / u.  An entry holds Q u and lim as floats and the two choices (bit 0
+// for even a / u, bit 1 for odd; bit 2 marks the entry usable), found by
+// running age_add on an even and an odd age of the binade.  Binades
+// 2^-64 .. 2^63; ages outside them, at or above lim, or zero take age_add.
+constexpr int kAgeTabMin = -64;
+constexpr int kAgeTabN = 128;
+
 // Per-scenario control block, written by the kernels (device memory).
 struct Control {
   unsigned long long n_used;
@@ -170,7 +183,13 @@ struct Control {
   // 1 while the current step runs for this scenario (set by the liquid step
   // from the step limit, before the plan kernel advances the step counter)
   unsigned int cycling;
-  unsigned int pad;
+  // 1 when this launch sequence is a whole main-loop iteration (the liquid
+  // step ran), so the plan kernel advances the relative time with the step
+  unsigned int t_advance;
+  // relative time of the main loop (Simulation::SimulationTimes::
+  // relative_time, simulation_times.hpp L12-L29): the sum of the time steps
+  // of the iterations so far, in order; feed schedules are evaluated at it
+  double t_rel;
 };
 
 // Scenario descriptor as the kernels see it (one per scenario, device memory).
@@ -226,6 +245,21 @@ struct ScenDev {
   int32_t feed_out[kMaxOutlets];
   double feed_flow[kMaxOutlets];
   double feed_conc[kMaxOutlets * kMaxSpecies];
+  // feed schedules (Simulation::Feed::FeedDescriptor::update): kind 0
+  // constant (feed_flow), 1 linear f0 + t * rate, 2 exponential
+  // f0 + exp(rate * t), at the relative time t; n_sched counts the feeds
+  // that are not constant
+  uint32_t n_sched;
+  int32_t feed_kind[kMaxOutlets];
+  double feed_f0[kMaxOutlets];
+  double feed_rate[kMaxOutlets];
+  uint32_t outlet_feed[kMaxOutlets];  // feed of each outlet
+  // -logf of every draw value, (2k + 1) 2^-24 for k < 2^23 (the exit test's
+  // float logarithm, from the host's C library); set with schedules
+  const float* nlog;
+  // age step table for the current dt (kAgeTabN entries, written by the
+  // per-dt kernel)
+  uint4* age_tab;
   // liquid
   double* C;  // two buffers of n_c * n_s; the current one is C + (step & 1) * n_c * n_s
   double* M;
@@ -349,6 +383,41 @@ __device__ __forceinline__ void philox_raw(unsigned long long seed, uint32_t id,
 
 // Integer form of a draw: the odd 24-bit integer x with u = x * 2^-24.
 __device__ __forceinline__ uint32_t draw_int(uint32_t r) { return (r >> 8) | 1u; }
+
+// Entry i of the age step table for the step d (binade e = kAgeTabMin + i).
+__device__ inline uint4 age_tab_entry(double d, const AgeStep& k, int i) {
+  const int e = kAgeTabMin + i;
+  const double u = __longlong_as_double((long long)(1023 + e - 23) << 52);
+  const double p2 = __longlong_as_double((long long)(1023 + e) << 52);
+  const double q = floor(__ddiv_rn(d, u));  // d / u is exact (u a power of two)
+  const double qu = __dmul_rn(q, u);        // exact
+  uint4 ent = make_uint4(0u, 0u, 0u, 0u);
+  if (q < 16777216.0 && qu < __dsub_rn(p2, u)) {
+    const float quf = (float)qu;
+    const float lim = (float)__dsub_rn(__dmul_rn(2.0, p2), qu);  // a multiple of u in the binade: exact
+    const float a_even = (float)p2, a_odd = (float)__dadd_rn(p2, u);
+    const unsigned inc_e = age_add(a_even, k) != __fadd_rn(a_even, quf) ? 1u : 0u;
+    const unsigned inc_o = age_add(a_odd, k) != __fadd_rn(a_odd, quf) ? 1u : 0u;
+    ent = make_uint4(__float_as_uint(quf), __float_as_uint(lim), inc_e | (inc_o << 1) | 4u, 0u);
+  }
+  return ent;
+}
+
+// (float)((double)a + d) through the table, age_add off the table.
+__device__ __forceinline__ float age_add_tab(float a, const uint4* __restrict__ tab, const AgeStep& k) {
+  const unsigned ab = __float_as_uint(a);
+  const unsigned ef = ab >> 23;
+  const unsigned i = ef - (unsigned)(127 + kAgeTabMin);
+  if (i < (unsigned)kAgeTabN) {
+    const uint4 ent = __ldg(tab + i);
+    if ((ent.z & 4u) && a < __uint_as_float(ent.y)) {
+      const float A = __fadd_rn(a, __uint_as_float(ent.x));  // exact
+      const unsigned inc = (ent.z >> (ab & 1u)) & 1u;
+      return inc ? __fadd_rn(A, __uint_as_float((ef - 23u) << 23)) : A;
+    }
+  }
+  return age_add(a, k);
+}
 
 // ---------------------------------------------------------------------------
 // Model plugins.  The ModelType concept of the reference
@@ -659,6 +728,72 @@ __device__ __forceinline__ float truncnorm_f(float u, float mu, float sd, float 
   return norminv_f(p, mu, sd);
 }
 }  // namespace sa_math
+
+// Flow of feed f at the relative time t (FeedDescriptor::update,
+// apps/libs/simulation/src/feed_descriptor.cpp L12-L36): constant, or
+// f0 + t * df (Linear), or f0 + exp(alpha * t) (Exponential; exp from IEEE
+// operations, sa_math::exp_d, as the CPU restatement).
+__device__ __forceinline__ double feed_flow_at(const ScenDev& S, unsigned f, double t) {
+  const int kind = S.feed_kind[f];
+  if (kind == 1) return __dadd_rn(S.feed_f0[f], __dmul_rn(t, S.feed_rate[f]));
+  if (kind == 2) return __dadd_rn(S.feed_f0[f], sa_math::exp_d(__dmul_rn(S.feed_rate[f], t)));
+  return S.feed_flow[f];
+}
+
+// Exit threshold on the integer draw x (odd, u = x 2^-24) of the
+// reference's exit test dt*F > -ln(u)*V with the float logarithm
+// (probability_leaving<precision_tag>, probability_leaving.hpp L18-L33):
+// nlog[k] = -logf((2k + 1) 2^-24) does not grow with k, so the draws that
+// exit are k >= k*, and x exits iff x > 2 k*.  k* is searched from the
+// previous threshold (a bracket grown by doubling steps, then bisection),
+// so a flow that changes little from step to step costs a few loads; every
+// loop is bounded by 24 rounds.  2^24 when no draw exits.
+__device__ __forceinline__ uint32_t exit_threshold_dev(const float* __restrict__ nlog, double dt, double flow,
+                                                       double volume, uint32_t thr_prev) {
+  const uint32_t N = 1u << 23;
+  const double lhs = __dmul_rn(dt, flow);
+  auto exits = [&](uint32_t k) { return lhs > __dmul_rn((double)nlog[k], volume); };
+  uint32_t k0 = thr_prev >> 1;
+  uint32_t lo = 0u, hi = N;  // k* in [lo, hi]; k < lo do not exit; hi exits or hi == N
+  if (k0 < N) {
+    if (exits(k0)) {
+      hi = k0;
+      uint32_t d = 1u;
+      for (int it = 0; it < 24; ++it) {
+        if (hi == 0u) break;
+        const uint32_t c = hi > d ? hi - d : 0u;
+        if (exits(c)) {
+          hi = c;
+          d <<= 1;
+        } else {
+          lo = c + 1u;
+          break;
+        }
+      }
+    } else {
+      lo = k0 + 1u;
+      uint32_t d = 1u;
+      for (int it = 0; it < 24; ++it) {
+        const uint32_t c = lo + d - 1u;
+        if (c >= N) break;
+        if (exits(c)) {
+          hi = c;
+          break;
+        }
+        lo = c + 1u;
+        d <<= 1;
+      }
+    }
+  }
+  for (int it = 0; it < 24 && lo < hi; ++it) {
+    const uint32_t mid = lo + (hi - lo) / 2u;
+    if (exits(mid))
+      hi = mid;
+    else
+      lo = mid + 1u;
+  }
+  return lo >= N ? (1u << 24) : 2u * lo;
+}
 
 // The reference's SimpleAcetate model (apps/libs/models/public/models/
 // simple_acetate.hpp L26-L250): float state {length, l_max, a_p, a_max,

@@ -83,6 +83,17 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
     ctl->exits = 0ull;
     ctl->moves = 0ull;
     ctl->cycling = scen_finished(S, ctl) ? 0u : 1u;
+    ctl->t_advance = do_scalar ? 1u : 0u;
+  }
+  // feed schedules: the outlets' leaving flows and exit thresholds of this
+  // step (SimulationUnit::update_feed -> ReactorDomain::set_leaving_flow,
+  // simulation.model.cpp L90-L104), for the cycle that follows
+  if (blockIdx.x == 0 && S.n_sched > 0u && threadIdx.x < S.n_outlets && !scen_finished(S, ctl)) {
+    const unsigned o = threadIdx.x;
+    const double fl = feed_flow_at(S, S.outlet_feed[o], ctl->t_rel);
+    ScenDev& W = sc[blockIdx.y];
+    W.outlet_flow[o] = fl;
+    W.exit_thr[o] = exit_threshold_dev(S.nlog, S.dt, fl, S.volume[S.outlet_idx[o]], S.exit_thr[o]);
   }
   {
     // per-tile birth / inactive counters of this step start at zero (the
@@ -118,12 +129,14 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
       const double dt = S.dt;
       double srcv = S.src[e];
       double sinkj = 0.0;
+      const double t_rel = ctl->t_rel;
       for (unsigned f = 0; f < S.n_feeds; ++f) {
+        const double ff = feed_flow_at(S, f, t_rel);
         if (S.feed_in[f] == j) {
           const double cf = S.feed_conc[f * kMaxSpecies + sp];
-          if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(S.feed_flow[f], cf));
+          if (cf != 0.0) srcv = __dadd_rn(srcv, __dmul_rn(ff, cf));
         }
-        if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, S.feed_flow[f]);
+        if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, ff);
       }
       S.src[e] = srcv;
       double acc = 0.0;
@@ -447,6 +460,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const F dtF = (F)dt;
     const float dtf = (float)dt;
     const AgeStep ak = age_step(dt);
+    const uint4* __restrict__ age_tab = S.age_tab;
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
     const int qe0 = S.q_exp[0];
@@ -525,7 +539,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             philox_raw(seed, idv[k], step, 0u, r);
             // ages(i, 1) += d_t in the model's float type
             if constexpr (sizeof(F) == 8)
-              ad[k] = age_add(ad[k], ak);
+              ad[k] = age_add_tab(ad[k], age_tab, ak);
             else
               ad[k] = __fadd_rn(ad[k], dtf);
             F rr[(Model::n_upd + 1) & ~1];
@@ -570,7 +584,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
               pv[k] = p;
             }
             if (n_out > 0) {
-              ah[k] = age_add(ah[k], ak);  // ages(i, 0) += d_t (double)
+              ah[k] = age_add_tab(ah[k], age_tab, ak);  // ages(i, 0) += d_t (double)
               for (unsigned o = 0; o < n_out; ++o) {
                 if (S.outlet_idx[o] == p) {
                   if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
@@ -659,6 +673,7 @@ struct CycleScen {
   F dtF;
   float dtf;
   AgeStep ak;
+  const uint4* age_tab;
   int qe0;
   unsigned rep_mask, rep_stride;  // accumulator copies - 1, copy stride
 };
@@ -905,6 +920,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.dtF = (F)S.dt;
         sr.dtf = (float)S.dt;
         sr.ak = age_step(S.dt);
+        sr.age_tab = S.age_tab;
         sr.n_out = S.n_outlets;
         sr.qe0 = S.q_exp[0];
         sr.crec = reinterpret_cast<const F*>(S.crec);
@@ -944,7 +960,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           uint32_t rd[4];
           philox_raw(sr.seed, bid[slot], sr.step, 0u, rd);
           // ages(i, 1) += d_t in the model's float type
-          const float ad = sizeof(F) == 8 ? age_add(bad[slot], sr.ak) : __fadd_rn(bad[slot], sr.dtf);
+          const float ad = sizeof(F) == 8 ? age_add_tab(bad[slot], sr.age_tab, sr.ak) : __fadd_rn(bad[slot], sr.dtf);
           F rr[(Model::n_upd + 1) & ~1];
           const uint32_t mthr = load_rec<Model::n_upd>(sr.crec + (size_t)p0 * 8, rr);
           F xx[NV];
@@ -992,7 +1008,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             __stcs(S.pos + gi, p);
           }
           if (sr.n_out > 0) {
-            float ah = age_add(bah[slot], sr.ak);  // ages(i, 0) += d_t (double)
+            float ah = age_add_tab(bah[slot], sr.age_tab, sr.ak);  // ages(i, 0) += d_t (double)
             for (unsigned o = 0; o < sr.n_out; ++o) {
               if (S.outlet_idx[o] == p) {
                 if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {
@@ -1143,6 +1159,7 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     ctl->next_id += births;
     if (S.n_maps > 0u) ctl->map_cur = (ctl->step / S.n_per_map) % S.n_maps;
     ctl->step += 1u;
+    if (ctl->t_advance) ctl->t_rel = __dadd_rn(ctl->t_rel, S.dt);  // SimulationUnit::advance
     ctl->last_births = births;
     ctl->last_exits = ctl->exits;
     ctl->last_moves = ctl->moves;
@@ -1383,6 +1400,10 @@ template <class F>
 __global__ void k_move_thr(ScenDev* __restrict__ sc) {
   const ScenDev& S = sc[blockIdx.y];
   F* rec = reinterpret_cast<F*>(S.crec);
+  if (blockIdx.x == 0 && S.age_tab) {  // the age step table of this dt
+    const AgeStep ak = age_step(S.dt);
+    for (int i = (int)threadIdx.x; i < kAgeTabN; i += (int)blockDim.x) S.age_tab[i] = age_tab_entry(S.dt, ak, i);
+  }
   for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x) {
     const double p = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
     uint32_t t;

@@ -177,8 +177,39 @@ int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint
 int bmc_set_concentrations(bmc_scenario* s, const double* conc);
 
 /* Feeds (SimulationUnit::update_feed, simulation.model.cpp L73-L111, with
- * ReactorDomain::set_leaving_flow, domain.cpp L97-L108). At most 8. */
+ * ReactorDomain::set_leaving_flow, domain.cpp L97-L108). At most 8.  The
+ * feeds are constant (bmc_feed.flow) until bmc_set_feed_schedules is
+ * called; setting the feeds again clears their schedules. */
 int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds);
+
+/* Time-varying feed flows, the reference's FeedDescriptor variants
+ * Constant | Linear | Exponential (apps/libs/simulation/public/simulation/
+ * feed_descriptor.hpp L39-L60, L91-L100; FeedDescriptor::update,
+ * apps/libs/simulation/src/feed_descriptor.cpp L12-L36, L100-L103):
+ * flow(t) = bmc_feed.flow (constant), f0 + t * rate (linear, rate = df in
+ * m^3/s^2) or f0 + exp(rate * t) (exponential, rate = alpha in 1/s), at the
+ * scenario's relative time t: 0 at creation, advanced by dt after every
+ * main-loop step (bmc_step, bmc_step_read, bmc_run and batch runs; not by
+ * bmc_cycle), as SimulationUnit::advance does.  Every main-loop step
+ * evaluates the flows on the device, inside captured graphs and batches:
+ * the inlet sources flow(t) * conc, the outlet sink flow(t), and the
+ * outlet's leaving flow with its exit threshold (update_feed,
+ * simulation.model.cpp L79-L108).  One schedule per feed of bmc_set_feeds,
+ * same order.  A schedule on a feed with an outlet makes the library build
+ * a 32 MiB table on the device (held until exit). */
+#define BMC_FEED_CONSTANT 0
+#define BMC_FEED_LINEAR 1
+#define BMC_FEED_EXPONENTIAL 2
+typedef struct bmc_feed_schedule {
+  int32_t kind;  /* BMC_FEED_* */
+  int32_t pad;
+  double f0;     /* m^3/s */
+  double rate;   /* df (linear) or alpha (exponential) */
+} bmc_feed_schedule;
+int bmc_set_feed_schedules(bmc_scenario* s, uint32_t n_feeds, const bmc_feed_schedule* schedules);
+/* The scenario's relative time t (s) at which the next step evaluates its
+ * feed schedules (Getter::relative_time, simulation.getset.cpp L154-L158). */
+int bmc_feed_time(bmc_scenario* s, double* t);
 
 /* MC::init + post_init_weight (apps/libs/mc/src/unit.cpp L102-L163,
  * L233-L306): n particles, model init, position uniform in [0, n_c) (or 0

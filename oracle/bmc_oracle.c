@@ -728,8 +728,21 @@ void orc_set_outlets(orc_state* s) {
   }
 }
 
+/* FeedDescriptor::update (feed_descriptor.cpp L12-L36): Linear f0 + t*df,
+ * Exponential f0 + exp(alpha*t) (exp from IEEE operations, sa_exp, as the
+ * device computes it; the reference calls the C library's exp). */
+double orc_feed_flow(int32_t kind, double flow, double f0, double rate, double t) {
+  if (kind == 1) return f0 + t * rate;
+  if (kind == 2) return f0 + sa_exp(rate * t);
+  return flow;
+}
+
 void orc_step(orc_state* s, double dt, int n_threads) {
   const uint32_t ns = s->n_s;
+  /* update_feed at the relative time of this iteration (simulation.model.cpp
+   * L73-L111): sources, sinks and the outlets' leaving flows */
+  for (uint32_t f = 0; f < s->n_feeds; ++f)
+    s->feed_flow[f] = orc_feed_flow(s->feed_kind[f], s->feed_flow[f], s->feed_f0[f], s->feed_rate[f], s->t_rel);
   for (uint32_t j = 0; j < s->n_c; ++j) s->sink[j] = 0.0;
   for (uint32_t f = 0; f < s->n_feeds; ++f) {
     for (uint32_t sp = 0; sp < ns; ++sp) {
@@ -744,6 +757,7 @@ void orc_step(orc_state* s, double dt, int n_threads) {
   orc_cycle(s, dt, n_threads);
   orc_post_cycle(s);
   s->step++;
+  s->t_rel += dt; /* SimulationUnit::advance */
 }
 
 void orc_run(orc_state* s, double dt, uint32_t n_steps, int n_threads) {

@@ -181,6 +181,17 @@ typedef struct orc_state {
   int32_t gfeed_out[ORC_MAX_OUTLETS];
   double gfeed_flow[ORC_MAX_OUTLETS];
   double gfeed_conc[ORC_MAX_OUTLETS * 8];
+
+  /* feed schedules (Simulation::Feed::FeedDescriptor, feed_descriptor.hpp
+   * L39-L100; FeedDescriptor::update, feed_descriptor.cpp L12-L36): kind 0
+   * constant (feed_flow), 1 linear f0 + t * rate, 2 exponential
+   * f0 + exp(rate * t), evaluated by orc_step at the relative time t_rel
+   * (the sum of the time steps of the steps so far, simulation_times.hpp
+   * L12-L29) */
+  int32_t feed_kind[ORC_MAX_OUTLETS];
+  double feed_f0[ORC_MAX_OUTLETS];
+  double feed_rate[ORC_MAX_OUTLETS];
+  double t_rel;
 } orc_state;
 
 void orc_set_outlets(orc_state* s);
@@ -227,6 +238,7 @@ float orc_pin_norminv_f(float p, float mean, float sd);
 double orc_pin_std_normal(float u);
 float orc_pin_truncnorm_f(double u, float mu, float sd, float lower, float upper);
 int32_t orc_logf_monotone_over_draws(uint32_t* bad_k);
+double orc_feed_flow(int32_t kind, double flow, double f0, double rate, double t);
 
 #ifdef __cplusplus
 }

@@ -55,6 +55,8 @@ class OrcState(ct.Structure):
         ("henry", ct.c_double * 8), ("n_gfeeds", ct.c_uint32), ("gfeed_in", ct.c_uint32 * MAXO),
         ("gfeed_out", ct.c_int32 * MAXO), ("gfeed_flow", ct.c_double * MAXO),
         ("gfeed_conc", ct.c_double * (MAXO * 8)),
+        ("feed_kind", ct.c_int32 * MAXO), ("feed_f0", ct.c_double * MAXO), ("feed_rate", ct.c_double * MAXO),
+        ("t_rel", ct.c_double),
     ]
 
 
@@ -201,6 +203,9 @@ class Oracle:
             s.feed_flow[f] = fd.flow
             for sp in range(ns):
                 s.feed_conc[f * 8 + sp] = float(fd.conc[sp])
+            s.feed_kind[f] = getattr(fd, "kind", 0)
+            s.feed_f0[f] = float(getattr(fd, "f0", 0.0))
+            s.feed_rate[f] = float(getattr(fd, "rate", 0.0))
         s.draw_mode = draw_mode
         s.seed = scen.seed
         s.step = 0

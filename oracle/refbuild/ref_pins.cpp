@@ -15,7 +15,13 @@
 //   apps/libs/models/public/models/utils.hpp L64-L69 (check_div)
 //   apps/libs/mc/public/mc/prng/prng_extension.hpp L82-L147 (erfinv,
 //     norminv) and TruncatedNormal::draw_from
+//   apps/libs/simulation/src/feed_descriptor.cpp L12-L36, L100-L103
+//     (FeedDescriptor::update, compiled from the source file) and
+//   apps/libs/simulation/public/simulation/simulation_times.hpp L15-L18
+//     (SimulatimeTimes::advance)
 #include <simulation/kernels/move_kernel.hpp>
+#include <simulation/feed_descriptor.hpp>
+#include <simulation/simulation_times.hpp>
 #include <models/fixed_length.hpp>
 #include <models/simple_acetate.hpp>
 
@@ -170,4 +176,27 @@ float ref_truncnorm_f(double u, float mu, float sigma, float lower, float upper)
 }
 
 int32_t ref_check_div_f(float l, float lc) { return static_cast<int32_t>(Models::check_div<float>(l, lc)); }
+
+// FeedDescriptor::update on a feed of the given kind (0 constant, 1
+// Linear{f0, df = rate}, 2 Exponential{f0, alpha = rate}) at time t.
+double ref_feed_flow(int32_t kind, double f0, double rate, double t, double dt) {
+  Simulation::Feed::FeedDescriptor fd;
+  fd.flow = f0;
+  if (kind == 1)
+    fd.extra = Simulation::Feed::Linear{f0, rate};
+  else if (kind == 2)
+    fd.extra = Simulation::Feed::Exponential{f0, rate};
+  else
+    fd.extra = Simulation::Feed::Constant{};
+  fd.update(t, dt);
+  return fd.flow;
 }
+
+// Relative time after n calls of SimulatimeTimes::advance(dt).
+double ref_relative_time(double dt, uint32_t n) {
+  Simulation::SimulatimeTimes times;
+  for (uint32_t k = 0; k < n; ++k) times.advance(dt);
+  return times.relative();
+}
+}
+

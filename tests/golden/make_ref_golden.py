@@ -22,6 +22,9 @@ Functions recorded (paths relative to the BioCMA-MCST tree):
 * erfinv_f / erfinv_d / norminv_f / truncnorm_f (prng_extension.hpp
   L82-L147 and TruncatedNormal::draw_from)
 * check_div (apps/libs/models/public/models/utils.hpp L64-L69)
+* feed_flow: FeedDescriptor::update (apps/libs/simulation/src/
+  feed_descriptor.cpp L12-L36) of Linear and Exponential feeds at relative
+  times accumulated by SimulatimeTimes::advance (simulation_times.hpp L15-L18)
 
 Floats are stored as their IEEE bit patterns (uint32 / uint64) so the file
 round-trips exactly.
@@ -68,6 +71,8 @@ def load(ref_root: str):
         "ref_norminv_f": (F32, [F32, F32, F32]),
         "ref_truncnorm_f": (F32, [F64, F32, F32, F32, F32]),
         "ref_check_div_f": (I32, [F32, F32]),
+        "ref_feed_flow": (F64, [I32, F64, F64, F64, F64]),
+        "ref_relative_time": (F64, [F64, U32]),
         "ref_assert_failures": (ct.c_long, []),
     }
     for name, (res, args) in sig.items():
@@ -323,6 +328,18 @@ def main(ref_root: str):
         b = a if rng.random() < 0.3 else np.float32(rng.uniform(0, 3))
         cd.append({"l": b32(a), "lc": b32(b), "status": int(L.ref_check_div_f(float(a), float(b)))})
     out["check_div"] = cd
+    feeds = []
+    for _ in range(600):
+        kind = int(rng.integers(1, 3))
+        f0 = float(10 ** rng.uniform(-7, -3))
+        rate = float(rng.choice([-1.0, 1.0]) * 10 ** rng.uniform(-11, -7)) if kind == 1 else \
+            float(rng.choice([-1.0, 1.0]) * 10 ** rng.uniform(-6, -2))
+        dt = float(rng.choice([0.05, 0.1, rng.uniform(0.001, 1.0)]))
+        n = int(rng.integers(0, 20000))
+        t = L.ref_relative_time(dt, n)
+        feeds.append({"kind": kind, "f0": b64(f0), "rate": b64(rate), "dt": b64(dt), "n": n, "t": b64(t),
+                      "flow": b64(L.ref_feed_flow(kind, f0, rate, t, dt))})
+    out["feed_flow"] = feeds
     out["assert_failures"] = int(L.ref_assert_failures())
     with open(os.path.join(HERE, "ref_pins.json"), "w") as f:
         json.dump(out, f, separators=(",", ":"))

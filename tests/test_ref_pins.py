@@ -52,6 +52,7 @@ def L(oracle_mod):
         "orc_pin_norminv_f": (F32, [F32, F32, F32]),
         "orc_pin_truncnorm_f": (F32, [F64, F32, F32, F32, F32]),
         "orc_logf_monotone_over_draws": (I32, [VP]),
+        "orc_feed_flow": (F64, [I32, F64, F64, F64, F64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -220,6 +221,28 @@ def test_truncated_normal(pins, L):
     for c in pins["truncnorm_f"]:
         y = L.orc_pin_truncnorm_f(float(f32(c["u"])), f32(c["mu"]), f32(c["sd"]), f32(c["lo"]), f32(c["hi"]))
         assert bits32(y) == c["y"], c
+
+
+def test_feed_schedules(pins, L):
+    """Relative time accumulated step by step as SimulatimeTimes::advance;
+    linear feeds bit for bit; exponential feeds through the oracle's exp
+    (the reference calls the C library's exp): equal bits on most, within
+    one unit in the last place of the exponential otherwise."""
+    same_exp = n_exp = 0
+    for c in pins["feed_flow"]:
+        dt, t = f64(c["dt"]), 0.0
+        for _ in range(c["n"]):
+            t += dt
+        assert bits64(t) == c["t"], c
+        y = L.orc_feed_flow(c["kind"], 0.0, f64(c["f0"]), f64(c["rate"]), t)
+        ref = f64(c["flow"])
+        if c["kind"] == 1:
+            assert bits64(y) == c["flow"], c
+        else:
+            n_exp += 1
+            same_exp += bits64(y) == c["flow"]
+            assert abs(y - ref) <= 2.3e-16 * abs(ref - f64(c["f0"])) + 1.2e-16 * abs(ref), c
+    assert n_exp > 100 and same_exp >= 0.8 * n_exp, (same_exp, n_exp)
 
 
 def test_check_div(pins):
