@@ -63,7 +63,7 @@ class UdfHostModel(ct.Structure):
     """bmc_udf_host_model: the model's functions compiled for the CPU."""
     _fields_ = [("n_var", c_u32), ("n_ctb", c_u32), ("n_rates", c_u32), ("separable", c_i32),
                 ("rates", VP), ("update", VP), ("coef", VP), ("division", VP), ("init", VP),
-                ("mass", VP)]
+                ("mass", VP), ("update_ctx", VP)]
 
 
 class BmcError(RuntimeError):
@@ -110,6 +110,7 @@ SIGNATURES = {
     "bmc_set_shape": [VP, c_u32, c_u32, c_u32],
     "bmc_set_step_limit": [VP, c_u32],
     "bmc_batch_synchronize": [VP],
+    "bmc_debug_age_add": [VP, c_u64, c_dbl, VP],
     "bmc_debug_draws": [c_u64, VP, c_u64, c_u32, c_u32, VP],
     "bmc_launch_count": [VP],
     "bmc_step_timed": [VP, c_dbl, VP, VP],

@@ -809,8 +809,6 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     cv.add(&p_vinv, n_c);
     double* p_rec = nullptr;
     cv.add(&p_rec, (size_t)n_c * 8);
-    uint4* p_age = nullptr;
-    cv.add(&p_age, (size_t)bmc::kAgeTabN);
     cv.add(&h.C, 2 * ne);
     cv.add(&h.M, ne);
     cv.add(&h.src, ne);
@@ -825,7 +823,6 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
     h.diag = p_diag;
     h.vinv = p_vinv;
     h.crec = p_rec;
-    h.age_tab = p_age;
     BMC_CUDA(cudaMemsetAsync(s->darena, 0, cv.off, s->stream));
     s->has_conc = false;
     s->has_transition = false;
@@ -1941,6 +1938,25 @@ int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t ste
   cudaFree(d_ids);
   if (d_out) cudaFree(d_out);
   if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug draws: ") + cudaGetErrorString(e));
+  return BMC_OK;
+}
+
+int bmc_debug_age_add(const float* ages, uint64_t n, double dt, float* out) {
+  if (!ages || !out || n == 0 || !(dt >= 0.0)) return fail(BMC_E_INVALID, "bad arguments");
+  float* d_a = nullptr;
+  float* d_out = nullptr;
+  BMC_CUDA(cudaMalloc(&d_a, n * 4));
+  cudaError_t e = cudaMalloc(&d_out, n * 4);
+  if (e == cudaSuccess) e = counted_memcpy(d_a, ages, n * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    bmc::launch_debug_age_add(0, d_a, n, dt, d_out);
+    g_launches++;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = counted_memcpy(out, d_out, n * 4, cudaMemcpyDeviceToHost);
+  cudaFree(d_a);
+  if (d_out) cudaFree(d_out);
+  if (e != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug age add: ") + cudaGetErrorString(e));
   return BMC_OK;
 }
 

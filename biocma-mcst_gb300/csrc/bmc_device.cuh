@@ -23,6 +23,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 namespace bmc {
 
@@ -54,6 +55,7 @@ struct AgeStep {
   int ed;
   float d_rounded;  // (float)d: the result for a == 0
   int zero;         // d == 0: the age does not change
+  float dl_abs;     // bound on |d - (float)d| (age_add_fast)
 };
 
 __host__ __device__ inline AgeStep age_step(double d) {
@@ -71,6 +73,9 @@ __host__ __device__ inline AgeStep age_step(double d) {
   k.md = m;
   k.ed = e;
   k.d_rounded = (float)d;
+  // |d - (float)d| rounded to float, raised past its rounding error
+  const double dl = d - (double)k.d_rounded;
+  k.dl_abs = (float)(dl < 0.0 ? -dl : dl) * (1.0f + 0x1p-22f);
   return k;
 }
 
@@ -133,18 +138,36 @@ __host__ __device__ inline float age_add(float a, const AgeStep& k) {
   return f;
 }
 
-// Table of the age step by binade of the age, for a fast exact path.  For a
-// in [2^e, 2^(e+1)) with ulp u = 2^(e-23), write d = Q u + rho (Q integer,
-// 0 <= rho < u).  While A = a + Q u stays below 2^(e+1) (a < lim =
-// 2^(e+1) - Q u), the sum A + rho lies in the same binade: rounding it to 53
-// bits rounds rho alone (A has no bits below u), and rounding that to 24
-// bits adds 0 or u to A, the choice depending only on rho and on the parity
-// of a / u.  An entry holds Q u and lim as floats and the two choices (bit 0
-// for even a / u, bit 1 for odd; bit 2 marks the entry usable), found by
-// running age_add on an even and an odd age of the binade.  Binades
-// 2^-64 .. 2^63; ages outside them, at or above lim, or zero take age_add.
-constexpr int kAgeTabMin = -64;
-constexpr int kAgeTabN = 128;
+// The same sum with float operations where that is exact: s = fl(a + dh)
+// with dh = (float)d, and e = the rounding error of that addition (Fast2Sum
+// of the larger and the smaller operand).  The exact sum is s + e + dl with
+// dl = d - dh; when |e| + |dl| stays below half an ulp of s by a margin
+// (2^-20 of it, far more than the 2^-29 the rounding to 53 bits can move
+// the sum), both roundings return s (when s is a power of two the float
+// below it is half an ulp of s away, and the half of that counts).
+// Otherwise (near a rounding tie, or s below 2^-81) age_add decides.  On ages advanced step by step this
+// leaves age_add to a handful of steps in a run.
+__host__ __device__ inline float age_add_fast(float a, const AgeStep& k) {
+  if (k.zero) return a;
+  const float dh = k.d_rounded;
+  const float s = a + dh;
+  const float big = a > dh ? a : dh, small = a > dh ? dh : a;
+  const float e = small - (s - big);
+  unsigned sb;
+  memcpy(&sb, &s, 4);
+  const unsigned se = sb & 0x7f800000u;  // exponent field of s (s >= 0)
+  if (se >= (46u << 23) && se < (255u << 23)) {
+    // half an ulp of s; below a power of two the neighbour is half as far
+    const unsigned hb = se - ((sb & 0x7fffffu) == 0u ? (25u << 23) : (24u << 23));
+    const unsigned mb = hb - (20u << 23);
+    float h, m;
+    memcpy(&h, &hb, 4);
+    memcpy(&m, &mb, 4);  // 2^-20 of it
+    const float thr = (h - m) - k.dl_abs;
+    if ((e < 0.0f ? -e : e) < thr) return s;
+  }
+  return age_add(a, k);
+}
 
 // Per-scenario control block, written by the kernels (device memory).
 struct Control {
@@ -257,9 +280,6 @@ struct ScenDev {
   // -logf of every draw value, (2k + 1) 2^-24 for k < 2^23 (the exit test's
   // float logarithm, from the host's C library); set with schedules
   const float* nlog;
-  // age step table for the current dt (kAgeTabN entries, written by the
-  // per-dt kernel)
-  uint4* age_tab;
   // liquid
   double* C;  // two buffers of n_c * n_s; the current one is C + (step & 1) * n_c * n_s
   double* M;
@@ -384,40 +404,6 @@ __device__ __forceinline__ void philox_raw(unsigned long long seed, uint32_t id,
 // Integer form of a draw: the odd 24-bit integer x with u = x * 2^-24.
 __device__ __forceinline__ uint32_t draw_int(uint32_t r) { return (r >> 8) | 1u; }
 
-// Entry i of the age step table for the step d (binade e = kAgeTabMin + i).
-__device__ inline uint4 age_tab_entry(double d, const AgeStep& k, int i) {
-  const int e = kAgeTabMin + i;
-  const double u = __longlong_as_double((long long)(1023 + e - 23) << 52);
-  const double p2 = __longlong_as_double((long long)(1023 + e) << 52);
-  const double q = floor(__ddiv_rn(d, u));  // d / u is exact (u a power of two)
-  const double qu = __dmul_rn(q, u);        // exact
-  uint4 ent = make_uint4(0u, 0u, 0u, 0u);
-  if (q < 16777216.0 && qu < __dsub_rn(p2, u)) {
-    const float quf = (float)qu;
-    const float lim = (float)__dsub_rn(__dmul_rn(2.0, p2), qu);  // a multiple of u in the binade: exact
-    const float a_even = (float)p2, a_odd = (float)__dadd_rn(p2, u);
-    const unsigned inc_e = age_add(a_even, k) != __fadd_rn(a_even, quf) ? 1u : 0u;
-    const unsigned inc_o = age_add(a_odd, k) != __fadd_rn(a_odd, quf) ? 1u : 0u;
-    ent = make_uint4(__float_as_uint(quf), __float_as_uint(lim), inc_e | (inc_o << 1) | 4u, 0u);
-  }
-  return ent;
-}
-
-// (float)((double)a + d) through the table, age_add off the table.
-__device__ __forceinline__ float age_add_tab(float a, const uint4* __restrict__ tab, const AgeStep& k) {
-  const unsigned ab = __float_as_uint(a);
-  const unsigned ef = ab >> 23;
-  const unsigned i = ef - (unsigned)(127 + kAgeTabMin);
-  if (i < (unsigned)kAgeTabN) {
-    const uint4 ent = __ldg(tab + i);
-    if ((ent.z & 4u) && a < __uint_as_float(ent.y)) {
-      const float A = __fadd_rn(a, __uint_as_float(ent.x));  // exact
-      const unsigned inc = (ent.z >> (ab & 1u)) & 1u;
-      return inc ? __fadd_rn(A, __uint_as_float((ef - 23u) << 23)) : A;
-    }
-  }
-  return age_add(a, k);
-}
 
 // ---------------------------------------------------------------------------
 // Model plugins.  The ModelType concept of the reference
@@ -440,6 +426,27 @@ __device__ __forceinline__ float age_add_tab(float a, const uint4* __restrict__ 
 // are applied once per compartment.  A general model (separable = false)
 // writes its n_ctb contributions per particle.  Every expression keeps the
 // operation order of the CPU restatement, so both round identically.
+//
+// A model whose update is not a function of per-compartment factors alone,
+// or that draws random numbers in update (the reference's
+// Model::update(random_pool, d_t, idx, arr, contribs, position, c),
+// traits.hpp L117, called at model_kernel.hpp L234-L240), declares
+//   static constexpr bool uses_context = true;
+//   update_ctx(dt, x, r, out, pf, ctx) -> st
+// and the cycle calls update_ctx instead of update / update_general, with
+// out the basis (separable) or the n_ctb contributions (general) and ctx the
+// particle's four uniform draws of the step (Philox keyed by (seed, id,
+// step, purpose 3)), the compartment's concentrations and its index.
+struct UpdateContext {
+  const float* draws;   // 4 uniforms in (0, 1)
+  const double* c;      // concentrations of the particle's compartment [n_species]
+  uint32_t position;    // compartment index
+  uint32_t n_species;
+};
+template <class M, class = void>
+struct has_context : std::false_type {};
+template <class M>
+struct has_context<M, std::void_t<decltype(M::uses_context)>> : std::integral_constant<bool, M::uses_context> {};
 
 template <class F>
 struct MonodModel {

@@ -33,6 +33,47 @@ __host__ __device__ constexpr int rate_slot(int k) {
   return k < Model::n_upd ? 7 - Model::n_upd + k : k - Model::n_upd;
 }
 
+// Model::update of one Idle particle at compartment p0: the per-compartment
+// factor form (update / update_general), or update_ctx with the particle's
+// draws of the step (purpose 3) and its compartment's concentrations (the
+// current buffer of the step: the liquid step wrote it, the step counter
+// still holds this step) for models that declare uses_context.
+template <class Model, class F>
+__device__ __forceinline__ int update_separable(F dt, F* x, const F* r, F& basis, const F* pf, const ScenDev& S,
+                                                uint32_t id, uint32_t step, uint32_t p0) {
+  if constexpr (has_context<Model>::value) {
+    const Draws d = philox_draws(S.seed, id, step, 3u);
+    const size_t ne = (size_t)S.n_c * S.n_s;
+    const UpdateContext ctx{d.u, S.C + ((step & 1u) ^ 1u) * ne + (size_t)p0 * S.n_s, p0, S.n_s};
+    F out[1];
+    const int st = Model::update_ctx(dt, x, r, out, pf, ctx);
+    basis = out[0];
+    return st;
+  } else {
+    (void)S;
+    (void)id;
+    (void)step;
+    (void)p0;
+    return Model::update(dt, x, r, basis, pf);
+  }
+}
+template <class Model, class F>
+__device__ __forceinline__ int update_general_of(F dt, F* x, const F* r, F* ctb, const F* pf, const ScenDev& S,
+                                                 uint32_t id, uint32_t step, uint32_t p0) {
+  if constexpr (has_context<Model>::value) {
+    const Draws d = philox_draws(S.seed, id, step, 3u);
+    const size_t ne = (size_t)S.n_c * S.n_s;
+    const UpdateContext ctx{d.u, S.C + ((step & 1u) ^ 1u) * ne + (size_t)p0 * S.n_s, p0, S.n_s};
+    return Model::update_ctx(dt, x, r, ctb, pf, ctx);
+  } else {
+    (void)S;
+    (void)id;
+    (void)step;
+    (void)p0;
+    return Model::update_general(dt, x, r, ctb, pf);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // k_liquid: one thread per (compartment j, species s) entry; a block holds
 // kLiquidThreads / n_species whole compartments (grid x over compartment chunks, grid
@@ -460,7 +501,6 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const F dtF = (F)dt;
     const float dtf = (float)dt;
     const AgeStep ak = age_step(dt);
-    const uint4* __restrict__ age_tab = S.age_tab;
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
     const int qe0 = S.q_exp[0];
@@ -539,10 +579,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
             philox_raw(seed, idv[k], step, 0u, r);
             // ages(i, 1) += d_t in the model's float type
             if constexpr (sizeof(F) == 8)
-              ad[k] = age_add_tab(ad[k], age_tab, ak);
+              ad[k] = age_add_fast(ad[k], ak);
             else
               ad[k] = __fadd_rn(ad[k], dtf);
-            F rr[(Model::n_upd + 1) & ~1];
+            F rr[Model::n_upd > 0 ? ((Model::n_upd + 1) & ~1) : 2];
             const uint32_t mthr = load_rec<Model::n_upd>(crec + (size_t)p0 * 8, rr);
             F xx[NV];
 #pragma unroll
@@ -550,7 +590,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             int st;
             if constexpr (Model::separable) {
               F basis;
-              st = Model::update(dtF, xx, rr, basis, s_pf);
+              st = update_separable<Model, F>(dtF, xx, rr, basis, s_pf, S, idv[k], step, p0);
               const long long q = quantize(basis, qe0, my_clamp, my_err);
               if constexpr (AGG) {
                 qv[k] = q;
@@ -560,7 +600,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
               }
             } else {
               F ctb[NC];
-              st = Model::update_general(dtF, xx, rr, ctb, s_pf);
+              st = update_general_of<Model, F>(dtF, xx, rr, ctb, s_pf, S, idv[k], step, p0);
 #pragma unroll
               for (int j = 0; j < NC; ++j) {
                 const double val = __dmul_rn(S.weight, (double)ctb[j]);
@@ -584,7 +624,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
               pv[k] = p;
             }
             if (n_out > 0) {
-              ah[k] = age_add_tab(ah[k], age_tab, ak);  // ages(i, 0) += d_t (double)
+              ah[k] = age_add_fast(ah[k], ak);  // ages(i, 0) += d_t (double)
               for (unsigned o = 0; o < n_out; ++o) {
                 if (S.outlet_idx[o] == p) {
                   if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
@@ -673,7 +713,6 @@ struct CycleScen {
   F dtF;
   float dtf;
   AgeStep ak;
-  const uint4* age_tab;
   int qe0;
   unsigned rep_mask, rep_stride;  // accumulator copies - 1, copy stride
 };
@@ -920,7 +959,6 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.dtF = (F)S.dt;
         sr.dtf = (float)S.dt;
         sr.ak = age_step(S.dt);
-        sr.age_tab = S.age_tab;
         sr.n_out = S.n_outlets;
         sr.qe0 = S.q_exp[0];
         sr.crec = reinterpret_cast<const F*>(S.crec);
@@ -960,8 +998,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           uint32_t rd[4];
           philox_raw(sr.seed, bid[slot], sr.step, 0u, rd);
           // ages(i, 1) += d_t in the model's float type
-          const float ad = sizeof(F) == 8 ? age_add_tab(bad[slot], sr.age_tab, sr.ak) : __fadd_rn(bad[slot], sr.dtf);
-          F rr[(Model::n_upd + 1) & ~1];
+          const float ad = sizeof(F) == 8 ? age_add_fast(bad[slot], sr.ak) : __fadd_rn(bad[slot], sr.dtf);
+          F rr[Model::n_upd > 0 ? ((Model::n_upd + 1) & ~1) : 2];
           const uint32_t mthr = load_rec<Model::n_upd>(sr.crec + (size_t)p0 * 8, rr);
           F xx[NV];
 #pragma unroll
@@ -970,7 +1008,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           int st;
           if constexpr (Model::separable) {
             F basis;
-            st = Model::update(sr.dtF, xx, rr, basis, s_pf);
+            st = update_separable<Model, F>(sr.dtF, xx, rr, basis, s_pf, S, bid[slot], sr.step, p0);
             const long long q = quantize(basis, sr.qe0, my_clamp, my_err);
             if constexpr (AGG) {
               qv = q;
@@ -984,7 +1022,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             }
           } else {
             F ctb[NC];
-            st = Model::update_general(sr.dtF, xx, rr, ctb, s_pf);
+            st = update_general_of<Model, F>(sr.dtF, xx, rr, ctb, s_pf, S, bid[slot], sr.step, p0);
 #pragma unroll
             for (int j = 0; j < NC; ++j) {
               const double val = __dmul_rn(S.weight, (double)ctb[j]);
@@ -1008,7 +1046,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             __stcs(S.pos + gi, p);
           }
           if (sr.n_out > 0) {
-            float ah = age_add_tab(bah[slot], sr.age_tab, sr.ak);  // ages(i, 0) += d_t (double)
+            float ah = age_add_fast(bah[slot], sr.ak);  // ages(i, 0) += d_t (double)
             for (unsigned o = 0; o < sr.n_out; ++o) {
               if (S.outlet_idx[o] == p) {
                 if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {
@@ -1400,10 +1438,6 @@ template <class F>
 __global__ void k_move_thr(ScenDev* __restrict__ sc) {
   const ScenDev& S = sc[blockIdx.y];
   F* rec = reinterpret_cast<F*>(S.crec);
-  if (blockIdx.x == 0 && S.age_tab) {  // the age step table of this dt
-    const AgeStep ak = age_step(S.dt);
-    for (int i = (int)threadIdx.x; i < kAgeTabN; i += (int)blockDim.x) S.age_tab[i] = age_tab_entry(S.dt, ak, i);
-  }
   for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < S.n_c; c += gridDim.x * blockDim.x) {
     const double p = __ddiv_rn(__dmul_rn(S.dt, S.out_flow[c]), S.volume[c]);
     uint32_t t;

@@ -27,6 +27,15 @@ __global__ void k_debug_draws(unsigned long long seed, const uint32_t* __restric
   }
 }
 
+// The age step of the cycle kernels on n ages (a >= 0), for its test
+// against (float)((double)a + dt) on the CPU.
+__global__ void k_debug_age_add(const float* __restrict__ a, unsigned long long n, double dt, float* __restrict__ out) {
+  const AgeStep k = age_step(dt);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    out[i] = age_add_fast(a[i], k);
+}
+
 // Self-test of the bounded wait the cycle kernels use on their mbarriers:
 // one thread waits on phase 0 of a barrier expecting one arrival, which it
 // makes first (`arrive` != 0: the wait succeeds) or that nothing makes (the
@@ -74,6 +83,9 @@ void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive,
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out) {
   k_debug_draws<<<256, 256, 0, st>>>(seed, ids, n, step, purpose, out);
+}
+void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out) {
+  k_debug_age_add<<<256, 256, 0, st>>>(a, n, dt, out);
 }
 
 }  // namespace bmc

@@ -15,7 +15,7 @@ namespace bmc {
 
 // Layout version of KernelSet; a plugin built against another layout is
 // refused at load time.
-constexpr int kKernelSetAbi = 8;
+constexpr int kKernelSetAbi = 9;
 // Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
 // whole compartments per block, so a small domain still spreads over many SMs.
 constexpr unsigned kLiquidThreads = 32;
@@ -100,6 +100,7 @@ const KernelSet* set_simple_acetate();
 const KernelSet* udf_kernel_set(int model, int f64);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive, unsigned long long* out);
+void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);
 

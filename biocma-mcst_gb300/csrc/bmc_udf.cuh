@@ -24,8 +24,18 @@
 //   BMC_UDF_FN static void init(F* x, const float* draws, const double* params);
 //   BMC_UDF_FN static double mass(const F* x, const double* params);
 // update() returns bmc::kIdle or bmc::kDivision (Model::update's Status);
-// pf holds the 16 parameters converted to F.  Every function is compiled
-// for the device (the kernels) and for the host (bmc_udf_get_host_model).
+// pf holds the 16 parameters converted to F.  A model whose update draws
+// random numbers or reads the compartment's concentrations directly (the
+// reference's update(random_pool, d_t, idx, arr, contribs, position, c))
+// declares instead of update / update_general:
+//   static constexpr bool uses_context = true;
+//   BMC_UDF_FN static int update_ctx(F dt, F* x, const F* r, F* out, const F* pf,
+//                                    const bmc::UpdateContext& ctx);
+// with out the basis (separable) or the n_ctb contributions (general), and
+// ctx.draws four uniforms of the particle and step, ctx.c the n_species
+// concentrations of its compartment, ctx.position the compartment.  Every
+// function is compiled for the device (the kernels) and for the host
+// (bmc_udf_get_host_model).
 //
 // Build with the library's flags (bmc/udf.py build_udf): sm_103a,
 // --fmad=false, -ffp-contract=off, hidden visibility; only the entry points
@@ -54,13 +64,31 @@ struct HostModel {
   static int32_t update(double dt, void* x, const void* r, void* out, const double* p) {
     F pf[16];
     for (int k = 0; k < 16; ++k) pf[k] = (F)p[k];
-    if constexpr (Model::separable) {
+    if constexpr (has_context<Model>::value) {
+      (void)dt;
+      (void)x;
+      (void)r;
+      (void)out;
+      return -1;  // the model updates through update_ctx
+    } else if constexpr (Model::separable) {
       F b = (F)0;
       const int st = Model::update((F)dt, static_cast<F*>(x), static_cast<const F*>(r), b, pf);
       *static_cast<F*>(out) = b;
       return st;
     } else {
       return Model::update_general((F)dt, static_cast<F*>(x), static_cast<const F*>(r), static_cast<F*>(out), pf);
+    }
+  }
+  static int32_t update_ctx(double dt, void* x, const void* r, void* out, const double* p, const float* draws,
+                            const double* c, uint32_t position, uint32_t n_species) {
+    if constexpr (has_context<Model>::value) {
+      F pf[16];
+      for (int k = 0; k < 16; ++k) pf[k] = (F)p[k];
+      const UpdateContext ctx{draws, c, position, n_species};
+      return Model::update_ctx((F)dt, static_cast<F*>(x), static_cast<const F*>(r), static_cast<F*>(out), pf, ctx);
+    } else {
+      (void)dt, (void)x, (void)r, (void)out, (void)p, (void)draws, (void)c, (void)position, (void)n_species;
+      return -1;
     }
   }
   static double coef(const void* r, int32_t j) {
@@ -85,6 +113,7 @@ struct HostModel {
     o->division = &division;
     o->init = &init;
     o->mass = &mass;
+    o->update_ctx = has_context<Model>::value ? &update_ctx : nullptr;
   }
 };
 

@@ -23,7 +23,7 @@ extern "C" {
 #endif
 
 #define BMC_VERSION_MAJOR 1
-#define BMC_VERSION_MINOR 0
+#define BMC_VERSION_MINOR 1
 
 /* Return codes (reference: ApiResult::to_c_ret_code,
  * apps/api/public/api/results.hpp; ErrorCodes,
@@ -468,6 +468,12 @@ typedef struct bmc_udf_host_model {
   void (*division)(void* x, void* child, const float* draws, const double* params);
   void (*init)(void* x, const float* draws, const double* params);
   double (*mass)(const void* x, const double* params);
+  /* Models that update with their context (uses_context in the model
+   * source): update_ctx replaces update, with the particle's four draws of
+   * the step, its compartment's n_species concentrations c and the
+   * compartment index; NULL for the other models. */
+  int32_t (*update_ctx)(double dt, void* x, const void* r, void* out, const double* params, const float* draws,
+                        const double* c, uint32_t position, uint32_t n_species);
 } bmc_udf_host_model;
 int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* out);
 
@@ -476,6 +482,11 @@ int bmc_udf_get_host_model(int32_t model_id, int32_t f64, bmc_udf_host_model* ou
  * computed on the device (checks the draw source against the oracle). */
 int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step,
                     uint32_t purpose, float* out);
+/* The cycle kernels' age step on n ages >= 0 computed on the device:
+ * out[k] = (float)((double)ages[k] + dt), the reference's `ages(i, 0) +=
+ * d_t` with float ages and a double time step (move_kernel.hpp L356),
+ * evaluated by the kernels with float and integer operations. */
+int bmc_debug_age_add(const float* ages, uint64_t n, double dt, float* out);
 /* Self-test of the bounded barrier wait of the cycle kernels: one thread
  * waits on an mbarrier whose single arrival it makes first (arrive != 0) or
  * that nothing makes; in the second case the wait gives up after limit_ns

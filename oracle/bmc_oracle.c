@@ -177,11 +177,21 @@ static double model_coef(const orc_state* s, const void* r, int j) {
  * writes its contribution w-free into ctb[0]. */
 static int model_update(const orc_state* s, double dt, uint64_t i, const void* r, double* basis, double* ctb) {
   const uint64_t cap = s->phys_capacity;
+  float ctx_draws[4];
+  const double* ctx_c = NULL;
+  if (s->udf && s->udf->update_ctx) {
+    /* the reference's update(random_pool, d_t, idx, arr, contribs, position,
+     * c): the particle's draws of the step and its compartment's
+     * concentrations */
+    draws_for(s, s->id[i], 3u, ctx_draws);
+    ctx_c = s->C + (uint64_t)s->pos[i] * s->n_s;
+  }
   if (s->udf && s->f64) {
     double* st = (double*)s->state;
     double x[16], out[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    const int res = s->udf->update(dt, x, r, out, s->params);
+    const int res = ctx_c ? s->udf->update_ctx(dt, x, r, out, s->params, ctx_draws, ctx_c, s->pos[i], s->n_s)
+                          : s->udf->update(dt, x, r, out, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
     *basis = out[0];
     for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = out[j];
@@ -191,7 +201,9 @@ static int model_update(const orc_state* s, double dt, uint64_t i, const void* r
     float* st = (float*)s->state;
     float x[16], out[16] = {0};
     for (uint32_t v = 0; v < s->n_var; ++v) x[v] = st[v * cap + i];
-    const int res = s->udf->update((double)(float)dt, x, r, out, s->params);
+    const int res = ctx_c ? s->udf->update_ctx((double)(float)dt, x, r, out, s->params, ctx_draws, ctx_c, s->pos[i],
+                                               s->n_s)
+                          : s->udf->update((double)(float)dt, x, r, out, s->params);
     for (uint32_t v = 0; v < s->n_var; ++v) st[v * cap + i] = x[v];
     *basis = (double)out[0];
     for (uint32_t j = 0; j < s->n_ctb; ++j) ctb[j] = (double)out[j];

@@ -61,6 +61,10 @@ typedef struct orc_udf_model {
   void (*division)(void* x, void* child, const float* draws, const double* params);
   void (*init)(void* x, const float* draws, const double* params);
   double (*mass)(const void* x, const double* params);
+  /* update with the particle's context (draws of purpose 3, the
+   * compartment's concentrations and index), NULL when the model has none */
+  int32_t (*update_ctx)(double dt, void* x, const void* r, void* out, const double* params, const float* draws,
+                        const double* c, uint32_t position, uint32_t n_species);
 } orc_udf_model;
 
 #define ORC_MAX_OUTLETS 8

@@ -65,7 +65,7 @@ class OrcUdfModel(ct.Structure):
     _fields_ = [("n_var", ct.c_uint32), ("n_ctb", ct.c_uint32), ("n_rates", ct.c_uint32),
                 ("separable", ct.c_int32), ("rates", ct.c_void_p), ("update", ct.c_void_p),
                 ("coef", ct.c_void_p), ("division", ct.c_void_p), ("init", ct.c_void_p),
-                ("mass", ct.c_void_p)]
+                ("mass", ct.c_void_p), ("update_ctx", ct.c_void_p)]
 
 
 def udf_host_model(path: str, f64: bool):

@@ -37,7 +37,7 @@ def test_version_and_error_without_gpu():
     L = _lib.load()
     a, b = ct.c_int32(), ct.c_int32()
     assert L.bmc_version(ct.byref(a), ct.byref(b)) == 0
-    assert (a.value, b.value) == (1, 0)
+    assert (a.value, b.value) == (1, 1)
     # argument validation happens before any device work
     assert L.bmc_scenario_create(None, None) == -1
     assert b"null" in L.bmc_last_error()

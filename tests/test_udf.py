@@ -162,3 +162,62 @@ def test_gpu_library_model_matches_oracle(oracle_mod, shape):
         births += gs["births"]
     assert births > 0
     assert_same_particles(g, o, "end")
+
+
+STOCHASTIC_PARAMS = [2e-8, 2e-6, 1e-3, 0.6e-6, 0.5, 0.01]  # ..., p_div
+
+
+def stochastic_udf_spec(f64: bool):
+    lin = np.float32(1000) * np.float32(np.pi) * np.float32(0.6e-6) ** 2 / np.float32(4)
+    phi_max = float(np.float32(2e-8) * lin / np.float32(0.5))
+    return udf.udf_model(udf.example("stochastic_udf.cu"), f64, params=STOCHASTIC_PARAMS,
+                         value_bound=[4.0 * phi_max])
+
+
+def test_context_model_host_functions(oracle_mod):
+    """A model that draws in update and reads its compartment's
+    concentrations: the library exports update_ctx (no update), and the
+    oracle drives it with the draws of purpose 3 and the concentrations."""
+    spec = stochastic_udf_spec(False)
+    hm = udf.host_model(spec.model_id, False)
+    assert hm.update_ctx and hm.update_ctx != hm.update
+    assert not udf.host_model(monod_udf_spec(False).model_id, False).update_ctx
+    sc = scenarios.small_ring(4000, f64=False, model=spec, feeds=True)
+    sc.alloc_factor = 2.0
+    o1, o2 = oracle_mod.Oracle(sc), oracle_mod.Oracle(sc)
+    o1.init_particles()
+    o2.init_particles()
+    births = 0
+    for _ in range(20):
+        s1, s2 = o1.step(), o2.step()
+        assert s1 == s2
+        births += s1["births"]
+    assert births > 0  # chance divisions (p_div = 0.01 per step)
+    # the draws matter: another seed gives other lengths
+    o3 = oracle_mod.Oracle(scenarios.small_ring(4000, f64=False, model=spec, feeds=True, seed=9))
+    o3.init_particles()
+    o3.step()
+    assert not np.array_equal(o3.particles()["state"], o1.particles()["state"][:, : o3.n_used])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("f64", [False, True])
+@pytest.mark.parametrize("shape", [None, (256, 2, 0)])
+def test_gpu_context_model_matches_oracle(oracle_mod, f64, shape):
+    """update_ctx with draws and raw concentrations: GPU kernels from the
+    library against the oracle driving the library's host functions."""
+    from test_gpu_parity import assert_same_liquid, assert_same_particles, assert_same_stats, make_pair
+
+    sc = scenarios.small_ring(12000, f64=f64, model=stochastic_udf_spec(f64), feeds=True)
+    sc.alloc_factor = 2.0
+    g, o = make_pair(oracle_mod, sc)
+    if shape:
+        g.set_shape(*shape)
+    births = 0
+    for k in range(25):
+        gs, os_ = g.step(), o.step()
+        assert_same_stats(gs, os_, f"step {k}")
+        assert_same_liquid(g, o, f"step {k}")
+        births += gs["births"]
+    assert births > 0
+    assert_same_particles(g, o, "end")
