@@ -13,7 +13,10 @@ the host admits new requests (their initialisation uses their own streams)
 and they take their slots as soon as the chunk ends, so admission overlaps
 device work.
 
-Latency of a request = completion time - arrival time.
+Latency of a request = completion time - arrival time.  Particle-steps
+are counted from live particles: for every completed request, its step
+count times the mean of its live particles at admission and at completion
+(births between the two are counted half).
 """
 from __future__ import annotations
 
@@ -173,10 +176,11 @@ class Server:
                 r, g, need, st, slot = a
                 adv = min(chunk, r.steps - st)
                 a[3] = st + adv
-                steps_done += float(r.scen.n_particles) * adv
                 if a[3] >= r.steps:
                     r.finished = done_at
                     r.result = g.stats()
+                    alive_end = r.result["n_used"] - r.result["inactive"]
+                    steps_done += 0.5 * (float(r.scen.n_particles) + float(alive_end)) * r.steps
                     if on_finish is not None:
                         on_finish(r, g)
                     batch.set_slot(slot, None)
@@ -196,6 +200,7 @@ class Server:
         lat = np.array([r.latency for r in done]) if done else np.array([np.nan])
         return {
             "requests": len(reqs), "completed": len(done), "wall_s": wall, "gpu_busy_s": busy,
+            "utilisation": busy / wall if wall > 0 else 0.0,
             "particle_steps": steps_done, "particle_steps_per_s": steps_done / wall if wall > 0 else 0.0,
             "latency_p50_s": float(np.nanpercentile(lat, 50)), "latency_p99_s": float(np.nanpercentile(lat, 99)),
             "latency_mean_s": float(np.nanmean(lat)), "slots": self.n_slots,

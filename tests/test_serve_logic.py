@@ -43,7 +43,8 @@ def make_fakes(world, budget_probe):
             self.limit = n
 
         def stats(self):
-            return {"step": self.steps}
+            # one birth per step, nothing removed
+            return {"step": self.steps, "n_used": self.scen.n_particles + self.steps, "inactive": 0}
 
         def close(self):
             world.live.discard(self)
@@ -102,7 +103,9 @@ def test_every_request_runs_exactly_its_steps(monkeypatch):
         assert r.result["step"] == r.steps
         assert r.finished >= r.arrival and r.latency >= 0
     assert not world.live  # every scenario released
-    assert out["particle_steps"] == sum(r.scen.n_particles * r.steps for r in reqs)
+    # counted from live particles: the mean of the counts at admission and completion
+    assert out["particle_steps"] == pytest.approx(sum((r.scen.n_particles + 0.5 * r.steps) * r.steps for r in reqs))
+    assert 0.0 < out["utilisation"] <= 1.0
     assert max(world.batches) > 1  # scenarios shared launches
 
 
