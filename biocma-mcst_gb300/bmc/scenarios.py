@@ -162,7 +162,7 @@ class Scenario:
 
     def quantum_exponents(self, weight: float) -> np.ndarray:
         """Exponent e of the accumulator quantum 2^e per column, chosen so
-        that the value bound is 2^42 quanta (ceil(log2) taken exactly)."""
+        that the value bound is 2^QBITS quanta (ceil(log2) taken exactly)."""
         e = np.zeros(8, dtype=np.int32)
         cols = 1 if self.model.separable else self.model.n_ctb
         for j in range(cols):
@@ -170,7 +170,7 @@ class Scenario:
             if not self.model.separable:
                 vmax *= weight
             m, ex = math.frexp(vmax)
-            e[j] = (ex - 1 if m == 0.5 else ex) - 42
+            e[j] = (ex - 1 if m == 0.5 else ex) - QBITS
         return e
 
     def algorithmic_bytes(self) -> int:
@@ -179,7 +179,8 @@ class Scenario:
         return 2 * (self.model.n_var * self.model.itemsize + 4 + 1 + 8)
 
 
-CTB_QMAX = 1 << 42
+QBITS = 26  # a value at its bound is 2^QBITS quanta of the exact sums
+CTB_QMAX = 1 << QBITS
 
 
 def weight_from_mass(total_mass: float, x0: float, total_volume: float) -> float:

@@ -534,14 +534,14 @@ int set_quanta(bmc_scenario* s) {
   // Separable models accumulate one basis value per particle (column 0,
   // bounded by value_bound[0]); general models accumulate weight *
   // contribution j per particle (column j, bounded by weight *
-  // value_bound[j]).  The quantum 2^e puts the bound at 2^42 quanta.
+  // value_bound[j]).  The quantum 2^e puts the bound at 2^kQBits quanta.
   const int cols = s->ks->separable ? 1 : s->ks->n_ctb;
   for (int j = 0; j < bmc::kMaxSpecies; ++j) {
     int e = 0;
     if (j < cols) {
       const double vmax = s->ks->separable ? s->desc.value_bound[j] : s->h.weight * s->desc.value_bound[j];
       if (!(vmax > 0.0) || !std::isfinite(vmax)) return fail(BMC_E_INVALID, "value bounds must be > 0");
-      e = ceil_log2(vmax) - 42;
+      e = ceil_log2(vmax) - bmc::kQBits;
     }
     s->h.q_exp[j] = e;
     s->h.q_scale_up[j] = std::ldexp(1.0, e);

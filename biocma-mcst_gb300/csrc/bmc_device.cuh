@@ -31,7 +31,13 @@ constexpr int kMaxOutlets = 8;
 constexpr int kMaxSpecies = 8;
 constexpr int kMaxVar = 16;
 constexpr int kMaxRates = 8;
-constexpr long long kQMax = 1LL << 42;  // |quantised value| bound
+// Fixed point of the contribution sums: a value at its bound is 2^kQBits
+// quanta (resolution 2^-26 of the bound, finer than a float's 2^-24 of the
+// value for every value above a quarter of the bound).  |q| < 2^32 keeps the
+// carry into an accumulator entry's high word rare (at most 2^26 / 2^32 of
+// the adds), so most particles spend one shared-memory atomic.
+constexpr int kQBits = 26;
+constexpr long long kQMax = 1LL << kQBits;  // |quantised value| bound
 // A block flushes its shared-memory accumulator before it has summed more
 // than 2^20 particles, so |partial| <= 2^62 and no int64 sum can overflow.
 constexpr unsigned kFlushParticles = 1u << 20;

@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
 
 // ---------------------------------------------------------------------------
 // Quantisation of a value to the accumulator's fixed point: the nearest
-// integer multiple of 2^e (ties to even), clamped to |q| <= 2^42.  Done on
+// integer multiple of 2^e (ties to even), clamped to |q| <= kQMax.  Done on
 // the integer pipe from the IEEE fields of v, so no FP64 instruction is
 // spent per particle; the result equals rint(v * 2^-e) evaluated in double.
 template <int MBITS, int EBITS, int BIAS, class U>

@@ -211,7 +211,9 @@ class Oracle:
         s.step = 0
         s.dead_ratio_threshold = scen.dead_ratio_threshold
         s.min_removal = scen.min_removal
-        s.q_max = 1 << 42
+        from bmc.scenarios import CTB_QMAX
+
+        s.q_max = CTB_QMAX
         s.separable = 1 if m.separable else 0
         s.quirk_tag3d = 1 if quirk_tag3d else 0
         self._udf = None
