@@ -362,10 +362,9 @@ def run_gpu(args):
     g.close()
     forms = None
     if rank == 0 and world == 1 and not args.no_forms:
-        batched = batched_form(args.forms_steps)
         forms = {"precision": precision_form(args.forms_steps),
-                 "batched": batched,
-                 "served": served_forms(args.serve_window, batched.get("batched_value"))}
+                 "batched": batched_form(args.forms_steps),
+                 "served": served_forms(args.serve_window)}
 
     if rank == 0:
         cfg = workload_config(scen)
@@ -552,20 +551,20 @@ def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):
     return out
 
 
-def served_forms(window_s: float, batched_capacity: float | None):
-    """The configured load (50 requests/s) and a sub-saturating one: the
-    arrival rate at which demand is about 70 % of the batched form's measured
-    particle-steps/s."""
+def served_forms(window_s: float):
+    """The configured load (50 requests/s, which saturates the server) and a
+    sub-saturating one: the arrival rate at which demand is about 70 % of the
+    throughput the server sustained under the configured load."""
     from bmc import serve
 
-    out = {"configured_load": served_form(window_s)}
-    if batched_capacity:
-        probe = serve.poisson_requests(50.0, max(window_s, 10.0), seed=2027)
-        per_request = sum(r.particle_steps for r in probe) / len(probe)
-        rate = 0.7 * batched_capacity / per_request
-        sub = served_form(window_s, rate=rate)
-        sub["target_demand_fraction_of_batched"] = 0.7
-        out["sub_saturating_load"] = sub
+    conf = served_form(window_s)
+    out = {"configured_load": conf}
+    probe = serve.poisson_requests(50.0, max(window_s, 10.0), seed=2027)
+    per_request = sum(r.particle_steps for r in probe) / len(probe)
+    rate = 0.7 * conf["particle_steps_per_s"] / per_request
+    sub = served_form(window_s, rate=rate)
+    sub["target_demand_fraction_of_saturated_throughput"] = 0.7
+    out["sub_saturating_load"] = sub
     return out
 
 
@@ -577,7 +576,7 @@ def main():
                                       compare_plain=False)))
         return
     if args.served_only:
-        print(json.dumps(served_forms(args.serve_window, None)))
+        print(json.dumps(served_forms(args.serve_window)))
         return
     if args.impl == "reference":
         run_reference(args)

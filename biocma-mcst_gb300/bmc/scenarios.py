@@ -179,7 +179,7 @@ class Scenario:
         return 2 * (self.model.n_var * self.model.itemsize + 4 + 1 + 8)
 
 
-QBITS = 26  # a value at its bound is 2^QBITS quanta of the exact sums
+QBITS = 42  # a value at its bound is 2^QBITS quanta of the exact sums
 CTB_QMAX = 1 << QBITS
 
 

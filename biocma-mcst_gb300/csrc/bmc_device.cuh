@@ -32,11 +32,11 @@ constexpr int kMaxSpecies = 8;
 constexpr int kMaxVar = 16;
 constexpr int kMaxRates = 8;
 // Fixed point of the contribution sums: a value at its bound is 2^kQBits
-// quanta (resolution 2^-26 of the bound, finer than a float's 2^-24 of the
-// value for every value above a quarter of the bound).  |q| < 2^32 keeps the
-// carry into an accumulator entry's high word rare (at most 2^26 / 2^32 of
-// the adds), so most particles spend one shared-memory atomic.
-constexpr int kQBits = 26;
+// quanta (resolution 2^-42 of the bound).  A coarser 2^26, which keeps most
+// adds to one 32-bit shared atomic (no carry into the high word), was slower
+// on the batched workload (cycle 2.12 -> 2.25 ms): a warp still issues the
+// second atomic whenever one of its lanes carries.
+constexpr int kQBits = 42;
 constexpr long long kQMax = 1LL << kQBits;  // |quantised value| bound
 // A block flushes its shared-memory accumulator before it has summed more
 // than 2^20 particles, so |partial| <= 2^62 and no int64 sum can overflow.

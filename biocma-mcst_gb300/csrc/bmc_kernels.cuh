@@ -331,13 +331,11 @@ __device__ __forceinline__ bool consumer_any(bool v, unsigned n_threads) {
 // Exact add of q to a shared-memory accumulator entry, kept as two 32-bit
 // words {low: unsigned, high: signed}: the low word takes a 32-bit atomic
 // whose old value gives the carry, the high word a second one with q >> 32
-// plus the carry (skipped when 0: with |q| <= 2^26 that is every add whose
-// low word does not wrap).  Read as one 64-bit word (little endian) the
-// entry is the two's-complement sum while the high word stays in int32:
+// plus the carry (skipped when 0).  Read as one 64-bit word (little endian)
+// the entry is the two's-complement sum while the high word stays in int32:
 // between flushes an entry takes at most kFlushParticles (2^20) particles'
-// values of |q| <= 2^42 (the arithmetic holds up to there; kQMax is 2^26),
-// so every partial sum of the high adds is below 2^20 * (2^10 + 1) in
-// magnitude (a warp-aggregated add of up to 32 values counts as their sum:
+// values of |q| <= 2^42 (kQMax), so every partial sum of the high adds is
+// below 2^20 * (2^10 + 1) in magnitude (a warp-aggregated add of up to 32 values counts as their sum:
 // below 2^30 + 2^21).  32-bit shared atomics are native; a 64-bit one took
 // about 18 shared-memory wavefronts per warp instruction.
 __device__ __forceinline__ void acc_add(unsigned long long* e, long long q) {
