@@ -92,6 +92,8 @@ SIGNATURES = {
     "bmc_cycle": [VP, c_dbl, VP],
     "bmc_cycle_external": [VP, c_dbl, VP, VP, c_i32, VP],
     "bmc_step": [VP, c_dbl, VP],
+    "bmc_step_enqueue": [VP, c_dbl, VP, VP],
+    "bmc_step_collect": [VP],
     "bmc_run": [VP, c_dbl, c_u32, VP],
     "bmc_run_async": [VP, c_dbl, c_u32],
     "bmc_synchronize": [VP],

@@ -218,6 +218,19 @@ class GpuScenario:
         call("bmc_step_read", self.handle, dt or self.scen.dt, ct.byref(st), _p(conc))
         return st.as_dict()
 
+    def step_enqueue(self, stats, conc: np.ndarray, dt: float | None = None):
+        """bmc_step_enqueue: one step and the read-back of its counters into
+        `stats` (a StepStats) and concentrations into `conc` (float64
+        [n_c, n_species], C-contiguous), filled by the matching
+        step_collect; the buffers must stay alive until then."""
+        n = self.scen.net.n_c * self.scen.n_species
+        if conc.dtype != np.float64 or not conc.flags.c_contiguous or conc.size != n:
+            raise ValueError(f"conc must be a C-contiguous float64 array of {n} values")
+        call("bmc_step_enqueue", self.handle, dt or self.scen.dt, ct.byref(stats), _p(conc))
+
+    def step_collect(self):
+        call("bmc_step_collect", self.handle)
+
     def step_timed(self, dt: float | None = None):
         """One step with per-kernel CUDA-event durations (ms): liquid, cycle,
         plan, divide, compact, merge."""

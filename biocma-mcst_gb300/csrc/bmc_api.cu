@@ -205,6 +205,23 @@ struct bmc_scenario {
   // gas phase of a two-phase flow (device arrays in garena)
   void* garena = nullptr;
   std::vector<double> gvol;
+  // steps enqueued by bmc_step_enqueue, collected in order by
+  // bmc_step_collect: pinned copies of each step's control block and
+  // concentrations, an event, and the caller's buffers
+  struct Pending {
+    Control* ctl = nullptr;      // pinned
+    double* conc = nullptr;      // pinned, room for both buffers
+    cudaEvent_t done = nullptr;
+    bmc_step_stats* stats = nullptr;
+    double* out = nullptr;
+    int parity = -1;             // buffer copied (-1: both)
+  };
+  Pending pend[2];
+  unsigned pend_head = 0, pend_count = 0;
+  size_t pend_ne = 0;
+  // the step counter after the last enqueued step, when known on the host
+  long long pred_step = -1;
+  bool enqueuing = false;  // inside bmc_step_enqueue
 };
 
 struct bmc_batch {
@@ -496,33 +513,36 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
   return BMC_OK;
 }
 
+void stats_from_ctl(const Control& c, bmc_step_stats* out) {
+  std::memset(out, 0, sizeof(*out));
+  out->n_used = c.n_used;
+  out->inactive = c.inactive;
+  out->births = c.last_births;
+  out->exits = c.last_exits;
+  out->moves = c.last_moves;
+  out->overflow = c.last_overflow;
+  out->requested_divisions = c.last_req_div;
+  out->clamped = c.clamped;
+  out->next_id = c.next_id;
+  out->step = c.step;
+  out->compacted = c.last_compacted;
+  out->error = c.error;
+  for (int k = 0; k < 8; ++k) out->mass_balance[k] = c.mass_balance[k];
+}
+
 int read_ctl(bmc_scenario* s, bmc_step_stats* out) {
   BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
   BMC_CUDA(cudaStreamSynchronize(s->stream));
   s->ctl_fresh = true;
-  if (out) {
-    const Control& c = *s->h_ctl;
-    std::memset(out, 0, sizeof(*out));
-    out->n_used = c.n_used;
-    out->inactive = c.inactive;
-    out->births = c.last_births;
-    out->exits = c.last_exits;
-    out->moves = c.last_moves;
-    out->overflow = c.last_overflow;
-    out->requested_divisions = c.last_req_div;
-    out->clamped = c.clamped;
-    out->next_id = c.next_id;
-    out->step = c.step;
-    out->compacted = c.last_compacted;
-    out->error = c.error;
-    for (int k = 0; k < 8; ++k) out->mass_balance[k] = c.mass_balance[k];
-  }
+  if (out) stats_from_ctl(*s->h_ctl, out);
   if (s->h_ctl->error) return fail(BMC_E_DEVICE, "device error word set: " + std::to_string(s->h_ctl->error));
   return BMC_OK;
 }
 
 int check_ready(bmc_scenario* s, bool need_liquid) {
   if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (s->pend_count > 0 && !s->enqueuing)
+    return fail(BMC_E_STATE, "steps enqueued by bmc_step_enqueue are not collected yet");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update)");
   if (!s->has_conc) return fail(BMC_E_STATE, "concentrations not set (bmc_set_concentrations)");
   if (!s->has_weight) return fail(BMC_E_STATE, "particles not initialised (bmc_init_particles / bmc_set_weight)");
@@ -705,6 +725,11 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->garena) cudaFree(s->garena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->h_cstage) cudaFreeHost(s->h_cstage);
+  for (auto& q : s->pend) {
+    if (q.ctl) cudaFreeHost(q.ctl);
+    if (q.conc) cudaFreeHost(q.conc);
+    if (q.done) cudaEventDestroy(q.done);
+  }
   cudaStreamDestroy(s->stream);
   delete s;
   return BMC_OK;
@@ -2193,6 +2218,83 @@ int bmc_feed_time(bmc_scenario* s, double* t) {
   const int rc = read_ctl(s, nullptr);
   if (rc && rc != BMC_E_DEVICE) return rc;
   *t = s->h_ctl->t_rel;
+  return BMC_OK;
+}
+
+// ---- pipelined main loop --------------------------------------------------------------
+int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc) {
+  if (!s || !stats || !conc) return fail(BMC_E_INVALID, "null argument");
+  if (s->pend_count >= 2) return fail(BMC_E_STATE, "two steps in flight: collect one first");
+  if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  if (s->pend_ne < ne) {
+    if (s->pend_count > 0) return fail(BMC_E_STATE, "the domain grew while steps are in flight");
+    for (auto& q : s->pend) {
+      if (q.conc) cudaFreeHost(q.conc);
+      q.conc = nullptr;
+    }
+    s->pend_ne = 0;
+    for (auto& q : s->pend) BMC_CUDA(cudaMallocHost(&q.conc, 2 * ne * sizeof(double)));
+    s->pend_ne = ne;
+  }
+  bmc_scenario::Pending& q = s->pend[(s->pend_head + s->pend_count) % 2];
+  if (!q.ctl) BMC_CUDA(cudaMallocHost(&q.ctl, sizeof(Control)));
+  if (!q.done) BMC_CUDA(cudaEventCreateWithFlags(&q.done, cudaEventDisableTiming));
+  // the step counter after this step, when the host knows the one before it
+  // (a step advances it by one unless the step limit holds it)
+  long long before = -1;
+  if (s->pend_count == 0)
+    before = s->ctl_fresh ? (long long)s->h_ctl->step : -1;
+  else
+    before = s->pred_step;
+  long long after = -1;
+  if (before >= 0) {
+    const bool held = s->h.step_limit != 0u && (unsigned long long)before >= s->h.step_limit;
+    after = held ? before : before + 1;
+  }
+  s->enqueuing = true;
+  const int rc = scenario_steps(s, dt, 1, 1, true);
+  s->enqueuing = false;
+  if (rc) return rc;
+  BMC_CUDA(counted_memcpy_async(q.ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
+  if (after >= 0) {
+    q.parity = (int)(after & 1);
+    BMC_CUDA(counted_memcpy_async(q.conc + q.parity * ne, s->h.C + q.parity * ne, ne * sizeof(double),
+                                  cudaMemcpyDeviceToHost, s->stream));
+  } else {
+    q.parity = -1;
+    BMC_CUDA(counted_memcpy_async(q.conc, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  }
+  BMC_CUDA(cudaEventRecord(q.done, s->stream));
+  q.stats = stats;
+  q.out = conc;
+  s->pred_step = after;
+  s->pend_count++;
+  return BMC_OK;
+}
+
+int bmc_step_collect(bmc_scenario* s) {
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (s->pend_count == 0) return fail(BMC_E_STATE, "no step enqueued");
+  bmc_scenario::Pending& q = s->pend[s->pend_head];
+  BMC_CUDA(cudaEventSynchronize(q.done));
+  s->pend_head = (s->pend_head + 1) % 2;
+  s->pend_count--;
+  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
+  const int cur = (int)(q.ctl->step & 1u);
+  if (q.parity >= 0 && q.parity != cur) {
+    // not expected: the buffer the counter names is still intact (a step in
+    // flight writes the other one)
+    BMC_CUDA(counted_memcpy(q.conc + cur * ne, s->h.C + cur * ne, ne * sizeof(double), cudaMemcpyDeviceToHost));
+    s->pred_step = -1;
+  }
+  std::memcpy(q.out, q.conc + cur * ne, ne * sizeof(double));
+  stats_from_ctl(*q.ctl, q.stats);
+  if (s->pend_count == 0) {
+    std::memcpy(s->h_ctl, q.ctl, sizeof(Control));
+    s->ctl_fresh = true;
+  }
+  if (q.ctl->error) return fail(BMC_E_DEVICE, "device error word set: " + std::to_string(q.ctl->error));
   return BMC_OK;
 }
 

@@ -255,6 +255,19 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
  * the field every iteration). */
 int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc);
 
+/* A main loop that reads the field back every iteration, pipelined: the
+ * host enqueues step k+1 before it waits for the results of step k, so the
+ * device does not idle while the host handles them.  bmc_step_enqueue
+ * enqueues one iteration (as bmc_step) and the copy of its counters and
+ * concentrations [n_c][n_s] into pinned staging, without waiting; at most
+ * two steps are in flight.  bmc_step_collect waits for the oldest enqueued
+ * step and writes its results into the stats and conc buffers given to its
+ * bmc_step_enqueue (returns BMC_E_DEVICE when that step set the error
+ * word).  Other stepping calls on the scenario are refused (BMC_E_STATE)
+ * until every enqueued step is collected. */
+int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc);
+int bmc_step_collect(bmc_scenario* s);
+
 /* n_steps iterations on the device without host round trips (one captured
  * CUDA graph replayed).  Statistics are those of the last step. */
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats);
