@@ -131,6 +131,9 @@ SIGNATURES = {
     "bmc_cma_transition": [c_u32, c_u64, VP, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_cma_time_step": [c_dbl, c_u32, c_u32, VP, VP, VP],
     "bmc_cma_read_field": [ct.c_char_p, c_u64, VP, VP],
+    "bmc_cma_read_case": [ct.c_char_p, VP, VP, VP],
+    "bmc_cma_case_entry": [ct.c_char_p, ct.c_uint32, VP, VP, c_u64],
+    "bmc_cma_read_flowmap": [ct.c_char_p, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_flowmap_add": [VP, VP, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_flowmap_period": [VP, c_dbl],
     "bmc_flowmap_clear": [VP],

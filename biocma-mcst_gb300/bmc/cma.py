@@ -78,6 +78,88 @@ def read_field(path: str) -> np.ndarray:
     return out
 
 
+# Entry kinds of a case descriptor (those of the reference's 0-D fixture).
+KIND_LIQUID_FLOW = 0
+KIND_LIQUID_VOLUME = 3
+
+
+def read_case(path: str) -> dict:
+    """A case descriptor (bmc_cma_read_case / bmc_cma_case_entry): the four
+    header words and the float as stored, and the entries as (kind, path)
+    pairs in file order."""
+    words = (ct.c_uint32 * 4)()
+    t0, n = ct.c_double(), ct.c_uint32()
+    call("bmc_cma_read_case", path.encode(), words, ct.byref(t0), ct.byref(n))
+    entries = []
+    for k in range(n.value):
+        kind = ct.c_uint32()
+        name = ct.create_string_buffer(4096)
+        call("bmc_cma_case_entry", path.encode(), k, ct.byref(kind), name, len(name))
+        entries.append((kind.value, name.value.decode()))
+    return {"words": list(words), "t0": t0.value, "entries": entries}
+
+
+def read_flowmap(path: str):
+    """A liquid flow map file (bmc_cma_read_flowmap): (rows, columns, row
+    indices, column indices, flows)."""
+    nr, nc, nnz = ct.c_uint32(), ct.c_uint32(), ct.c_uint64()
+    call("bmc_cma_read_flowmap", path.encode(), ct.byref(nr), ct.byref(nc), ct.byref(nnz), 0, None, None, None)
+    r = np.zeros(nnz.value, np.uint64)
+    c = np.zeros(nnz.value, np.uint64)
+    f = np.zeros(nnz.value)
+    if nnz.value:
+        call("bmc_cma_read_flowmap", path.encode(), ct.byref(nr), ct.byref(nc), ct.byref(nnz), nnz.value, _p(r), _p(c),
+             _p(f))
+    return nr.value, nc.value, r, c, f
+
+
+def load_case(folder: str, descriptor: str = "cma_case") -> networks.Network:
+    """The Network of a CMA case folder: the descriptor names the liquid
+    volume field and the liquid flow map (paths relative to the folder); the
+    map must be square over the volumes' compartments."""
+    import os
+
+    case = read_case(os.path.join(folder, descriptor))
+    files = {}
+    for kind, name in case["entries"]:
+        files.setdefault(kind, os.path.normpath(os.path.join(folder, name)))
+    if KIND_LIQUID_VOLUME not in files or KIND_LIQUID_FLOW not in files:
+        raise ValueError("the case descriptor names no liquid volume field or no liquid flow map")
+    vol = read_field(files[KIND_LIQUID_VOLUME])
+    nr, nc, r, c, f = read_flowmap(files[KIND_LIQUID_FLOW])
+    if not (nr == nc == len(vol)):
+        raise ValueError(f"flow map of {nr} x {nc} over {len(vol)} compartment volumes")
+    return network(vol, r, c, f)
+
+
+def write_case(folder: str, volumes, rows, cols, flows, words=(1, 1, 1, 0), t0: float = 0.0) -> None:
+    """Writes a case folder in the layout the readers take: cma_case naming
+    ./vofL.raw (kind 3) and ./flowL.raw (kind 0), as the reference's 0-D
+    fixture does, the volume field and the flow map."""
+    import os
+    import struct
+
+    vol = np.ascontiguousarray(volumes, dtype="<f8")
+    r = np.ascontiguousarray(rows, dtype="<u8")
+    c = np.ascontiguousarray(cols, dtype="<u8")
+    f = np.ascontiguousarray(flows, dtype="<f8")
+    if not (len(r) == len(c) == len(f)):
+        raise ValueError("rows, cols and flows differ in length")
+    os.makedirs(folder, exist_ok=True)
+    desc = struct.pack("<4Id", *words, t0) + struct.pack("<Q", 2)
+    for kind, name in ((KIND_LIQUID_VOLUME, b"./vofL.raw"), (KIND_LIQUID_FLOW, b"./flowL.raw")):
+        desc += struct.pack("<BI", kind, len(name)) + name
+    with open(os.path.join(folder, "cma_case"), "wb") as fh:
+        fh.write(desc)
+    with open(os.path.join(folder, "vofL.raw"), "wb") as fh:
+        fh.write(struct.pack("<I", len(vol)) + vol.tobytes())
+    n = len(vol)
+    with open(os.path.join(folder, "flowL.raw"), "wb") as fh:
+        fh.write(struct.pack("<II", n, n))
+        for a in (r, c, f):
+            fh.write(struct.pack("<Q", len(a)) + a.tobytes())
+
+
 def network(volume, rows, cols, flows) -> networks.Network:
     """A Network (the form scenarios carry) from a flow map: the merged
     links of the derived transition, with neighbours, out-flows and

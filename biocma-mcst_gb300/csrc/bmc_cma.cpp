@@ -66,12 +66,61 @@ uint32_t read_u32_le(const unsigned char* b) {
   return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
 }
 
-double read_f64_le(const unsigned char* b) {
+uint64_t read_u64_le(const unsigned char* b) {
   uint64_t u = 0;
   for (int k = 7; k >= 0; --k) u = (u << 8) | (uint64_t)b[k];
+  return u;
+}
+
+double read_f64_le(const unsigned char* b) {
+  const uint64_t u = read_u64_le(b);
   double d;
   std::memcpy(&d, &u, 8);
   return d;
+}
+
+// Whole file into buf; false when it cannot be opened.
+bool slurp(const char* path, std::vector<unsigned char>& buf) {
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return false;
+  buf.clear();
+  unsigned char chunk[65536];
+  size_t got;
+  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  std::fclose(f);
+  return true;
+}
+
+// Entry of a case descriptor: kind byte and the path's bytes in the file.
+struct CaseEntry {
+  uint32_t kind;
+  uint32_t len;
+  size_t off;
+};
+
+// Case descriptor: 4 uint32 words, one float64, a uint64 entry count, then
+// per entry a uint8 kind, a uint32 length and the path's bytes; the whole
+// file and nothing more.  Returns an error message or nullptr.
+const char* parse_case(const std::vector<unsigned char>& b, std::vector<CaseEntry>& out) {
+  const size_t n = b.size();
+  if (n < 32) return "case descriptor shorter than its 32-byte header";
+  const uint64_t count = read_u64_le(b.data() + 24);
+  if (count > (n - 32) / 5) return "case descriptor entry count exceeds what the file can hold";
+  out.clear();
+  size_t o = 32;
+  for (uint64_t k = 0; k < count; ++k) {
+    if (o + 5 > n) return "case descriptor ends inside an entry header";
+    CaseEntry e;
+    e.kind = b[o];
+    e.len = read_u32_le(b.data() + o + 1);
+    o += 5;
+    if (e.len == 0 || e.len > n - o) return "case descriptor entry path runs past the end of the file";
+    e.off = o;
+    o += e.len;
+    out.push_back(e);
+  }
+  if (o != n) return "case descriptor has bytes after its last entry";
+  return nullptr;
 }
 
 }  // namespace
@@ -164,13 +213,8 @@ int bmc_cma_time_step(double user_dt, uint32_t n_maps, uint32_t n_c, const doubl
 
 int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t* n) {
   if (!path || !n) return bmc::api_fail(BMC_E_INVALID, "null argument");
-  FILE* f = std::fopen(path, "rb");
-  if (!f) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
   std::vector<unsigned char> buf;
-  unsigned char chunk[65536];
-  size_t got;
-  while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
-  std::fclose(f);
+  if (!slurp(path, buf)) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
   if (buf.size() < 4) return bmc::api_fail(BMC_E_INVALID, "field file shorter than its count");
   const uint64_t count = read_u32_le(buf.data());
   if (buf.size() != 4 + 8 * count)
@@ -179,6 +223,78 @@ int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t*
   if (!values) return BMC_OK;
   if (cap < count) return bmc::api_fail(BMC_E_INVALID, "cap is below the value count");
   for (uint64_t k = 0; k < count; ++k) values[k] = read_f64_le(buf.data() + 4 + 8 * k);
+  return BMC_OK;
+}
+
+int bmc_cma_read_case(const char* path, uint32_t* words, double* t0, uint32_t* n_entries) {
+  if (!path || !n_entries) return bmc::api_fail(BMC_E_INVALID, "null argument");
+  std::vector<unsigned char> buf;
+  if (!slurp(path, buf)) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
+  std::vector<CaseEntry> ent;
+  const char* err = parse_case(buf, ent);
+  if (err) return bmc::api_fail(BMC_E_INVALID, err);
+  if (words)
+    for (int k = 0; k < 4; ++k) words[k] = read_u32_le(buf.data() + 4 * k);
+  if (t0) *t0 = read_f64_le(buf.data() + 16);
+  *n_entries = (uint32_t)ent.size();
+  return BMC_OK;
+}
+
+int bmc_cma_case_entry(const char* path, uint32_t index, uint32_t* kind, char* name, uint64_t name_cap) {
+  if (!path || !kind) return bmc::api_fail(BMC_E_INVALID, "null argument");
+  std::vector<unsigned char> buf;
+  if (!slurp(path, buf)) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
+  std::vector<CaseEntry> ent;
+  const char* err = parse_case(buf, ent);
+  if (err) return bmc::api_fail(BMC_E_INVALID, err);
+  if (index >= ent.size()) return bmc::api_fail(BMC_E_INVALID, "entry index out of range");
+  const CaseEntry& e = ent[index];
+  *kind = e.kind;
+  if (!name) return BMC_OK;
+  if (name_cap < (uint64_t)e.len + 1u) return bmc::api_fail(BMC_E_INVALID, "name_cap is below the path length + 1");
+  std::memcpy(name, buf.data() + e.off, e.len);
+  name[e.len] = '\0';
+  return BMC_OK;
+}
+
+int bmc_cma_read_flowmap(const char* path, uint32_t* n_rows, uint32_t* n_cols, uint64_t* nnz, uint64_t cap,
+                         uint64_t* rows, uint64_t* cols, double* flows) {
+  if (!path || !n_rows || !n_cols || !nnz) return bmc::api_fail(BMC_E_INVALID, "null argument");
+  std::vector<unsigned char> buf;
+  if (!slurp(path, buf)) return bmc::api_fail(BMC_E_INVALID, std::string("cannot open ") + path);
+  const size_t n = buf.size();
+  if (n < 32) return bmc::api_fail(BMC_E_INVALID, "flow map shorter than its header and three array lengths");
+  const uint32_t nr = read_u32_le(buf.data()), nc = read_u32_le(buf.data() + 4);
+  // three arrays, each a uint64 length then its elements (8 bytes each)
+  size_t o = 8;
+  uint64_t len[3];
+  size_t at[3];
+  for (int a = 0; a < 3; ++a) {
+    if (o + 8 > n) return bmc::api_fail(BMC_E_INVALID, "flow map ends inside an array length");
+    len[a] = read_u64_le(buf.data() + o);
+    o += 8;
+    if (len[a] > (n - o) / 8) return bmc::api_fail(BMC_E_INVALID, "flow map array runs past the end of the file");
+    at[a] = o;
+    o += 8 * (size_t)len[a];
+  }
+  if (o != n) return bmc::api_fail(BMC_E_INVALID, "flow map size differs from its header and array lengths");
+  if (len[0] != len[1] || len[1] != len[2])
+    return bmc::api_fail(BMC_E_INVALID, "flow map arrays (rows, columns, flows) differ in length");
+  for (uint64_t k = 0; k < len[0]; ++k) {
+    const uint64_t r = read_u64_le(buf.data() + at[0] + 8 * k), c = read_u64_le(buf.data() + at[1] + 8 * k);
+    if (r >= nr || c >= nc) return bmc::api_fail(BMC_E_INVALID, "flow map entry outside its rows and columns");
+  }
+  *n_rows = nr;
+  *n_cols = nc;
+  *nnz = len[0];
+  if (!rows && !cols && !flows) return BMC_OK;
+  if (!rows || !cols || !flows) return bmc::api_fail(BMC_E_INVALID, "give all three arrays or none");
+  if (cap < len[0]) return bmc::api_fail(BMC_E_INVALID, "cap is below the entry count");
+  for (uint64_t k = 0; k < len[0]; ++k) {
+    rows[k] = read_u64_le(buf.data() + at[0] + 8 * k);
+    cols[k] = read_u64_le(buf.data() + at[1] + 8 * k);
+    flows[k] = read_f64_le(buf.data() + at[2] + 8 * k);
+  }
   return BMC_OK;
 }
 

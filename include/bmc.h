@@ -388,6 +388,40 @@ int bmc_cma_time_step(double user_dt, uint32_t n_maps, uint32_t n_c, const doubl
  * written when values is non-NULL and cap >= count. */
 int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t* n);
 
+/* Case descriptor of a CMA case (the `cma_case` file of a case folder; the
+ * reference hands its path to rcmtool v1.4, a crate outside its tree,
+ * through get_dtransitioner, apps/core/src/global_initaliser.cpp L201-L243).
+ * Layout read as the reference's one fixture holds it
+ * (apps/api/tests/data/0d/cma_case, 63 bytes): four little-endian uint32
+ * words, one float64, a uint64 entry count, then per entry a uint8 kind, a
+ * uint32 byte length and the path of a file of the case, relative to the
+ * case folder, without terminator.  Kinds in the fixture: 3 = liquid volumes
+ * (./vofL.raw), 0 = liquid flow map (./flowL.raw).  The words and the float
+ * are returned as stored (the fixture holds 1, 1, 1, 0 and 0.0); their
+ * meaning, and the layout of cases with more compartments, are not pinned
+ * by any file of the reference.  A file whose size does not match this
+ * layout is refused (BMC_E_INVALID).
+ * bmc_cma_read_case: words[4] (may be NULL), *t0 (may be NULL), *n_entries.
+ * bmc_cma_case_entry: entry `index`: *kind and, when name is non-NULL, its
+ * path NUL-terminated into name (name_cap >= path length + 1). */
+int bmc_cma_read_case(const char* path, uint32_t* words, double* t0, uint32_t* n_entries);
+int bmc_cma_case_entry(const char* path, uint32_t index, uint32_t* kind, char* name, uint64_t name_cap);
+
+/* Liquid flow map file of a CMA case (flowL.raw): uint32 rows, uint32
+ * columns, then the flows F(i, j) in COO form as three arrays, each a
+ * uint64 length followed by its elements: row indices (uint64), column
+ * indices (uint64), flows (float64, m^3/s).  The reference's fixture
+ * (apps/api/tests/data/0d/flowL.raw, 32 bytes: a 1 x 1 map, three empty
+ * arrays) fits this reading; it fits "uint32 n, uint32 entry count, then
+ * (uint64 row, uint64 column, float64 flow) triplets" as well (one zero
+ * self-flow, which gives the same domain), so the layout of larger maps is
+ * not pinned.  Refused (BMC_E_INVALID): sizes that do not add up, arrays of
+ * different lengths, entries outside the rows and columns.  *nnz = entry
+ * count; with the three arrays non-NULL (cap >= count) the entries.  The
+ * result feeds bmc_cma_derive / bmc_cma_transition. */
+int bmc_cma_read_flowmap(const char* path, uint32_t* n_rows, uint32_t* n_cols, uint64_t* nnz, uint64_t cap,
+                         uint64_t* rows, uint64_t* cols, double* flows);
+
 /* ---- two-phase flow: gas phase ------------------------------------------- */
 /* A gas phase on the scenario's mesh (SimulationUnit with
  * is_two_phase_flow; apps/libs/simulation/src/simulation.cpp L47-L81):

@@ -22,7 +22,9 @@ the reference's source code; nothing is computed by this repository's code:
   P(I_j | L) = F(i, j) / sum_k F(i, k) (documentation/pages/03_cma.md), and
   the bytes of the two field files of the reference's 0-D case fixture
   (apps/api/tests/data/0d/vofL.raw and turbE.raw.raw, 12 bytes each: uint32
-  count 1, then float64 0.02 and 0.5).
+  count 1, then float64 0.02 and 0.5), and the bytes of the same fixture's
+  case descriptor (cma_case, 63 bytes) and liquid flow map (flowL.raw, 32
+  bytes), typed in from the fixture with the fields they hold.
 """
 import json
 import os
@@ -73,6 +75,17 @@ def main():
             {"file": "vofL.raw", "hex": "010000007b14ae47e17a943f", "values": [0.02]},
             {"file": "turbE.raw.raw", "hex": "01000000000000000000e03f", "values": [0.5]},
         ],
+        # the fixture's descriptor: words 1, 1, 1, 0; float 0.0; two entries
+        # (kind 3 "./vofL.raw", kind 0 "./flowL.raw"); its flow map: 1 x 1
+        # with three zero uint64 words after the dimensions
+        "case_0d": {
+            "cma_case": "01000000" "01000000" "01000000" "00000000" "0000000000000000" "0200000000000000"
+                        "03" "0a000000" + b"./vofL.raw".hex() + "00" "0b000000" + b"./flowL.raw".hex(),
+            "flowL.raw": "01000000" "01000000" + "00" * 24,
+            "words": [1, 1, 1, 0], "t0": 0.0,
+            "entries": [[3, "./vofL.raw"], [0, "./flowL.raw"]],
+            "n_rows": 1, "n_cols": 1, "nnz": 0, "volume": [0.02],
+        },
     }
     for name, obj in (("philox_kat.json", philox), ("move_cases.json", move),
                       ("container_counts.json", container), ("cma_cases.json", cma)):

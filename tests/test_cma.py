@@ -66,6 +66,76 @@ def test_field_files_of_the_0d_case(tmp_path):
         cma.read_field(str(tmp_path / "missing.raw"))
 
 
+def write_fixture_case(folder):
+    g = golden()
+    c0 = g["case_0d"]
+    (folder / "cma_case").write_bytes(bytes.fromhex(c0["cma_case"]))
+    (folder / "flowL.raw").write_bytes(bytes.fromhex(c0["flowL.raw"]))
+    (folder / "vofL.raw").write_bytes(bytes.fromhex(g["fields_0d"][0]["hex"]))
+    return c0
+
+
+def test_case_descriptor_and_flow_map_of_the_0d_case(tmp_path):
+    """The reference's 0-D case: the descriptor's words, float and entries,
+    and its 1 x 1 flow map with no flow."""
+    c0 = write_fixture_case(tmp_path)
+    case = cma.read_case(str(tmp_path / "cma_case"))
+    assert case["words"] == c0["words"] and case["t0"] == c0["t0"]
+    assert [list(e) for e in case["entries"]] == c0["entries"]
+    nr, nc, r, c, f = cma.read_flowmap(str(tmp_path / "flowL.raw"))
+    assert (nr, nc, len(r)) == (c0["n_rows"], c0["n_cols"], c0["nnz"])
+    net = cma.load_case(str(tmp_path))
+    assert net.n_c == 1 and net.volume.tolist() == c0["volume"]
+    assert net.out_flow.tolist() == [0.0] and net.neighbors.ravel().tolist() == [0]
+
+
+def test_written_case_reads_back(tmp_path):
+    """A case written in the readers' layout loads into the Network the
+    flow map gives directly (bit for bit)."""
+    net0 = networks.lattice_vortex(4, seed=5)
+    cma.write_case(str(tmp_path), net0.volume, net0.src, net0.dst, net0.flow)
+    net = cma.load_case(str(tmp_path))
+    ref = cma.network(net0.volume, net0.src, net0.dst, net0.flow)
+    for k in ("volume", "neighbors", "out_flow", "cdf", "in_ptr", "in_idx", "in_flow"):
+        assert np.array_equal(np.asarray(getattr(net, k)).view(np.uint8), np.asarray(getattr(ref, k)).view(np.uint8)), k
+    # the descriptor the writer makes has the fixture's header and entries
+    c0 = golden()["case_0d"]
+    assert bytes.fromhex(c0["cma_case"]) == (tmp_path / "cma_case").read_bytes()
+
+
+@pytest.mark.parametrize("what,msg", [
+    ("case_short", "shorter"), ("case_tail", "after its last entry"), ("case_count", "entry count"),
+    ("case_path", "past the end"), ("flow_short", "shorter"), ("flow_size", "size differs"),
+    ("flow_lengths", "differ in length"), ("flow_range", "outside"),
+])
+def test_malformed_case_files_are_refused(tmp_path, what, msg):
+    import struct
+
+    c0 = golden()["case_0d"]
+    case = bytes.fromhex(c0["cma_case"])
+    flow = struct.pack("<II", 2, 2) + struct.pack("<Q", 1) + struct.pack("<Q", 0) + struct.pack("<Q", 1) + \
+        struct.pack("<Q", 1) + struct.pack("<Q", 1) + struct.pack("<d", 1e-3)
+    bad = {
+        "case_short": case[:20], "case_tail": case + b"\0", "case_count": case[:24] + struct.pack("<Q", 99) + case[32:],
+        "case_path": case[:-3], "flow_short": flow[:20], "flow_size": flow + b"\0" * 8,
+        "flow_lengths": struct.pack("<II", 2, 2) + struct.pack("<Q", 1) + struct.pack("<Q", 0) + struct.pack("<Q", 0) +
+        struct.pack("<Q", 1) + struct.pack("<d", 1e-3),
+        "flow_range": struct.pack("<II", 2, 2) + struct.pack("<Q", 1) + struct.pack("<Q", 2) + struct.pack("<Q", 1) +
+        struct.pack("<Q", 1) + struct.pack("<Q", 1) + struct.pack("<d", 1e-3),
+    }[what]
+    p = tmp_path / "file"
+    p.write_bytes(bad)
+    with pytest.raises(BmcError, match=msg):
+        if what.startswith("case"):
+            cma.read_case(str(p))
+        else:
+            cma.read_flowmap(str(p))
+    # the well-formed two-compartment map of this test reads
+    p.write_bytes(flow)
+    nr, nc, r, c, f = cma.read_flowmap(str(p))
+    assert (nr, nc, r.tolist(), c.tolist(), f.tolist()) == (2, 2, [0], [1], [1e-3])
+
+
 @pytest.mark.parametrize("net", [networks.lattice_vortex(8, seed=3), networks.lattice_vortex(4, seed=9),
                                  networks.ring_network(10, 2, seed=42, max_courant=0.5, dt=0.1)],
                          ids=["lattice8", "lattice4", "ring10"])
@@ -144,6 +214,16 @@ def test_gpu_domain_from_a_flow_map(oracle_mod):
     sc = scenarios.workload(2, n_particles=50000)
     F = sc.net
     sc.net = cma.network(F.volume, F.src, F.dst, F.flow)
+    # and through a case folder written and read back (bmc_cma_read_case,
+    # bmc_cma_read_field, bmc_cma_read_flowmap)
+    import tempfile
+
+    with tempfile.TemporaryDirectory() as d:
+        cma.write_case(d, F.volume, F.src, F.dst, F.flow)
+        from_case = cma.load_case(d)
+    for k in ("neighbors", "out_flow", "cdf", "in_ptr", "in_idx", "in_flow"):
+        assert np.array_equal(getattr(from_case, k), getattr(sc.net, k)), k
+    sc.net = from_case
     g, o = make_pair(oracle_mod, sc)
     # the same flow map installed again through the C-ABI on a second scenario
     g2 = GpuScenario(sc)  # same seed: the same initial particles and weight
