@@ -865,6 +865,25 @@ double orc_pin_erfinv_d(double x) { return sa_erfinv_d(x); }
 float orc_pin_norminv_f(float p, float mean, float sd) { return sa_norminv_f(p, mean, sd); }
 double orc_pin_std_normal(float u) { return sa_std_normal(u); }
 
+/* Draw tables of a container (the reference-cycle comparison hands them to
+ * the reference's compiled cycle): out[i][0..3] = the four draws of purpose
+ * `purpose` of the particle with id ids[i] at step `step`; with normals set,
+ * lanes 0 and 1 are replaced by the standard normals the SimpleAcetate
+ * division takes from them (sa_std_normal) and the table is double. */
+void orc_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, uint32_t purpose, float* out) {
+  for (uint64_t i = 0; i < n; ++i) orc_draws(seed, ids[i], step, purpose, out + 4 * i);
+}
+void orc_division_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, double* out) {
+  for (uint64_t i = 0; i < n; ++i) {
+    float d[4];
+    orc_draws(seed, ids[i], step, 1u, d);
+    out[4 * i + 0] = sa_std_normal(d[0]);
+    out[4 * i + 1] = sa_std_normal(d[1]);
+    out[4 * i + 2] = (double)d[2];
+    out[4 * i + 3] = (double)d[3];
+  }
+}
+
 /* TruncatedNormal<float>::draw_from (prng_extension.hpp L379-L414) with
  * the bounds' probabilities computed as the reference does, 0.5 *
  * erfc(-z / sqrt2) in double from the float z, rounded to float. */

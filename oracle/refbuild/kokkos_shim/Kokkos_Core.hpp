@@ -1,11 +1,19 @@
 // Minimal single-threaded stand-in for the parts of Kokkos 5.1 that the
 // reference's per-particle headers name, so those headers compile unmodified
 // with a plain C++20 compiler for the oracle's pin tests.  It is not Kokkos:
-// views are host arrays with Kokkos' index layouts, parallel dispatch is a
-// serial loop, and the random pool hands out values from a caller-filled tape
-// (so a test injects exactly the draws it wants).  Math functions forward to
-// the C library with Kokkos' overload set (float in, float out), which is what
-// the reference's OpenMP (host) build calls.
+// views are host arrays with Kokkos' index layouts (resize keeps elements by
+// index), parallel dispatch is a serial loop in index order (league ranks in
+// order, one thread per team; tagged policies call the functor with the tag,
+// as Kokkos does; reductions start from the value type's zero or the
+// reducer's init; a scan is one pass with final = true, as the Serial
+// backend runs it), a scatter view writes straight into its view with
+// Kokkos' ScatterValue rounding (the right-hand side converted to the
+// element type, then added), and the random pool hands out values from a
+// caller-filled tape or from a caller's draw provider, which sees the tag,
+// league rank and loop index of the code that asks (so a test injects
+// exactly the draws it wants).  Math functions forward to the C library with
+// Kokkos' overload set (float in, float out), which is what the reference's
+// OpenMP (host) build calls.
 #ifndef BMC_REFPIN_KOKKOS_SHIM_HPP
 #define BMC_REFPIN_KOKKOS_SHIM_HPP
 
@@ -34,6 +42,35 @@ namespace refpin {
 inline long& assert_failures() {
   static long n = 0;
   return n;
+}
+// Where the serial dispatch is: the work tag of the running policy (an
+// address unique to the tag type, nullptr untagged), the league rank of the
+// running team and the index of the innermost running range loop.
+struct Ctx {
+  const void* tag = nullptr;
+  std::size_t league = 0;
+  std::size_t index = 0;
+};
+inline Ctx& ctx() {
+  static Ctx c;
+  return c;
+}
+template <class T>
+const void* tag_id() {
+  static const char c = 0;
+  return &c;
+}
+// Draw provider: when set, every draw of the random pool asks it (kind 0:
+// uniform float, 1: uniform double, 2: standard normal, 3: integer) instead
+// of reading the tape.
+using DrawFn = double (*)(void* user, int kind);
+struct Provider {
+  DrawFn fn = nullptr;
+  void* user = nullptr;
+};
+inline Provider& provider() {
+  static Provider p;
+  return p;
 }
 }  // namespace refpin
 #define KOKKOS_ASSERT(x)                              \
@@ -133,6 +170,22 @@ struct Scratch {
 struct ALL_t {};
 inline constexpr ALL_t ALL{};
 
+struct WithoutInitializing_t {};
+inline constexpr WithoutInitializing_t WithoutInitializing{};
+namespace Impl {
+struct ViewAlloc {
+  std::string label;
+};
+}  // namespace Impl
+template <class... A>
+Impl::ViewAlloc view_alloc(A... a) {
+  Impl::ViewAlloc r;
+  ((void)[&](const auto& x) {
+    if constexpr (std::is_convertible_v<decltype(x), std::string>) r.label = x;
+  }(a), ...);
+  return r;
+}
+
 template <class DataType, class... Props>
 class View {
  public:
@@ -161,6 +214,7 @@ class View {
     ptr_ = holder_.get();
   }
   explicit View(const char* label, std::size_t n0 = 0, std::size_t n1 = 0) : View(std::string(label), n0, n1) {}
+  View(const Impl::ViewAlloc& a, std::size_t n0 = 0, std::size_t n1 = 0) : View(a.label, n0, n1) {}
   // unmanaged wrap of caller memory: View(ptr, n0[, n1])
   View(value_type* p, std::size_t n0, std::size_t n1 = 0) : ptr_(p) { set_extents(n0, n1); }
   // team scratch
@@ -227,6 +281,31 @@ class View {
 template <class V, class... Args>
 using Subview = View<typename V::non_const_value_type*, typename V::array_layout>;
 
+// Kokkos::resize: a new allocation of the new extents holding every element
+// whose indices exist in both (LayoutLeft or LayoutRight alike).
+template <class D, class... P>
+void resize(View<D, P...>& v, std::size_t n0, std::size_t n1 = 0) {
+  View<D, P...> w(v.label(), n0, n1);
+  const std::size_t e0 = std::min(v.extent(0), w.extent(0)), e1 = std::min(v.extent(1), w.extent(1));
+  if constexpr (View<D, P...>::rank == 1) {
+    for (std::size_t i = 0; i < e0; ++i) w(i) = v(i);
+  } else if constexpr (View<D, P...>::rank == 2) {
+    for (std::size_t i = 0; i < e0; ++i)
+      for (std::size_t j = 0; j < e1; ++j) w(i, j) = v(i, j);
+  }
+  v = w;
+}
+// Kokkos::realloc: a new zeroed allocation (contents not kept).
+template <class D, class... P>
+void realloc(View<D, P...>& v, std::size_t n0, std::size_t n1 = 0) {
+  v = View<D, P...>(v.label(), n0, n1);
+}
+// subview of a rank-1 view over [a, b)
+template <class D, class... P, class I>
+View<D, P...> subview(const View<D, P...>& v, std::pair<I, I> r) {
+  return View<D, P...>(v.data() + r.first, static_cast<std::size_t>(r.second - r.first));
+}
+
 template <class V, class T>
 void deep_copy(const V& v, const T& value) {
   for (std::size_t i = 0; i < v.span(); ++i) v.data()[i] = static_cast<typename V::non_const_value_type>(value);
@@ -263,6 +342,16 @@ inline T atomic_fetch_inc(T* p) {
 template <class T>
 inline void atomic_increment(T* p) {
   ++(*p);
+}
+template <class T>
+inline T atomic_load(const T* p) {
+  return *p;
+}
+template <class T, class U>
+inline T atomic_exchange(T* p, U v) {
+  T old = *p;
+  *p = static_cast<T>(v);
+  return old;
 }
 
 // ---- math: Kokkos' overload set over the C library ------------------------------
@@ -352,21 +441,60 @@ struct Array {
 
 template <class... Args>
 inline int printf(const char* fmt, Args... args) {
-  return std::printf(fmt, args...);
+  if constexpr (sizeof...(Args) == 0)
+    return std::fputs(fmt, stdout);
+  else
+    return std::printf(fmt, args...);
 }
 
 // ---- dispatch (serial) ------------------------------------------------------------
-template <class Exec = DefaultExecutionSpace, class... P>
+struct AUTO_t {
+  constexpr const AUTO_t& operator()() const { return *this; }
+};
+inline constexpr AUTO_t AUTO{};
+
+namespace Impl {
+template <class T>
+struct IsSpace : std::bool_constant<std::is_same_v<T, Serial>> {};
+// work tag of a policy: its first template argument that is not an
+// execution space (void when none)
+template <class... P>
+struct TagOf {
+  using type = void;
+};
+template <class F, class... R>
+struct TagOf<F, R...> {
+  using type = std::conditional_t<IsSpace<F>::value || std::is_void_v<F>, typename TagOf<R...>::type, F>;
+};
+template <class Tag, class F, class... A>
+void call(const F& f, A&&... a) {
+  if constexpr (std::is_void_v<Tag>)
+    f(std::forward<A>(a)...);
+  else
+    f(Tag{}, std::forward<A>(a)...);
+}
+template <class Tag>
+const void* tag_ptr() {
+  if constexpr (std::is_void_v<Tag>)
+    return nullptr;
+  else
+    return ::refpin::tag_id<Tag>();
+}
+}  // namespace Impl
+
+template <class... P>
 struct RangePolicy {
-  using execution_space = Exec;
+  using execution_space = DefaultExecutionSpace;
+  using work_tag = typename Impl::TagOf<P...>::type;
   std::size_t b = 0, e = 0;
   RangePolicy(std::size_t b_, std::size_t e_) : b(b_), e(e_) {}
-  RangePolicy(const Exec&, std::size_t b_, std::size_t e_) : b(b_), e(e_) {}
+  RangePolicy(const Serial&, std::size_t b_, std::size_t e_) : b(b_), e(e_) {}
 };
 
 struct TeamMember {
-  int league_rank() const { return 0; }
-  int league_size() const { return 1; }
+  std::size_t rank = 0, size = 1;
+  int league_rank() const { return static_cast<int>(rank); }
+  int league_size() const { return static_cast<int>(size); }
   int team_rank() const { return 0; }
   int team_size() const { return 1; }
   void team_barrier() const {}
@@ -374,15 +502,34 @@ struct TeamMember {
   Impl::Scratch thread_scratch(int) const { return {}; }
 };
 
-template <class Exec = DefaultExecutionSpace, class... P>
+struct PerTeamTag {
+  std::size_t bytes = 0;
+};
+struct PerThreadTag {
+  std::size_t bytes = 0;
+};
+inline PerTeamTag PerTeam(const TeamMember&) { return {}; }
+inline PerThreadTag PerThread(const TeamMember&) { return {}; }
+inline PerTeamTag PerTeam(std::size_t b) { return {b}; }
+inline PerThreadTag PerThread(std::size_t b) { return {b}; }
+
+template <class... P>
 struct TeamPolicy {
   using execution_space = DefaultExecutionSpace;
   using member_type = TeamMember;
+  using work_tag = typename Impl::TagOf<P...>::type;
+  std::size_t league = 1;
   TeamPolicy() = default;
-  template <class... A>
-  TeamPolicy(A...) {}
+  template <class N, class... R, std::enable_if_t<std::is_integral_v<N>, int> = 0>
+  TeamPolicy(N n, R...) : league(static_cast<std::size_t>(n)) {}
+  template <class N, class... R, std::enable_if_t<std::is_integral_v<N>, int> = 0>
+  TeamPolicy(const Serial&, N n, R...) : league(static_cast<std::size_t>(n)) {}
   template <class S>
   TeamPolicy set_scratch_size(int, S) const {
+    return *this;
+  }
+  template <class S, class T>
+  TeamPolicy set_scratch_size(int, S, T) const {
     return *this;
   }
 };
@@ -395,33 +542,135 @@ inline ThreadRange TeamThreadRange(const TeamMember&, std::size_t e) { return {0
 inline ThreadRange TeamVectorRange(const TeamMember&, std::size_t b, std::size_t e) { return {b, e}; }
 inline ThreadRange TeamVectorRange(const TeamMember&, std::size_t e) { return {0, e}; }
 inline ThreadRange ThreadVectorRange(const TeamMember&, std::size_t b, std::size_t e) { return {b, e}; }
+inline ThreadRange ThreadVectorRange(const TeamMember&, std::size_t e) { return {0, e}; }
 
+// nested range loops (inside a team)
 template <class F>
 void parallel_for(const ThreadRange& r, const F& f) {
-  for (std::size_t i = r.b; i < r.e; ++i) f(i);
+  for (std::size_t i = r.b; i < r.e; ++i) {
+    ::refpin::ctx().index = i;
+    f(i);
+  }
 }
+template <class F, class T>
+void parallel_reduce(const ThreadRange& r, const F& f, T& value) {
+  value = T{};
+  for (std::size_t i = r.b; i < r.e; ++i) {
+    ::refpin::ctx().index = i;
+    f(i, value);
+  }
+}
+
+// top-level dispatch
 template <class F>
 void parallel_for(std::size_t n, const F& f) {
-  for (std::size_t i = 0; i < n; ++i) f(i);
+  ::refpin::ctx().tag = nullptr;
+  for (std::size_t i = 0; i < n; ++i) {
+    ::refpin::ctx().index = i;
+    f(i);
+  }
 }
-template <class E, class... P, class F>
-void parallel_for(const RangePolicy<E, P...>& r, const F& f) {
-  for (std::size_t i = r.b; i < r.e; ++i) f(i);
+template <class... P, class F>
+void parallel_for(const RangePolicy<P...>& r, const F& f) {
+  using Tag = typename RangePolicy<P...>::work_tag;
+  ::refpin::ctx().tag = Impl::tag_ptr<Tag>();
+  for (std::size_t i = r.b; i < r.e; ++i) {
+    ::refpin::ctx().index = i;
+    Impl::call<Tag>(f, i);
+  }
+}
+template <class... P, class F>
+void parallel_for(const TeamPolicy<P...>& t, const F& f) {
+  using Tag = typename TeamPolicy<P...>::work_tag;
+  for (std::size_t r = 0; r < t.league; ++r) {
+    ::refpin::ctx().tag = Impl::tag_ptr<Tag>();
+    ::refpin::ctx().league = r;
+    Impl::call<Tag>(f, TeamMember{r, t.league});
+  }
 }
 template <class Pol, class F>
 void parallel_for(const std::string&, const Pol& p, const F& f) {
   parallel_for(p, f);
 }
-template <class Pol, class F, class R>
-void parallel_reduce(const Pol&, const F&, R&) {}
-template <class Pol, class F, class R>
-void parallel_reduce(const std::string&, const Pol&, const F&, R&) {}
+
+namespace Impl {
+template <class R, class = void>
+struct IsReducer : std::false_type {};
+template <class R>
+struct IsReducer<R, std::void_t<typename R::reducer>> : std::true_type {};
+template <class R, class = void>
+struct IsView : std::false_type {};
+template <class R>
+struct IsView<R, std::void_t<typename R::array_layout, typename R::non_const_value_type>> : std::true_type {};
+
+// runs body(acc) over the policy with the result's type, then stores it
+template <class Res, class Body>
+void reduce_into(Res&& result, const Body& body) {
+  using R = std::decay_t<Res>;
+  if constexpr (IsReducer<R>::value) {
+    typename R::value_type acc;
+    result.init(acc);
+    body(acc);
+    result.reference() = acc;
+  } else if constexpr (IsView<R>::value) {
+    typename R::non_const_value_type acc{};
+    body(acc);
+    result() = acc;
+  } else {
+    R acc{};
+    body(acc);
+    result = acc;
+  }
+}
+}  // namespace Impl
+
+template <class... P, class F, class Res>
+void parallel_reduce(const RangePolicy<P...>& r, const F& f, Res&& result) {
+  using Tag = typename RangePolicy<P...>::work_tag;
+  Impl::reduce_into(std::forward<Res>(result), [&](auto& acc) {
+    ::refpin::ctx().tag = Impl::tag_ptr<Tag>();
+    for (std::size_t i = r.b; i < r.e; ++i) {
+      ::refpin::ctx().index = i;
+      Impl::call<Tag>(f, i, acc);
+    }
+  });
+}
+template <class... P, class F, class Res>
+void parallel_reduce(const TeamPolicy<P...>& t, const F& f, Res&& result) {
+  using Tag = typename TeamPolicy<P...>::work_tag;
+  Impl::reduce_into(std::forward<Res>(result), [&](auto& acc) {
+    for (std::size_t r = 0; r < t.league; ++r) {
+      ::refpin::ctx().tag = Impl::tag_ptr<Tag>();
+      ::refpin::ctx().league = r;
+      Impl::call<Tag>(f, TeamMember{r, t.league}, acc);
+    }
+  });
+}
+template <class Pol, class F, class Res>
+void parallel_reduce(const std::string&, const Pol& p, const F& f, Res&& result) {
+  parallel_reduce(p, f, std::forward<Res>(result));
+}
+
+// one pass with final = true, as the Serial backend runs a scan
+template <class... P, class F>
+void parallel_scan(const RangePolicy<P...>& r, const F& f) {
+  using Tag = typename RangePolicy<P...>::work_tag;
+  ::refpin::ctx().tag = Impl::tag_ptr<Tag>();
+  std::size_t update = 0;
+  for (std::size_t i = r.b; i < r.e; ++i) {
+    ::refpin::ctx().index = i;
+    if constexpr (std::is_void_v<Tag>)
+      f(static_cast<int>(i), update, true);
+    else
+      f(Tag{}, static_cast<int>(i), update, true);
+  }
+}
+template <class Pol, class F>
+void parallel_scan(const std::string&, const Pol& p, const F& f) {
+  parallel_scan(p, f);
+}
 inline void fence(const std::string& = "") {}
 
-struct PerTeamTag {};
-struct PerThreadTag {};
-inline PerTeamTag PerTeam(const TeamMember&) { return {}; }
-inline PerThreadTag PerThread(const TeamMember&) { return {}; }
 template <class T, class F>
 void single(T, const F& f) {
   f();
@@ -449,20 +698,27 @@ inline DrawTape& tape() {
 }
 }  // namespace Impl
 
+namespace Impl {
+inline double draw(int kind) {
+  const auto& p = ::refpin::provider();
+  return p.fn ? p.fn(p.user, kind) : tape().next();
+}
+}  // namespace Impl
+
 template <class Device>
 class Random_XorShift1024 {
  public:
-  float frand() { return static_cast<float>(Impl::tape().next()); }
+  float frand() { return static_cast<float>(Impl::draw(0)); }
   float frand(float b) { return b * frand(); }
   float frand(float a, float b) { return a + (b - a) * frand(); }
-  double drand() { return Impl::tape().next(); }
+  double drand() { return Impl::draw(1); }
   double drand(double b) { return b * drand(); }
   double drand(double a, double b) { return a + (b - a) * drand(); }
-  uint64_t urand64() { return static_cast<uint64_t>(Impl::tape().next()); }
+  uint64_t urand64() { return static_cast<uint64_t>(Impl::draw(3)); }
   uint64_t urand64(uint64_t b) { return urand64() % (b ? b : 1); }
   uint64_t urand64(uint64_t a, uint64_t b) { return a + urand64(b - a); }
-  uint32_t urand() { return static_cast<uint32_t>(Impl::tape().next()); }
-  double normal() { return Impl::tape().next(); }
+  uint32_t urand() { return static_cast<uint32_t>(Impl::draw(3)); }
+  double normal() { return Impl::draw(2); }
   double normal(double mean, double stddev) { return mean + stddev * normal(); }
 };
 
@@ -488,19 +744,54 @@ struct fill_random_functor_begin_end {
 template <class V, class P, class B, class E>
 void fill_random(V, P, B, E) {}
 
-// ---- scatter views (only their types are named on this path) ------------------------
+// ---- scatter views: serial, straight into the target view ----------------------------
 namespace Experimental {
+// Kokkos' ScatterValue::operator+= takes the element type: the right-hand
+// side is converted to it, then added.
+template <class T>
+struct ScatterRef {
+  T* p;
+  void operator+=(const T& v) const { *p += v; }
+  void operator-=(const T& v) const { *p -= v; }
+};
 template <class DataType, class Layout = LayoutRight, class Exec = DefaultExecutionSpace>
 struct ScatterView {
-  void reset() {}
+  using view_type = View<DataType, Layout>;
+  using value_type = typename view_type::non_const_value_type;
+  view_type v;
+  ScatterView() = default;
+  explicit ScatterView(const view_type& x) : v(x) {}
+  void reset() { deep_copy(v, 0); }
+  struct Access {
+    view_type v;
+    template <class... I>
+    ScatterRef<value_type> operator()(I... i) const {
+      return ScatterRef<value_type>{&v(i...)};
+    }
+  };
+  Access access() const { return Access{v}; }
   template <class V>
   void contribute_into(const V&) const {}
 };
 template <class D, class... P>
-ScatterView<D> create_scatter_view(const View<D, P...>&) {
-  return {};
+ScatterView<D, typename View<D, P...>::array_layout> create_scatter_view(const View<D, P...>& v) {
+  return ScatterView<D, typename View<D, P...>::array_layout>(View<D, typename View<D, P...>::array_layout>(v));
 }
+template <class V, class S>
+void contribute(const V&, const S&) {}
 }  // namespace Experimental
+
+// ---- sorting: only the names the container's (unused) sort member spells --------------
+template <class V>
+struct BinOp1D {
+  template <class... A>
+  BinOp1D(A...) {}
+};
+template <class V, class Op>
+struct BinSort {
+  template <class... A>
+  BinSort(A...) {}
+};
 
 namespace Profiling {
 struct ScopedRegion {

@@ -9,6 +9,13 @@ from the reference tree, so the compiled headers see the reference's own
 compile-time flags (event counter on, probes off).
 
     python make_config.py <reference root> <output header>
+    python make_config.py --variant <reference root> <output header>
+
+With --variant it writes the model-variant header instead
+(apps/autogenerated/variant_model.hxx, which the reference's
+devutils/generate_model_loader.py fills with its model list): the container
+variant over the two reference models the cycle pins run, FixedLength and
+SimpleAcetate.
 """
 import re
 import sys
@@ -60,5 +67,20 @@ def main(ref_root: str, out: str) -> None:
         f.write(src)
 
 
+MODELS = ("fixed_length", "FixedLength"), ("simple_acetate", "SimpleAcetate")
+
+
+def variant(ref_root: str, out: str) -> None:
+    src = open(f"{ref_root}/apps/autogenerated/variant_model.hxx").read()
+    inc = "\n".join(f"#include <models/{h}.hpp>" for h, _ in MODELS)
+    types = ", ".join(f"::MC::ParticlesContainer<::Models::{t}>" for _, t in MODELS)
+    src = src.replace("@INCLUDES@", inc).replace("@VARIANT_TYPE@", types)
+    with open(out, "w") as f:
+        f.write(src)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1], sys.argv[2])
+    if sys.argv[1] == "--variant":
+        variant(sys.argv[2], sys.argv[3])
+    else:
+        main(sys.argv[1], sys.argv[2])
