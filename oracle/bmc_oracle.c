@@ -772,6 +772,30 @@ void orc_step(orc_state* s, double dt, int n_threads) {
   s->t_rel += dt; /* SimulationUnit::advance */
 }
 
+/* orc_step without the cycle: the feeds, the liquid step from the sources
+ * the caller left in src (the previous cycle's contributions), sources
+ * cleared for the caller's next contributions, the step counter and the
+ * relative time advanced.  For driving another implementation's particle
+ * cycle with this liquid. */
+void orc_liquid_step(orc_state* s, double dt) {
+  const uint32_t ns = s->n_s;
+  for (uint32_t f = 0; f < s->n_feeds; ++f)
+    s->feed_flow[f] = orc_feed_flow(s->feed_kind[f], s->feed_flow[f], s->feed_f0[f], s->feed_rate[f], s->t_rel);
+  for (uint32_t j = 0; j < s->n_c; ++j) s->sink[j] = 0.0;
+  for (uint32_t f = 0; f < s->n_feeds; ++f) {
+    for (uint32_t sp = 0; sp < ns; ++sp) {
+      const double cf = s->feed_conc[f * 8 + sp];
+      if (cf != 0.0) s->src[(uint64_t)s->feed_in[f] * ns + sp] += s->feed_flow[f] * cf;
+    }
+    if (s->feed_out[f] >= 0) s->sink[(uint32_t)s->feed_out[f]] += s->feed_flow[f];
+  }
+  orc_set_outlets(s);
+  orc_scalar_step(s, dt);
+  memset(s->src, 0, sizeof(double) * (size_t)s->n_c * ns);
+  s->step++;
+  s->t_rel += dt;
+}
+
 void orc_run(orc_state* s, double dt, uint32_t n_steps, int n_threads) {
   for (uint32_t k = 0; k < n_steps; ++k) orc_step(s, dt, n_threads);
 }

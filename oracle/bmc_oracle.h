@@ -210,6 +210,7 @@ void orc_scalar_step(orc_state* s, double dt);
 void orc_cycle(orc_state* s, double dt, int n_threads);
 void orc_post_cycle(orc_state* s);
 void orc_step(orc_state* s, double dt, int n_threads);
+void orc_liquid_step(orc_state* s, double dt);
 void orc_run(orc_state* s, double dt, uint32_t n_steps, int n_threads);
 void orc_remove_inactive(orc_state* s, uint64_t to_remove);
 

@@ -93,6 +93,8 @@ def ref_lib():
         L.ref_cycle_read.argtypes = [VP, ct.c_uint64, VP, VP, VP, VP, VP]
         L.ref_cycle_misses.restype = ct.c_long
         L.ref_cycle_misses.argtypes = [VP]
+        L.ref_cycle_step_stream.restype = ct.c_int32
+        L.ref_cycle_step_stream.argtypes = [VP, ct.c_double, VP, ct.c_uint64, VP, VP, VP, VP]
         L.ref_assert_failures.restype = ct.c_long
         _LIB = L
     return _LIB
@@ -204,6 +206,30 @@ class RefCycle:
             raise RuntimeError("reference cycle refused the step (empty container)")
         return self.compare(stats, ex.reshape(self.n_ctb, self.n_c), ab.reshape(self.n_ctb, self.n_c),
                             sc.reshape(self.n_ctb, self.n_c), inactive_before)
+
+    def run_free(self, n_steps: int, seed: int) -> int:
+        """Free-running: n_steps main-loop iterations of the reference's
+        cycle drawing from its own xorshift1024* stream (seeded with `seed`),
+        coupled to the oracle's liquid step, which receives the exact sums of
+        the reference's contribution operands.  The oracle's own particles
+        are not used.  Returns the births counted."""
+        o = self.o
+        L = _orc.lib()
+        L.orc_liquid_step.argtypes = [VP, ct.c_double]
+        stats = np.zeros(8, np.uint64)
+        ex = np.zeros(self.n_ctb * self.n_c)
+        ab = np.zeros_like(ex)
+        sc = np.zeros(self.n_ctb * self.n_c, np.float32)
+        births = 0
+        for _ in range(n_steps):
+            L.orc_liquid_step(ct.byref(o.s), o.scen.dt)
+            conc = np.ascontiguousarray(o.C, np.float64)
+            if ref_lib().ref_cycle_step_stream(self.h, o.scen.dt, _p(conc), seed, _p(stats), _p(ex), _p(ab),
+                                               _p(sc)) != 0:
+                break
+            o.src[:, :self.n_ctb] = ex.reshape(self.n_ctb, self.n_c).T
+            births += int(stats[1])
+        return births
 
     def compare(self, stats, exact, absum, scatter, inactive_before) -> dict:
         o = self.o

@@ -57,6 +57,60 @@ namespace {
 using Exec = ComputeSpace;
 namespace KI = Simulation::KernelInline;
 
+// xorshift1024* (Vigna, "An experimental exploration of Marsaglia's
+// xorshift generators, scrambled", 2016), the generator family of the
+// reference's pool (Kokkos::Random_XorShift1024_Pool), seeded through
+// splitmix64 as its author recommends; for free-running runs, where the
+// draws need no slot.
+struct Xorshift1024 {
+  uint64_t s[16];
+  int p = 0;
+  bool have_normal = false;
+  double spare = 0.0;
+  explicit Xorshift1024(uint64_t seed) {
+    uint64_t z = seed;
+    for (auto& w : s) {
+      z += 0x9e3779b97f4a7c15ull;
+      uint64_t x = z;
+      x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+      x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+      w = x ^ (x >> 31);
+    }
+  }
+  uint64_t next() {
+    const uint64_t s0 = s[p];
+    uint64_t s1 = s[p = (p + 1) & 15];
+    s1 ^= s1 << 31;
+    s[p] = s1 ^ s0 ^ (s1 >> 11) ^ (s0 >> 30);
+    return s[p] * 1181783497276652981ull;
+  }
+  // uniforms in [0, 1): 24 and 53 top bits
+  double uniform_f() { return (double)(next() >> 40) * 0x1p-24; }
+  double uniform_d() { return (double)(next() >> 11) * 0x1p-53; }
+  // standard normal by the Box-Muller transform, pairs
+  double normal() {
+    if (have_normal) {
+      have_normal = false;
+      return spare;
+    }
+    double u1 = uniform_d();
+    while (u1 <= 0.0) u1 = uniform_d();
+    const double u2 = uniform_d();
+    const double r = std::sqrt(-2.0 * std::log(u1)), a = 6.283185307179586 * u2;
+    spare = r * std::sin(a);
+    have_normal = true;
+    return r * std::cos(a);
+  }
+};
+
+double draw_stream(void* user, int kind) {
+  Xorshift1024& g = *static_cast<Xorshift1024*>(user);
+  if (kind == 2) return g.normal();
+  if (kind == 1) return g.uniform_d();
+  if (kind == 3) return (double)(g.next() >> 32);
+  return g.uniform_f();
+}
+
 // Draws of one cycle, per container slot at the cycle's start.
 struct StepDraws {
   uint64_t n = 0;
@@ -105,8 +159,9 @@ double draw_for(void* user, int kind) {
 
 struct CycleBase {
   virtual ~CycleBase() = default;
-  virtual int step(double dt, const double* conc, StepDraws& d, uint64_t* stats, double* exact, double* exact_abs,
-                   float* scatter) = 0;
+  // with `stream` set, every draw comes from it instead of the slot tables
+  virtual int step(double dt, const double* conc, StepDraws& d, Xorshift1024* stream, uint64_t* stats,
+                   double* exact, double* exact_abs, float* scatter) = 0;
   virtual uint64_t read(uint64_t cap, float* state, uint64_t* pos, uint8_t* status, float* age_h,
                         float* age_d) const = 0;
   virtual uint32_t n_var() const = 0;
@@ -184,15 +239,18 @@ struct Cycle final : CycleBase {
     return v;
   }
 
-  int step(double dt, const double* c_in, StepDraws& d, uint64_t* stats, double* exact, double* exact_abs,
-           float* scat) override {
+  int step(double dt, const double* c_in, StepDraws& d, Xorshift1024* stream, uint64_t* stats, double* exact,
+           double* exact_abs, float* scat) override {
     std::memcpy(conc.data(), c_in, conc.size() * sizeof(double));
     const std::size_t n_particle = container.n_particles();
     if (n_particle == 0) return 1;
     d.n = n_particle;
     d.ppt_model = opt.m_p_p_team_model;
     d.ppt_move = opt.m_p_p_team_move;
-    refpin::provider() = {&draw_for, &d};
+    if (stream)
+      refpin::provider() = {&draw_stream, stream};
+    else
+      refpin::provider() = {&draw_for, &d};
     const uint64_t e_new0 = events.get<MC::EventType::NewParticle>(), e_exit0 = events.get<MC::EventType::Exit>(),
                    e_move0 = events.get<MC::EventType::Move>(), e_over0 = events.get<MC::EventType::Overflow>();
     // SimulationUnit::cycleProcess (simulation.hpp L184-L212)
@@ -258,6 +316,7 @@ struct Cycle final : CycleBase {
 
 struct Handle {
   std::unique_ptr<CycleBase> c;
+  std::unique_ptr<Xorshift1024> stream;
   long misses = 0;
 };
 }  // namespace
@@ -315,9 +374,20 @@ int32_t ref_cycle_step(void* hv, double dt, const double* conc, const float* mov
   d.exit = exit_u;
   d.div = div;
   d.div_kind = div_kind;
-  const int rc = h->c->step(dt, conc, d, stats, exact, exact_abs, scatter);
+  const int rc = h->c->step(dt, conc, d, nullptr, stats, exact, exact_abs, scatter);
   h->misses += d.misses;
   return rc;
+}
+
+// Free-running: the draws come, in the order the cycle asks for them, from
+// one xorshift1024* stream seeded once with `seed` (the first call seeds
+// it).  Outputs as ref_cycle_step.
+int32_t ref_cycle_step_stream(void* hv, double dt, const double* conc, uint64_t seed, uint64_t* stats,
+                              double* exact, double* exact_abs, float* scatter) {
+  auto* h = static_cast<Handle*>(hv);
+  if (!h->stream) h->stream = std::make_unique<Xorshift1024>(seed);
+  StepDraws d;
+  return h->c->step(dt, conc, d, h->stream.get(), stats, exact, exact_abs, scatter);
 }
 
 // The container: particles [0, n) into arrays of capacity cap (state
