@@ -113,6 +113,7 @@ SIGNATURES = {
     "bmc_set_step_limit": [VP, c_u32],
     "bmc_batch_synchronize": [VP],
     "bmc_debug_age_add": [VP, c_u64, c_dbl, VP],
+    "bmc_debug_quantize": [VP, c_u64, c_i32, VP],
     "bmc_debug_draws": [c_u64, VP, c_u64, c_u32, c_u32, VP],
     "bmc_launch_count": [VP],
     "bmc_step_timed": [VP, c_dbl, VP, VP],

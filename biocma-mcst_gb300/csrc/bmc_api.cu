@@ -1985,6 +1985,25 @@ int bmc_debug_age_add(const float* ages, uint64_t n, double dt, float* out) {
   return BMC_OK;
 }
 
+int bmc_debug_quantize(const float* values, uint64_t n, int32_t e, int64_t* out) {
+  if (!values || !out || n == 0) return fail(BMC_E_INVALID, "bad arguments");
+  float* d_v = nullptr;
+  long long* d_out = nullptr;
+  BMC_CUDA(cudaMalloc(&d_v, n * 4));
+  cudaError_t err = cudaMalloc(&d_out, n * 16);
+  if (err == cudaSuccess) err = counted_memcpy(d_v, values, n * 4, cudaMemcpyHostToDevice);
+  if (err == cudaSuccess) {
+    bmc::launch_debug_quantize(0, d_v, n, e, d_out);
+    g_launches++;
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = counted_memcpy(out, d_out, n * 16, cudaMemcpyDeviceToHost);
+  cudaFree(d_v);
+  if (d_out) cudaFree(d_out);
+  if (err != cudaSuccess) return fail(BMC_E_CUDA, std::string("debug quantize: ") + cudaGetErrorString(err));
+  return BMC_OK;
+}
+
 int bmc_debug_wait(uint64_t limit_ns, int32_t arrive, uint32_t* error_word, uint64_t* waited_ns) {
   if (!error_word || !waited_ns) return fail(BMC_E_INVALID, "null argument");
   if (limit_ns > 2000000000ull) return fail(BMC_E_INVALID, "limit above the kernels' own 2 s");

@@ -289,6 +289,35 @@ __device__ __forceinline__ long long quantize(float v, int e, unsigned& clamped,
   return quantize_bits<23, 8, 127>((unsigned)__float_as_uint(v), e, clamped, err);
 }
 
+// 2^-e as a float when the float quantisation below may use it (a normal
+// power of two no larger than 2^125), else 0.
+__device__ __forceinline__ float quantize_scale(int e) {
+  return (e >= -125 && e <= 126) ? __int_as_float((127 - e) << 23) : 0.0f;
+}
+
+// quantize(float) through one scaled conversion: v * 2^-e is exact (a
+// power-of-two scale; a product too small to be a normal float lies below
+// half a quantum, where any rounding still gives 0, as does a subnormal v
+// while the scale is at most 2^125), and the conversion rounds to the
+// nearest integer, ties to even: the integer quantize_bits computes, with
+// the same clamping (inf saturates the conversion, NaN is caught apart).
+// scale = quantize_scale(e), nonzero.
+__device__ __forceinline__ long long quantize_scaled(float v, float scale, unsigned& clamped, unsigned& err) {
+  long long q = __float2ll_rn(v * scale);
+  if (q > kQMax || q < -kQMax || v != v) {
+    q = signbit(v) ? -kQMax : kQMax;
+    ++clamped;
+    err |= 2u;
+  }
+  return q;
+}
+__device__ __forceinline__ long long quantize_fast(float v, int e, float scale, unsigned& clamped, unsigned& err) {
+  return scale != 0.0f ? quantize_scaled(v, scale, clamped, err) : quantize(v, e, clamped, err);
+}
+__device__ __forceinline__ long long quantize_fast(double v, int e, float, unsigned& clamped, unsigned& err) {
+  return quantize(v, e, clamped, err);
+}
+
 // Move threshold stored in slot 7 of a compartment record.
 __device__ __forceinline__ uint32_t rec_move_thr(float v) { return __float_as_uint(v); }
 __device__ __forceinline__ uint32_t rec_move_thr(double v) { return (uint32_t)__double_as_longlong(v); }
@@ -504,6 +533,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const bool do_move = n_c > 1;
     const unsigned n_out = S.n_outlets;
     const int qe0 = S.q_exp[0];
+    const float qs0 = quantize_scale(qe0);
     const F* __restrict__ crec = reinterpret_cast<const F*>(S.crec);
     const int2* __restrict__ mrow = S.mrow;
     F* __restrict__ state = reinterpret_cast<F*>(S.state);
@@ -591,7 +621,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
             if constexpr (Model::separable) {
               F basis;
               st = update_separable<Model, F>(dtF, xx, rr, basis, s_pf, S, idv[k], step, p0);
-              const long long q = quantize(basis, qe0, my_clamp, my_err);
+              const long long q = quantize_fast(basis, qe0, qs0, my_clamp, my_err);
               if constexpr (AGG) {
                 qv[k] = q;
                 has_q[k] = true;
@@ -714,6 +744,7 @@ struct CycleScen {
   float dtf;
   AgeStep ak;
   int qe0;
+  float qs0;                      // quantize_scale(qe0)
   unsigned rep_mask, rep_stride;  // accumulator copies - 1, copy stride
 };
 
@@ -961,6 +992,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
         sr.ak = age_step(S.dt);
         sr.n_out = S.n_outlets;
         sr.qe0 = S.q_exp[0];
+        sr.qs0 = quantize_scale(S.q_exp[0]);
         sr.crec = reinterpret_cast<const F*>(S.crec);
         sr.mrow = S.mrow;
         sr.mrow16 = S.mrow16;
@@ -1009,7 +1041,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           if constexpr (Model::separable) {
             F basis;
             st = update_separable<Model, F>(sr.dtF, xx, rr, basis, s_pf, S, bid[slot], sr.step, p0);
-            const long long q = quantize(basis, sr.qe0, my_clamp, my_err);
+            const long long q = quantize_fast(basis, sr.qe0, sr.qs0, my_clamp, my_err);
             if constexpr (AGG) {
               qv = q;
               qkey = p0;

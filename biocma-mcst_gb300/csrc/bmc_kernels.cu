@@ -36,6 +36,21 @@ __global__ void k_debug_age_add(const float* __restrict__ a, unsigned long long 
     out[i] = age_add_fast(a[i], k);
 }
 
+// The cycle kernels' float quantisation on n values with quantum 2^e:
+// out[2k] through the scaled conversion (quantize_fast), out[2k + 1] from
+// the IEEE fields (quantize_bits), for their test against each other and
+// against rint(v * 2^-e) on the CPU.
+__global__ void k_debug_quantize(const float* __restrict__ v, unsigned long long n, int e,
+                                 long long* __restrict__ out) {
+  const float sc = quantize_scale(e);
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    unsigned c = 0u, er = 0u;
+    out[2 * i] = quantize_fast(v[i], e, sc, c, er);
+    out[2 * i + 1] = quantize(v[i], e, c, er);
+  }
+}
+
 // Self-test of the bounded wait the cycle kernels use on their mbarriers:
 // one thread waits on phase 0 of a barrier expecting one arrival, which it
 // makes first (`arrive` != 0: the wait succeeds) or that nothing makes (the
@@ -86,6 +101,10 @@ void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t
 }
 void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out) {
   k_debug_age_add<<<256, 256, 0, st>>>(a, n, dt, out);
+}
+
+void launch_debug_quantize(cudaStream_t st, const float* v, unsigned long long n, int e, long long* out) {
+  k_debug_quantize<<<256, 256, 0, st>>>(v, n, e, out);
 }
 
 }  // namespace bmc

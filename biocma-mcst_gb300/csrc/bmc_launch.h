@@ -101,6 +101,7 @@ const KernelSet* udf_kernel_set(int model, int f64);
 void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* counts, int grid);
 void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive, unsigned long long* out);
 void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out);
+void launch_debug_quantize(cudaStream_t st, const float* v, unsigned long long n, int e, long long* out);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);
 

@@ -534,6 +534,12 @@ int bmc_debug_draws(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t ste
  * d_t` with float ages and a double time step (move_kernel.hpp L356),
  * evaluated by the kernels with float and integer operations. */
 int bmc_debug_age_add(const float* ages, uint64_t n, double dt, float* out);
+/* The cycle kernels' quantisation of float contribution values to the
+ * accumulators' fixed point (the nearest multiple of 2^e, ties to even,
+ * clamped to 2^42 quanta) on n values: out[2k] by the scaled conversion the
+ * kernels use, out[2k + 1] from the IEEE fields (the form used when 2^-e is
+ * not a float of at most 2^125). */
+int bmc_debug_quantize(const float* values, uint64_t n, int32_t e, int64_t* out);
 /* Self-test of the bounded barrier wait of the cycle kernels: one thread
  * waits on an mbarrier whose single arrival it makes first (arrive != 0) or
  * that nothing makes; in the second case the wait gives up after limit_ns

@@ -55,3 +55,30 @@ def test_age_step_at_rounding_ties():
             dt = ulp / 2
         got = device_age_add(a, dt)
         assert np.array_equal(got.view(np.uint32), reference(a, dt).view(np.uint32)), dt
+
+
+def test_float_quantisation_forms_agree():
+    """The scaled-conversion quantisation of the cycle kernels equals the
+    IEEE-field form and rint(v * 2^-e) (the oracle's quantisation) on
+    random values, rounding ties, subnormals, zeros, clamped magnitudes,
+    infinities and NaN, for quantum exponents across the float range."""
+    from bmc import _lib
+
+    rng = np.random.default_rng(17)
+    qmax = 1 << 42
+    for e in (-160, -126, -125, -90, -64, -40, -20, 0, 20, 100, 126, 127):
+        v = np.concatenate([
+            (rng.standard_normal(200000) * np.exp2(rng.uniform(-40, 50, 200000) + e)).astype(np.float32),
+            # exact ties: odd multiples of half a quantum
+            np.clip((rng.integers(-2**22, 2**22, 20000) * 2 + 1) * 2.0 ** (e - 1), -3e38, 3e38).astype(np.float32),
+            np.array([0.0, -0.0, 1e-45, -1e-45, 1.1754942e-38, np.inf, -np.inf, np.nan, 3.4e38, -3.4e38],
+                     np.float32)])
+        out = np.zeros(2 * len(v), np.int64)
+        _lib.call("bmc_debug_quantize", ct.c_void_p(v.ctypes.data), len(v), e, ct.c_void_p(out.ctypes.data))
+        fast, bits = out[0::2], out[1::2]
+        assert np.array_equal(fast, bits), e
+        fin = np.isfinite(v)
+        ref = np.rint(np.ldexp(v[fin].astype(np.float64), -e))
+        ref = np.clip(ref, -qmax, qmax).astype(np.int64)
+        sub = np.abs(v[fin]) < np.float32(1.1754944e-38)  # subnormal inputs quantise to 0 on the device
+        assert np.array_equal(np.where(sub, 0, ref), fast[fin]), e
