@@ -348,16 +348,19 @@ __device__ __forceinline__ bool scen_finished(const ScenDev& S, const Control* c
 }
 
 // ---------------------------------------------------------------------------
-// Draw source: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), keyed by
-// the scenario seed, counter (particle id, step, purpose, 0).
+// Draw source: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) with
+// counter (particle id, seed low word, step, seed high word) and key
+// (purpose, 0): one stream per (seed, particle, step, purpose).  The purpose
+// is a constant at every call site, so the key schedule of the ten rounds
+// folds into immediates instead of two additions a round per particle.
 struct Draws {
   float u[4];
 };
 
 __device__ __forceinline__ Draws philox_draws(unsigned long long seed, uint32_t id, uint32_t step,
                                               uint32_t purpose) {
-  uint32_t c0 = id, c1 = step, c2 = purpose, c3 = 0u;
-  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  uint32_t c0 = id, c1 = (uint32_t)seed, c2 = step, c3 = (uint32_t)(seed >> 32);
+  uint32_t k0 = purpose, k1 = 0u;
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     const uint32_t lo0 = 0xD2511F53u * c0;
@@ -384,8 +387,8 @@ __device__ __forceinline__ Draws philox_draws(unsigned long long seed, uint32_t 
 
 __device__ __forceinline__ void philox_raw(unsigned long long seed, uint32_t id, uint32_t step,
                                            uint32_t purpose, uint32_t out[4]) {
-  uint32_t c0 = id, c1 = step, c2 = purpose, c3 = 0u;
-  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  uint32_t c0 = id, c1 = (uint32_t)seed, c2 = step, c3 = (uint32_t)(seed >> 32);
+  uint32_t k0 = purpose, k1 = 0u;
 #pragma unroll
   for (int r = 0; r < 10; ++r) {
     const uint32_t lo0 = 0xD2511F53u * c0;

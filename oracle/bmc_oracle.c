@@ -21,8 +21,9 @@
 /* Draw source.  The reference draws from Kokkos::Random_XorShift1024_Pool
  * (apps/libs/mc/public/mc/alias.hpp L98), which cannot be replayed outside
  * Kokkos.  Both this oracle and the GPU path use Philox4x32-10 (Salmon et al.,
- * SC'11, "Parallel random numbers: as easy as 1, 2, 3"), keyed by the
- * scenario seed and countered by (particle id, step, purpose). */
+ * SC'11, "Parallel random numbers: as easy as 1, 2, 3") with counter
+ * (particle id, seed low word, step, seed high word) and key (purpose, 0):
+ * one stream per (seed, particle, step, purpose). */
 
 static inline void mulhilo32(uint32_t a, uint32_t b, uint32_t* hi, uint32_t* lo) {
   uint64_t p = (uint64_t)a * (uint64_t)b;
@@ -56,11 +57,16 @@ void orc_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint3
  * 2^-24, exactly representable, never 0 or 1. */
 float orc_u01(uint32_t x) { return (float)((x >> 8) | 1u) * 0x1p-24f; }
 
-void orc_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]) {
-  uint32_t ctr[4] = {id, step, purpose, 0u};
-  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
-  uint32_t r[4];
+/* The four raw 32-bit words of the stream (seed, id, step, purpose). */
+static void draws_raw(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, uint32_t r[4]) {
+  uint32_t ctr[4] = {id, (uint32_t)seed, step, (uint32_t)(seed >> 32)};
+  uint32_t key[2] = {purpose, 0u};
   orc_philox4x32_10(ctr, key, r);
+}
+
+void orc_draws(uint64_t seed, uint32_t id, uint32_t step, uint32_t purpose, float out[4]) {
+  uint32_t r[4];
+  draws_raw(seed, id, step, purpose, r);
   for (int k = 0; k < 4; ++k) out[k] = orc_u01(r[k]);
 }
 
@@ -340,10 +346,9 @@ void orc_init_particles(orc_state* s, uint64_t n, uint32_t pos_lo, uint32_t pos_
   for (uint64_t i = 0; i < n; ++i) {
     float d[4];
     const uint32_t pid = (uint32_t)i;
-    uint32_t ctr[4] = {pid, 0xFFFFFFFFu, 2u, 0u};
-    uint32_t key[2] = {(uint32_t)s->seed, (uint32_t)(s->seed >> 32)};
+    /* step word 0xFFFFFFFF: no main-loop step draws with it */
     uint32_t r[4];
-    orc_philox4x32_10(ctr, key, r);
+    draws_raw(s->seed, pid, 0xFFFFFFFFu, 2u, r);
     for (int k = 0; k < 4; ++k) d[k] = orc_u01(r[k]);
     model_init(s, i, d);
     s->pos[i] = pos_lo + (uint32_t)(((uint64_t)r[0] * (uint64_t)span) >> 32);
