@@ -206,22 +206,30 @@ struct bmc_scenario {
   void* garena = nullptr;
   std::vector<double> gvol;
   // steps enqueued by bmc_step_enqueue, collected in order by
-  // bmc_step_collect: pinned copies of each step's control block and
-  // concentrations, an event, and the caller's buffers
+  // bmc_step_collect: an event after each step's export and the caller's
+  // buffers; pending entry k exports into slot k of h_export
   struct Pending {
-    Control* ctl = nullptr;      // pinned
-    double* conc = nullptr;      // pinned, room for both buffers
     cudaEvent_t done = nullptr;
     bmc_step_stats* stats = nullptr;
     double* out = nullptr;
-    int parity = -1;             // buffer copied (-1: both)
+    size_t ne = 0;
   };
   Pending pend[2];
   unsigned pend_head = 0, pend_count = 0;
-  size_t pend_ne = 0;
-  // the step counter after the last enqueued step, when known on the host
-  long long pred_step = -1;
+  // host memory mapped into the device address space, two slots of
+  // [control block | concentrations], written by the export kernel
+  unsigned char* h_export = nullptr;
+  unsigned char* d_export = nullptr;
+  size_t export_ne = 0, export_slot = 0, export_conc = 0;
   bool enqueuing = false;  // inside bmc_step_enqueue
+  // staging of descriptor uploads in host memory mapped into the device
+  // address space (a ring, each slot reused once the upload from it has
+  // completed)
+  static constexpr int kUpSlots = 4;
+  ScenDev* h_up = nullptr;
+  ScenDev* d_up = nullptr;  // device address of h_up
+  cudaEvent_t up_done[kUpSlots] = {};
+  unsigned up_next = 0;
 };
 
 struct bmc_batch {
@@ -256,8 +264,46 @@ int variant_of(unsigned threads, unsigned ppt) {
   return -1;
 }
 
+// Makes `dev` the calling thread's current device for one scope and puts the
+// caller's device back at its end.
+struct DeviceScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceScope(int dev) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+    else if (err == cudaSuccess) prev = -1;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// The host descriptor to the device, stream-ordered: staged in mapped
+// pinned host memory and copied by a one-block kernel (a copy engine
+// transfer of these few kilobytes between two steps costs several
+// microseconds of stream time; a copy from pageable memory may also wait
+// for the stream).
 int upload_desc(bmc_scenario* s) {
-  BMC_CUDA(counted_memcpy_async(s->d_desc, &s->h, sizeof(ScenDev), cudaMemcpyHostToDevice, s->stream));
+  if (!s->h_up) {
+    void* hp = nullptr;
+    BMC_CUDA(cudaHostAlloc(&hp, bmc_scenario::kUpSlots * sizeof(ScenDev), cudaHostAllocMapped));
+    s->h_up = static_cast<ScenDev*>(hp);
+    void* dp = nullptr;
+    BMC_CUDA(cudaHostGetDevicePointer(&dp, hp, 0));
+    s->d_up = static_cast<ScenDev*>(dp);
+    for (auto& e : s->up_done) BMC_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  const unsigned k = s->up_next++ % bmc_scenario::kUpSlots;
+  BMC_CUDA(cudaEventSynchronize(s->up_done[k]));  // the upload that last read the slot
+  std::memcpy(s->h_up + k, &s->h, sizeof(ScenDev));
+  bmc::launch_upload_desc(s->stream, s->d_up + k, s->d_desc);
+  g_launches++;
+  BMC_CUDA(cudaGetLastError());
+  count_copy(sizeof(ScenDev), cudaMemcpyHostToDevice);
+  BMC_CUDA(cudaEventRecord(s->up_done[k], s->stream));
   return BMC_OK;
 }
 
@@ -725,11 +771,12 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->garena) cudaFree(s->garena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   if (s->h_cstage) cudaFreeHost(s->h_cstage);
-  for (auto& q : s->pend) {
-    if (q.ctl) cudaFreeHost(q.ctl);
-    if (q.conc) cudaFreeHost(q.conc);
+  for (auto& q : s->pend)
     if (q.done) cudaEventDestroy(q.done);
-  }
+  if (s->h_export) cudaFreeHost(s->h_export);
+  for (auto& e : s->up_done)
+    if (e) cudaEventDestroy(e);
+  if (s->h_up) cudaFreeHost(s->h_up);
   cudaStreamDestroy(s->stream);
   delete s;
   return BMC_OK;
@@ -1309,20 +1356,6 @@ namespace {
 std::mutex g_scratch_mu;
 std::array<unsigned long long*, 64> g_scratch_ptr{};  // device address of the array, by device ordinal
 
-// Makes `dev` the calling thread's current device for one scope and puts the
-// caller's device back at its end.
-struct DeviceScope {
-  int prev = -1;
-  cudaError_t err = cudaSuccess;
-  explicit DeviceScope(int dev) {
-    err = cudaGetDevice(&prev);
-    if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
-    else if (err == cudaSuccess) prev = -1;
-  }
-  ~DeviceScope() {
-    if (prev >= 0) cudaSetDevice(prev);
-  }
-};
 }  // namespace
 
 int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
@@ -2245,49 +2278,40 @@ int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* 
   if (!s || !stats || !conc) return fail(BMC_E_INVALID, "null argument");
   if (s->pend_count >= 2) return fail(BMC_E_STATE, "two steps in flight: collect one first");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
+  DeviceScope on(s->device);
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
-  if (s->pend_ne < ne) {
+  if (s->export_ne < ne) {
     if (s->pend_count > 0) return fail(BMC_E_STATE, "the domain grew while steps are in flight");
-    for (auto& q : s->pend) {
-      if (q.conc) cudaFreeHost(q.conc);
-      q.conc = nullptr;
-    }
-    s->pend_ne = 0;
-    for (auto& q : s->pend) BMC_CUDA(cudaMallocHost(&q.conc, 2 * ne * sizeof(double)));
-    s->pend_ne = ne;
+    if (s->h_export) cudaFreeHost(s->h_export);
+    s->h_export = s->d_export = nullptr;
+    s->export_ne = 0;
+    s->export_conc = align_up(sizeof(Control), 256);
+    s->export_slot = align_up(s->export_conc + ne * sizeof(double), 256);
+    void* hp = nullptr;
+    BMC_CUDA(cudaHostAlloc(&hp, 2 * s->export_slot, cudaHostAllocMapped));
+    s->h_export = static_cast<unsigned char*>(hp);
+    void* dp = nullptr;
+    BMC_CUDA(cudaHostGetDevicePointer(&dp, hp, 0));
+    s->d_export = static_cast<unsigned char*>(dp);
+    s->export_ne = ne;
   }
-  bmc_scenario::Pending& q = s->pend[(s->pend_head + s->pend_count) % 2];
-  if (!q.ctl) BMC_CUDA(cudaMallocHost(&q.ctl, sizeof(Control)));
+  const unsigned k = (s->pend_head + s->pend_count) % 2u;
+  bmc_scenario::Pending& q = s->pend[k];
   if (!q.done) BMC_CUDA(cudaEventCreateWithFlags(&q.done, cudaEventDisableTiming));
-  // the step counter after this step, when the host knows the one before it
-  // (a step advances it by one unless the step limit holds it)
-  long long before = -1;
-  if (s->pend_count == 0)
-    before = s->ctl_fresh ? (long long)s->h_ctl->step : -1;
-  else
-    before = s->pred_step;
-  long long after = -1;
-  if (before >= 0) {
-    const bool held = s->h.step_limit != 0u && (unsigned long long)before >= s->h.step_limit;
-    after = held ? before : before + 1;
-  }
   s->enqueuing = true;
   const int rc = scenario_steps(s, dt, 1, 1, true);
   s->enqueuing = false;
   if (rc) return rc;
-  BMC_CUDA(counted_memcpy_async(q.ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
-  if (after >= 0) {
-    q.parity = (int)(after & 1);
-    BMC_CUDA(counted_memcpy_async(q.conc + q.parity * ne, s->h.C + q.parity * ne, ne * sizeof(double),
-                                  cudaMemcpyDeviceToHost, s->stream));
-  } else {
-    q.parity = -1;
-    BMC_CUDA(counted_memcpy_async(q.conc, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-  }
+  // the step's counters and concentrations straight into the slot: one
+  // small kernel on the step's stream instead of two copies
+  bmc::launch_export(s->stream, s->d_desc, s->d_export + k * s->export_slot, s->export_conc, ne);
+  g_launches++;
+  BMC_CUDA(cudaGetLastError());
+  g_d2h += sizeof(Control) + ne * sizeof(double);
   BMC_CUDA(cudaEventRecord(q.done, s->stream));
   q.stats = stats;
   q.out = conc;
-  s->pred_step = after;
+  q.ne = ne;
   s->pend_count++;
   return BMC_OK;
 }
@@ -2295,25 +2319,21 @@ int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* 
 int bmc_step_collect(bmc_scenario* s) {
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (s->pend_count == 0) return fail(BMC_E_STATE, "no step enqueued");
-  bmc_scenario::Pending& q = s->pend[s->pend_head];
+  const unsigned k = s->pend_head;
+  bmc_scenario::Pending& q = s->pend[k];
   BMC_CUDA(cudaEventSynchronize(q.done));
-  s->pend_head = (s->pend_head + 1) % 2;
+  s->pend_head = (s->pend_head + 1) % 2u;
   s->pend_count--;
-  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
-  const int cur = (int)(q.ctl->step & 1u);
-  if (q.parity >= 0 && q.parity != cur) {
-    // not expected: the buffer the counter names is still intact (a step in
-    // flight writes the other one)
-    BMC_CUDA(counted_memcpy(q.conc + cur * ne, s->h.C + cur * ne, ne * sizeof(double), cudaMemcpyDeviceToHost));
-    s->pred_step = -1;
-  }
-  std::memcpy(q.out, q.conc + cur * ne, ne * sizeof(double));
-  stats_from_ctl(*q.ctl, q.stats);
+  const unsigned char* slot = s->h_export + k * s->export_slot;
+  Control c;
+  std::memcpy(&c, slot, sizeof(Control));
+  std::memcpy(q.out, slot + s->export_conc, q.ne * sizeof(double));
+  stats_from_ctl(c, q.stats);
   if (s->pend_count == 0) {
-    std::memcpy(s->h_ctl, q.ctl, sizeof(Control));
+    *s->h_ctl = c;
     s->ctl_fresh = true;
   }
-  if (q.ctl->error) return fail(BMC_E_DEVICE, "device error word set: " + std::to_string(q.ctl->error));
+  if (c.error) return fail(BMC_E_DEVICE, "device error word set: " + std::to_string(c.error));
   return BMC_OK;
 }
 

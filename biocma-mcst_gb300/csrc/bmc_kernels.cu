@@ -1,5 +1,6 @@
 // bmc_kernels.cu -- the table of the built-in model plugins' kernel sets and
 // the model-independent kernels (repartition, draw dump).
+#include <algorithm>
 #include <cstdio>
 
 #include "bmc_kernel_templates.cuh"
@@ -34,6 +35,35 @@ __global__ void k_debug_age_add(const float* __restrict__ a, unsigned long long 
   const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
   for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
     out[i] = age_add_fast(a[i], k);
+}
+
+// Export of one step's results to host memory mapped into the device
+// address space: the control block (4-byte words) at dst, then the
+// concentrations the step left (buffer step & 1, [n_c][n_s]) at dst +
+// conc_offset.  Launched after the step on its stream; the host reads dst
+// once an event recorded after this kernel has completed.
+__global__ void k_export(const ScenDev* __restrict__ sc, unsigned char* __restrict__ dst,
+                         unsigned long long conc_offset) {
+  static_assert(sizeof(Control) % 4 == 0, "control block in 4-byte words");
+  const ScenDev& S = *sc;
+  const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
+  if (blockIdx.x == 0) {
+    const unsigned* cw = reinterpret_cast<const unsigned*>(S.ctl);
+    unsigned* ow = reinterpret_cast<unsigned*>(dst);
+    for (unsigned i = threadIdx.x; i < sizeof(Control) / 4; i += blockDim.x) ow[i] = cw[i];
+  }
+  const unsigned long long ne = (unsigned long long)S.n_c * S.n_s;
+  const double* c = S.C + (unsigned long long)(S.ctl->step & 1u) * ne;
+  double* oc = reinterpret_cast<double*>(dst + conc_offset);
+  for (unsigned long long i = tid; i < ne; i += nth) oc[i] = c[i];
+}
+
+// Upload of a scenario descriptor staged in host memory mapped into the
+// device address space: one block copies it into the device descriptor,
+// stream-ordered like a copy but without a copy-engine round trip.
+__global__ void k_upload_desc(const unsigned* __restrict__ src, unsigned* __restrict__ dst) {
+  static_assert(sizeof(ScenDev) % 4 == 0, "descriptor in 4-byte words");
+  for (unsigned i = threadIdx.x; i < sizeof(ScenDev) / 4; i += blockDim.x) dst[i] = src[i];
 }
 
 // The cycle kernels' float quantisation on n values with quantum 2^e:
@@ -101,6 +131,16 @@ void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t
 }
 void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out) {
   k_debug_age_add<<<256, 256, 0, st>>>(a, n, dt, out);
+}
+
+void launch_export(cudaStream_t st, const ScenDev* sc, unsigned char* dst, unsigned long long conc_offset,
+                   unsigned long long ne) {
+  const unsigned blocks = (unsigned)std::min<unsigned long long>(64ull, (ne + 2047ull) / 2048ull + 1ull);
+  k_export<<<blocks, 256, 0, st>>>(sc, dst, conc_offset);
+}
+
+void launch_upload_desc(cudaStream_t st, const ScenDev* src_mapped, ScenDev* dst) {
+  k_upload_desc<<<1, 256, 0, st>>>(reinterpret_cast<const unsigned*>(src_mapped), reinterpret_cast<unsigned*>(dst));
 }
 
 void launch_debug_quantize(cudaStream_t st, const float* v, unsigned long long n, int e, long long* out) {

@@ -102,6 +102,13 @@ void launch_repartition(cudaStream_t st, const ScenDev* sc, unsigned long long* 
 void launch_debug_wait(cudaStream_t st, unsigned long long limit_ns, int arrive, unsigned long long* out);
 void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n, double dt, float* out);
 void launch_debug_quantize(cudaStream_t st, const float* v, unsigned long long n, int e, long long* out);
+// Copies a descriptor staged in mapped host memory (device address
+// src_mapped) to the device descriptor (k_upload_desc).
+void launch_upload_desc(cudaStream_t st, const ScenDev* src_mapped, ScenDev* dst);
+// Copies a step's control block and current concentrations to mapped host
+// memory (k_export); ne = compartments * species.
+void launch_export(cudaStream_t st, const ScenDev* sc, unsigned char* dst, unsigned long long conc_offset,
+                   unsigned long long ne);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);
 
