@@ -714,8 +714,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // read state variables, compartments, ids, ages and statuses, STAGES tiles
 // ahead, with the tile's scenario and extent in the stage's meta record.
 // THREADS consumer threads wait on the stage, process slots r*THREADS + tid
-// from shared memory, write results straight to global memory (streaming
-// stores), and release the stage on its "empty" mbarrier.  The loads in
+// from shared memory, write results straight to global memory (stores that
+// do not allocate in L1), and release the stage on its "empty" mbarrier.  The loads in
 // flight no longer live in registers, so the memory pipeline stays full at
 // any occupancy.  Every wait is bounded; consumers vote after each wait, so
 // if one gives up (BMC_ERR_TIMEOUT) all stop at the same point with their
@@ -1071,7 +1071,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             }
           }
 #pragma unroll
-          for (int v = 0; v < NV; ++v) __stcs(sr.state + (size_t)v * sr.cap + gi, xx[v]);
+          for (int v = 0; v < NV; ++v) st_na(sr.state + (size_t)v * sr.cap + gi, xx[v]);
           if (st == kDivision) {
             div = true;
             S.bpos[gi] = p0;
@@ -1083,7 +1083,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
               p = (uint32_t)next_compartment(sr.mrow, sr.mrow16, p0, sr.K, (int)draw_int(rd[1]));
               ++my_move;
             }
-            __stcs(S.pos + gi, p);
+            st_na(S.pos + gi, p);
           }
           if (sr.n_out > 0) {
             float ah = age_add_fast(bah[slot], sr.ak);  // ages(i, 0) += d_t (double)
@@ -1098,9 +1098,9 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
                 break;
               }
             }
-            __stcs(S.age_h + gi, ah);
+            st_na(S.age_h + gi, ah);
           }
-          __stcs(S.age_d + gi, ad);
+          st_na(S.age_d + gi, ad);
         }
       }
       if constexpr (Model::separable && AGG) warp_aggregated_add(sacc, qkey, qv, has_q);

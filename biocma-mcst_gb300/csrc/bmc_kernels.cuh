@@ -68,31 +68,57 @@ __device__ __forceinline__ void ld_stream(const T* p, T* out) {
   }
 }
 
+// Global stores that do not allocate in L1: the cycle kernels write each
+// particle's results once and never read them back in the launch, and
+// allocating them evicted the compartment records and neighbour rows the
+// kernels gather through L1 (same-box A/B against cache-streaming stores:
+// FP64 512-compartment cycle 0.2015 -> 0.1897 ms, batched 1.956 -> 1.914 ms).
+__device__ __forceinline__ void st_na(double* p, double v) {
+  asm volatile("st.global.L1::no_allocate.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void st_na(float* p, float v) {
+  asm volatile("st.global.L1::no_allocate.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_na(uint32_t* p, uint32_t v) {
+  asm volatile("st.global.L1::no_allocate.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_na(unsigned short* p, unsigned short v) {
+  asm volatile("st.global.L1::no_allocate.u16 [%0], %1;" ::"l"(p), "h"(v) : "memory");
+}
+__device__ __forceinline__ void st_na(uint2* p, uint2 v) {
+  asm volatile("st.global.L1::no_allocate.v2.u32 [%0], {%1, %2};" ::"l"(p), "r"(v.x), "r"(v.y) : "memory");
+}
+__device__ __forceinline__ void st_na(uint4* p, uint4 v) {
+  asm volatile("st.global.L1::no_allocate.v4.u32 [%0], {%1, %2, %3, %4};" ::"l"(p), "r"(v.x), "r"(v.y), "r"(v.z),
+               "r"(v.w)
+               : "memory");
+}
+
 template <class T, int N>
 __device__ __forceinline__ void st_stream(T* p, const T* in) {
   constexpr int bytes = sizeof(T) * N;
   if constexpr (bytes == 16) {
     uint4 r;
     memcpy(&r, in, 16);
-    __stcs(reinterpret_cast<uint4*>(p), r);
+    st_na(reinterpret_cast<uint4*>(p), r);
   } else if constexpr (bytes == 32) {
     uint4 a, b;
     memcpy(&a, in, 16);
     memcpy(&b, reinterpret_cast<const char*>(in) + 16, 16);
-    __stcs(reinterpret_cast<uint4*>(p), a);
-    __stcs(reinterpret_cast<uint4*>(p) + 1, b);
+    st_na(reinterpret_cast<uint4*>(p), a);
+    st_na(reinterpret_cast<uint4*>(p) + 1, b);
   } else if constexpr (bytes == 8) {
     uint2 r;
     memcpy(&r, in, 8);
-    __stcs(reinterpret_cast<uint2*>(p), r);
+    st_na(reinterpret_cast<uint2*>(p), r);
   } else if constexpr (bytes == 4) {
     unsigned r;
     memcpy(&r, in, 4);
-    __stcs(reinterpret_cast<unsigned*>(p), r);
+    st_na(reinterpret_cast<uint32_t*>(p), r);
   } else if constexpr (bytes == 2) {
     unsigned short r;
     memcpy(&r, in, 2);
-    __stcs(reinterpret_cast<unsigned short*>(p), r);
+    st_na(reinterpret_cast<unsigned short*>(p), r);
   } else {
 #pragma unroll
     for (int k = 0; k < N; ++k) p[k] = in[k];
