@@ -93,6 +93,7 @@ def ref_lib():
         L.ref_cycle_read.argtypes = [VP, ct.c_uint64, VP, VP, VP, VP, VP]
         L.ref_cycle_misses.restype = ct.c_long
         L.ref_cycle_misses.argtypes = [VP]
+        L.ref_cycle_set_leaving.argtypes = [VP, ct.c_uint32, VP]
         L.ref_cycle_step_stream.restype = ct.c_int32
         L.ref_cycle_step_stream.argtypes = [VP, ct.c_double, VP, ct.c_uint64, VP, VP, VP, VP]
         L.ref_assert_failures.restype = ct.c_long
@@ -195,6 +196,11 @@ class RefCycle:
         tab = draw_tables(o)
         o.step()
         conc = np.ascontiguousarray(o.C, np.float64)
+        # the outlets' flows this step's cycle used (scheduled feeds change them)
+        n_out = int(o.s.n_outlets)
+        if n_out:
+            flows = np.array([o.s.outlet_flow[k] for k in range(n_out)], np.float64)
+            ref_lib().ref_cycle_set_leaving(self.h, n_out, _p(flows))
         stats = np.zeros(8, np.uint64)
         ex = np.zeros(self.n_ctb * self.n_c)
         ab = np.zeros(self.n_ctb * self.n_c)

@@ -27,9 +27,12 @@
 //   apps/libs/models/public/models/fixed_length.hpp, simple_acetate.hpp
 //   apps/libs/common/src/common.cpp (Common::c_league_size, from the source
 //     file)
-// The one part restated here is the order in which SimulationUnit calls
-// them, SimulationUnit::cycleProcess and post_cycle
-// (apps/libs/simulation/public/simulation/simulation.hpp L184-L239):
+// The parts restated here: the leaving flows of each cycle, which
+// SimulationUnit::update_feed hands to the domain before the cycle
+// (simulation.model.cpp L101-L108; the caller passes them), and the order in
+// which SimulationUnit calls the rest, SimulationUnit::cycleProcess and
+// post_cycle (apps/libs/simulation/public/simulation/simulation.hpp
+// L184-L239):
 //   pre_cycle (functors.update), contribs_scatter.reset(), launch_model,
 //   launch_move when need_launch(), then the host reductions,
 //   update_and_remove_inactive(out, dead), merge_buffer.
@@ -166,6 +169,7 @@ struct CycleBase {
                         float* age_d) const = 0;
   virtual uint32_t n_var() const = 0;
   virtual uint32_t n_ctb() const = 0;
+  virtual void set_leaving(uint32_t n, const double* flow) = 0;
   virtual uint64_t capacity() const = 0;
 };
 
@@ -311,6 +315,11 @@ struct Cycle final : CycleBase {
   }
   uint32_t n_var() const override { return M::n_var; }
   uint32_t n_ctb() const override { return M::n_c; }
+  // the outlets' flows of the coming cycle (SimulationUnit::update_feed sets
+  // them through ReactorDomain::set_leaving_flow before each cycle)
+  void set_leaving(uint32_t n, const double* flow) override {
+    for (uint32_t o = 0; o < n && o < lf.size(); ++o) lf[o].flow = flow[o];
+  }
   uint64_t capacity() const override { return container.capacity(); }
 };
 
@@ -388,6 +397,12 @@ int32_t ref_cycle_step_stream(void* hv, double dt, const double* conc, uint64_t 
   if (!h->stream) h->stream = std::make_unique<Xorshift1024>(seed);
   StepDraws d;
   return h->c->step(dt, conc, d, h->stream.get(), stats, exact, exact_abs, scatter);
+}
+
+// Flows of the outlets (in the order ref_cycle_new took them) for the next
+// cycle.
+void ref_cycle_set_leaving(void* h, uint32_t n, const double* flow) {
+  static_cast<Handle*>(h)->c->set_leaving(n, flow);
 }
 
 // The container: particles [0, n) into arrays of capacity cap (state

@@ -75,7 +75,15 @@ def cases():
         sc.feeds[0].flow = 2e-5
         return sc
 
+    def acetate_ring_scheduled_outlet():
+        # the outlet's flow grows linearly from 1e-5 to 4e-4 m^3/s over the 40 steps
+        sc = scenarios.small_ring(3000, model=scenarios.simple_acetate(), feeds=True, seed=17)
+        fd = sc.feeds[0]
+        fd.kind, fd.f0, fd.rate = scenarios.FEED_LINEAR, 1e-5, 1e-4
+        return sc
+
     return [("fixed_ring", fixed_ring, {}), ("acetate_ring", acetate_ring, {}),
+            ("acetate_ring_scheduled_outlet", acetate_ring_scheduled_outlet, {}),
             ("fixed_ring_compact_every_step", fixed_ring_compact_every_step, {}), ("acetate_0d", acetate_0d, {}),
             ("acetate_lattice", acetate_lattice, {}), ("fixed_ring_chunk_quirk", fixed_ring, {"quirk_tag3d": True}),
             ("acetate_ring_chunk_quirk", acetate_ring, {"quirk_tag3d": True})]

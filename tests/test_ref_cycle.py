@@ -63,7 +63,8 @@ def test_golden_made_without_assert_failures(golden):
     assert tot["births"] > 1000 and tot["exits"] > 1000 and tot["moves"] > 10000 and tot["compactions"] > 40
 
 
-CASES = ["fixed_ring", "acetate_ring", "fixed_ring_compact_every_step", "acetate_0d", "acetate_lattice",
+CASES = ["fixed_ring", "acetate_ring", "acetate_ring_scheduled_outlet", "fixed_ring_compact_every_step",
+         "acetate_0d", "acetate_lattice",
          "fixed_ring_chunk_quirk", "acetate_ring_chunk_quirk"]
 
 
