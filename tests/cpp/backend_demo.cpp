@@ -2,14 +2,16 @@
 // maintainer adding to the reference (class BmcBackend), compiled as a C++
 // program against include/bmc.h and linked to libbmc.so.
 //
-//   backend_demo <input.bin> <output.bin>
+//   backend_demo <input.bin> <output.bin> [pipelined]
 //
 // The input holds one scenario (sizes, model descriptor, domain, liquid
 // transition, concentrations, feeds, run length); the program sets it up
 // through the C-ABI, runs the main loop with step_and_export (bmc_step_read
-// every iteration, growth on overflow), then writes the per-step counters,
-// the concentrations of every step and the final particles.  The test
-// compares these with the Python binding's run bit for bit.
+// every iteration, growth on overflow) or, with `pipelined`, with
+// bmc_step_enqueue / bmc_step_collect and two steps in flight (feeds set
+// again before every enqueue), then writes the per-step counters, the
+// concentrations of every step and the final particles.  The test compares
+// these with the Python binding's run bit for bit.
 extern "C" {
 #include "bmc.h"
 }
@@ -50,6 +52,17 @@ class BmcBackend {
     if (st.overflow > 0) check(bmc_reserve(s_, (uint64_t)((double)(st.n_used + st.overflow) * alloc_factor)));
     return st;
   }
+  // the main loop with the host's work on step k overlapped with step k+1
+  // on the device: counters and fields of every step into st / c
+  void run_pipelined(double dt, uint32_t n_steps, const std::vector<bmc_feed>& feeds,
+                     std::vector<bmc_step_stats>& st, std::vector<std::vector<double>>& c) {
+    for (uint32_t k = 0; k < n_steps; ++k) {
+      check(bmc_set_feeds(s_, (uint32_t)feeds.size(), feeds.data()));
+      check(bmc_step_enqueue(s_, dt, &st[k], c[k].data()));
+      if (k > 0) check(bmc_step_collect(s_));
+    }
+    if (n_steps > 0) check(bmc_step_collect(s_));
+  }
   bmc_scenario* handle() { return s_; }
 
  private:
@@ -82,10 +95,11 @@ void put(FILE* f, const T* p, size_t n) {
 }  // namespace
 
 int main(int argc, char** argv) {
-  if (argc != 3) {
-    std::fprintf(stderr, "usage: %s input.bin output.bin\n", argv[0]);
+  if (argc != 3 && !(argc == 4 && std::strcmp(argv[3], "pipelined") == 0)) {
+    std::fprintf(stderr, "usage: %s input.bin output.bin [pipelined]\n", argv[0]);
     return 2;
   }
+  const bool pipelined = argc == 4;
   try {
     FILE* in = std::fopen(argv[1], "rb");
     if (!in) throw std::runtime_error("cannot open input");
@@ -118,11 +132,23 @@ int main(int argc, char** argv) {
     if (!out) throw std::runtime_error("cannot open output");
     put(out, &w, 1);
     std::vector<double> c((size_t)n_c * n_s);
-    for (uint32_t k = 0; k < n_steps; ++k) {
-      const bmc_step_stats st = backend.step_and_export(dt, c, alloc);
-      const uint64_t row[6] = {st.n_used, st.births, st.exits, st.moves, st.overflow, st.error};
-      put(out, row, 6);
-      put(out, c.data(), c.size());
+    if (pipelined) {
+      std::vector<bmc_step_stats> sts(n_steps);
+      std::vector<std::vector<double>> cs(n_steps, std::vector<double>((size_t)n_c * n_s));
+      backend.run_pipelined(dt, n_steps, feeds, sts, cs);
+      for (uint32_t k = 0; k < n_steps; ++k) {
+        const bmc_step_stats& st = sts[k];
+        const uint64_t row[6] = {st.n_used, st.births, st.exits, st.moves, st.overflow, st.error};
+        put(out, row, 6);
+        put(out, cs[k].data(), cs[k].size());
+      }
+    } else {
+      for (uint32_t k = 0; k < n_steps; ++k) {
+        const bmc_step_stats st = backend.step_and_export(dt, c, alloc);
+        const uint64_t row[6] = {st.n_used, st.births, st.exits, st.moves, st.overflow, st.error};
+        put(out, row, 6);
+        put(out, c.data(), c.size());
+      }
     }
     // the final particles: SoA state, compartments, statuses, ids
     bmc_step_stats st{};

@@ -3,7 +3,8 @@ compiled as a program against include/bmc.h and linked to libbmc.so
 (tests/cpp/backend_demo.cpp).  On the CPU it must compile and link; on the
 GPU it runs a scenario through bmc_step_read every iteration and its
 counters, fields and final particles must equal the Python binding's run of
-the same scenario bit for bit."""
+the same scenario bit for bit; its pipelined loop (bmc_step_enqueue /
+bmc_step_collect) must write the same bytes."""
 import os
 import struct
 import subprocess
@@ -98,3 +99,18 @@ def test_cpp_binding_equals_python_binding(tmp_path):
     off += n
     assert np.array_equal(np.frombuffer(raw, np.uint32, n, off), p["id"])
     g.close()
+
+
+@pytest.mark.gpu
+def test_cpp_pipelined_loop_equals_step_read_loop(tmp_path):
+    """The same program with bmc_step_enqueue / bmc_step_collect (two steps
+    in flight, feeds set before every enqueue) writes the same bytes as with
+    bmc_step_read every iteration."""
+    sc = scenarios.workload(2, n_particles=200_000)
+    exe = build_demo(tmp_path)
+    inp = str(tmp_path / "in.bin")
+    write_input(inp, sc, 12)
+    a, b = str(tmp_path / "a.bin"), str(tmp_path / "b.bin")
+    subprocess.run([exe, inp, a], check=True)
+    subprocess.run([exe, inp, b, "pipelined"], check=True)
+    assert open(a, "rb").read() == open(b, "rb").read()
