@@ -167,10 +167,19 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
     if (!do_scalar) {
       cn = Cold[e];
     } else {
+      // every load of the element that depends on no other, issued before
+      // any store (the stores go through double pointers the compiler must
+      // assume may alias these): the element's time on the step's critical
+      // path is a few memory round trips, not one per operand
       const double dt = S.dt;
       double srcv = S.src[e];
-      double sinkj = 0.0;
+      const double cj = Cold[e];
+      const double mold = S.M[e];
+      const double diag_j = S.diag[j];
+      const double vinv_j = S.vinv[j];
+      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
       const double t_rel = ctl->t_rel;
+      double sinkj = 0.0;
       for (unsigned f = 0; f < S.n_feeds; ++f) {
         const double ff = feed_flow_at(S, f, t_rel);
         if (S.feed_in[f] == j) {
@@ -179,13 +188,11 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
         }
         if (S.feed_out[f] == (int)j) sinkj = __dadd_rn(sinkj, ff);
       }
-      S.src[e] = srcv;
       double acc = 0.0;
-      const unsigned e0 = S.in_ptr[j], e1 = S.in_ptr[j + 1];
       for (unsigned q = e0; q < e1; ++q)
         acc = __dadd_rn(acc, __dmul_rn(Cold[(size_t)S.in_idx[q] * nsp + sp], S.in_flow[q]));
-      const double cj = Cold[e];
-      acc = __dadd_rn(acc, __dmul_rn(cj, S.diag[j]));
+      S.src[e] = srcv;
+      acc = __dadd_rn(acc, __dmul_rn(cj, diag_j));
       double dmdt = __dadd_rn(__dsub_rn(acc, __dmul_rn(cj, sinkj)), srcv);
       double mt = 0.0;
       if (S.gas) {
@@ -211,10 +218,9 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
         S.Cg[(parity ^ 1u) * ne + e] = __dmul_rn(mg, S.gvinv[j]);
         dmdt = __dadd_rn(dmdt, mt);  // Sign::LiquidToGas
       }
-      const double mold = S.M[e];
       const double mnew = __dadd_rn(mold, __dmul_rn(dt, dmdt));
       S.M[e] = mnew;
-      cn = __dmul_rn(mnew, S.vinv[j]);
+      cn = __dmul_rn(mnew, vinv_j);
       // two-phase: tiny negative liquid concentrations are cleared
       // (ScalarSimulation::clearNegs, implScalar.cpp L266-L293)
       if (S.gas && cn < 0.0 && fabs(cn) < kClearNegTol) cn = 0.0;
@@ -1141,8 +1147,6 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
   Control* ctl = S.ctl;
   const int tid = threadIdx.x;
   __shared__ unsigned long long sh64[33];
-  __shared__ unsigned long long p_n, p_req, p_rm, p_after;
-  __shared__ int p_compact;
   // (not scen_finished: slice 0 advances the step counter while the other
   // slices may still be starting)
   if (!ctl->cycling) {
@@ -1201,68 +1205,69 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     }
   }
   if (blockIdx.y != 0) return;
+  // The plan: every thread loads the control words it reads and computes the
+  // same plan; after one barrier (every load performed) thread 0 writes it
+  // back while the others go on to the scans, which need nothing from it.
+  const unsigned long long n = ctl->n_used;
+  const unsigned long long req = ctl->req_div;
+  const unsigned long long c_exits = ctl->exits, c_moves = ctl->moves, c_next = ctl->next_id;
+  const unsigned long long c_inactive = ctl->inactive;
+  const unsigned c_step = ctl->step, c_tadv = ctl->t_advance;
+  const double c_trel = ctl->t_rel;
+  const unsigned long long inactive_after = c_inactive + c_exits;
+  const unsigned long long ratio_thr = (unsigned long long)((double)n * S.dead_ratio);
+  const unsigned long long thr = S.min_removal > ratio_thr ? S.min_removal : ratio_thr;
+  int compact = inactive_after > thr ? 1 : 0;
+  unsigned long long rm = compact ? inactive_after : 0ull;
+  const bool bad_rm = rm > n;
+  if (bad_rm) {
+    rm = 0ull;
+    compact = 0;
+  }
+  const unsigned long long after = n - rm;
+  const unsigned long long room = S.cap > after ? S.cap - after : 0ull;
+  const unsigned long long n_births = req < room ? req : room;
+  __syncthreads();
   if (tid == 0) {
-    const unsigned long long n = ctl->n_used;
-    const unsigned long long req = ctl->req_div;
-    const unsigned long long inactive_after = ctl->inactive + ctl->exits;
-    const unsigned long long ratio_thr = (unsigned long long)((double)n * S.dead_ratio);
-    const unsigned long long thr = S.min_removal > ratio_thr ? S.min_removal : ratio_thr;
-    int compact = inactive_after > thr ? 1 : 0;
-    unsigned long long rm = compact ? inactive_after : 0ull;
-    if (rm > n) {
-      ctl->error |= 8u;
-      rm = 0ull;
-      compact = 0;
-    }
-    const unsigned long long after = n - rm;
-    const unsigned long long room = S.cap > after ? S.cap - after : 0ull;
-    const unsigned long long births = req < room ? req : room;
-    p_n = n;
-    p_req = req;
-    p_rm = rm;
-    p_after = after;
-    p_compact = compact;
+    if (bad_rm) ctl->error |= 8u;
     ctl->plan_n_old = n;
     ctl->plan_to_remove = rm;
     ctl->plan_n_after = after;
-    ctl->plan_births = births;
-    ctl->plan_overflow = req - births;
-    ctl->plan_next_id = ctl->next_id;
-    ctl->plan_step = ctl->step;
+    ctl->plan_births = n_births;
+    ctl->plan_overflow = req - n_births;
+    ctl->plan_next_id = c_next;
+    ctl->plan_step = c_step;
     ctl->plan_compact = (unsigned)compact;
     ctl->plan_gaps = 0ull;
-    if (ctl->next_id + births > 0x100000000ull) ctl->error |= 4u;
-    ctl->n_used = after + births;
+    if (c_next + n_births > 0x100000000ull) ctl->error |= 4u;
+    ctl->n_used = after + n_births;
     ctl->inactive = compact ? 0ull : inactive_after;
-    ctl->next_id += births;
-    if (S.n_maps > 0u) ctl->map_cur = (ctl->step / S.n_per_map) % S.n_maps;
-    ctl->step += 1u;
-    if (ctl->t_advance) ctl->t_rel = __dadd_rn(ctl->t_rel, S.dt);  // SimulationUnit::advance
-    ctl->last_births = births;
-    ctl->last_exits = ctl->exits;
-    ctl->last_moves = ctl->moves;
-    ctl->last_overflow = req - births;
+    ctl->next_id = c_next + n_births;
+    if (S.n_maps > 0u) ctl->map_cur = (c_step / S.n_per_map) % S.n_maps;
+    ctl->step = c_step + 1u;
+    if (c_tadv) ctl->t_rel = __dadd_rn(c_trel, S.dt);  // SimulationUnit::advance
+    ctl->last_births = n_births;
+    ctl->last_exits = c_exits;
+    ctl->last_moves = c_moves;
+    ctl->last_overflow = req - n_births;
     ctl->last_req_div = req;
     ctl->last_compacted = (unsigned)compact;
     unsigned fl = 0u;
     if (req > 0ull) fl |= kFlagDivide;
     if (compact && after > 0ull && rm < n) fl |= kFlagCompact;
-    if (births > 0ull) fl |= kFlagMerge;
+    if (n_births > 0ull) fl |= kFlagMerge;
     if (fl) atomicOr(&bctl->flags, fl);
   }
-  __syncthreads();
-  const unsigned long long n = p_n;
   const unsigned n_t = (unsigned)((n + kTile - 1) / kTile);
   const unsigned* __restrict__ births = S.tile_births;
   const unsigned* __restrict__ inact = S.tile_inactive;
-  if (p_req > 0) {
+  if (req > 0) {
     // birth ranks: births in earlier tiles
     block_exscan_items(
         n_t, [&](unsigned t) { return (unsigned long long)births[t]; },
         [&](unsigned t, unsigned long long pre, unsigned long long) { S.tile_boff[t] = (unsigned)pre; }, sh64);
   }
-  if (p_compact && p_after > 0 && p_rm < n) {
-    const unsigned long long after = p_after;
+  if (compact && after > 0 && rm < n) {
     // gap offsets for tiles t <= after / kTile (ascending prefix of inactive)
     const unsigned tg_end = min((unsigned)(after / kTile) + 1u, n_t);
     block_exscan_items(
