@@ -902,6 +902,16 @@ double orc_pin_std_normal(float u) { return sa_std_normal(u); }
 void orc_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, uint32_t purpose, float* out) {
   for (uint64_t i = 0; i < n; ++i) orc_draws(seed, ids[i], step, purpose, out + 4 * i);
 }
+/* Standard normals of the draw values u[k] by the reference's inverse-CDF
+ * form (sa_std_normal), and truncated normals of the same draws
+ * (orc_pin_truncnorm_f), for the distribution tests. */
+void orc_std_normal_table(const float* u, uint64_t n, double* out) {
+  for (uint64_t i = 0; i < n; ++i) out[i] = sa_std_normal(u[i]);
+}
+void orc_truncnorm_table(const float* u, uint64_t n, float mu, float sd, float lo, float hi, float* out) {
+  for (uint64_t i = 0; i < n; ++i) out[i] = orc_pin_truncnorm_f((double)u[i], mu, sd, lo, hi);
+}
+
 void orc_division_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, double* out) {
   for (uint64_t i = 0; i < n; ++i) {
     float d[4];

@@ -243,6 +243,8 @@ float orc_pin_norminv_f(float p, float mean, float sd);
 double orc_pin_std_normal(float u);
 void orc_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, uint32_t purpose, float* out);
 void orc_division_draw_table(uint64_t seed, const uint32_t* ids, uint64_t n, uint32_t step, double* out);
+void orc_std_normal_table(const float* u, uint64_t n, double* out);
+void orc_truncnorm_table(const float* u, uint64_t n, float mu, float sd, float lo, float hi, float* out);
 float orc_pin_truncnorm_f(double u, float mu, float sd, float lower, float upper);
 int32_t orc_logf_monotone_over_draws(uint32_t* bad_k);
 double orc_feed_flow(int32_t kind, double flow, double f0, double rate, double t);
