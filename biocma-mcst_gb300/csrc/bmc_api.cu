@@ -221,6 +221,10 @@ struct bmc_scenario {
   unsigned char* h_export = nullptr;
   unsigned char* d_export = nullptr;
   size_t export_ne = 0, export_slot = 0, export_conc = 0;
+  // pending entry whose export is not launched yet (-1: none): it goes out
+  // with the next descriptor upload, or alone before anything else uses the
+  // stream (settle_export)
+  int export_deferred = -1;
   bool enqueuing = false;  // inside bmc_step_enqueue
   // staging of descriptor uploads in host memory mapped into the device
   // address space (a ring, each slot reused once the upload from it has
@@ -299,11 +303,39 @@ int upload_desc(bmc_scenario* s) {
   const unsigned k = s->up_next++ % bmc_scenario::kUpSlots;
   BMC_CUDA(cudaEventSynchronize(s->up_done[k]));  // the upload that last read the slot
   std::memcpy(s->h_up + k, &s->h, sizeof(ScenDev));
-  bmc::launch_upload_desc(s->stream, s->d_up + k, s->d_desc);
-  g_launches++;
-  BMC_CUDA(cudaGetLastError());
+  if (s->export_deferred >= 0) {
+    // the export of the step in flight and this upload in one launch
+    const int q = s->export_deferred;
+    s->export_deferred = -1;
+    bmc::launch_export(s->stream, s->d_ctl, s->h.C, s->pend[q].ne, s->d_export + q * s->export_slot,
+                       s->export_conc, s->d_up + k, s->d_desc);
+    g_launches++;
+    BMC_CUDA(cudaGetLastError());
+    BMC_CUDA(cudaEventRecord(s->pend[q].done, s->stream));
+  } else {
+    bmc::launch_upload_desc(s->stream, s->d_up + k, s->d_desc);
+    g_launches++;
+    BMC_CUDA(cudaGetLastError());
+  }
   count_copy(sizeof(ScenDev), cudaMemcpyHostToDevice);
   BMC_CUDA(cudaEventRecord(s->up_done[k], s->stream));
+  return BMC_OK;
+}
+
+// Launches the export of the pending step whose export was deferred, alone.
+// Every entry point that uses the scenario's stream (other than a descriptor
+// upload, which takes the export along) calls it first, so the exported
+// results are those the step left.
+int settle_export(bmc_scenario* s) {
+  if (!s || s->export_deferred < 0) return BMC_OK;
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  const int q = s->export_deferred;
+  s->export_deferred = -1;
+  bmc::launch_export(s->stream, s->d_ctl, s->h.C, s->pend[q].ne, s->d_export + q * s->export_slot, s->export_conc);
+  g_launches++;
+  BMC_CUDA(cudaGetLastError());
+  BMC_CUDA(cudaEventRecord(s->pend[q].done, s->stream));
   return BMC_OK;
 }
 
@@ -783,6 +815,7 @@ int bmc_scenario_destroy(bmc_scenario* s) {
 }
 
 int bmc_reserve(bmc_scenario* s, uint64_t capacity) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (capacity == 0 || capacity > 0xFFFFFFFFull - kTile) return fail(BMC_E_INVALID, "capacity must be in [1, 2^32 - 1024]");
   const unsigned long long cap = align_up(capacity, kTile);
@@ -844,6 +877,7 @@ int bmc_reserve(bmc_scenario* s, uint64_t capacity) {
 
 int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* volume, const uint64_t* neighbors,
                       const double* out_flows, const double* cdf) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !volume || !out_flows || n_c == 0 || K == 0) return fail(BMC_E_INVALID, "bad domain arguments");
   if (n_c > 1 && (!neighbors || !cdf)) return fail(BMC_E_INVALID, "neighbors and cdf required when n_c > 1");
   if (!s->maps.empty()) return fail(BMC_E_STATE, "the domain follows the flow-map cycle (bmc_flowmap_clear first)");
@@ -937,6 +971,7 @@ int bmc_domain_update(bmc_scenario* s, uint32_t n_c, uint32_t K, const double* v
 
 int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
                            const double* values) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || (nnz && (!rows || !cols || !values))) return fail(BMC_E_INVALID, "bad transition arguments");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   if (n != s->h.n_c) return fail(BMC_E_INVALID, "transition size differs from n_compartments");
@@ -973,6 +1008,7 @@ int bmc_set_transition_coo(bmc_scenario* s, uint32_t n, uint64_t nnz, const uint
 }
 
 int bmc_set_concentrations(bmc_scenario* s, const double* conc) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !conc) return fail(BMC_E_INVALID, "null argument");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   const size_t n_c = s->h.n_c, ns = s->h.n_s;
@@ -1020,6 +1056,7 @@ int bmc_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
 }
 
 int bmc_set_weight(bmc_scenario* s, double weight) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !(weight > 0.0)) return fail(BMC_E_INVALID, "weight must be > 0");
   s->h.weight = weight;
   int rc = set_quanta(s);
@@ -1046,6 +1083,7 @@ static int write_ctl_fresh(bmc_scenario* s, unsigned long long n, unsigned long 
 }
 
 int bmc_init_particles(bmc_scenario* s, uint64_t n, int32_t uniform_init, double x0, double* weight_out) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   if (n > s->h.cap) return fail(BMC_E_CAPACITY, "more particles than capacity");
@@ -1077,6 +1115,7 @@ int bmc_init_particles(bmc_scenario* s, uint64_t n, int32_t uniform_init, double
 
 int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint32_t* pos, const uint8_t* status,
                       const float* age_h, const float* age_d, const uint32_t* id, uint64_t next_id) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !state || !pos || !status || !age_h || !age_d || !id) return fail(BMC_E_INVALID, "null argument");
   if (n > s->h.cap) return fail(BMC_E_CAPACITY, "more particles than capacity");
   const size_t fsz = s->h.f64 ? 8 : 4;
@@ -1176,6 +1215,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
 }
 
 int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   int rc = scenario_steps(s, dt, 1, 0, false);
   if (rc) return rc;
   return read_ctl(s, stats);
@@ -1183,6 +1223,7 @@ int bmc_cycle(bmc_scenario* s, double dt, bmc_step_stats* stats) {
 
 int bmc_cycle_external(bmc_scenario* s, double dt, const double* conc, double* sources, int32_t on_device,
                        bmc_step_stats* stats) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !conc || !sources) return fail(BMC_E_INVALID, "null argument");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
@@ -1200,12 +1241,14 @@ int bmc_cycle_external(bmc_scenario* s, double dt, const double* conc, double* s
 }
 
 int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   int rc = scenario_steps(s, dt, 1, 1, true);
   if (rc) return rc;
   return read_ctl(s, stats);
 }
 
 int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!conc) return fail(BMC_E_INVALID, "null concentrations");
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   // When the host mirror of the control block is current, the step counter
@@ -1248,14 +1291,17 @@ int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* con
 }
 
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   int rc = scenario_steps(s, dt, n_steps, 1, true);
   if (rc) return rc;
   return read_ctl(s, stats);
 }
 
-int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps) { return scenario_steps(s, dt, n_steps, 1, true); }
+int bmc_run_async(bmc_scenario* s, double dt, uint32_t n_steps) {
+  if (const int rc_settle = settle_export(s)) return rc_settle; return scenario_steps(s, dt, n_steps, 1, true); }
 
 int bmc_run_timed(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats, float* elapsed_ms) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   int rc = check_ready(s, true);
   if (rc) return rc;
   rc = set_dt(s, dt, true);  // outside the timed region
@@ -1276,18 +1322,21 @@ int bmc_run_timed(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* 
 }
 
 int bmc_synchronize(bmc_scenario* s) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   BMC_CUDA(cudaStreamSynchronize(s->stream));
   return BMC_OK;
 }
 
 int bmc_read_stats(bmc_scenario* s, bmc_step_stats* stats) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   return read_ctl(s, stats);
 }
 
 int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* pos, uint8_t* status, float* age_h,
                        float* age_d, uint32_t* id, uint64_t* n_out) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   int rc = read_ctl(s, nullptr);
   if (rc && rc != BMC_E_DEVICE) return rc;
@@ -1310,6 +1359,7 @@ int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* p
 }
 
 int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
@@ -1326,6 +1376,7 @@ int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources
 }
 
 int bmc_repartition(bmc_scenario* s, uint64_t* counts) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !counts) return fail(BMC_E_INVALID, "null argument");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   unsigned long long* d = nullptr;
@@ -1359,6 +1410,7 @@ std::array<unsigned long long*, 64> g_scratch_ptr{};  // device address of the a
 }  // namespace
 
 int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !counts) return fail(BMC_E_INVALID, "null argument");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set");
   if (s->h.n_c > BMC_REPARTITION_STATIC_MAX)
@@ -1393,6 +1445,7 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts) {
 }
 
 int bmc_force_remove_dead(bmc_scenario* s) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   int rc = read_ctl(s, nullptr);
   if (rc) return rc;
@@ -1536,6 +1589,7 @@ int bmc_batch_destroy(bmc_batch* b) {
 }
 
 int bmc_set_step_limit(bmc_scenario* s, uint32_t step_limit) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   s->h.step_limit = step_limit;
   int rc = upload_desc(s);
@@ -1545,6 +1599,7 @@ int bmc_set_step_limit(bmc_scenario* s, uint32_t step_limit) {
 }
 
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (threads || ppt) {  // 0 and 0 keep the current variant (the automatic one included)
     const unsigned cur = s->variant == bmc::kVariantAuto ? bmc::kAutoStaged : s->variant;
@@ -1638,6 +1693,7 @@ extern "C" {
 
 int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
                 const double* values, const double* henry, const double* kla) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !gas_volume || !henry || !kla || (nnz && (!rows || !cols || !values)))
     return fail(BMC_E_INVALID, "bad gas arguments");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update fixes n_compartments)");
@@ -1696,6 +1752,7 @@ int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const u
 }
 
 int bmc_gas_set_concentrations(bmc_scenario* s, const double* conc) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !conc) return fail(BMC_E_INVALID, "null argument");
   if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
   const size_t n_c = s->h.n_c, ns = s->h.n_s;
@@ -1713,6 +1770,7 @@ int bmc_gas_set_concentrations(bmc_scenario* s, const double* conc) {
 }
 
 int bmc_gas_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || (n_feeds && !feeds)) return fail(BMC_E_INVALID, "null argument");
   if (n_feeds > (uint32_t)bmc::kMaxOutlets) return fail(BMC_E_INVALID, "at most 8 gas feeds");
   if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
@@ -1733,6 +1791,7 @@ int bmc_gas_set_feeds(bmc_scenario* s, uint32_t n_feeds, const bmc_feed* feeds) 
 }
 
 int bmc_gas_read(bmc_scenario* s, double* conc, double* mass, double* transfer) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
   const size_t ne = (size_t)s->h.n_c * s->h.n_s;
@@ -1858,6 +1917,7 @@ extern "C" {
 
 int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neighbors, const double* out_flows,
                     const double* cdf, uint64_t nnz, const uint64_t* rows, const uint64_t* cols, const double* values) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !volume || !out_flows || (nnz && (!rows || !cols || !values)))
     return fail(BMC_E_INVALID, "bad flow-map arguments");
   if (!s->has_domain) return fail(BMC_E_STATE, "domain not set (bmc_domain_update fixes n_compartments and K)");
@@ -1882,6 +1942,7 @@ int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neigh
 }
 
 int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !(t_per_flowmap >= 0.0)) return fail(BMC_E_INVALID, "t_per_flowmap must be >= 0");
   s->t_per_map = t_per_flowmap;
   int rc = refresh_map_tables(s);
@@ -1893,6 +1954,7 @@ int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap) {
 }
 
 int bmc_flowmap_clear(bmc_scenario* s) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");
   s->maps.clear();
   return upload_maps(s);
@@ -1903,6 +1965,7 @@ int bmc_flowmap_clear(bmc_scenario* s) {
 // ---- diagnostics -----------------------------------------------------------------
 
 int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* kernel_ms) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   int rc = check_ready(s, true);
   if (rc) return rc;
   rc = set_dt(s, dt, true);
@@ -2266,6 +2329,7 @@ int bmc_set_feed_schedules(bmc_scenario* s, uint32_t n_feeds, const bmc_feed_sch
 }
 
 int bmc_feed_time(bmc_scenario* s, double* t) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s || !t) return fail(BMC_E_INVALID, "null argument");
   const int rc = read_ctl(s, nullptr);
   if (rc && rc != BMC_E_DEVICE) return rc;
@@ -2298,17 +2362,17 @@ int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* 
   const unsigned k = (s->pend_head + s->pend_count) % 2u;
   bmc_scenario::Pending& q = s->pend[k];
   if (!q.done) BMC_CUDA(cudaEventCreateWithFlags(&q.done, cudaEventDisableTiming));
+  int rc = settle_export(s);  // the previous step's export, if still deferred
+  if (rc) return rc;
   s->enqueuing = true;
-  const int rc = scenario_steps(s, dt, 1, 1, true);
+  rc = scenario_steps(s, dt, 1, 1, true);
   s->enqueuing = false;
   if (rc) return rc;
-  // the step's counters and concentrations straight into the slot: one
-  // small kernel on the step's stream instead of two copies
-  bmc::launch_export(s->stream, s->d_desc, s->d_export + k * s->export_slot, s->export_conc, ne);
-  g_launches++;
-  BMC_CUDA(cudaGetLastError());
+  // the step's counters and concentrations go straight into slot k by a
+  // small kernel (no copies), launched with the next descriptor upload when
+  // one comes before anything else (bmc_set_feeds in a loop), else alone
+  s->export_deferred = (int)k;
   g_d2h += sizeof(Control) + ne * sizeof(double);
-  BMC_CUDA(cudaEventRecord(q.done, s->stream));
   q.stats = stats;
   q.out = conc;
   q.ne = ne;
@@ -2321,6 +2385,10 @@ int bmc_step_collect(bmc_scenario* s) {
   if (s->pend_count == 0) return fail(BMC_E_STATE, "no step enqueued");
   const unsigned k = s->pend_head;
   bmc_scenario::Pending& q = s->pend[k];
+  if (s->export_deferred == (int)k) {
+    const int rc = settle_export(s);
+    if (rc) return rc;
+  }
   BMC_CUDA(cudaEventSynchronize(q.done));
   s->pend_head = (s->pend_head + 1) % 2u;
   s->pend_count--;

@@ -39,21 +39,26 @@ __global__ void k_debug_age_add(const float* __restrict__ a, unsigned long long 
 
 // Export of one step's results to host memory mapped into the device
 // address space: the control block (4-byte words) at dst, then the
-// concentrations the step left (buffer step & 1, [n_c][n_s]) at dst +
-// conc_offset.  Launched after the step on its stream; the host reads dst
-// once an event recorded after this kernel has completed.
-__global__ void k_export(const ScenDev* __restrict__ sc, unsigned char* __restrict__ dst,
-                         unsigned long long conc_offset) {
+// concentrations the step left (buffer step & 1 of C, [n_c][n_s], ne
+// values) at dst + conc_offset.  Launched after the step on its stream; the
+// host reads dst once an event recorded after this kernel has completed.
+// With up_src set, block 0 then also copies a descriptor staged in mapped
+// host memory (device address up_src) into up_dst: the upload that precedes
+// the next step, in the same launch.
+__global__ void k_export(const Control* __restrict__ ctl, const double* __restrict__ C, unsigned long long ne,
+                         unsigned char* __restrict__ dst, unsigned long long conc_offset,
+                         const unsigned* __restrict__ up_src, unsigned* __restrict__ up_dst) {
   static_assert(sizeof(Control) % 4 == 0, "control block in 4-byte words");
-  const ScenDev& S = *sc;
+  static_assert(sizeof(ScenDev) % 4 == 0, "descriptor in 4-byte words");
   const unsigned tid = blockIdx.x * blockDim.x + threadIdx.x, nth = gridDim.x * blockDim.x;
   if (blockIdx.x == 0) {
-    const unsigned* cw = reinterpret_cast<const unsigned*>(S.ctl);
+    const unsigned* cw = reinterpret_cast<const unsigned*>(ctl);
     unsigned* ow = reinterpret_cast<unsigned*>(dst);
     for (unsigned i = threadIdx.x; i < sizeof(Control) / 4; i += blockDim.x) ow[i] = cw[i];
+    if (up_src)
+      for (unsigned i = threadIdx.x; i < sizeof(ScenDev) / 4; i += blockDim.x) up_dst[i] = up_src[i];
   }
-  const unsigned long long ne = (unsigned long long)S.n_c * S.n_s;
-  const double* c = S.C + (unsigned long long)(S.ctl->step & 1u) * ne;
+  const double* c = C + (unsigned long long)(ctl->step & 1u) * ne;
   double* oc = reinterpret_cast<double*>(dst + conc_offset);
   for (unsigned long long i = tid; i < ne; i += nth) oc[i] = c[i];
 }
@@ -133,10 +138,11 @@ void launch_debug_age_add(cudaStream_t st, const float* a, unsigned long long n,
   k_debug_age_add<<<256, 256, 0, st>>>(a, n, dt, out);
 }
 
-void launch_export(cudaStream_t st, const ScenDev* sc, unsigned char* dst, unsigned long long conc_offset,
-                   unsigned long long ne) {
+void launch_export(cudaStream_t st, const Control* ctl, const double* C, unsigned long long ne, unsigned char* dst,
+                   unsigned long long conc_offset, const ScenDev* up_src, ScenDev* up_dst) {
   const unsigned blocks = (unsigned)std::min<unsigned long long>(64ull, (ne + 2047ull) / 2048ull + 1ull);
-  k_export<<<blocks, 256, 0, st>>>(sc, dst, conc_offset);
+  k_export<<<blocks, 256, 0, st>>>(ctl, C, ne, dst, conc_offset, reinterpret_cast<const unsigned*>(up_src),
+                                   reinterpret_cast<unsigned*>(up_dst));
 }
 
 void launch_upload_desc(cudaStream_t st, const ScenDev* src_mapped, ScenDev* dst) {

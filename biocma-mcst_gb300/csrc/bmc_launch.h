@@ -105,10 +105,12 @@ void launch_debug_quantize(cudaStream_t st, const float* v, unsigned long long n
 // Copies a descriptor staged in mapped host memory (device address
 // src_mapped) to the device descriptor (k_upload_desc).
 void launch_upload_desc(cudaStream_t st, const ScenDev* src_mapped, ScenDev* dst);
-// Copies a step's control block and current concentrations to mapped host
-// memory (k_export); ne = compartments * species.
-void launch_export(cudaStream_t st, const ScenDev* sc, unsigned char* dst, unsigned long long conc_offset,
-                   unsigned long long ne);
+// Copies a step's control block and current concentrations (ne =
+// compartments * species values of C's current buffer) to mapped host memory
+// (k_export); with up_src set, also a descriptor staged in mapped host memory
+// into up_dst.
+void launch_export(cudaStream_t st, const Control* ctl, const double* C, unsigned long long ne, unsigned char* dst,
+                   unsigned long long conc_offset, const ScenDev* up_src = nullptr, ScenDev* up_dst = nullptr);
 void launch_debug_draws(cudaStream_t st, unsigned long long seed, const uint32_t* ids, unsigned long long n,
                         uint32_t step, uint32_t purpose, float* out);
 
