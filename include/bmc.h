@@ -258,13 +258,17 @@ int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* con
 /* A main loop that reads the field back every iteration, pipelined: the
  * host enqueues step k+1 before it waits for the results of step k, so the
  * device does not idle while the host handles them.  bmc_step_enqueue
- * enqueues one iteration (as bmc_step) and the copy of its counters and
- * concentrations [n_c][n_s] into pinned staging, without waiting; at most
- * two steps are in flight.  bmc_step_collect waits for the oldest enqueued
- * step and writes its results into the stats and conc buffers given to its
- * bmc_step_enqueue (returns BMC_E_DEVICE when that step set the error
- * word).  Other stepping calls on the scenario are refused (BMC_E_STATE)
- * until every enqueued step is collected. */
+ * enqueues one iteration (as bmc_step) and the transfer of its counters and
+ * concentrations [n_c][n_s] into pinned host memory (mapped into the device
+ * address space; allocated at the first call, freed with the scenario),
+ * without waiting; at most two steps are in flight.  The transfer of a step
+ * goes out with the next call on the scenario (in one launch with the
+ * descriptor upload of a bmc_set_feeds between two enqueues), always before
+ * anything else uses the scenario's stream.  bmc_step_collect waits for the
+ * oldest enqueued step and writes its results into the stats and conc
+ * buffers given to its bmc_step_enqueue (returns BMC_E_DEVICE when that step
+ * set the error word).  Other stepping calls on the scenario are refused
+ * (BMC_E_STATE) until every enqueued step is collected. */
 int bmc_step_enqueue(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc);
 int bmc_step_collect(bmc_scenario* s);
 
