@@ -174,8 +174,6 @@ struct bmc_scenario {
   Control* d_ctl = nullptr;
   BatchCtl* d_bctl = nullptr;
   Control* h_ctl = nullptr;  // pinned
-  double* h_cstage = nullptr;  // pinned: both concentration buffers (bmc_step_read)
-  size_t cstage_n = 0;
   bool has_domain = false, has_transition = false, has_conc = false, has_weight = false;
   std::vector<double> volume;
   std::vector<bmc_feed> feeds;
@@ -802,7 +800,6 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->marena) cudaFree(s->marena);
   if (s->garena) cudaFree(s->garena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
-  if (s->h_cstage) cudaFreeHost(s->h_cstage);
   for (auto& q : s->pend)
     if (q.done) cudaEventDestroy(q.done);
   if (s->h_export) cudaFreeHost(s->h_export);
@@ -1248,46 +1245,16 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats) {
 }
 
 int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc) {
-  if (const int rc_settle = settle_export(s)) return rc_settle;
-  if (!conc) return fail(BMC_E_INVALID, "null concentrations");
   if (!s) return fail(BMC_E_INVALID, "null scenario");
-  // When the host mirror of the control block is current, the step counter
-  // after this step is known before it runs (it advances by one unless the
-  // step limit holds it), so only the concentration buffer that step writes
-  // is copied back; otherwise both are, and the parity read back with the
-  // control block names the current one.
-  int predicted = -1;
-  if (s->ctl_fresh) {
-    const uint32_t step = s->h_ctl->step;
-    const bool held = s->h.step_limit != 0u && step >= s->h.step_limit;
-    predicted = (int)((held ? step : step + 1u) & 1u);
-  }
-  int rc = scenario_steps(s, dt, 1, 1, true);
+  if (!conc) return fail(BMC_E_INVALID, "null concentrations");
+  if (s->pend_count > 0) return fail(BMC_E_STATE, "steps enqueued by bmc_step_enqueue are not collected yet");
+  // The pipelined pair with nothing else in flight: the step, then one small
+  // kernel writing its control block and the concentration buffer it left
+  // into mapped host memory, waited for at once.
+  bmc_step_stats unused;
+  const int rc = bmc_step_enqueue(s, dt, stats ? stats : &unused, conc);
   if (rc) return rc;
-  const size_t ne = (size_t)s->h.n_c * s->h.n_s;
-  if (s->cstage_n < ne) {
-    if (s->h_cstage) cudaFreeHost(s->h_cstage);
-    s->h_cstage = nullptr;
-    s->cstage_n = 0;
-    BMC_CUDA(cudaMallocHost(&s->h_cstage, 2 * ne * sizeof(double)));
-    s->cstage_n = ne;
-  }
-  if (predicted >= 0)
-    BMC_CUDA(counted_memcpy_async(s->h_cstage + predicted * ne, s->h.C + predicted * ne, ne * sizeof(double),
-                                  cudaMemcpyDeviceToHost, s->stream));
-  else
-    BMC_CUDA(counted_memcpy_async(s->h_cstage, s->h.C, 2 * ne * sizeof(double), cudaMemcpyDeviceToHost,
-                                  s->stream));
-  rc = read_ctl(s, stats);
-  if (rc && rc != BMC_E_DEVICE) return rc;
-  const int cur = (int)(s->h_ctl->step & 1u);
-  if (predicted >= 0 && predicted != cur) {  // not expected: fetch the buffer the counter names
-    BMC_CUDA(counted_memcpy_async(s->h_cstage + cur * ne, s->h.C + cur * ne, ne * sizeof(double),
-                                  cudaMemcpyDeviceToHost, s->stream));
-    BMC_CUDA(cudaStreamSynchronize(s->stream));
-  }
-  std::memcpy(conc, s->h_cstage + cur * ne, ne * sizeof(double));
-  return rc;
+  return bmc_step_collect(s);
 }
 
 int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats) {

@@ -252,7 +252,9 @@ int bmc_step(bmc_scenario* s, double dt, bmc_step_stats* stats);
 /* bmc_step followed by bmc_read_liquid(conc) with a single device
  * synchronisation: the step, the control block and the concentrations
  * [n_c][n_s] after the step travel back together (the host loop that reads
- * the field every iteration). */
+ * the field every iteration).  It is bmc_step_enqueue followed at once by
+ * bmc_step_collect (the mapped host buffer below is allocated at the first
+ * call); refused with BMC_E_STATE while enqueued steps are not collected. */
 int bmc_step_read(bmc_scenario* s, double dt, bmc_step_stats* stats, double* conc);
 
 /* A main loop that reads the field back every iteration, pipelined: the

@@ -263,6 +263,40 @@ def test_pipelined_steps_equal_step_read():
     assert g2.step() == g1.step()
 
 
+def test_pipelined_steps_with_other_calls_between():
+    """A step's transfer goes out with the next call on the scenario: calls
+    between an enqueue and its collect (counter and field reads, feeds, a
+    liquid read, the weight through a descriptor upload) see and leave the
+    results bmc_step_read gives."""
+    from bmc import _lib
+    from bmc.sim import GpuScenario
+
+    sc = scenarios.small_ring(5000, feeds=True)
+    g1, g2 = GpuScenario(sc), GpuScenario(sc)
+    shape = (sc.net.n_c, sc.n_species)
+    feeds = (_lib.Feed * len(sc.feeds))()
+    for k, fd in enumerate(sc.feeds):
+        feeds[k].inlet, feeds[k].outlet, feeds[k].flow = fd.inlet, fd.outlet, fd.flow
+        for sp in range(len(fd.conc)):
+            feeds[k].conc[sp] = float(fd.conc[sp])
+    for k in range(6):
+        c1 = np.zeros(shape)
+        s1 = g1.step_read(c1)
+        st, c2 = _lib.StepStats(), np.zeros(shape)
+        g2.step_enqueue(st, c2)
+        if k % 3 == 0:
+            g2.stats()
+        elif k % 3 == 1:
+            g2.liquid()
+        else:
+            _lib.call("bmc_set_feeds", g2.handle, len(sc.feeds), feeds)
+            g2.set_weight(g2.weight)
+        g2.step_collect()
+        assert st.as_dict() == s1, k
+        assert np.array_equal(c1.view(np.uint64), c2.view(np.uint64)), k
+    assert np.array_equal(g1.liquid()["C"].view(np.uint64), g2.liquid()["C"].view(np.uint64))
+
+
 def test_bounded_wait_gives_up_with_the_timeout_bit():
     """The bounded mbarrier wait of the cycle kernels, on a barrier nothing
     completes, returns after its limit with BMC_ERR_TIMEOUT; the context
