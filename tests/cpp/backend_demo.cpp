@@ -1,6 +1,6 @@
-// backend_demo.cpp -- the binding INTEGRATION.md section 2 shows a
-// maintainer adding to the reference (class BmcBackend), compiled as a C++
-// program against include/bmc.h and linked to libbmc.so.
+// backend_demo.cpp -- the binding a maintainer adds to the reference's
+// simulation core to hand its particle cycle to libbmc (class BmcBackend),
+// compiled as a C++ program against include/bmc.h and linked to libbmc.so.
 //
 //   backend_demo <input.bin> <output.bin> [pipelined]
 //

@@ -1,5 +1,5 @@
-"""The C-ABI from C++: the BmcBackend binding of INTEGRATION.md section 2,
-compiled as a program against include/bmc.h and linked to libbmc.so
+"""The C-ABI from C++: the BmcBackend binding a maintainer adds to the
+reference's simulation core, compiled as a program against include/bmc.h and linked to libbmc.so
 (tests/cpp/backend_demo.cpp).  On the CPU it must compile and link; on the
 GPU it runs a scenario through bmc_step_read every iteration and its
 counters, fields and final particles must equal the Python binding's run of
