@@ -187,6 +187,7 @@ struct bmc_scenario {
   // last cycle-launch sizing (prepare_cycle), reused while its inputs stay
   unsigned prep_variant = ~0u, prep_bps = 0u, prep_grid = 0u, prep_run = 0u;
   size_t prep_in = 0, prep_out = 0;
+  bool prep_global = false;
   unsigned graph_liq = 0, graph_plan = 0;
   int graph_scatter = 0;
   // flow-map cycle (host copies; device copies in marena)
@@ -251,6 +252,7 @@ struct bmc_batch {
   size_t graph_smem = 0;
   unsigned graph_grid = 0, graph_variant = 0;
   unsigned run_variant = 0;  // variant of the last prepared launch
+  bool run_global = false;   // ... and whether it scatters into the global accumulator
   unsigned plan_y = 1;       // k_plan slices of the last prepared launch
   unsigned graph_liq = 0, graph_plan = 0;
   int graph_scatter = 0;
@@ -453,19 +455,34 @@ static int size_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_r
 
 // Dynamic shared memory and grid of the cycle launch for the requested
 // variant; resolves kVariantAuto (*run_out: the variant to launch).
+// *global_out: the launch sums contributions straight into the global
+// accumulator (kScatterGlobal, tile-staging variants only), chosen when the
+// shared accumulator and the stage buffers do not fit one block.  Measured on
+// 1e7 particles (ms per step, 10,648 compartments): the tile-staging kernel
+// at one block per SM with its shared accumulator 0.321 (FP64) / 0.239
+// (FP32), with the global accumulator at two blocks per SM 0.329 / 0.304,
+// register streaming 0.532 / 0.360; so the shared accumulator is kept while
+// it fits.  Register-streaming shapes always keep the shared accumulator.
 int prepare_cycle(const bmc::KernelSet* ks, unsigned variant, unsigned bps_req, size_t* smem, int sm_count,
-                  unsigned* grid_out, unsigned* run_out) {
+                  unsigned* grid_out, unsigned* run_out, bool* global_out) {
   int fit = 0;
-  if (variant == bmc::kVariantAuto) {
-    size_t m = *smem;
-    unsigned g = 0;
-    if (size_cycle(ks, bmc::kAutoStaged, bps_req, &m, sm_count, &g, &fit) == BMC_OK && fit >= 2) {
-      *smem = m;
-      *grid_out = g;
-      *run_out = bmc::kAutoStaged;
-      return BMC_OK;
+  *global_out = false;
+  const bool staged = variant == bmc::kVariantAuto || ks->cycle_extra_smem[variant] > 0;
+  if (staged) {
+    const unsigned v = variant == bmc::kVariantAuto ? bmc::kAutoStaged : variant;
+    for (int glob = 0; glob < 2; ++glob) {
+      size_t m = glob ? 0 : *smem;
+      unsigned g = 0;
+      if (size_cycle(ks, v, bps_req, &m, sm_count, &g, &fit) == BMC_OK) {
+        *smem = m;
+        *grid_out = g;
+        *run_out = v;
+        *global_out = glob != 0;
+        return BMC_OK;
+      }
+      (void)cudaGetLastError();  // a refused size is not an error of the step
     }
-    (void)cudaGetLastError();  // a refused size is not an error of the step
+    if (variant != bmc::kVariantAuto) return fail(BMC_E_UNSUPPORTED, "cycle kernel cannot be resident with this shape");
     variant = bmc::kAutoStreamed;
   }
   int rc = size_cycle(ks, variant, bps_req, smem, sm_count, grid_out, &fit);
@@ -493,6 +510,8 @@ int enqueue_step(const bmc::KernelSet* ks, cudaStream_t st, ScenDev* d_table, in
     ks->flowmap(n_scen, st, d_table);
     g_launches += 1;
   }
+  if (scatter == bmc::kScatterGlobal && ks->cycle_extra_smem[variant] == 0)
+    return fail(BMC_E_UNSUPPORTED, "the global accumulator form needs a tile-staging launch shape");
   ks->liquid(n_scen, liq_grid, st, d_table, d_bctl, do_scalar);
   ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, d_table, n_scen, d_bctl, scatter);
   ks->plan(n_scen, plan_y, st, d_table, d_bctl);
@@ -520,6 +539,7 @@ bool batch_tiny(const bmc_batch* b) {
   return true;
 }
 int batch_scatter(const bmc_batch* b) {
+  if (b->run_global) return bmc::kScatterGlobal;
   if (batch_tiny(b)) return bmc::kScatterWarp;
   for (const bmc_scenario* m : b->scen)
     if (m && copy_domain(b->ks, m->h)) return bmc::kScatterCopied;
@@ -580,7 +600,8 @@ int batch_prepare(bmc_batch* b, double dt, int* n_out, unsigned* max_nc_out, siz
     b->dt = dt;
     b->total_tiles = tiles;
   }
-  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->sm_count, grid_out, &b->run_variant);
+  int rc = prepare_cycle(b->ks, b->variant, b->blocks_per_sm, &smem, b->sm_count, grid_out, &b->run_variant,
+                         &b->run_global);
   if (rc) return rc;
   *n_out = n;
   *max_nc_out = max_nc;
@@ -1130,9 +1151,8 @@ int bmc_set_particles(bmc_scenario* s, uint64_t n, const void* state, const uint
   return write_ctl_fresh(s, n, next_id, inactive);
 }
 
-static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned variant) {
+static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned variant, int scatter) {
   const unsigned liq = liquid_grid(s->h), plan = plan_slices(s->h);
-  const int scatter = scenario_scatter(s->ks, s->h);
   if (s->graph && s->graph_smem == smem && s->graph_grid == grid && s->graph_variant == variant &&
       s->graph_liq == liq && s->graph_plan == plan && s->graph_scatter == scatter)
     return BMC_OK;
@@ -1165,16 +1185,20 @@ static int ensure_graph(bmc_scenario* s, unsigned grid, size_t smem, unsigned va
 // prepare_cycle for a scenario, reusing the last answer while the launch
 // shape and the accumulator size are unchanged (no attribute or occupancy
 // query per step).
-static int scenario_prepare(bmc_scenario* s, size_t* smem, unsigned* grid, unsigned* variant) {
+static int scenario_prepare(bmc_scenario* s, size_t* smem, unsigned* grid, unsigned* variant, int* scatter) {
   if (s->prep_variant == s->variant && s->prep_bps == s->blocks_per_sm && s->prep_in == *smem) {
     *smem = s->prep_out;
     *grid = s->prep_grid;
     *variant = s->prep_run;
+    *scatter = s->prep_global ? bmc::kScatterGlobal : scenario_scatter(s->ks, s->h);
     return BMC_OK;
   }
   const size_t in = *smem;
-  int rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, grid, variant);
+  bool glob = false;
+  int rc = prepare_cycle(s->ks, s->variant, s->blocks_per_sm, smem, s->sm_count, grid, variant, &glob);
   if (rc) return rc;
+  *scatter = glob ? bmc::kScatterGlobal : scenario_scatter(s->ks, s->h);
+  s->prep_global = glob;
   s->prep_run = *variant;
   s->prep_variant = s->variant;
   s->prep_bps = s->blocks_per_sm;
@@ -1192,10 +1216,11 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   s->ctl_fresh = false;
   size_t smem = cycle_smem(s->h);
   unsigned grid = 0, variant = 0;
-  rc = scenario_prepare(s, &smem, &grid, &variant);
+  int scatter = 0;
+  rc = scenario_prepare(s, &smem, &grid, &variant, &scatter);
   if (rc) return rc;
   if (use_graph && do_scalar) {
-    rc = ensure_graph(s, grid, smem, variant);
+    rc = ensure_graph(s, grid, smem, variant, scatter);
     if (rc) return rc;
     for (uint32_t k = 0; k < n_steps; ++k) {
       BMC_CUDA(cudaGraphLaunch(s->graph, s->stream));
@@ -1205,7 +1230,7 @@ static int scenario_steps(bmc_scenario* s, double dt, uint32_t n_steps, int do_s
   }
   for (uint32_t k = 0; k < n_steps; ++k) {
     rc = enqueue_step(s->ks, s->stream, s->d_desc, 1, liquid_grid(s->h), plan_slices(s->h), s->d_bctl, do_scalar,
-                      variant, grid, smem, s->sm_count, s->h.n_maps > 0, scenario_scatter(s->ks, s->h));
+                      variant, grid, smem, s->sm_count, s->h.n_maps > 0, scatter);
     if (rc) return rc;
   }
   return BMC_OK;
@@ -1939,7 +1964,8 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   if (rc) return rc;
   size_t smem = cycle_smem(s->h);
   unsigned grid = 0, variant = 0;
-  rc = scenario_prepare(s, &smem, &grid, &variant);
+  int scatter = 0;
+  rc = scenario_prepare(s, &smem, &grid, &variant, &scatter);
   if (rc) return rc;
   cudaEvent_t ev[7];
   for (auto& e : ev) BMC_CUDA(cudaEventCreate(&e));
@@ -1952,7 +1978,7 @@ int bmc_step_timed(bmc_scenario* s, double dt, bmc_step_stats* stats, float* ker
   s->ks->liquid(1, liquid_grid(s->h), st, s->d_desc, s->d_bctl, 1);
   BMC_CUDA(cudaEventRecord(ev[1], st));
   s->ks->cycle[variant](dim3(grid), dim3(bmc::kVariantThreads[variant]), smem, st, s->d_desc, 1, s->d_bctl,
-                        scenario_scatter(s->ks, s->h));
+                        scatter);
   BMC_CUDA(cudaEventRecord(ev[2], st));
   s->ks->plan(1, plan_slices(s->h), st, s->d_desc, s->d_bctl);
   BMC_CUDA(cudaEventRecord(ev[3], st));

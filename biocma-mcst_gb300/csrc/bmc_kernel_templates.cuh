@@ -726,7 +726,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // any occupancy.  Every wait is bounded; consumers vote after each wait, so
 // if one gives up (BMC_ERR_TIMEOUT) all stop at the same point with their
 // barriers matched, the producer issues nothing more and drains its copies
-// in flight.
+// in flight.  SCATTER (ScatterForm) chooses where the contributions are
+// summed: the shared accumulator (plain, warp-aggregated or in copies,
+// flushed to the scenario's global accumulator), or, for domains whose
+// shared accumulator would not leave two blocks per SM, the global
+// accumulator directly (the dynamic shared memory then holds the stages
+// only).
 
 __host__ __device__ constexpr unsigned popcount_c(unsigned v) { return v == 0u ? 0u : (v & 1u) + popcount_c(v >> 1); }
 
@@ -774,6 +779,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     k_cycle_tma(const ScenDev* __restrict__ sc, int n_scen, BatchCtl* __restrict__ bctl) {
   constexpr bool AGG = SCATTER == kScatterWarp;
   constexpr bool COPIES = SCATTER == kScatterCopied;
+  constexpr bool GLOBAL = SCATTER == kScatterGlobal;  // no shared accumulator
   using TS = TileStage<Model, F>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   unsigned long long* sacc = reinterpret_cast<unsigned long long*>(smem_raw);
@@ -913,7 +919,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
     const ScenDev& P = sc[cur];
     const unsigned n_ent = P.n_c * NA;
     const unsigned copies = COPIES ? sr.rep_mask + 1u : 1u, cstride = sr.rep_stride;
-    if (!aborted)
+    if (!GLOBAL && !aborted)
       for (unsigned e = tid; e < n_ent; e += THREADS) {
         unsigned long long u = sacc[e];
         for (unsigned c = 1; c < copies; ++c) u += sacc[e + c * cstride];
@@ -982,7 +988,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
           aborted = true;
           my_err |= 32u;  // BMC_ERR_SMEM
         }
-      if (!aborted)
+      if (!GLOBAL && !aborted)
         for (unsigned e = tid; e < n_zero; e += THREADS) sacc[e] = 0ull;
       if (tid < 16) s_pf[tid] = (F)S.params[tid];
       cur = s;
@@ -1063,6 +1069,8 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             } else {
               if constexpr (COPIES)
                 acc_add(&sacc[p0 + ((unsigned)lane & sr.rep_mask) * sr.rep_stride], q);
+              else if constexpr (GLOBAL)
+                acc_add_global(S.acc_hi + p0, S.acc_lo + p0, q);
               else
                 acc_add(&sacc[p0], q);
             }
@@ -1073,7 +1081,10 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
             for (int j = 0; j < NC; ++j) {
               const double val = __dmul_rn(S.weight, (double)ctb[j]);
               const long long q = quantize(val, S.q_exp[j], my_clamp, my_err);
-              acc_add(&sacc[p0 * NC + j], q);
+              if constexpr (GLOBAL)
+                acc_add_global(S.acc_hi + (size_t)p0 * NC + j, S.acc_lo + (size_t)p0 * NC + j, q);
+              else
+                acc_add(&sacc[p0 * NC + j], q);
             }
           }
 #pragma unroll
@@ -1581,6 +1592,8 @@ void launch_cycle_tma_t(dim3 grid, dim3 block, size_t smem, cudaStream_t st, con
     k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterWarp><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
   else if (scatter == kScatterCopied)
     k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterCopied><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
+  else if (scatter == kScatterGlobal)
+    k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterGlobal><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
   else
     k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterPlain><<<grid, THREADS + 32, smem, st>>>(sc, n, b);
 }
@@ -1638,6 +1651,10 @@ int setup_cycle_tma_t(size_t smem, int* blocks_per_sm) {
                      THREADS + 32, smem, blocks_per_sm);
   if (e) return e;
   e = setup_fn(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterCopied>),
+               THREADS + 32, smem, &b2);
+  if (e) return e;
+  if (b2 < *blocks_per_sm) *blocks_per_sm = b2;
+  e = setup_fn(reinterpret_cast<const void*>(&k_cycle_tma<Model, F, THREADS, MINB, STAGES, kScatterGlobal>),
                THREADS + 32, smem, &b2);
   if (b2 < *blocks_per_sm) *blocks_per_sm = b2;
   return e;

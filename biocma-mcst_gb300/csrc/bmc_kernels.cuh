@@ -372,6 +372,18 @@ __device__ __forceinline__ void acc_add(unsigned long long* e, long long q) {
   if (hi != 0) atomicAdd(reinterpret_cast<int*>(w + 1), hi);
 }
 
+// Exact add of q to a scenario's global accumulator entry {hi, lo} (the
+// entry a shared-memory flush adds to): q >> 32 (arithmetic) to hi, the low
+// 32 bits of q to lo.  hi 2^32 + lo is the exact total however the values
+// are grouped, and fixed_to_double folds lo's carries.  The results are not
+// read back, so the adds compile to reductions.
+__device__ __forceinline__ void acc_add_global(long long* hi, unsigned long long* lo, long long q) {
+  const long long h = q >> 32;
+  const unsigned long long l = (unsigned long long)q & 0xffffffffull;
+  if (h != 0) atomicAdd(reinterpret_cast<unsigned long long*>(hi), (unsigned long long)h);
+  if (l != 0) atomicAdd(lo, l);
+}
+
 // ------------------------------------------------------------------------
 // Warp-aggregated scatter into the shared-memory accumulator: lanes whose
 // `on` is set add q to acc[p]; lanes of one compartment are summed first and

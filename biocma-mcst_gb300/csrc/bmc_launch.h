@@ -26,8 +26,11 @@ constexpr unsigned kLiquidThreads = 32;
 // Scatter form of a cycle launch: plain shared-memory atomics; warp-aggregated
 // (every domain of the launch at most kAggregateMaxCompartments
 // compartments); accumulator copies (some domain of a separable model at most
-// kScatterCopyMaxCompartments compartments, tile-staging kernel only).
-enum ScatterForm : int { kScatterPlain = 0, kScatterWarp = 1, kScatterCopied = 2 };
+// kScatterCopyMaxCompartments compartments, tile-staging kernel only); global
+// (no shared accumulator: each value goes straight to the scenario's exact
+// global accumulator, for domains whose shared accumulator would not leave
+// the tile-staging kernel two blocks per SM; tile-staging kernel only).
+enum ScatterForm : int { kScatterPlain = 0, kScatterWarp = 1, kScatterCopied = 2, kScatterGlobal = 3 };
 using CycleLaunch = void (*)(dim3, dim3, size_t, cudaStream_t, const ScenDev*, int, BatchCtl*, int scatter);
 using DivideLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
 using CopyLaunch = void (*)(dim3, cudaStream_t, const ScenDev*, int, const BatchCtl*);
@@ -48,8 +51,9 @@ constexpr int kCycleVariants = 7;
 constexpr unsigned kVariantThreads[kCycleVariants] = {256, 256, 256, 512, 1024, 288, 544};
 constexpr unsigned kVariantPPT[kCycleVariants] = {1, 2, 4, 2, 1, 4, 2};
 // Launch shape a scenario or batch starts with: resolved per launch to the
-// tile-staging 544 x 2 shape when two of its blocks fit on an SM (shared
-// accumulator plus stage buffers), else to register streaming 256 x 2.
+// tile-staging 544 x 2 shape, with the shared accumulator while it and the
+// stage buffers fit a block, else with the global accumulator
+// (kScatterGlobal); register streaming 256 x 2 only if neither fits.
 constexpr unsigned kVariantAuto = kCycleVariants;
 constexpr unsigned kAutoStaged = 6, kAutoStreamed = 1;
 // Domains of at most kScatterCopyMaxCompartments compartments (separable

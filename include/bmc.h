@@ -284,8 +284,12 @@ int bmc_run(bmc_scenario* s, double dt, uint32_t n_steps, bmc_step_stats* stats)
  * are 256 or 512 consumer threads plus a producer warp staging tiles through
  * the copy engine), resident blocks per SM (0 = as many as fit); threads and
  * ppt both 0 keep the current variant.  A new scenario starts in the
- * automatic shape: 544 x 2 when two of its blocks fit on an SM (shared
- * accumulator plus stage buffers), else 256 x 2. */
+ * automatic shape, 544 x 2.  The staging shapes sum the contributions in
+ * shared memory (n_compartments x accumulator columns x 8 bytes, beside
+ * the stage buffers) while that fits a block, else straight into the
+ * scenario's global accumulator, so every domain size runs; the
+ * register-streaming shapes always sum in shared memory and are refused
+ * (BMC_E_UNSUPPORTED) on a domain whose accumulator does not fit. */
 int bmc_set_shape(bmc_scenario* s, uint32_t threads, uint32_t ppt, uint32_t blocks_per_sm);
 
 /* Step budget: once the scenario's step counter reaches step_limit its

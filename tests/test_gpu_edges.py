@@ -96,10 +96,10 @@ def test_long_neighbour_rows(oracle_mod, shape, n_c):
     _parity(g, o, 6, f"K={net.K}")
 
 
-def test_automatic_shape_on_a_domain_too_large_for_tile_staging(oracle_mod):
-    """10,648 compartments: the shared accumulator and two blocks of stage
-    buffers do not fit on an SM, so the automatic shape streams particles
-    through registers instead; results stay those of the CPU restatement."""
+def test_automatic_shape_with_one_staging_block_per_sm(oracle_mod):
+    """10,648 compartments: the shared accumulator and the stage buffers of
+    two blocks do not fit on an SM, so the automatic shape runs one
+    tile-staging block per SM; results stay those of the CPU restatement."""
     from test_gpu_parity import make_pair
 
     net = networks.lattice_vortex(22, side=1.0, peak_velocity=0.5, noise=0.1, seed=7, max_courant=0.4, dt=0.05)
@@ -109,6 +109,78 @@ def test_automatic_shape_on_a_domain_too_large_for_tile_staging(oracle_mod):
     sc.feeds[0].outlet = net.n_c - 1
     g, o = make_pair(oracle_mod, sc)
     _parity(g, o, 3, "n_c=10648")
+
+
+def _on_lattice(sc, n):
+    """The scenario moved onto an n^3 vortex lattice (outlet in the last
+    compartment, the first compartment's concentrations everywhere)."""
+    net = networks.lattice_vortex(n, side=1.0, peak_velocity=0.5, noise=0.1, seed=7, max_courant=0.4, dt=sc.dt)
+    sc.net = net
+    sc.c0 = np.tile(sc.c0[:1], (net.n_c, 1))
+    for f in sc.feeds:
+        f.outlet = net.n_c - 1
+    return sc
+
+
+def test_domain_beyond_any_shared_accumulator(oracle_mod):
+    """32,768 compartments: a shared accumulator (256 KiB) fits no block, so
+    the contributions go straight to the scenario's global accumulator;
+    results stay those of the CPU restatement."""
+    from test_gpu_parity import make_pair
+
+    sc = _on_lattice(scenarios.workload(2, n_particles=200000, f64=True), 32)
+    assert sc.net.n_c == 32768
+    g, o = make_pair(oracle_mod, sc)
+    _parity(g, o, 3, "n_c=32768")
+
+
+def test_general_model_beyond_the_shared_accumulator(oracle_mod):
+    """The per-particle contribution path (FixedLength through its general
+    form) on 32,768 compartments, summed in the global accumulator."""
+    from test_gpu_parity import make_pair
+
+    sc = _on_lattice(scenarios.small_ring(100000, model=scenarios.fixed_length(general=True), feeds=True,
+                                          dt=0.05), 32)
+    g, o = make_pair(oracle_mod, sc)
+    _parity(g, o, 3, "general n_c=32768")
+
+
+def test_batch_with_a_domain_beyond_the_shared_accumulator():
+    """A batch holding one 32,768-compartment domain sums every member's
+    contributions in the global accumulators; each member still equals its
+    run alone (where the small ones use the shared accumulator)."""
+    from bmc.sim import GpuBatch, GpuScenario
+    from test_gpu_batch import assert_same
+
+    scens = [_on_lattice(scenarios.workload(2, n_particles=100000, f64=True), 32)]
+    scens += [scenarios.small_ring(20000, model=scenarios.overflow(f64=True), feeds=True, seed=s, dt=0.05)
+              for s in (3, 4)]
+    members = [GpuScenario(s) for s in scens]
+    alone = [GpuScenario(s) for s in scens]
+    b = GpuBatch(members)
+    b.run(3, 0.05)
+    b.synchronize()
+    for g in alone:
+        g.run(3)
+    for k, (gb, ga) in enumerate(zip(members, alone)):
+        assert gb.stats()["step"] == 3 and gb.stats()["error"] == 0
+        assert_same(gb, ga, f"member {k} ({scens[k].net.n_c} compartments)")
+    b.close()
+
+
+def test_register_streaming_shape_refuses_a_domain_beyond_shared_memory():
+    """The register-streaming kernels keep a shared accumulator: asked for on
+    a domain whose accumulator fits no block, the step is refused."""
+    from bmc import _lib
+    from bmc.sim import GpuScenario
+
+    sc = _on_lattice(scenarios.workload(2, n_particles=20000, f64=True), 32)
+    g = GpuScenario(sc)
+    g.set_shape(256, 2, 0)
+    with pytest.raises(_lib.BmcError) as e:
+        g.step()
+    assert e.value.code == -6  # BMC_E_UNSUPPORTED
+    assert g.stats()["step"] == 0
 
 
 def test_particle_id_space_exhaustion():
