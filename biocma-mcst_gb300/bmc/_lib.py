@@ -103,6 +103,9 @@ SIGNATURES = {
     "bmc_repartition": [VP, VP],
     "bmc_repartition_static": [VP, VP],
     "bmc_force_remove_dead": [VP],
+    "bmc_probe_enable": [VP, c_u64],
+    "bmc_probe_read": [VP, c_i32, VP, c_u64, VP],
+    "bmc_probe_clear": [VP, c_i32],
     "bmc_batch_create": [VP, c_u32, VP],
     "bmc_batch_create_slots": [c_u32, c_i32, c_i32, VP],
     "bmc_batch_set_slot": [VP, c_u32, VP],

@@ -297,6 +297,22 @@ class GpuScenario:
     def force_remove_dead(self):
         call("bmc_force_remove_dead", self.handle)
 
+    # time-event probes: 0 leaving times, 1 division times (include/bmc.h)
+    def probe_enable(self, capacity: int):
+        call("bmc_probe_enable", self.handle, capacity)
+        self.probe_capacity = capacity
+
+    def probe_read(self, probe: int) -> tuple[np.ndarray, int]:
+        """(stored values, events counted) of one probe."""
+        cap = getattr(self, "probe_capacity", 0)
+        out = np.zeros(max(cap, 1), dtype=np.float64)
+        n = ct.c_uint64()
+        call("bmc_probe_read", self.handle, probe, _p(out), cap, ct.byref(n))
+        return out[:min(cap, n.value)].copy(), int(n.value)
+
+    def probe_clear(self, probe: int):
+        call("bmc_probe_clear", self.handle, probe)
+
 
 def debug_draws(seed: int, ids: np.ndarray, step: int, purpose: int) -> np.ndarray:
     ids = np.ascontiguousarray(ids, dtype=np.uint32)

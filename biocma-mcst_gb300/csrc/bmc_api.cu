@@ -203,6 +203,7 @@ struct bmc_scenario {
   uint32_t* d_map_exit = nullptr;
   // gas phase of a two-phase flow (device arrays in garena)
   void* garena = nullptr;
+  void* probe_arena = nullptr;  // time-event probe buffers (bmc_probe_enable)
   std::vector<double> gvol;
   // steps enqueued by bmc_step_enqueue, collected in order by
   // bmc_step_collect: an event after each step's export and the caller's
@@ -820,6 +821,7 @@ int bmc_scenario_destroy(bmc_scenario* s) {
   if (s->tarena) cudaFree(s->tarena);
   if (s->marena) cudaFree(s->marena);
   if (s->garena) cudaFree(s->garena);
+  if (s->probe_arena) cudaFree(s->probe_arena);
   if (s->h_ctl) cudaFreeHost(s->h_ctl);
   for (auto& q : s->pend)
     if (q.done) cudaEventDestroy(q.done);
@@ -1474,6 +1476,84 @@ int bmc_force_remove_dead(bmc_scenario* s) {
   for (int v = 0; v < nv; ++v) std::memcpy(&st2[(size_t)v * head * fsz], &st[(size_t)v * n * fsz], head * fsz);
   return bmc_set_particles(s, head, st2.data(), pos.data(), status.data(), ah.data(), ad.data(), id.data(),
                            s->h_ctl->next_id);
+}
+
+// ---- time-event probes ---------------------------------------------------------------
+}  // extern "C"
+
+// Reads, changes and writes back the control block between steps.
+template <class Fn>
+static int ctl_update(bmc_scenario* s, Fn fn) {
+  BMC_CUDA(counted_memcpy_async(s->h_ctl, s->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  Control c = *s->h_ctl;
+  fn(c);
+  *s->h_ctl = c;
+  BMC_CUDA(counted_memcpy_async(s->d_ctl, &c, sizeof(Control), cudaMemcpyHostToDevice, s->stream));
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  return BMC_OK;
+}
+
+extern "C" {
+
+int bmc_probe_enable(bmc_scenario* s, uint64_t capacity) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (s->pend_count > 0) return fail(BMC_E_STATE, "steps enqueued by bmc_step_enqueue are not collected yet");
+  if (capacity > (1ull << 32)) return fail(BMC_E_INVALID, "probe capacity above 2^32 values");
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  BMC_CUDA(cudaStreamSynchronize(s->stream));
+  if (s->probe_arena) cudaFree(s->probe_arena);
+  s->probe_arena = nullptr;
+  s->h.probe_buf[0] = s->h.probe_buf[1] = nullptr;
+  s->h.probe_cap = 0;
+  if (capacity > 0) {
+    BMC_CUDA(cudaMalloc(&s->probe_arena, 2 * capacity * sizeof(double)));
+    BMC_CUDA(cudaMemsetAsync(s->probe_arena, 0, 2 * capacity * sizeof(double), s->stream));
+    s->h.probe_buf[0] = static_cast<double*>(s->probe_arena);
+    s->h.probe_buf[1] = s->h.probe_buf[0] + capacity;
+    s->h.probe_cap = capacity;
+  }
+  int rc = ctl_update(s, [](Control& c) { c.probe_n[0] = c.probe_n[1] = 0ull; });
+  if (rc) return rc;
+  s->ctl_fresh = false;
+  return upload_desc(s);
+}
+
+int bmc_probe_read(bmc_scenario* s, int32_t probe, double* out, uint64_t max_values, uint64_t* count) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s || !count) return fail(BMC_E_INVALID, "null argument");
+  if (probe != BMC_PROBE_LEAVING_TIME && probe != BMC_PROBE_DIVISION_TIME) return fail(BMC_E_INVALID, "unknown probe");
+  if (max_values > 0 && !out) return fail(BMC_E_INVALID, "null output");
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  const uint64_t n = s->h_ctl->probe_n[probe];
+  *count = n;
+  const uint64_t stored = std::min<uint64_t>(std::min<uint64_t>(n, s->h.probe_cap), max_values);
+  if (stored > 0) {
+    BMC_CUDA(counted_memcpy_async(out, s->h.probe_buf[probe], stored * sizeof(double), cudaMemcpyDeviceToHost,
+                                  s->stream));
+    BMC_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  return BMC_OK;
+}
+
+int bmc_probe_clear(bmc_scenario* s, int32_t probe) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  if (probe != BMC_PROBE_LEAVING_TIME && probe != BMC_PROBE_DIVISION_TIME) return fail(BMC_E_INVALID, "unknown probe");
+  if (s->pend_count > 0) return fail(BMC_E_STATE, "steps enqueued by bmc_step_enqueue are not collected yet");
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  if (s->h.probe_cap > 0)
+    BMC_CUDA(cudaMemsetAsync(s->h.probe_buf[probe], 0, s->h.probe_cap * sizeof(double), s->stream));
+  int rc = ctl_update(s, [probe](Control& c) { c.probe_n[probe] = 0ull; });
+  if (rc) return rc;
+  s->ctl_fresh = false;
+  return BMC_OK;
 }
 
 // ---- batching ------------------------------------------------------------------

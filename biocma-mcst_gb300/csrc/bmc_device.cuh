@@ -219,7 +219,17 @@ struct Control {
   // relative_time, simulation_times.hpp L12-L29): the sum of the time steps
   // of the iterations so far, in order; feed schedules are evaluated at it
   double t_rel;
+  // time-event probes (ScenDev::probe_buf): events counted so far, per probe
+  // (kProbeLeaving, kProbeDivision), including those a full buffer dropped
+  unsigned long long probe_n[2];
+  // division events counted before this step (written by the plan kernel;
+  // the division records of the step follow it in slot order)
+  unsigned long long plan_probe_base;
 };
+
+// Probes of the reference's Simulation::Probes (probe.hpp L14-L18).
+constexpr int kProbeLeaving = 0;   // ProbeType::LeavingTime: ages(i, 0) at exit
+constexpr int kProbeDivision = 1;  // ProbeType::DivisionTime: ages(i, 1) at a division request
 
 // Scenario descriptor as the kernels see it (one per scenario, device memory).
 struct ScenDev {
@@ -340,7 +350,18 @@ struct ScenDev {
   int32_t gfeed_out[kMaxOutlets];
   double gfeed_flow[kMaxOutlets];
   double gfeed_conc[kMaxOutlets * kMaxSpecies];
+  // Time-event probes (the reference's Simulation::Probes with use_probe,
+  // probe.hpp L38-L146): probe_cap values per probe (0: probes off)
+  double* probe_buf[2];
+  unsigned long long probe_cap;
 };
+
+// Probes::set (probe.hpp L61-L79): the event is counted; its value is kept
+// while the buffer has room.
+__device__ __forceinline__ void probe_set(const ScenDev& S, int k, double v) {
+  const unsigned long long j = atomicAdd(&S.ctl->probe_n[k], 1ull);
+  if (j < S.probe_cap) S.probe_buf[k][j] = v;
+}
 
 // A scenario whose step counter has reached its limit is left untouched.
 __device__ __forceinline__ bool scen_finished(const ScenDev& S, const Control* ctl) {

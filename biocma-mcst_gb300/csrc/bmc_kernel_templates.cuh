@@ -665,6 +665,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
                 if (S.outlet_idx[o] == p) {
                   if (S.outlet_flow[o] != 0.0 && draw_int(r[2]) > S.exit_thr[o]) {
                     stv[k] = kExit;
+                    if (S.probe_cap) probe_set(S, kProbeLeaving, (double)ah[k]);  // before the reset
                     ah[k] = 0.0f;
                     ++my_exit;
                     st_changed = true;
@@ -1108,6 +1109,7 @@ __global__ void __launch_bounds__(THREADS + 32, MINB)
               if (S.outlet_idx[o] == p) {
                 if (S.outlet_flow[o] != 0.0 && draw_int(rd[2]) > S.exit_thr[o]) {
                   stv = kExit;
+                  if (S.probe_cap) probe_set(S, kProbeLeaving, (double)ah);  // before the reset
                   ah = 0.0f;
                   ++my_exit;
                   S.status[gi] = kExit;
@@ -1250,6 +1252,11 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     ctl->plan_step = c_step;
     ctl->plan_compact = (unsigned)compact;
     ctl->plan_gaps = 0ull;
+    // every division request of the step is a division-time event, refused
+    // or not (model_kernel.hpp L245-L251); k_divide records them in slot order
+    const unsigned long long pb = ctl->probe_n[kProbeDivision];
+    ctl->plan_probe_base = pb;
+    if (S.probe_cap) ctl->probe_n[kProbeDivision] = pb + req;
     if (c_next + n_births > 0x100000000ull) ctl->error |= 4u;
     ctl->n_used = after + n_births;
     ctl->inactive = compact ? 0ull : inactive_after;
@@ -1339,6 +1346,11 @@ __global__ void __launch_bounds__(256) k_divide(const ScenDev* __restrict__ sc, 
       for (int k = 0; k < 4; ++k) {
         if (!((bits >> k) & 1u)) continue;
         const unsigned long long slot = first + k;
+        if (S.probe_cap) {
+          // ages(i, 1) of the request, before a division resets it
+          const unsigned long long j = ctl->plan_probe_base + rank;
+          if (j < S.probe_cap) S.probe_buf[kProbeDivision][j] = (double)S.age_d[slot];
+        }
         if (rank < births) {
           F x[NV], y[NV];
 #pragma unroll

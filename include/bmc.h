@@ -335,6 +335,37 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts);
  * force_remove_dead, particles_container.hpp L460-L465). */
 int bmc_force_remove_dead(bmc_scenario* s);
 
+/* ---- time-event probes ---------------------------------------------------- */
+/* The reference's Simulation::Probes (apps/libs/simulation/public/simulation/
+ * probe.hpp L38-L146), which its cycle fills when built with use_probe
+ * (off in its default build): with capacity > 0 every step of the scenario
+ * records, in double,
+ *   BMC_PROBE_LEAVING_TIME: ages(i, 0) of each particle leaving through an
+ *     outlet, before its reset (ProbeType::LeavingTime, move_kernel.hpp
+ *     L629-L635), in the order the device's threads reach the exit, as the
+ *     reference's atomic counter orders them;
+ *   BMC_PROBE_DIVISION_TIME: ages(i, 1) of each particle whose update asks to
+ *     divide, before the division is attempted, refused or not
+ *     (ProbeType::DivisionTime, model_kernel.hpp L245-L251), in slot order
+ *     within a step;
+ * each into its own buffer of `capacity` values on the device.  Events after
+ * a full buffer are counted but not stored (Probes::set), so once a leaving
+ * buffer has filled, which values it kept can differ between runs.
+ * bmc_probe_enable(s, 0) turns them off (the default); enabling empties both
+ * buffers.  Graph runs and batches record too. */
+#define BMC_PROBE_LEAVING_TIME 0
+#define BMC_PROBE_DIVISION_TIME 1
+int bmc_probe_enable(bmc_scenario* s, uint64_t capacity);
+/* Probes::get and need_export: writes the number of events counted since
+ * the probe was last emptied to *count, and copies the stored values
+ * (min(capacity, count) of them, at most max_values) into out.  The buffer
+ * needs exporting once *count >= capacity. */
+int bmc_probe_read(bmc_scenario* s, int32_t probe, double* out, uint64_t max_values, uint64_t* count);
+/* Probes::clear: the probe's count and values back to 0 (the exporter's
+ * save_probes, apps/core/src/post_process.cpp L30-L46, clears after each
+ * write). */
+int bmc_probe_clear(bmc_scenario* s, int32_t probe);
+
 /* ---- flow-map cycle ------------------------------------------------------- */
 /* Several flow-map states of the same mesh (the reference's CMA case with
  * n_different_maps > 1, replayed by its FlowMapTransitionner): each map

@@ -475,18 +475,30 @@ static inline int exit_test(double dt, double flow, double volume, float u) {
  * tested, and on exit the status becomes Exit and age(0) is reset.
  * Returns 1 on exit. */
 static inline int leave_one(const orc_state* s, double dt, float dtf, uint32_t p, uint8_t* status, float* age_h,
-                            float u) {
+                            float u, float* age_at_exit) {
   (void)dtf;
   *age_h = (float)((double)*age_h + dt); /* ages(idx, 0) += d_t, d_t double */
   for (uint32_t o = 0; o < s->n_outlets; ++o) {
     if (s->outlet_index[o] == p) {
       if (s->outlet_flow[o] != 0.0 && exit_test(dt, s->outlet_flow[o], s->outlet_volume[o], u)) {
         *status = ORC_EXIT;
+        if (age_at_exit) *age_at_exit = *age_h; /* the leaving-time probe's value */
         *age_h = 0.0f;
         return 1;
       }
       return 0;
     }
+  }
+  return 0;
+}
+
+/* Probes::set (probe.hpp L61-L79): the event is counted; its value is kept
+ * while the buffer has room (returns 1 then). */
+int orc_probe_set(orc_state* s, int k, double v) {
+  const uint64_t j = s->probe_n[k]++;
+  if (j < s->probe_cap) {
+    s->probe_buf[k][j] = v;
+    return 1;
   }
   return 0;
 }
@@ -536,6 +548,9 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
   }
   uint64_t moves = 0, exits = 0, reqdiv = 0;
   const size_t acc_len = (size_t)s->n_c * ncol;
+  /* leaving times of this step, recorded in slot order after the loop */
+  uint8_t* left = s->probe_cap && do_leave ? (uint8_t*)calloc(n ? n : 1, 1) : NULL;
+  float* left_age = left ? (float*)malloc(sizeof(float) * (n ? n : 1)) : NULL;
   if (n_threads < 1) n_threads = 1;
   uint64_t clamped = 0;
 #ifdef _OPENMP
@@ -586,7 +601,11 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
         moves += (uint64_t)moved;
         s->pos[i] = p;
       }
-      if (do_leave) exits += (uint64_t)leave_one(s, dt, dtf, p, &s->status[i], &s->age_h[i], d[2]);
+      if (do_leave) {
+        const int ex = leave_one(s, dt, dtf, p, &s->status[i], &s->age_h[i], d[2], left ? &left_age[i] : NULL);
+        exits += (uint64_t)ex;
+        if (ex && left) left[i] = 1;
+      }
     }
   }
 #ifndef _OPENMP
@@ -618,6 +637,12 @@ void orc_cycle(orc_state* s, double dt, int n_threads) {
   s->ctb_clamped += clamped;
   free(partial);
   free(contrib_ok);
+  if (left) {
+    for (uint64_t i = 0; i < n; ++i)
+      if (left[i]) (void)orc_probe_set(s, 0, (double)left_age[i]);
+    free(left);
+    free(left_age);
+  }
   free(rates);
   if (pmove != pmove_small) free(pmove);
   s->moves = moves;
@@ -691,6 +716,8 @@ void orc_post_cycle(orc_state* s) {
   for (uint64_t i = 0; i < n; ++i) {
     if (!s->div_flag[i]) continue;
     s->div_flag[i] = 0;
+    /* every request is a division-time event, refused or not */
+    if (s->probe_cap) (void)orc_probe_set(s, 1, (double)s->age_d[i]);
     if (births < room) {
       model_division(s, i, births);
       s->child_pos[births] = s->div_pos[i];
@@ -853,7 +880,7 @@ int32_t orc_pin_leave(uint32_t n_outlets, const uint32_t* index, const double* f
     t.outlet_volume[o] = volume[o];
   }
   if (*status != ORC_IDLE) return 0; /* TagLeave skips particles that are not Idle */
-  return leave_one(&t, dt, (float)dt, pos, status, age_h, u);
+  return leave_one(&t, dt, (float)dt, pos, status, age_h, u, NULL);
 }
 
 int32_t orc_pin_exit_test(double dt, double flow, double volume, float u) { return exit_test(dt, flow, volume, u); }

@@ -196,6 +196,18 @@ typedef struct orc_state {
   double feed_f0[ORC_MAX_OUTLETS];
   double feed_rate[ORC_MAX_OUTLETS];
   double t_rel;
+
+  /* time-event probes (reference Simulation::Probes, apps/libs/simulation/
+   * public/simulation/probe.hpp L38-L146, with use_probe): probe_buf[0]
+   * leaving times (ages(i,0) of a particle leaving through an outlet,
+   * before its reset, move_kernel.hpp L629-L635), probe_buf[1] division
+   * times (ages(i,1) of a particle whose update asks to divide, before the
+   * division is attempted, model_kernel.hpp L245-L251), both in slot order
+   * within a step; probe_n counts every event, a value is stored while its
+   * index is below probe_cap (0: probes off) */
+  uint64_t probe_cap;
+  double* probe_buf[2];
+  uint64_t probe_n[2];
 } orc_state;
 
 void orc_set_outlets(orc_state* s);
@@ -207,6 +219,9 @@ void orc_init_particles(orc_state* s, uint64_t n, uint32_t pos_lo, uint32_t pos_
 double orc_total_mass(const orc_state* s);
 
 void orc_scalar_step(orc_state* s, double dt);
+/* Probes::set (probe.hpp L61-L79): counts the event of probe k and stores
+ * v while the buffer has room; returns 1 if stored. */
+int orc_probe_set(orc_state* s, int k, double v);
 void orc_cycle(orc_state* s, double dt, int n_threads);
 void orc_post_cycle(orc_state* s);
 void orc_step(orc_state* s, double dt, int n_threads);

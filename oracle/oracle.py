@@ -57,6 +57,7 @@ class OrcState(ct.Structure):
         ("gfeed_conc", ct.c_double * (MAXO * 8)),
         ("feed_kind", ct.c_int32 * MAXO), ("feed_f0", ct.c_double * MAXO), ("feed_rate", ct.c_double * MAXO),
         ("t_rel", ct.c_double),
+        ("probe_cap", ct.c_uint64), ("probe_buf", ct.c_void_p * 2), ("probe_n", ct.c_uint64 * 2),
     ]
 
 
@@ -120,6 +121,8 @@ def lib():
             getattr(L, name).restype = ct.c_double
         L.orc_sa_truncnorm.argtypes = [ct.c_float] * 5
         L.orc_sa_truncnorm.restype = ct.c_float
+        L.orc_probe_set.argtypes = [P, ct.c_int, ct.c_double]
+        L.orc_probe_set.restype = ct.c_int
         _lib = L
     return _lib
 
@@ -377,3 +380,24 @@ class Oracle:
         out = np.zeros(self.scen.net.n_c, dtype=np.uint64)
         lib().orc_repartition(ct.byref(self.s), _ptr(out))
         return out
+
+    # -- time-event probes (0: leaving times, 1: division times) ---------------
+    def probe_enable(self, capacity: int):
+        self._probe = [np.zeros(max(capacity, 1)), np.zeros(max(capacity, 1))]
+        self.s.probe_cap = capacity
+        for k in range(2):
+            self.s.probe_buf[k] = _ptr(self._probe[k])
+            self.s.probe_n[k] = 0
+
+    def probe_set(self, probe: int, value: float) -> bool:
+        """Probes::set: counts the event, stores the value while there is room."""
+        return bool(lib().orc_probe_set(ct.byref(self.s), probe, value))
+
+    def probe_read(self, probe: int) -> tuple[np.ndarray, int]:
+        """(stored values, events counted) of one probe."""
+        n = int(self.s.probe_n[probe])
+        return self._probe[probe][:min(n, int(self.s.probe_cap))].copy(), n
+
+    def probe_clear(self, probe: int):
+        self._probe[probe][:] = 0.0
+        self.s.probe_n[probe] = 0
