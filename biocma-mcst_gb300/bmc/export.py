@@ -12,6 +12,8 @@ partial_exporter.cpp L25-L160, host_export_handler.cpp L70-L115):
   records/mtr                   [n_export, n_compartments, n_species]  (two-phase)
   records/number_particle       [n_export, n_compartments]
   records/tallies               [n_export, n_tallies]
+  probes/LeavingTime            [n_leaving]   (with time-event probes on)
+  probes/DivisionTime           [n_division]
 
 plus `initial_parameters/*` and `final_result/*` scalars.  `Records`
 collects the same arrays from a device scenario (read-backs between graph
@@ -23,6 +25,9 @@ from __future__ import annotations
 import numpy as np
 
 TALLIES = ("births", "exits", "moves", "overflow", "n_used", "inactive")
+# probe names of the reference's exporter (map_probe_name, probe.hpp L21-L22),
+# in the order of the library's probe indices
+PROBES = ("LeavingTime", "DivisionTime")
 
 
 class Records:
@@ -62,6 +67,22 @@ class Records:
         self._append("records/number_particle", self.g.repartition().astype(np.uint64))
         st = self.g.stats()
         self._append("records/tallies", np.array([st[k] for k in TALLIES], dtype=np.uint64))
+        self.save_probes()
+
+    def save_probes(self, force: bool = False):
+        """The reference's save_probes (apps/core/src/post_process.cpp
+        L30-L60, called at every export and, forced, at the end of the run):
+        each probe whose buffer is full, or every probe with `force`, has its
+        stored values appended to probes/<name> and is emptied.  Nothing
+        while the scenario's probes are off."""
+        cap = getattr(self.g, "probe_capacity", 0)
+        if not cap:
+            return
+        for k, name in enumerate(PROBES):
+            values, n = self.g.probe_read(k)
+            if n >= cap or force:
+                self.rows.setdefault(f"probes/{name}", []).append(values)
+                self.g.probe_clear(k)
 
     def run(self, n_steps: int, dump_interval: int, t0: float = 0.0):
         """Advance n_steps in graph-replayed runs of dump_interval steps,
@@ -75,6 +96,7 @@ class Records:
             self.g.run(k)
             done += k
             self.record(t0 + done * dt)
+        self.save_probes(force=True)
         st = self.g.stats()
         self.final = {
             "final_result/number_particles": st["n_used"] - st["inactive"],
@@ -83,7 +105,7 @@ class Records:
         return self
 
     def arrays(self) -> dict:
-        out = {k: np.stack(v) for k, v in self.rows.items()}
+        out = {k: (np.concatenate(v) if k.startswith("probes/") else np.stack(v)) for k, v in self.rows.items()}
         out.update({k: np.asarray(v) for k, v in self.initial.items()})
         out.update({k: np.asarray(v) for k, v in self.final.items()})
         return out

@@ -34,6 +34,16 @@ class FakeScenario:
         st["n_used"], st["inactive"] = int(self.o.s.n_used), int(self.o.s.inactive)
         return st
 
+    def probe_enable(self, cap):
+        self.o.probe_enable(cap)
+        self.probe_capacity = cap
+
+    def probe_read(self, k):
+        return self.o.probe_read(k)
+
+    def probe_clear(self, k):
+        self.o.probe_clear(k)
+
 
 def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
     sc = scenarios.small_ring(3000, feeds=True)
@@ -53,6 +63,51 @@ def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
     back = export.load(path)
     for k, v in a.items():
         assert np.array_equal(back[k], v), k
+
+
+def _probe_scenario():
+    sc = scenarios.zero_d(3000, model=scenarios.monod(f64=True, m_div=1.0), outlet=True)
+    sc.feeds[0].flow = 1e-3
+    return sc
+
+
+def test_probes_exported_as_the_reference_exporter(oracle_mod):
+    """A full buffer goes to probes/<name> at the next export and is emptied;
+    the end of the run exports whatever is left (save_probes(force))."""
+    sc = _probe_scenario()
+    small = FakeScenario(oracle_mod, sc)
+    small.probe_enable(300)
+    a = export.Records(small).run(12, dump_interval=3).arrays()
+    big = FakeScenario(oracle_mod, sc)
+    big.probe_enable(1 << 20)
+    b = export.Records(big).run(12, dump_interval=3).arrays()
+    for name in export.PROBES:
+        full = b[f"probes/{name}"]
+        part = a[f"probes/{name}"]
+        assert len(full) > 300 and 0 < len(part) <= len(full)
+    # division times are in slot order: what the small buffers kept is a
+    # sequence of stretches of the complete list
+    div = b["probes/DivisionTime"]
+    assert set(a["probes/DivisionTime"].tolist()) <= set(div.tolist())
+
+
+@pytest.mark.gpu
+def test_gpu_probe_records_match_the_restatement(oracle_mod):
+    from bmc.sim import GpuScenario
+
+    sc = _probe_scenario()
+    g = GpuScenario(sc, capacity=4096)
+    g.probe_enable(1 << 18)
+    a = export.Records(g).run(10, dump_interval=5).arrays()
+    f = FakeScenario(oracle_mod, sc)
+    f.o = oracle_mod.Oracle(sc, phys_capacity=g.cap)
+    f.o.init_particles()
+    f.o.set_weight(g.weight)
+    f.probe_enable(1 << 18)
+    b = export.Records(f).run(10, dump_interval=5).arrays()
+    assert np.array_equal(a["probes/DivisionTime"], b["probes/DivisionTime"])
+    assert np.array_equal(np.sort(a["probes/LeavingTime"]), np.sort(b["probes/LeavingTime"]))
+    assert len(a["probes/DivisionTime"]) > 0 and len(a["probes/LeavingTime"]) > 0
 
 
 @pytest.mark.gpu
