@@ -15,7 +15,13 @@ partial_exporter.cpp L25-L160, host_export_handler.cpp L70-L115):
   probes/LeavingTime            [n_leaving]   (with time-event probes on)
   probes/DivisionTime           [n_division]
 
-plus `initial_parameters/*` and `final_result/*` scalars.  `Records`
+plus `initial_parameters/*` and `final_result/*` (the live particle count,
+event totals, the final liquid and gas fields).  records/tallies holds the
+reference's event counts (MC::EventType order) accumulated since the
+previous export, which clears them (host_export_handler.cpp L118-L122);
+final_result/events/* are totals over the run (the reference reads its
+counters after the last export cleared them, so its values cover only the
+steps after the last export).  `Records`
 collects the same arrays from a device scenario (read-backs between graph
 runs) and writes them under the same names: with h5py to an HDF5 file,
 without it (this image) to a NumPy archive whose keys are the dataset paths.
@@ -24,7 +30,7 @@ from __future__ import annotations
 
 import numpy as np
 
-TALLIES = ("births", "exits", "moves", "overflow", "n_used", "inactive")
+TALLIES = ("NewParticle", "Exit", "Move", "Death", "Overflow", "ChangeWeight")
 # probe names of the reference's exporter (map_probe_name, probe.hpp L21-L22),
 # in the order of the library's probe indices
 PROBES = ("LeavingTime", "DivisionTime")
@@ -47,6 +53,7 @@ class Records:
             "initial_parameters/t_per_flow_map": getattr(sc, "t_per_flowmap", 0.0),
         }
         self.final: dict[str, float] = {}
+        self.totals = dict.fromkeys(TALLIES, 0)
 
     def _append(self, name: str, value):
         self.rows.setdefault(name, []).append(np.asarray(value))
@@ -65,8 +72,10 @@ class Records:
             self._append("records/volume_gas", np.asarray(sc.gas.net.volume, dtype=float))
             self._append("records/mtr", gas["mtr"])
         self._append("records/number_particle", self.g.repartition().astype(np.uint64))
-        st = self.g.stats()
-        self._append("records/tallies", np.array([st[k] for k in TALLIES], dtype=np.uint64))
+        ev = self.g.events(clear=True)
+        self._append("records/tallies", np.array([ev[k] for k in TALLIES], dtype=np.uint64))
+        for k in TALLIES:
+            self.totals[k] += ev[k]
         self.save_probes()
 
     def save_probes(self, force: bool = False):
@@ -98,10 +107,18 @@ class Records:
             self.record(t0 + done * dt)
         self.save_probes(force=True)
         st = self.g.stats()
+        ev = self.g.events(clear=True)  # steps after the last export (none here)
+        tot = {k: self.totals[k] + ev[k] for k in TALLIES}
         self.final = {
             "final_result/number_particles": st["n_used"] - st["inactive"],
-            "final_result/events/total_exit": st["exits"],
+            "final_result/events/move": tot["Move"],
+            "final_result/events/total_division": tot["NewParticle"],
+            "final_result/events/total_death": tot["Death"],
+            "final_result/events/total_exit": tot["Exit"],
+            "final_result/concentration_liquid": self.g.liquid()["C"],
         }
+        if getattr(self.g.scen, "gas", None) is not None:
+            self.final["final_result/concentration_gas"] = self.g.gas()["Cg"]
         return self
 
     def arrays(self) -> dict:

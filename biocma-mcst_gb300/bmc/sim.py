@@ -17,6 +17,9 @@ import numpy as np
 from . import _lib
 from ._lib import Feed, ScenarioDesc, StepStats, call
 
+# the reference's MC::EventType order (events.hpp L17-L26)
+EVENTS = ("NewParticle", "Exit", "Move", "Death", "Overflow", "ChangeWeight")
+
 
 def _p(a: np.ndarray):
     return ct.c_void_p(a.ctypes.data)
@@ -296,6 +299,12 @@ class GpuScenario:
 
     def force_remove_dead(self):
         call("bmc_force_remove_dead", self.handle)
+
+    def events(self, clear: bool = False) -> dict:
+        """Event tallies since the last clear (EVENTS order, include/bmc.h)."""
+        out = np.zeros(len(EVENTS), dtype=np.uint64)
+        call("bmc_read_events", self.handle, _p(out), 1 if clear else 0)
+        return {k: int(v) for k, v in zip(EVENTS, out)}
 
     # time-event probes: 0 leaving times, 1 division times (include/bmc.h)
     def probe_enable(self, capacity: int):

@@ -1496,6 +1496,24 @@ static int ctl_update(bmc_scenario* s, Fn fn) {
 
 extern "C" {
 
+int bmc_read_events(bmc_scenario* s, uint64_t* counts, int32_t clear) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s || !counts) return fail(BMC_E_INVALID, "null argument");
+  if (clear && s->pend_count > 0) return fail(BMC_E_STATE, "steps enqueued by bmc_step_enqueue are not collected yet");
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  for (int k = 0; k < BMC_N_EVENTS; ++k) counts[k] = s->h_ctl->events[k];
+  if (!clear) return BMC_OK;
+  rc = ctl_update(s, [](Control& c) {
+    for (auto& e : c.events) e = 0ull;
+  });
+  if (rc) return rc;
+  s->ctl_fresh = false;
+  return BMC_OK;
+}
+
 int bmc_probe_enable(bmc_scenario* s, uint64_t capacity) {
   if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");

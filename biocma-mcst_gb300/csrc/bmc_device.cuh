@@ -225,6 +225,10 @@ struct Control {
   // division events counted before this step (written by the plan kernel;
   // the division records of the step follow it in slot order)
   unsigned long long plan_probe_base;
+  // event tallies since the host last cleared them (MC::EventContainer,
+  // events.hpp L17-L26): NewParticle (every division request, refused or
+  // not), Exit, Move, Death, Overflow, ChangeWeight; added by the plan kernel
+  unsigned long long events[6];
 };
 
 // Probes of the reference's Simulation::Probes (probe.hpp L14-L18).

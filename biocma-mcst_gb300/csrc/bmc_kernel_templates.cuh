@@ -1257,6 +1257,13 @@ __global__ void __launch_bounds__(1024) k_plan(ScenDev* __restrict__ sc, BatchCt
     const unsigned long long pb = ctl->probe_n[kProbeDivision];
     ctl->plan_probe_base = pb;
     if (S.probe_cap) ctl->probe_n[kProbeDivision] = pb + req;
+    // the cycle's event counts (model_kernel.hpp L253-L259, move_kernel.hpp
+    // L434 and L643): a division request is a NewParticle event whether or
+    // not it finds room
+    ctl->events[0] += req;
+    ctl->events[1] += c_exits;
+    ctl->events[2] += c_moves;
+    ctl->events[4] += req - n_births;
     if (c_next + n_births > 0x100000000ull) ctl->error |= 4u;
     ctl->n_used = after + n_births;
     ctl->inactive = compact ? 0ull : inactive_after;

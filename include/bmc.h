@@ -335,6 +335,27 @@ int bmc_repartition_static(bmc_scenario* s, uint64_t* counts);
  * force_remove_dead, particles_container.hpp L460-L465). */
 int bmc_force_remove_dead(bmc_scenario* s);
 
+/* ---- event tallies ---------------------------------------------------------- */
+/* The reference's MC::EventContainer (apps/libs/mc/public/mc/events.hpp
+ * L17-L26, L149): counts accumulated over every step since the last clear,
+ * inside graph runs and batches too, in the reference's order.  As its
+ * cycle does (model_kernel.hpp L253-L259), every division request counts as
+ * a NewParticle event, refused or not (the refused ones also as Overflow);
+ * Exit and Move as in move_kernel.hpp L643 and L434; Death and ChangeWeight
+ * stay 0 (the cycle never sets them).  The exporter writes them as
+ * records/tallies and clears them at every export (host_export_handler.cpp
+ * L118-L122). */
+#define BMC_EVENT_NEW_PARTICLE 0
+#define BMC_EVENT_EXIT 1
+#define BMC_EVENT_MOVE 2
+#define BMC_EVENT_DEATH 3
+#define BMC_EVENT_OVERFLOW 4
+#define BMC_EVENT_CHANGE_WEIGHT 5
+#define BMC_N_EVENTS 6
+/* Copies the tallies into counts[BMC_N_EVENTS]; clear != 0 then sets them
+ * to 0 (EventContainer::get_span, clear). */
+int bmc_read_events(bmc_scenario* s, uint64_t* counts, int32_t clear);
+
 /* ---- time-event probes ---------------------------------------------------- */
 /* The reference's Simulation::Probes (apps/libs/simulation/public/simulation/
  * probe.hpp L38-L146), which its cycle fills when built with use_probe

@@ -15,10 +15,21 @@ class FakeScenario:
         self.o = oracle_mod.Oracle(sc)
         self.o.init_particles()
         self.last = {}
+        self.ev = dict.fromkeys(export.TALLIES, 0)
 
     def run(self, n):
         for _ in range(n):
             self.last = self.o.step()
+            self.ev["NewParticle"] += int(self.o.s.requested_divisions)
+            self.ev["Exit"] += self.last["exits"]
+            self.ev["Move"] += self.last["moves"]
+            self.ev["Overflow"] += self.last["overflow"]
+
+    def events(self, clear=False):
+        out = dict(self.ev)
+        if clear:
+            self.ev = dict.fromkeys(export.TALLIES, 0)
+        return out
 
     def liquid(self):
         return {"C": self.o.C.copy()}
@@ -56,9 +67,14 @@ def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
     assert a["records/volume_liquid"].shape == (n_exp, sc.net.n_c)
     assert a["records/number_particle"].shape == (n_exp, sc.net.n_c)
     assert a["records/tallies"].shape == (n_exp, len(export.TALLIES))
-    n_used = a["records/tallies"][:, list(export.TALLIES).index("n_used")]
-    inactive = a["records/tallies"][:, list(export.TALLIES).index("inactive")]
-    assert np.array_equal(a["records/number_particle"].sum(axis=1), n_used - inactive)
+    assert np.all(a["records/tallies"][0] == 0)  # nothing before the first step
+    col = {k: a["records/tallies"][:, i] for i, k in enumerate(export.TALLIES)}
+    assert col["Move"].sum() == a["final_result/events/move"] > 0
+    assert col["Exit"].sum() == a["final_result/events/total_exit"] > 0
+    assert col["NewParticle"].sum() == a["final_result/events/total_division"]
+    assert np.all(col["Death"] == 0) and np.all(col["ChangeWeight"] == 0)
+    assert a["records/number_particle"][-1].sum() == a["final_result/number_particles"]
+    assert np.array_equal(a["final_result/concentration_liquid"], a["records/concentration_liquid"][-1])
     path = rec.save(str(tmp_path / "run"))
     back = export.load(path)
     for k, v in a.items():

@@ -1,4 +1,5 @@
-"""Time-event probes on the GPU against the CPU restatement.
+"""Time-event probes and event tallies on the GPU against the CPU
+restatement.
 
 Division times are stored in slot order within a step on both sides, so
 they are compared value for value; leaving times are stored in the order
@@ -117,3 +118,48 @@ def test_probes_are_off_by_default():
     for p in (LEAVING, DIVISION):
         values, n = g.probe_read(p)
         assert n == 0 and len(values) == 0
+
+
+def _oracle_events(o, steps):
+    ev = dict.fromkeys(("NewParticle", "Exit", "Move", "Death", "Overflow", "ChangeWeight"), 0)
+    for _ in range(steps):
+        st = o.step()
+        ev["NewParticle"] += int(o.s.requested_divisions)
+        ev["Exit"] += st["exits"]
+        ev["Move"] += st["moves"]
+        ev["Overflow"] += st["overflow"]
+    return ev
+
+
+def test_event_tallies_accumulate_over_graph_runs(oracle_mod):
+    """MC::EventContainer: counts summed over every step since the last
+    clear, in captured graph runs too; a division request is a NewParticle
+    event whether or not it found room."""
+    sc = scenarios.small_ring(8000, model=scenarios.monod(f64=True, m_div=1.0), feeds=True)
+    g, o = make_pair(oracle_mod, sc, capacity=9216)  # room for a quarter of the first requests
+    g.run(7)
+    want = _oracle_events(o, 7)
+    got = g.events(clear=True)
+    assert got == want
+    assert want["Overflow"] > 0 and want["Move"] > 0 and want["Exit"] > 0
+    assert g.events() == dict.fromkeys(want, 0)
+    g.step()
+    g.run(4)
+    assert g.events() == _oracle_events(o, 5)
+
+
+def test_event_tallies_in_a_batch_equal_alone():
+    from bmc.sim import GpuBatch, GpuScenario
+
+    scens = [_scenario(), scenarios.small_ring(20000, model=scenarios.monod(f64=True, m_div=1.05), feeds=True)]
+    members = [GpuScenario(s, capacity=32768) for s in scens]
+    alone = [GpuScenario(s, capacity=32768) for s in scens]
+    b = GpuBatch(members)
+    b.run(5, 0.1)
+    b.synchronize()
+    for g in alone:
+        g.run(5, 0.1)
+    for gb, ga in zip(members, alone):
+        assert gb.events() == ga.events()
+        assert gb.events()["NewParticle"] > 0
+    b.close()
