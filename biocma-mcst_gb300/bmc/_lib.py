@@ -104,6 +104,7 @@ SIGNATURES = {
     "bmc_repartition_static": [VP, VP],
     "bmc_force_remove_dead": [VP],
     "bmc_read_events": [VP, VP, c_i32],
+    "bmc_read_mass": [VP, c_u64, VP, VP],
     "bmc_probe_enable": [VP, c_u64],
     "bmc_probe_read": [VP, c_i32, VP, c_u64, VP],
     "bmc_probe_clear": [VP, c_i32],

@@ -14,6 +14,8 @@ partial_exporter.cpp L25-L160, host_export_handler.cpp L70-L115):
   records/tallies               [n_export, n_tallies]
   probes/LeavingTime            [n_leaving]   (with time-event probes on)
   probes/DivisionTime           [n_division]
+  biological_model/<k>/<variable>, spatial/<variable>, mass, spatial/mass,
+                     age_hydro, age   (particle dump k, at every export)
 
 plus `initial_parameters/*` and `final_result/*` (the live particle count,
 event totals, the final liquid and gas fields).  records/tallies holds the
@@ -41,8 +43,14 @@ class Records:
     with `liquid()`, `repartition()`, `stats()`, `scen`, and `gas()` for a
     two-phase scenario)."""
 
-    def __init__(self, g):
+    def __init__(self, g, dump_particles: bool = True, export_age: bool = True):
+        """dump_particles and export_age: the reference's dump_particle_state
+        and export_age build flags (both on in its default build)."""
         self.g = g
+        self.dump_particles = dump_particles
+        self.export_age = export_age
+        self.n_dumps = 0
+        self.dumps: dict[str, np.ndarray] = {}
         self.rows: dict[str, list] = {}
         sc = g.scen
         self.initial = {
@@ -77,6 +85,36 @@ class Records:
         for k in TALLIES:
             self.totals[k] += ev[k]
         self.save_probes()
+        if self.dump_particles:
+            self.save_particle_state()
+
+    def save_particle_state(self):
+        """The reference's particle dump (save_particle_state, append_properties,
+        apps/core/src/post_process.cpp L64-L74, L146-L163; get_properties,
+        apps/core/public/core/post_process.hpp L85-L104, L170-L240): after
+        force_remove_dead, under biological_model/<k>/ (k counts the dumps)
+        each exported model variable and the mass (Model::mass, computed on
+        the device) per particle in float64, their sums per compartment under
+        spatial/<name>, and with export_age both ages (age_hydro = ages(i, 0),
+        age = ages(i, 1))."""
+        g = self.g
+        g.force_remove_dead()
+        p = g.particles()
+        mass = np.asarray(g.mass(), dtype=np.float64)
+        m = g.scen.model
+        n_c = g.scen.net.n_c
+        pos = p["pos"].astype(np.int64)
+        base = f"biological_model/{self.n_dumps}/"
+        cols = [(name, p["state"][k].astype(np.float64))
+                for name, k in zip(m.export_names, m.export_index) if name != "mass"]
+        cols.append(("mass", mass))
+        for name, v in cols:
+            self.dumps[base + name] = v
+            self.dumps[base + "spatial/" + name] = np.bincount(pos, weights=v, minlength=n_c)
+        if self.export_age:
+            self.dumps[base + "age_hydro"] = p["age_h"].astype(np.float64)
+            self.dumps[base + "age"] = p["age_d"].astype(np.float64)
+        self.n_dumps += 1
 
     def save_probes(self, force: bool = False):
         """The reference's save_probes (apps/core/src/post_process.cpp
@@ -123,6 +161,7 @@ class Records:
 
     def arrays(self) -> dict:
         out = {k: (np.concatenate(v) if k.startswith("probes/") else np.stack(v)) for k, v in self.rows.items()}
+        out.update(self.dumps)
         out.update({k: np.asarray(v) for k, v in self.initial.items()})
         out.update({k: np.asarray(v) for k, v in self.final.items()})
         return out

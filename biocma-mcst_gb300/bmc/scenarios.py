@@ -38,6 +38,11 @@ class ModelSpec:
     separable: bool = True
     read_vars: int = 2  # state variables the update reads (the others are outputs)
     udf_path: str | None = None  # model library (runtime-loaded model) it comes from
+    # variables of the particle dump (Model::names with get_number, the
+    # reference's partial export) and their state indices; the mass column
+    # is added by the exporter
+    export_names: tuple = ()
+    export_index: tuple = ()
 
     @property
     def itemsize(self) -> int:
@@ -49,7 +54,8 @@ def monod(f64: bool = True, mu_max: float = MU_MAX, ks: float = 0.01, y: float =
     p = np.zeros(16)
     p[:6] = [mu_max, ks, y, m_div, m_lo, m_span]
     # contribution = -(mu / Y) * mass: the basis is the particle mass
-    return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, np.array([4.0 * m_div]))
+    return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, np.array([4.0 * m_div]),
+                     export_names=("cycle_time",), export_index=(1,))
 
 
 def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
@@ -60,7 +66,8 @@ def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
     p = np.zeros(16)
     p[:13] = [qs_max, 0.01, qo_max, 1e-4, y_ox, y_of, y_ac, y_o, y_c, m_div, y_cof, 0.9, 0.2]
     # every contribution is a rate of the compartment times the mass
-    return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, np.array([4.0 * m_div]))
+    return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, np.array([4.0 * m_div]),
+                     export_names=("cycle_time", "mu", "q_s", "q_o2", "q_ac"), export_index=(1, 2, 3, 4, 5))
 
 
 def fixed_length(general: bool = False) -> ModelSpec:
@@ -73,9 +80,11 @@ def fixed_length(general: bool = False) -> ModelSpec:
     p = np.zeros(16)
     if general:
         return ModelSpec("fixed_length_general", MODEL_FIXED_LENGTH_GENERAL, 2, 1, False, p,
-                         np.array([4.0 * phi]), separable=False)
-    # contribution = -phi_s(C) per particle: basis 1
-    return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([1.0]))
+                         np.array([4.0 * phi]), separable=False, export_names=("length",), export_index=(0,))
+    # contribution = -phi_s(C) per particle: basis 1; the dump exports the
+    # length only (get_number, fixed_length.hpp L84-L97)
+    return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([1.0]),
+                     export_names=("length",), export_index=(0,))
 
 
 def simple_acetate() -> ModelSpec:
@@ -90,7 +99,9 @@ def simple_acetate() -> ModelSpec:
     bound = 4.0 * float(a_max) * float(lin) * 2.0
     p = np.zeros(16)
     return ModelSpec("simple_acetate", MODEL_SIMPLE_ACETATE, 9, 2, False, p, np.array([bound, bound]),
-                     separable=False, read_vars=4)
+                     separable=False, read_vars=4,
+                     export_names=("length", "l_max", "a_p", "a_max", "a_e", "a_e_s", "a_e_a", "phi_s", "phi_a"),
+                     export_index=tuple(range(9)))
 
 
 FEED_CONSTANT = 0

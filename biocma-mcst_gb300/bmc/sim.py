@@ -267,6 +267,14 @@ class GpuScenario:
         return st.as_dict()
 
     # -- readback -----------------------------------------------------------------
+    def mass(self) -> np.ndarray:
+        """Model::mass of each used slot, computed on the device."""
+        n = self.stats()["n_used"]
+        out = np.zeros(max(n, 1), dtype=np.float64)
+        got = ct.c_uint64()
+        call("bmc_read_mass", self.handle, max(n, 1), _p(out), ct.byref(got))
+        return out[:got.value]
+
     def particles(self) -> dict:
         n = self.stats()["n_used"]
         m = self.scen.model

@@ -98,5 +98,7 @@ def udf_model(src: str, f64: bool, params=None, value_bound=None, name: str | No
     if params is not None:
         p[: len(params)] = params
     vb = np.asarray(value_bound if value_bound is not None else [1.0], dtype=np.float64)
+    names = tuple(info["names"])
     return ModelSpec(name or os.path.splitext(os.path.basename(src))[0], mid, info["n_var"],
-                     info["n_ctb"], f64, p, vb, separable=info["separable"], udf_path=path)
+                     info["n_ctb"], f64, p, vb, separable=info["separable"], udf_path=path,
+                     export_names=names, export_index=tuple(range(len(names))))

@@ -1352,6 +1352,31 @@ int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* p
   return BMC_OK;
 }
 
+int bmc_read_mass(bmc_scenario* s, uint64_t max_n, double* mass, uint64_t* n_out) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s) return fail(BMC_E_INVALID, "null scenario");
+  DeviceScope on(s->device);
+  BMC_CUDA(on.err);
+  int rc = read_ctl(s, nullptr);
+  if (rc && rc != BMC_E_DEVICE) return rc;
+  const uint64_t n = s->h_ctl->n_used;
+  if (n_out) *n_out = n;
+  if (n > max_n) return fail(BMC_E_CAPACITY, "host buffer smaller than n_used");
+  if (n == 0 || !mass) return BMC_OK;
+  double* d = nullptr;
+  BMC_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), n * sizeof(double), s->stream));
+  s->ks->mass(s->stream, s->d_desc, n, d);
+  g_launches++;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = counted_memcpy_async(mass, d, n * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  const cudaError_t ef = cudaFreeAsync(d, s->stream);
+  if (e == cudaSuccess) e = ef;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  BMC_CUDA(e);
+  return BMC_OK;
+}
+
 int bmc_read_liquid(bmc_scenario* s, double* conc, double* mass, double* sources) {
   if (const int rc_settle = settle_export(s)) return rc_settle;
   if (!s) return fail(BMC_E_INVALID, "null scenario");

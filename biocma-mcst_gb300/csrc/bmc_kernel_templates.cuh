@@ -1476,6 +1476,22 @@ __global__ void __launch_bounds__(256) k_merge(const ScenDev* __restrict__ sc, i
 // ---------------------------------------------------------------------------
 // Set-up and diagnostics.
 
+// Model::mass of every slot [0, n) (the mass column of the reference's
+// particle dump, get_properties, apps/core/public/core/post_process.hpp
+// L96-L98).
+template <class Model, class F>
+__global__ void k_mass(const ScenDev* __restrict__ sc, unsigned long long n, double* __restrict__ out) {
+  const ScenDev& S = *sc;
+  const F* state = reinterpret_cast<const F*>(S.state);
+  for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
+       i += (unsigned long long)gridDim.x * blockDim.x) {
+    F x[Model::n_var];
+#pragma unroll
+    for (int v = 0; v < Model::n_var; ++v) x[v] = state[(size_t)v * S.cap + i];
+    out[i] = Model::mass(x, S.params);
+  }
+}
+
 // InitFunctor (apps/libs/mc/src/unit.cpp L102-L137): model init from the
 // particle's draws, position = lo + floor(u32 * span / 2^32), mass out.
 template <class Model, class F>
@@ -1679,6 +1695,11 @@ int setup_cycle_tma_t(size_t smem, int* blocks_per_sm) {
   return e;
 }
 inline int last_error_t() { return (int)cudaGetLastError(); }
+template <class Model, class F>
+void launch_mass_t(cudaStream_t st, const ScenDev* sc, unsigned long long n, double* out) {
+  const unsigned long long blocks = (n + 255) / 256;
+  k_mass<Model, F><<<(unsigned)(blocks < 4096 ? (blocks ? blocks : 1) : 4096), 256, 0, st>>>(sc, n, out);
+}
 template <class F>
 void launch_move_thr_t(int n_scen, cudaStream_t st, ScenDev* sc) {
   k_move_thr<F><<<dim3(4, n_scen), 256, 0, st>>>(sc);
@@ -1724,6 +1745,7 @@ KernelSet make_set(int model_id) {
   k.merge = &launch_merge_t<Model, F>;
   k.init = &launch_init_t<Model, F>;
   k.last_error = &last_error_t;
+  k.mass = &launch_mass_t<Model, F>;
   return k;
 }
 }  // namespace kset

@@ -16,7 +16,7 @@ namespace bmc {
 // Version of KernelSet's layout and of the meaning of its launch arguments
 // (such as the scatter forms a cycle launcher accepts); a plugin built
 // against another version is refused at load time.
-constexpr int kKernelSetAbi = 10;
+constexpr int kKernelSetAbi = 11;
 // Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
 // whole compartments per block, so a small domain still spreads over many SMs.
 constexpr unsigned kLiquidThreads = 32;
@@ -94,6 +94,8 @@ struct KernelSet {
   CopyLaunch merge;
   InitLaunch init;
   int (*last_error)();  // cudaGetLastError of the module owning the kernels
+  // Model::mass of slots [0, n) into out (device memory)
+  void (*mass)(cudaStream_t, const ScenDev*, unsigned long long n, double* out);
 };
 
 // Built-in sets first, then the sets of loaded plugins (bmc_udf_load).

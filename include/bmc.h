@@ -303,6 +303,10 @@ int bmc_synchronize(bmc_scenario* s);
 
 /* ---- readback ------------------------------------------------------------ */
 int bmc_read_stats(bmc_scenario* s, bmc_step_stats* stats);
+/* Model::mass of each of the n_used slots, computed on the device by the
+ * scenario's model (the mass column of the reference's particle dump,
+ * get_properties, apps/core/public/core/post_process.hpp L96-L98). */
+int bmc_read_mass(bmc_scenario* s, uint64_t max_n, double* mass, uint64_t* n_out);
 /* Host buffers sized for n_used particles (state as [n_var][n_used]). */
 int bmc_read_particles(bmc_scenario* s, uint64_t max_n, void* state, uint32_t* pos,
                        uint8_t* status, float* age_h, float* age_d, uint32_t* id,

@@ -369,6 +369,12 @@ double orc_total_mass(const orc_state* s) {
   return m;
 }
 
+/* Model::mass of every used slot (the mass column of the reference's
+ * particle dump, apps/core/public/core/post_process.hpp L96-L98). */
+void orc_particle_mass(const orc_state* s, double* out) {
+  for (uint64_t i = 0; i < s->n_used; ++i) out[i] = model_mass(s, i);
+}
+
 /* ------------------------------------------------------------------------ */
 /* Move: apps/libs/simulation/public/simulation/kernels/move_kernel.hpp
  * L62-L103.  First k with u <= CDF(c, k) over the K slots; the search is the

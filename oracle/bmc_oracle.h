@@ -222,6 +222,8 @@ void orc_scalar_step(orc_state* s, double dt);
 /* Probes::set (probe.hpp L61-L79): counts the event of probe k and stores
  * v while the buffer has room; returns 1 if stored. */
 int orc_probe_set(orc_state* s, int k, double v);
+/* Model::mass of every used slot into out[n_used]. */
+void orc_particle_mass(const orc_state* s, double* out);
 void orc_cycle(orc_state* s, double dt, int n_threads);
 void orc_post_cycle(orc_state* s);
 void orc_step(orc_state* s, double dt, int n_threads);

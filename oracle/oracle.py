@@ -121,6 +121,7 @@ def lib():
             getattr(L, name).restype = ct.c_double
         L.orc_sa_truncnorm.argtypes = [ct.c_float] * 5
         L.orc_sa_truncnorm.restype = ct.c_float
+        L.orc_particle_mass.argtypes = [P, ct.c_void_p]
         L.orc_probe_set.argtypes = [P, ct.c_int, ct.c_double]
         L.orc_probe_set.restype = ct.c_int
         _lib = L
@@ -380,6 +381,18 @@ class Oracle:
         out = np.zeros(self.scen.net.n_c, dtype=np.uint64)
         lib().orc_repartition(ct.byref(self.s), _ptr(out))
         return out
+
+    def mass(self) -> np.ndarray:
+        """Model::mass of every used slot."""
+        out = np.zeros(max(self.n_used, 1))
+        lib().orc_particle_mass(ct.byref(self.s), _ptr(out))
+        return out[:self.n_used]
+
+    def force_remove_dead(self):
+        """Every non-Idle particle removed (gap filling in slot order)."""
+        inactive = int(np.count_nonzero(self.status[:self.n_used] != 0))
+        self.s.inactive = inactive
+        lib().orc_remove_inactive(ct.byref(self.s), inactive)
 
     # -- time-event probes (0: leaving times, 1: division times) ---------------
     def probe_enable(self, capacity: int):

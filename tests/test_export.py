@@ -31,6 +31,15 @@ class FakeScenario:
             self.ev = dict.fromkeys(export.TALLIES, 0)
         return out
 
+    def force_remove_dead(self):
+        self.o.force_remove_dead()
+
+    def particles(self):
+        return self.o.particles()
+
+    def mass(self):
+        return self.o.mass()
+
     def liquid(self):
         return {"C": self.o.C.copy()}
 
@@ -79,6 +88,47 @@ def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
     back = export.load(path)
     for k, v in a.items():
         assert np.array_equal(back[k], v), k
+
+
+def test_particle_dumps_in_the_reference_layout(oracle_mod):
+    """biological_model/<k>/ after every export: each exported variable and
+    the mass per live particle, their sums per compartment, both ages."""
+    sc = scenarios.small_ring(3000, feeds=True, model=scenarios.overflow(f64=True))
+    f = FakeScenario(oracle_mod, sc)
+    a = export.Records(f).run(6, dump_interval=3).arrays()
+    for k in range(3):
+        base = f"biological_model/{k}/"
+        n = len(a[base + "mass"])
+        assert n == a["records/number_particle"][k].sum()
+        for name in ("cycle_time", "mu", "q_s", "q_o2", "q_ac", "mass"):
+            assert a[base + name].shape == (n,) and a[base + name].dtype == np.float64
+            assert a[base + "spatial/" + name].shape == (sc.net.n_c,)
+            assert np.isclose(a[base + "spatial/" + name].sum(), a[base + name].sum())
+        assert a[base + "age_hydro"].shape == (n,) and a[base + "age"].shape == (n,)
+    # the overflow model's mass is its first state variable
+    assert np.array_equal(a["biological_model/2/mass"], f.o.particles()["state"][0])
+    plain = export.Records(FakeScenario(oracle_mod, sc), dump_particles=False).run(6, dump_interval=3).arrays()
+    assert not any(k.startswith("biological_model/") for k in plain)
+
+
+@pytest.mark.gpu
+def test_gpu_particle_dumps_match_the_restatement(oracle_mod):
+    from bmc.sim import GpuScenario
+
+    for model in (scenarios.overflow(f64=True), scenarios.fixed_length()):
+        sc = scenarios.small_ring(4000, feeds=True, model=model)
+        sc.feeds[0].flow = 2e-3  # exits: the dumps remove them first
+        g = GpuScenario(sc)
+        a = export.Records(g).run(8, dump_interval=4).arrays()
+        f = FakeScenario(oracle_mod, sc)
+        f.o = oracle_mod.Oracle(sc, phys_capacity=g.cap)
+        f.o.init_particles()
+        f.o.set_weight(g.weight)
+        b = export.Records(f).run(8, dump_interval=4).arrays()
+        keys = [k for k in a if k.startswith("biological_model/")]
+        assert keys and sorted(keys) == sorted(k for k in b if k.startswith("biological_model/"))
+        for k in keys:
+            assert np.array_equal(a[k].view(np.uint64), b[k].view(np.uint64)), (model.name, k)
 
 
 def _probe_scenario():
