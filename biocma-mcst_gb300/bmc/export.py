@@ -53,12 +53,22 @@ class Records:
         self.dumps: dict[str, np.ndarray] = {}
         self.rows: dict[str, list] = {}
         sc = g.scen
+        # MainExporter::write_initial and its constructor (main_exporter.cpp
+        # L17-L50); final_time is set by run(); one host thread drives the
+        # device, one process
+        names = tuple(sc.model.species) or tuple(f"species_{k}" for k in range(sc.n_species))
         self.initial = {
-            "initial_parameters/number_compartment": sc.net.n_c,
-            "initial_parameters/delta_time": sc.dt,
             "initial_parameters/number_particles": sc.n_particles,
+            "initial_parameters/initial_weight": float(g.weight) if getattr(g, "weight", None) else 0.0,
+            "initial_parameters/initial_biomass_concentration": sc.x0,
+            "initial_parameters/number_compartment": sc.net.n_c,
+            "initial_parameters/final_time": 0.0,
+            "initial_parameters/delta_time": sc.dt,
             "initial_parameters/n_map": max(1, len(getattr(sc, "flowmaps", []) or [])),
             "initial_parameters/t_per_flow_map": getattr(sc, "t_per_flowmap", 0.0),
+            "misc/species_names": np.array([n.encode() for n in names[:sc.n_species]]),
+            "misc/n_node_thread": 1,
+            "misc/n_rank": 1,
         }
         self.final: dict[str, float] = {}
         self.totals = dict.fromkeys(TALLIES, 0)
@@ -136,6 +146,7 @@ class Records:
         recording the first state and after every run (the reference records
         the first and the last state as well, main_exporter.cpp L58)."""
         dt = self.g.scen.dt
+        self.initial["initial_parameters/final_time"] = t0 + n_steps * dt
         self.record(t0)
         done = 0
         while done < n_steps:

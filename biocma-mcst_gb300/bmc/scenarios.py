@@ -43,6 +43,7 @@ class ModelSpec:
     # is added by the exporter
     export_names: tuple = ()
     export_index: tuple = ()
+    species: tuple = ()  # liquid scalar names (the exporter's misc/species_names)
 
     @property
     def itemsize(self) -> int:
@@ -55,7 +56,7 @@ def monod(f64: bool = True, mu_max: float = MU_MAX, ks: float = 0.01, y: float =
     p[:6] = [mu_max, ks, y, m_div, m_lo, m_span]
     # contribution = -(mu / Y) * mass: the basis is the particle mass
     return ModelSpec("monod", MODEL_MONOD, 2, 1, f64, p, np.array([4.0 * m_div]),
-                     export_names=("cycle_time",), export_index=(1,))
+                     export_names=("cycle_time",), export_index=(1,), species=("glucose",))
 
 
 def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
@@ -67,7 +68,8 @@ def overflow(f64: bool = True, mu_max: float = MU_MAX) -> ModelSpec:
     p[:13] = [qs_max, 0.01, qo_max, 1e-4, y_ox, y_of, y_ac, y_o, y_c, m_div, y_cof, 0.9, 0.2]
     # every contribution is a rate of the compartment times the mass
     return ModelSpec("overflow", MODEL_OVERFLOW, 6, 4, f64, p, np.array([4.0 * m_div]),
-                     export_names=("cycle_time", "mu", "q_s", "q_o2", "q_ac"), export_index=(1, 2, 3, 4, 5))
+                     export_names=("cycle_time", "mu", "q_s", "q_o2", "q_ac"), export_index=(1, 2, 3, 4, 5),
+                     species=("glucose", "O2", "acetate", "CO2"))
 
 
 def fixed_length(general: bool = False) -> ModelSpec:
@@ -80,11 +82,12 @@ def fixed_length(general: bool = False) -> ModelSpec:
     p = np.zeros(16)
     if general:
         return ModelSpec("fixed_length_general", MODEL_FIXED_LENGTH_GENERAL, 2, 1, False, p,
-                         np.array([4.0 * phi]), separable=False, export_names=("length",), export_index=(0,))
+                         np.array([4.0 * phi]), separable=False, export_names=("length",), export_index=(0,),
+                         species=("glucose",))
     # contribution = -phi_s(C) per particle: basis 1; the dump exports the
     # length only (get_number, fixed_length.hpp L84-L97)
     return ModelSpec("fixed_length", MODEL_FIXED_LENGTH, 2, 1, False, p, np.array([1.0]),
-                     export_names=("length",), export_index=(0,))
+                     export_names=("length",), export_index=(0,), species=("glucose",))
 
 
 def simple_acetate() -> ModelSpec:
@@ -101,7 +104,7 @@ def simple_acetate() -> ModelSpec:
     return ModelSpec("simple_acetate", MODEL_SIMPLE_ACETATE, 9, 2, False, p, np.array([bound, bound]),
                      separable=False, read_vars=4,
                      export_names=("length", "l_max", "a_p", "a_max", "a_e", "a_e_s", "a_e_a", "phi_s", "phi_a"),
-                     export_index=tuple(range(9)))
+                     export_index=tuple(range(9)), species=("glucose", "acetate"))
 
 
 FEED_CONSTANT = 0

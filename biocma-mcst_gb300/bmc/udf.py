@@ -101,4 +101,5 @@ def udf_model(src: str, f64: bool, params=None, value_bound=None, name: str | No
     names = tuple(info["names"])
     return ModelSpec(name or os.path.splitext(os.path.basename(src))[0], mid, info["n_var"],
                      info["n_ctb"], f64, p, vb, separable=info["separable"], udf_path=path,
-                     export_names=names, export_index=tuple(range(len(names))))
+                     export_names=names, export_index=tuple(range(len(names))),
+                     species=tuple(info["species"]))

@@ -40,6 +40,10 @@ class FakeScenario:
     def mass(self):
         return self.o.mass()
 
+    @property
+    def weight(self):
+        return float(self.o.s.weight)
+
     def liquid(self):
         return {"C": self.o.C.copy()}
 
@@ -84,6 +88,9 @@ def test_layout_and_save_roundtrip(oracle_mod, tmp_path):
     assert np.all(col["Death"] == 0) and np.all(col["ChangeWeight"] == 0)
     assert a["records/number_particle"][-1].sum() == a["final_result/number_particles"]
     assert np.array_equal(a["final_result/concentration_liquid"], a["records/concentration_liquid"][-1])
+    assert a["initial_parameters/final_time"] == pytest.approx(10 * sc.dt)
+    assert a["initial_parameters/initial_weight"] > 0.0
+    assert a["misc/species_names"].tolist() == [b"glucose"]
     path = rec.save(str(tmp_path / "run"))
     back = export.load(path)
     for k, v in a.items():
