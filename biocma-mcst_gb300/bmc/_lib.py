@@ -136,6 +136,7 @@ SIGNATURES = {
     "bmc_cma_derive": [c_u32, c_u64, VP, VP, VP, VP, c_u32, VP, VP, VP],
     "bmc_cma_transition": [c_u32, c_u64, VP, VP, VP, VP, c_u64, VP, VP, VP],
     "bmc_cma_time_step": [c_dbl, c_u32, c_u32, VP, VP, VP],
+    "bmc_mtr_turbulence_kla": [c_u32, VP, VP, VP, c_dbl, VP],
     "bmc_cma_read_field": [ct.c_char_p, c_u64, VP, VP],
     "bmc_cma_read_case": [ct.c_char_p, VP, VP, VP],
     "bmc_cma_case_entry": [ct.c_char_p, ct.c_uint32, VP, VP, c_u64],

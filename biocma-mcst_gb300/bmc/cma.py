@@ -69,6 +69,21 @@ def time_step(volumes, out_flows, user_dt: float = 0.0) -> float:
     return dt.value
 
 
+def turbulence_kla(energy_dissipation, liquid_volume, gas_volume, bubble_diameter: float = 5e-3) -> np.ndarray:
+    """kla (1/s) of O2 per compartment under the reference's FlowmapTurbulence
+    mass-transfer model (from the case's turbulent energy dissipation and the
+    gas fraction; include/bmc.h bmc_mtr_turbulence_kla): the O2 column of a
+    two-phase scenario's kla (scenarios.with_gas(kla=...))."""
+    eps = np.ascontiguousarray(energy_dissipation, dtype=np.float64)
+    vl = np.ascontiguousarray(liquid_volume, dtype=np.float64)
+    vg = np.ascontiguousarray(gas_volume, dtype=np.float64)
+    if not (eps.shape == vl.shape == vg.shape) or eps.ndim != 1:
+        raise ValueError("one value per compartment in each array")
+    out = np.zeros(len(eps))
+    call("bmc_mtr_turbulence_kla", len(eps), _p(eps), _p(vl), _p(vg), float(bubble_diameter), _p(out))
+    return out
+
+
 def read_field(path: str) -> np.ndarray:
     """Values of a case field file (uint32 count + float64 values)."""
     n = ct.c_uint64()

@@ -211,6 +211,41 @@ int bmc_cma_time_step(double user_dt, uint32_t n_maps, uint32_t n_c, const doubl
   return BMC_OK;
 }
 
+// Kinematic viscosity of water (m^2/s) at temp degrees Celsius in (0, 370):
+// the sixth-degree fit (in mm^2/s) the reference takes from the Engineering
+// ToolBox water-viscosity table (c_kinematic_viscosity, apps/libs/simulation/
+// src/hydro/impl_mtr.cpp L56-L84), evaluated by Horner's rule and rounded to
+// 1e-10 m^2/s as the reference rounds it.
+static double water_kinematic_viscosity(double temp) {
+  static const double lo[7] = {1.79194000343777, -0.0607310297913931, 0.00144686943485654, -0.0000234079044336466,
+                               0.00000023336659710795, -0.00000000126441088087, 0.00000000000282244333};
+  static const double hi[7] = {1.08486933174497,         -0.0166081298727911,       0.000136367622445752,
+                               -0.00000064995487357883,  0.00000000181964246491, -0.00000000000277495333,
+                               0.00000000000000178038};
+  const double* c = temp < 85.0 ? lo : hi;
+  double p = c[6];
+  for (int k = 5; k >= 0; --k) p = p * temp + c[k];
+  return std::round(p * 0.000001 * 10000000000.0) / 10000000000.0;
+}
+
+int bmc_mtr_turbulence_kla(uint32_t n_c, const double* energy_dissipation, const double* liquid_volume,
+                           const double* gas_volume, double bubble_diameter, double* kla) {
+  if (!energy_dissipation || !liquid_volume || !gas_volume || !kla) return bmc::api_fail(BMC_E_INVALID, "null argument");
+  if (!(bubble_diameter > 0.0)) return bmc::api_fail(BMC_E_INVALID, "bubble diameter must be positive");
+  const double nu = water_kinematic_viscosity(20.0);  // the reference's temperature
+  const double schmidt = nu / 1e-9;                   // and oxygen diffusivity, m^2/s
+  for (uint32_t j = 0; j < n_c; ++j) {
+    const double vl = liquid_volume[j], vg = gas_volume[j], eps = energy_dissipation[j];
+    if (!(vl > 0.0) || !(vg >= 0.0) || !(eps >= 0.0))
+      return bmc::api_fail(BMC_E_INVALID, "volumes must be positive (gas: non-negative), dissipation non-negative");
+    const double alpha = vg / (vl + vg);
+    const double kl = 0.3 * std::pow(eps * nu, 0.25) * std::pow(schmidt, -0.5);
+    const double area = 6. * alpha / (bubble_diameter * (1 - alpha));
+    kla[j] = kl * area;
+  }
+  return BMC_OK;
+}
+
 int bmc_cma_read_field(const char* path, uint64_t cap, double* values, uint64_t* n) {
   if (!path || !n) return bmc::api_fail(BMC_E_INVALID, "null argument");
   std::vector<unsigned char> buf;

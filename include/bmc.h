@@ -439,6 +439,22 @@ int bmc_cma_transition(uint32_t n_c, uint64_t nnz, const uint64_t* rows, const u
                        const double* flows, uint64_t* t_nnz, uint64_t cap, uint64_t* t_rows, uint64_t* t_cols,
                        double* t_values);
 
+/* kla (1/s) of the transferred species (O2) per compartment under the
+ * reference's FlowmapTurbulence mass-transfer model
+ * (MassTransfer::Impl::flowmap_gas_liquid_mass_transfer,
+ * apps/libs/simulation/src/hydro/impl_mtr.cpp L100-L145, computed there at
+ * every hydro-state update, simulation.cpp L132-L138):
+ *   kla_j = 0.3 (eps_j nu)^(1/4) Sc^(-1/2) * 6 alpha_j / (db (1 - alpha_j)),
+ * alpha_j = Vg_j / (Vl_j + Vg_j) the gas fraction, nu the kinematic
+ * viscosity of water at 20 C (1.0023e-6 m^2/s from the reference's fit),
+ * Sc = nu / 1e-9 (oxygen diffusivity, m^2/s), eps the turbulent energy
+ * dissipation of the case (W/kg), db the bubble diameter (the reference's
+ * MassTransferModel sets 5e-3 m).  The result is the O2 column of the kla
+ * of bmc_gas_set (the model leaves the other species at 0; its Henry
+ * constant for O2 is 3.181e-2).  Host only. */
+int bmc_mtr_turbulence_kla(uint32_t n_c, const double* energy_dissipation, const double* liquid_volume,
+                           const double* gas_volume, double bubble_diameter, double* kla);
+
 /* Time step of a run (get_time_step, apps/core/src/global_initaliser.cpp
  * L51-L86, with CmaUtils::get_min_residence_time,
  * apps/libs/cma_utils/src/utils.cpp L47-L73): user_dt when > 0, else

@@ -75,3 +75,57 @@ def test_gpu_two_phase_matches_oracle(oracle_mod, f64):
     o.run(10)
     assert_same_liquid(g, o, "run")
     assert same_bits(g.gas()["Cg"], o.Cg)
+
+
+def test_turbulence_kla_as_the_reference_correlation():
+    """FlowmapTurbulence (impl_mtr.cpp L100-L145), evaluated independently:
+    water at 20 C (1.0023e-6 m^2/s after the reference's rounding), oxygen
+    diffusivity 1e-9 m^2/s, bubbles of 5 mm."""
+    from bmc import cma
+
+    rng = np.random.default_rng(4)
+    eps = rng.uniform(0.0, 2.0, 50)
+    vl = rng.uniform(0.5e-3, 2e-3, 50)
+    vg = vl * rng.uniform(0.0, 0.3, 50)
+    got = cma.turbulence_kla(eps, vl, vg)
+    nu = 1.0023e-6
+    alpha = vg / (vl + vg)
+    want = 0.3 * (eps * nu) ** 0.25 * (nu / 1e-9) ** -0.5 * (6.0 * alpha / (5e-3 * (1 - alpha)))
+    assert np.allclose(got, want, rtol=1e-14, atol=0.0)
+    assert got[vg == 0.0].size == 0 or np.all(got[vg == 0.0] == 0.0)
+    # no gas, no interface; no turbulence, no transfer
+    assert cma.turbulence_kla(np.ones(1), np.ones(1), np.zeros(1))[0] == 0.0
+    assert cma.turbulence_kla(np.zeros(1), np.ones(1), np.ones(1))[0] == 0.0
+
+
+@pytest.mark.parametrize("bad", [dict(vl=0.0), dict(vg=-1.0), dict(eps=-1.0), dict(db=0.0)])
+def test_turbulence_kla_refuses_bad_inputs(bad):
+    from bmc import _lib, cma
+
+    args = dict(eps=1.0, vl=1e-3, vg=1e-4, db=5e-3)
+    args.update(bad)
+    with pytest.raises(_lib.BmcError):
+        cma.turbulence_kla(np.array([args["eps"]]), np.array([args["vl"]]), np.array([args["vg"]]), args["db"])
+
+
+@pytest.mark.gpu
+def test_gpu_two_phase_with_turbulence_kla_matches_oracle(oracle_mod):
+    """The O2 transfer of a two-phase lattice with kla from a turbulence
+    field (FlowmapTurbulence): device and restatement step for step."""
+    from bmc import cma
+    from test_gpu_parity import assert_same_liquid, assert_same_stats, make_pair, same_bits
+
+    sc = two_phase(n_particles=20000)
+    eps = np.random.default_rng(8).lognormal(-1.0, 0.7, sc.net.n_c)
+    kla = cma.turbulence_kla(eps, sc.net.volume, sc.gas.net.volume)
+    sc.gas.kla[:, 1] = kla
+    sc.gas.henry[:] = 0.0
+    sc.gas.henry[1] = 3.181e-2
+    g, o = make_pair(oracle_mod, sc)
+    for k in range(8):
+        assert_same_stats(g.step(), o.step(), f"step {k}")
+        assert_same_liquid(g, o, f"step {k}")
+        gg = g.gas()
+        for key, ref in (("Cg", o.Cg), ("mtr", o.mtr)):
+            assert same_bits(gg[key], ref), f"step {k}: {key}"
+    assert np.any(g.gas()["mtr"][:, 1] != 0.0)
