@@ -89,8 +89,8 @@ template <class Model, class F>
 __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__ sc, BatchCtl* bctl, int do_scalar) {
   const ScenDev& S = sc[blockIdx.y];
   Control* ctl = S.ctl;
+  static_assert(kLiquidThreads == 32, "the mass-balance sums below reduce within one warp");
   __shared__ double cs[kLiquidThreads];
-  __shared__ double red[2][kMaxSpecies];
   if (blockIdx.x == 0 && blockIdx.y == 0) {
     // live tiles of every scenario (ceil(n_used / 1024), none once finished)
     // and their prefix: the cycle hands out only tiles that hold particles
@@ -159,8 +159,7 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
   const unsigned parity = ctl->step & 1u;
   const double* __restrict__ Cold = S.C + parity * ne;
   double* __restrict__ Cnew = S.C + (parity ^ 1u) * ne;
-  if (t < 2 * kMaxSpecies) red[t / kMaxSpecies][t % kMaxSpecies] = 0.0;
-  __syncthreads();
+  double mb_new = 0.0, mb_exp = 0.0;  // this thread's mass-balance terms
   if (active) {
     const size_t e = (size_t)j * nsp + sp;
     double cn;
@@ -224,9 +223,9 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
       // two-phase: tiny negative liquid concentrations are cleared
       // (ScalarSimulation::clearNegs, implScalar.cpp L266-L293)
       if (S.gas && cn < 0.0 && fabs(cn) < kClearNegTol) cn = 0.0;
-      // mass-balance sums (diagnostic): new mass, expected mass
-      atomicAdd(&red[0][sp], mnew);
-      atomicAdd(&red[1][sp], mold + dt * (srcv + mt - cj * sinkj));
+      // mass-balance terms (diagnostic): new mass, expected mass
+      mb_new = mnew;
+      mb_exp = mold + dt * (srcv + mt - cj * sinkj);
     }
     Cnew[e] = cn;
     if (!do_scalar && S.gas) S.Cg[(parity ^ 1u) * ne + e] = S.Cg[parity * ne + e];
@@ -240,9 +239,23 @@ __global__ void __launch_bounds__(kLiquidThreads) k_liquid(ScenDev* __restrict__
 #pragma unroll
     for (int k = 0; k < Model::n_rates; ++k) rec[rate_slot<Model>(k)] = r[k];
   }
-  if (do_scalar && t < nsp) {
-    atomicAdd(&ctl->mb_new[t], red[0][t]);
-    atomicAdd(&ctl->mb_exp[t], red[1][t]);
+  if (do_scalar) {
+    // per-species sums over the warp: lanes of one species lie nsp apart,
+    // so a tree over offsets nsp, 2 nsp, 4 nsp, ... leaves species l's sum
+    // in lane l (a diagnostic: its summation order is free, as the atomics
+    // that add the blocks make it anyway)
+    for (unsigned off = nsp; off < 32u; off <<= 1) {
+      const double a = __shfl_down_sync(0xffffffffu, mb_new, off);
+      const double b = __shfl_down_sync(0xffffffffu, mb_exp, off);
+      if (t + off < 32u) {
+        mb_new += a;
+        mb_exp += b;
+      }
+    }
+    if (t < nsp) {
+      atomicAdd(&ctl->mb_new[t], mb_new);
+      atomicAdd(&ctl->mb_exp[t], mb_exp);
+    }
   }
 }
 
