@@ -106,6 +106,7 @@ SIGNATURES = {
     "bmc_read_events": [VP, VP, c_i32],
     "bmc_read_mass": [VP, c_u64, VP, VP],
     "bmc_probe_enable": [VP, c_u64],
+    "bmc_flowmap_add_gas": [VP, c_u32, VP, c_u64, VP, VP, VP, VP],
     "bmc_probe_read": [VP, c_i32, VP, c_u64, VP],
     "bmc_probe_clear": [VP, c_i32],
     "bmc_batch_create": [VP, c_u32, VP],

@@ -138,6 +138,10 @@ class GasPhase:
     kla: np.ndarray
     c0: np.ndarray
     feeds: list = field(default_factory=list)
+    # gas state of each flow map of the scenario (same order; empty: the gas
+    # domain stays fixed while the maps cycle) and its kla (empty: `kla`)
+    flowmaps: list = field(default_factory=list)
+    kla_maps: list = field(default_factory=list)
 
 
 @dataclass

@@ -86,6 +86,9 @@ class GpuScenario:
             self.set_gas(scen.gas)
         for fm in scen.flowmaps:
             self.add_flowmap(fm)
+        if scen.gas is not None:
+            for k, gnet in enumerate(scen.gas.flowmaps):
+                self.add_flowmap_gas(k, gnet, scen.gas.kla_maps[k] if scen.gas.kla_maps else None)
         if scen.flowmaps:
             call("bmc_flowmap_period", self.handle, scen.t_per_flowmap)
         self.weight = None
@@ -162,6 +165,16 @@ class GpuScenario:
         cdf = np.ascontiguousarray(net.cdf, dtype=np.float64)
         r, c, v = transition_coo(net)
         call("bmc_flowmap_add", self.handle, _p(vol), _p(nbr), _p(outf), _p(cdf), len(v), _p(r), _p(c), _p(v))
+
+    def add_flowmap_gas(self, map_index: int, gnet, kla=None):
+        """Gas state of flow map `map_index` (bmc_flowmap_add_gas): gas
+        volumes and transition of `gnet`, kla [n_c, n_s] (None: the gas
+        phase's)."""
+        vol = np.ascontiguousarray(gnet.volume, dtype=np.float64)
+        r, c, v = transition_coo(gnet)
+        k = None if kla is None else np.ascontiguousarray(kla, dtype=np.float64)
+        call("bmc_flowmap_add_gas", self.handle, map_index, _p(vol), len(v), _p(r), _p(c), _p(v),
+             None if k is None else _p(k))
 
     def set_shape(self, threads: int = 0, ppt: int = 0, blocks_per_sm: int = 0):
         call("bmc_set_shape", self.handle, threads, ppt, blocks_per_sm)

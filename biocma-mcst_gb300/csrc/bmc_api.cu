@@ -196,6 +196,10 @@ struct bmc_scenario {
     std::vector<double> vol, vinv, outf, diag;
     std::vector<uint32_t> ptr, idx;
     std::vector<double> val;
+    // gas state (bmc_flowmap_add_gas): inverse volumes, transition, kla
+    bool has_gas = false;
+    std::vector<double> gvinv, gdiag, gval, kla;
+    std::vector<uint32_t> gptr, gidx;
   };
   std::vector<FlowMap> maps;
   double t_per_map = 0.0;
@@ -205,6 +209,13 @@ struct bmc_scenario {
   void* garena = nullptr;
   void* probe_arena = nullptr;  // time-event probe buffers (bmc_probe_enable)
   std::vector<double> gvol;
+  // the gas domain given to bmc_gas_set (device copies in garena), put back
+  // when the flow maps stop switching the gas
+  std::vector<double> g_vinv, g_diag, g_val, g_kla;
+  std::vector<uint32_t> g_ptr, g_idx;
+  uint32_t* g_cur_ptr = nullptr;  // garena's transition buffers
+  uint32_t* g_cur_idx = nullptr;
+  double* g_cur_flow = nullptr;
   // steps enqueued by bmc_step_enqueue, collected in order by
   // bmc_step_collect: an event after each step's export and the caller's
   // buffers; pending entry k exports into slot k of h_export
@@ -1804,6 +1815,10 @@ int bmc_batch_synchronize(bmc_batch* b) {
 // clearNegs), gas feeds (simulation.model.cpp L112-L119) and the FixedKla
 // transfer (hydro/impl_mtr.cpp L150-L166).
 
+namespace {
+int upload_maps(bmc_scenario* s);  // flow maps to the device (below)
+}  // namespace
+
 extern "C" {
 
 int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const uint64_t* rows, const uint64_t* cols,
@@ -1860,7 +1875,22 @@ int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const u
   for (int k = 0; k < bmc::kMaxSpecies; ++k) h.henry[k] = k < (int)h.n_s ? henry[k] : 0.0;
   h.gas = 1;
   s->gvol = gv;
-  int rc = upload_desc(s);
+  s->g_vinv = gvinv;
+  s->g_diag = diag;
+  s->g_ptr = ptr;
+  s->g_idx = idx;
+  s->g_val = val;
+  s->g_kla.assign(kla, kla + ne);
+  s->g_cur_ptr = p_ptr;
+  s->g_cur_idx = p_idx;
+  s->g_cur_flow = p_flow;
+  // gas states of the flow maps belonged to the previous gas domain
+  bool had = false;
+  for (auto& m : s->maps) {
+    had = had || m.has_gas;
+    m.has_gas = false;
+  }
+  int rc = had ? upload_maps(s) : upload_desc(s);
   if (rc) return rc;
   BMC_CUDA(cudaStreamSynchronize(s->stream));
   return BMC_OK;
@@ -1947,6 +1977,23 @@ int upload_maps(bmc_scenario* s) {
   }
   if (s->graph) cudaGraphExecDestroy(s->graph);
   s->graph = nullptr;
+  // the gas domain of bmc_gas_set back in place (a switch to a map's gas
+  // state overwrites it); the maps' gas states are carved below when every
+  // map has one
+  if (h.gas) {
+    h.g_in_ptr = s->g_cur_ptr;
+    h.g_in_idx = s->g_cur_idx;
+    h.g_in_flow = s->g_cur_flow;
+    BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.gvinv), s->g_vinv.data(), n_c * 8, cudaMemcpyHostToDevice,
+                                  s->stream));
+    BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.g_diag), s->g_diag.data(), n_c * 8, cudaMemcpyHostToDevice,
+                                  s->stream));
+    BMC_CUDA(counted_memcpy_async(const_cast<double*>(h.kla), s->g_kla.data(), s->g_kla.size() * 8,
+                                  cudaMemcpyHostToDevice, s->stream));
+  }
+  h.map_gvinv = h.map_g_diag = h.map_g_in_flow = h.map_kla = nullptr;
+  h.map_g_in_ptr = h.map_g_in_idx = nullptr;
+  h.map_g_nnz_max = 0;
   if (nm == 0) {
     h.n_maps = 0;
     h.n_per_map = 1;
@@ -1980,6 +2027,26 @@ int upload_maps(bmc_scenario* s) {
   cv.add(&c_ptr, n_c + 1);
   cv.add(&c_idx, nnz_max);
   cv.add(&c_flow, nnz_max);
+  // gas states, when every map has one, and the current gas transition
+  // lists, large enough for every map's
+  const bool gas_maps =
+      h.gas && std::all_of(s->maps.begin(), s->maps.end(), [](const bmc_scenario::FlowMap& m) { return m.has_gas; });
+  const size_t ne = n_c * h.n_s;
+  size_t gmax = 1;
+  double *q_gvinv = nullptr, *q_gdiag = nullptr, *q_gflow = nullptr, *q_kla = nullptr, *cg_flow = nullptr;
+  uint32_t *q_gptr = nullptr, *q_gidx = nullptr, *cg_ptr = nullptr, *cg_idx = nullptr;
+  if (gas_maps) {
+    for (const auto& m : s->maps) gmax = std::max(gmax, m.gidx.size());
+    cv.add(&q_gvinv, nm * n_c);
+    cv.add(&q_gdiag, nm * n_c);
+    cv.add(&q_gptr, nm * (n_c + 1));
+    cv.add(&q_gidx, nm * gmax);
+    cv.add(&q_gflow, nm * gmax);
+    cv.add(&q_kla, nm * ne);
+    cv.add(&cg_ptr, n_c + 1);
+    cv.add(&cg_idx, gmax);
+    cv.add(&cg_flow, gmax);
+  }
   BMC_CUDA(cudaMalloc(&s->marena, cv.off));
   cv.bind(s->marena);
   BMC_CUDA(cudaMemsetAsync(s->marena, 0, cv.off, s->stream));
@@ -2006,6 +2073,33 @@ int upload_maps(bmc_scenario* s) {
   h.map_in_flow = p_flow;
   h.map_exit_thr = p_exit;
   h.map_nnz_max = (uint32_t)nnz_max;
+  if (gas_maps) {
+    for (size_t m = 0; m < nm; ++m) {
+      const auto& f = s->maps[m];
+      BMC_CUDA(counted_memcpy_async(q_gvinv + m * n_c, f.gvinv.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+      BMC_CUDA(counted_memcpy_async(q_gdiag + m * n_c, f.gdiag.data(), n_c * 8, cudaMemcpyHostToDevice, s->stream));
+      BMC_CUDA(counted_memcpy_async(q_gptr + m * (n_c + 1), f.gptr.data(), (n_c + 1) * 4, cudaMemcpyHostToDevice,
+                                    s->stream));
+      if (!f.gidx.empty()) {
+        BMC_CUDA(counted_memcpy_async(q_gidx + m * gmax, f.gidx.data(), f.gidx.size() * 4, cudaMemcpyHostToDevice,
+                                      s->stream));
+        BMC_CUDA(counted_memcpy_async(q_gflow + m * gmax, f.gval.data(), f.gval.size() * 8, cudaMemcpyHostToDevice,
+                                      s->stream));
+      }
+      BMC_CUDA(counted_memcpy_async(q_kla + m * ne, f.kla.data(), ne * 8, cudaMemcpyHostToDevice, s->stream));
+    }
+    h.map_gvinv = q_gvinv;
+    h.map_g_diag = q_gdiag;
+    h.map_g_in_ptr = q_gptr;
+    h.map_g_in_idx = q_gidx;
+    h.map_g_in_flow = q_gflow;
+    h.map_kla = q_kla;
+    h.map_g_nnz_max = (uint32_t)gmax;
+    // filled by the first step's switch to a map
+    h.g_in_ptr = cg_ptr;
+    h.g_in_idx = cg_idx;
+    h.g_in_flow = cg_flow;
+  }
   s->d_map_exit = p_exit;
   h.in_ptr = c_ptr;
   h.in_idx = c_idx;
@@ -2053,6 +2147,36 @@ int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neigh
   if (nnz == 0)
     for (uint32_t j = 0; j < n_c; ++j) f.diag[j] = -f.outf[j];
   s->maps.push_back(std::move(f));
+  return upload_maps(s);
+}
+
+int bmc_flowmap_add_gas(bmc_scenario* s, uint32_t map, const double* gas_volume, uint64_t nnz, const uint64_t* rows,
+                        const uint64_t* cols, const double* values, const double* kla) {
+  if (const int rc_settle = settle_export(s)) return rc_settle;
+  if (!s || !gas_volume || (nnz && (!rows || !cols || !values))) return fail(BMC_E_INVALID, "bad gas flow-map arguments");
+  if (!s->h.gas) return fail(BMC_E_STATE, "no gas phase (bmc_gas_set)");
+  if (map >= s->maps.size()) return fail(BMC_E_INVALID, "no such flow map (bmc_flowmap_add first)");
+  const uint32_t n_c = s->h.n_c;
+  const size_t ne = (size_t)n_c * s->h.n_s;
+  bmc_scenario::FlowMap& f = s->maps[map];
+  std::vector<double> gvinv(n_c);
+  for (uint32_t j = 0; j < n_c; ++j) {
+    if (!(gas_volume[j] > 0.0)) return fail(BMC_E_INVALID, "gas volumes must be > 0");
+    gvinv[j] = 1.0 / gas_volume[j];
+  }
+  std::vector<double> k(kla ? kla : s->g_kla.data(), (kla ? kla : s->g_kla.data()) + ne);
+  for (double v : k)
+    if (!(v >= 0.0)) return fail(BMC_E_INVALID, "kla must be >= 0");
+  std::vector<uint32_t> ptr, idx;
+  std::vector<double> val, diag;
+  if (const char* why = build_csr(n_c, nnz, rows, cols, values, ptr, idx, val, diag)) return fail(BMC_E_INVALID, why);
+  f.gvinv = std::move(gvinv);
+  f.gdiag = std::move(diag);
+  f.gptr = std::move(ptr);
+  f.gidx = std::move(idx);
+  f.gval = std::move(val);
+  f.kla = std::move(k);
+  f.has_gas = true;
   return upload_maps(s);
 }
 

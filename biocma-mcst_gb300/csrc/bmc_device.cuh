@@ -333,6 +333,15 @@ struct ScenDev {
   const uint32_t* map_in_idx;    // [n_maps][map_nnz_max]
   const double* map_in_flow;     // [n_maps][map_nnz_max]
   const uint32_t* map_exit_thr;  // [n_maps][kMaxOutlets], for the current dt
+  // gas state of every flow map, switched with it (map_g_nnz_max == 0: the
+  // gas domain stays fixed while the maps cycle)
+  const double* map_gvinv;       // [n_maps][n_c]
+  const double* map_g_diag;      // [n_maps][n_c]
+  const uint32_t* map_g_in_ptr;  // [n_maps][n_c + 1]
+  const uint32_t* map_g_in_idx;  // [n_maps][map_g_nnz_max]
+  const double* map_g_in_flow;   // [n_maps][map_g_nnz_max]
+  const double* map_kla;         // [n_maps][n_c * n_s]
+  uint32_t map_g_nnz_max;
   // Gas phase of a two-phase flow (gas == 0: liquid only): its own volumes,
   // transition (incoming lists + diagonal) and feeds, concentrations double
   // buffered like C, and the gas-liquid transfer

@@ -1617,6 +1617,26 @@ __global__ void k_flowmap(ScenDev* __restrict__ sc) {
     const_cast<uint32_t*>(S.in_idx)[e] = S.map_in_idx[on + e];
     const_cast<double*>(S.in_flow)[e] = S.map_in_flow[on + e];
   }
+  if (S.map_g_nnz_max != 0u) {
+    // the map's gas state: volumes (as inverses), transition and kla; the
+    // gas masses are kept, as the liquid's (SimulationUnit::
+    // updateScalarHydro and MassTransferModel::update, simulation.cpp
+    // L120-L139)
+    const size_t ne = (size_t)n_c * S.n_s;
+    for (unsigned c = t0; c < n_c; c += stride) {
+      const_cast<double*>(S.gvinv)[c] = S.map_gvinv[o + c];
+      const_cast<double*>(S.g_diag)[c] = S.map_g_diag[o + c];
+    }
+    for (size_t e = t0; e < ne; e += stride) const_cast<double*>(S.kla)[e] = S.map_kla[(size_t)m * ne + e];
+    const uint32_t* gptr = S.map_g_in_ptr + (size_t)m * (n_c + 1);
+    for (unsigned c = t0; c <= n_c; c += stride) const_cast<uint32_t*>(S.g_in_ptr)[c] = gptr[c];
+    const unsigned gnnz = gptr[n_c];
+    const size_t gon = (size_t)m * S.map_g_nnz_max;
+    for (unsigned e = t0; e < gnnz; e += stride) {
+      const_cast<uint32_t*>(S.g_in_idx)[e] = S.map_g_in_idx[gon + e];
+      const_cast<double*>(S.g_in_flow)[e] = S.map_g_in_flow[gon + e];
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------

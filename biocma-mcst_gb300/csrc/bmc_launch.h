@@ -16,7 +16,7 @@ namespace bmc {
 // Version of KernelSet's layout and of the meaning of its launch arguments
 // (such as the scatter forms a cycle launcher accepts); a plugin built
 // against another version is refused at load time.
-constexpr int kKernelSetAbi = 11;
+constexpr int kKernelSetAbi = 12;
 // Threads per block of the liquid step (k_liquid): kLiquidThreads / n_species
 // whole compartments per block, so a small domain still spreads over many SMs.
 constexpr unsigned kLiquidThreads = 32;

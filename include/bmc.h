@@ -411,6 +411,16 @@ int bmc_flowmap_add(bmc_scenario* s, const double* volume, const uint64_t* neigh
                     const double* out_flows, const double* cdf, uint64_t nnz, const uint64_t* rows,
                     const uint64_t* cols, const double* values);
 int bmc_flowmap_period(bmc_scenario* s, double t_per_flowmap);
+/* The gas state of flow map `map` (two-phase cases: the gas volumes and gas
+ * transition in COO form, as bmc_gas_set, and the kla [n_c][n_s] of that
+ * state, e.g. from bmc_mtr_turbulence_kla on its volumes; NULL keeps
+ * bmc_gas_set's).  Once every flow map has one, each switch also replaces
+ * the gas domain and kla, keeping the gas masses, as SimulationUnit::
+ * updateScalarHydro and MassTransferModel::update do (apps/libs/simulation/
+ * src/simulation.cpp L120-L139); until then the gas domain stays fixed.
+ * bmc_gas_set drops the maps' gas states. */
+int bmc_flowmap_add_gas(bmc_scenario* s, uint32_t map, const double* gas_volume, uint64_t nnz, const uint64_t* rows,
+                        const uint64_t* cols, const double* values, const double* kla);
 int bmc_flowmap_clear(bmc_scenario* s);
 
 /* ---- CMA ingestion (host only) ------------------------------------------- */
@@ -518,7 +528,8 @@ int bmc_cma_read_flowmap(const char* path, uint32_t* n_rows, uint32_t* n_cols, u
  * performStepGL, implScalar.cpp L229-L249; SimulationUnit::ode_step,
  * simulation.model.cpp L132-L150) and clears tiny negative liquid
  * concentrations (clearNegs, implScalar.cpp L266-L293).  Particles see the
- * liquid only.  The gas domain stays fixed while flow maps cycle. */
+ * liquid only.  The gas domain stays fixed while flow maps cycle, unless
+ * every map has a gas state (bmc_flowmap_add_gas). */
 int bmc_gas_set(bmc_scenario* s, const double* gas_volume, uint64_t nnz, const uint64_t* rows,
                 const uint64_t* cols, const double* values, const double* henry, const double* kla);
 int bmc_gas_set_concentrations(bmc_scenario* s, const double* conc);

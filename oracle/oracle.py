@@ -230,7 +230,9 @@ class Oracle:
         self.s = s
         self.weight = None
         self._map_arrays = {}
-        self._map_cur = 0
+        # no flow map applied yet: the first step applies map 0, as the
+        # device's first switch does (its gas state included)
+        self._map_cur = -1
 
     def _setup_gas(self, s, gas):
         """Gas phase arrays (kept alive on the object) and feeds."""
@@ -323,6 +325,22 @@ class Oracle:
         })
         for name, arr in keep.items():
             setattr(self.s, name, _ptr(arr))
+        gas = self.scen.gas
+        if gas is not None and gas.flowmaps:
+            # the map's gas state (SimulationUnit::updateScalarHydro and
+            # MassTransferModel::update): volumes, transition, kla; the gas
+            # masses are kept
+            gn = gas.flowmaps[m]
+            gkeep = self._map_arrays.setdefault(("gas", m), {
+                "gvinv": 1.0 / np.ascontiguousarray(gn.volume, dtype=np.float64),
+                "g_in_ptr": np.ascontiguousarray(gn.in_ptr, dtype=np.uint32),
+                "g_in_idx": np.ascontiguousarray(gn.in_idx, dtype=np.uint32),
+                "g_in_flow": np.ascontiguousarray(gn.in_flow, dtype=np.float64),
+                "g_out_flow": np.ascontiguousarray(gn.out_flow, dtype=np.float64),
+                "kla": np.ascontiguousarray(gas.kla_maps[m] if gas.kla_maps else gas.kla, dtype=np.float64),
+            })
+            for name, arr in gkeep.items():
+                setattr(self.s, name, _ptr(arr))
         for o in range(self.s.n_outlets):
             self.s.outlet_volume[o] = float(keep["volume"][self.s.outlet_index[o]])
         self.vol, self.vinv = keep["volume"], keep["vinv"]
@@ -330,7 +348,7 @@ class Oracle:
 
     def _switch_map(self):
         fm = self.scen.flowmaps
-        if len(fm) <= 1:
+        if not fm:
             return
         m = (int(self.s.step) // self.scen.n_per_flowmap) % len(fm)
         if m != self._map_cur:
@@ -343,7 +361,7 @@ class Oracle:
         return self.stats()
 
     def run(self, n_steps: int, n_threads: int = 1):
-        if len(self.scen.flowmaps) > 1:
+        if self.scen.flowmaps:  # the map switch runs between steps
             for _ in range(n_steps):
                 self.step(n_threads)
             return

@@ -132,3 +132,79 @@ def test_gpu_domain_calls_refused_while_cycling():
     _lib.call("bmc_flowmap_clear", g.handle)
     _lib.call("bmc_domain_update", g.handle, net.n_c, net.K, vol.ctypes.data, nbr.ctypes.data,
               outf.ctypes.data, cdf.ctypes.data)
+
+
+def gas_flowmap_scenario(n_particles=20000, seed=3):
+    """The flow-map scenario with a gas phase whose state changes with the
+    maps: per map, a gas ring on 10 % of that map's liquid volumes (varied)
+    and the turbulence kla of a dissipation field of its own."""
+    from bmc import cma
+    from bmc.networks import Network
+
+    sc = scenarios.with_gas(flowmap_scenario(n_particles=n_particles), kla=0.05, henry=3.181e-2)
+    rng = np.random.default_rng(seed)
+    gmaps, klas = [], []
+    for net in sc.flowmaps:
+        vol = net.volume * 0.1 * rng.uniform(0.8, 1.2, size=net.n_c)
+        src = np.arange(net.n_c)
+        q = 0.2 * float(np.min(vol)) / sc.dt
+        gmaps.append(Network(net.n_c, vol, src, (src + 1) % net.n_c, q * rng.uniform(0.8, 1.2, size=net.n_c)).finalize())
+        kla = np.zeros((net.n_c, sc.n_species))
+        kla[:, 1] = cma.turbulence_kla(rng.lognormal(-1.0, 0.5, net.n_c), net.volume, vol)
+        klas.append(kla)
+    sc.gas.flowmaps = gmaps
+    sc.gas.kla_maps = klas
+    return sc
+
+
+def test_identical_gas_states_equal_a_fixed_gas_domain(oracle_mod):
+    """Maps whose gas states all equal the gas phase's domain run as the fixed
+    gas domain, bit for bit."""
+    sc = gas_flowmap_scenario(n_particles=5000)
+    same = dataclasses.replace(sc, gas=dataclasses.replace(sc.gas, flowmaps=[sc.gas.net] * 3, kla_maps=[]))
+    fixed = dataclasses.replace(sc, gas=dataclasses.replace(sc.gas, flowmaps=[], kla_maps=[]))
+    a, b = oracle_mod.Oracle(same), oracle_mod.Oracle(fixed)
+    a.init_particles()
+    b.init_particles()
+    for _ in range(13):
+        assert a.step() == b.step()
+    assert np.array_equal(a.Cg, b.Cg) and np.array_equal(a.C, b.C)
+
+
+def test_gas_states_switch_with_the_maps(oracle_mod):
+    """A switch replaces the gas volumes and keeps the gas masses; the run
+    then departs from the fixed gas domain."""
+    sc = gas_flowmap_scenario(n_particles=5000)
+    a = oracle_mod.Oracle(sc)
+    b = oracle_mod.Oracle(dataclasses.replace(sc, gas=dataclasses.replace(sc.gas, flowmaps=[], kla_maps=[])))
+    a.init_particles()
+    b.init_particles()
+    for _ in range(9):
+        a.step()
+        b.step()
+    assert a._map_cur == (9 - 1) // 4 % 3
+    assert not np.array_equal(a.Cg, b.Cg)
+    # the masses the switch keeps: Cg follows them through the new volumes
+    # at the next step, never jumps at the switch itself
+    assert np.all(np.isfinite(a.Cg)) and np.all(a.Mg >= 0)
+
+
+@pytest.mark.gpu
+def test_gpu_gas_flowmaps_match_oracle(oracle_mod):
+    """Two-phase run whose gas domain and kla switch with the flow maps:
+    device and restatement step for step, and in captured graph runs."""
+    from test_gpu_parity import assert_same_liquid, assert_same_particles, assert_same_stats, make_pair, same_bits
+
+    sc = gas_flowmap_scenario()
+    g, o = make_pair(oracle_mod, sc)
+    for k in range(14):
+        assert_same_stats(g.step(), o.step(), f"step {k}")
+        assert_same_liquid(g, o, f"step {k}")
+        gg = g.gas()
+        for key, ref in (("Cg", o.Cg), ("Mg", o.Mg), ("mtr", o.mtr)):
+            assert same_bits(gg[key], ref), f"step {k}: {key}"
+    assert_same_particles(g, o, "steps")
+    g.run(10)
+    o.run(10)
+    assert_same_liquid(g, o, "graph run")
+    assert same_bits(g.gas()["Cg"], o.Cg)
