@@ -81,13 +81,23 @@ class Records:
         flow map's when given), the particle count per compartment and the
         tallies of the last step."""
         sc = self.g.scen
+        # the flow map the domain holds: the one the last step ran on
+        fm = getattr(sc, "flowmaps", None) or []
+        m = None
+        if fm:
+            step = int(self.g.stats()["step"])
+            m = ((step - 1) // sc.n_per_flowmap) % len(fm) if step > 0 else 0
+        if volume is None:
+            volume = fm[m].volume if m is not None else sc.net.volume
         self._append("records/time", float(t))
         self._append("records/concentration_liquid", self.g.liquid()["C"])
-        self._append("records/volume_liquid", np.asarray(sc.net.volume if volume is None else volume, dtype=float))
+        self._append("records/volume_liquid", np.asarray(volume, dtype=float))
         if getattr(sc, "gas", None) is not None:
             gas = self.g.gas()
+            gfm = getattr(sc.gas, "flowmaps", None) or []
+            gvol = gfm[m].volume if (gfm and m is not None) else sc.gas.net.volume
             self._append("records/concentration_gas", gas["Cg"])
-            self._append("records/volume_gas", np.asarray(sc.gas.net.volume, dtype=float))
+            self._append("records/volume_gas", np.asarray(gvol, dtype=float))
             self._append("records/mtr", gas["mtr"])
         self._append("records/number_particle", self.g.repartition().astype(np.uint64))
         ev = self.g.events(clear=True)

@@ -47,6 +47,9 @@ class FakeScenario:
     def liquid(self):
         return {"C": self.o.C.copy()}
 
+    def gas(self):
+        return {"Cg": self.o.Cg.copy(), "Mg": self.o.Mg.copy(), "mtr": self.o.mtr.copy()}
+
     def repartition(self):
         p = self.o.particles()
         idle = p["status"] == 0
@@ -56,6 +59,7 @@ class FakeScenario:
         st = {k: 0 for k in ("births", "exits", "moves", "overflow")}
         st.update(self.last)
         st["n_used"], st["inactive"] = int(self.o.s.n_used), int(self.o.s.inactive)
+        st["step"] = int(self.o.s.step)
         return st
 
     def probe_enable(self, cap):
@@ -136,6 +140,24 @@ def test_gpu_particle_dumps_match_the_restatement(oracle_mod):
         assert keys and sorted(keys) == sorted(k for k in b if k.startswith("biological_model/"))
         for k in keys:
             assert np.array_equal(a[k].view(np.uint64), b[k].view(np.uint64)), (model.name, k)
+
+
+def test_volumes_follow_the_flow_maps(oracle_mod):
+    """With flow maps, each export carries the volumes of the map the last
+    step ran on (the reference exports the current state's volumes)."""
+    import sys
+    import os
+
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_flowmap import gas_flowmap_scenario
+
+    sc = gas_flowmap_scenario(n_particles=3000)  # 3 maps, 4 steps each
+    f = FakeScenario(oracle_mod, sc)
+    a = export.Records(f, dump_particles=False).run(12, dump_interval=2).arrays()
+    for k, done in enumerate(range(0, 13, 2)):
+        m = ((done - 1) // 4) % 3 if done > 0 else 0
+        assert np.array_equal(a["records/volume_liquid"][k], sc.flowmaps[m].volume), done
+        assert np.array_equal(a["records/volume_gas"][k], sc.gas.flowmaps[m].volume), done
 
 
 def _probe_scenario():
