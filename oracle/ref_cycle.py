@@ -39,8 +39,12 @@ import oracle as _orc
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_LIB = os.path.join(HERE, "_ref", "libbmc_ref.so")
+# the same cycle built with the reference's probes on (use_probe, a buffer of
+# 10,000 values per probe)
+REF_PROBE_LIB = os.path.join(HERE, "_ref", "libbmc_ref_probe.so")
+REF_PROBE_CAPACITY = 10000
 VP = ct.c_void_p
-_LIB = None
+_LIBS = {}
 
 # draw kinds of the stand-in's random pool: 0 float uniform, 1 double
 # uniform, 2 standard normal; SimpleAcetate::division draws two log-normal
@@ -74,14 +78,13 @@ def digest(p: dict, births: int, model_id: int) -> str:
     return h.hexdigest()[:32]
 
 
-def available() -> bool:
-    return os.path.exists(REF_LIB)
+def available(probes: bool = False) -> bool:
+    return os.path.exists(REF_PROBE_LIB if probes else REF_LIB)
 
 
-def ref_lib():
-    global _LIB
-    if _LIB is None:
-        L = ct.CDLL(REF_LIB)
+def ref_lib(probes: bool = False):
+    if probes not in _LIBS:
+        L = ct.CDLL(REF_PROBE_LIB if probes else REF_LIB)
         L.ref_cycle_new.restype = VP
         L.ref_cycle_new.argtypes = [ct.c_int32, ct.c_uint32, ct.c_uint32, ct.c_uint32, VP, VP, VP, VP, ct.c_uint32,
                                     VP, VP, VP, ct.c_uint64, VP, VP, VP, VP, ct.c_double, ct.c_uint64, ct.c_double,
@@ -96,9 +99,12 @@ def ref_lib():
         L.ref_cycle_set_leaving.argtypes = [VP, ct.c_uint32, VP]
         L.ref_cycle_step_stream.restype = ct.c_int32
         L.ref_cycle_step_stream.argtypes = [VP, ct.c_double, VP, ct.c_uint64, VP, VP, VP, VP]
-        L.ref_assert_failures.restype = ct.c_long
-        _LIB = L
-    return _LIB
+        if hasattr(L, "ref_assert_failures"):  # the pin library's (not the probe build's)
+            L.ref_assert_failures.restype = ct.c_long
+        L.ref_cycle_probe.restype = ct.c_uint64
+        L.ref_cycle_probe.argtypes = [VP, ct.c_int32, VP, ct.c_uint64, VP]
+        _LIBS[probes] = L
+    return _LIBS[probes]
 
 
 def _p(a: np.ndarray):
@@ -126,7 +132,9 @@ class RefCycle:
     """The reference's compiled cycle holding a copy of the oracle's
     container (after init_particles)."""
 
-    def __init__(self, o, particles_per_team: int = 64):
+    def __init__(self, o, particles_per_team: int = 64, probes: bool = False):
+        """probes: run the cycle built with the reference's probes on."""
+        self.L = ref_lib(probes)
         sc = o.scen
         net = sc.net
         m = sc.model
@@ -155,7 +163,7 @@ class RefCycle:
             kinds=np.array(DIV_KINDS[self.model], np.int32),
         )
         k = self._keep
-        self.h = ref_lib().ref_cycle_new(self.model, net.n_c, net.K, sc.n_species, _p(k["vol"]), _p(k["out_flow"]),
+        self.h = self.L.ref_cycle_new(self.model, net.n_c, net.K, sc.n_species, _p(k["vol"]), _p(k["out_flow"]),
                                          _p(k["nbr"]), _p(k["cdf"]), len(outs), _p(k["oi"]), _p(k["of"]),
                                          _p(k["ov"]), n, _p(k["state"]), _p(k["pos"]), _p(k["age_h"]),
                                          _p(k["age_d"]), float(o.weight), int(o.s.min_removal),
@@ -165,17 +173,17 @@ class RefCycle:
 
     def close(self):
         if self.h:
-            ref_lib().ref_cycle_free(self.h)
+            self.L.ref_cycle_free(self.h)
             self.h = None
 
     def __del__(self):
         self.close()
 
     def misses(self) -> int:
-        return int(ref_lib().ref_cycle_misses(self.h))
+        return int(self.L.ref_cycle_misses(self.h))
 
     def particles(self) -> dict:
-        L = ref_lib()
+        L = self.L
         n = int(L.ref_cycle_read(self.h, 0, None, None, None, None, None))
         cap = max(n, 1)
         st = np.zeros((self.n_var, cap), np.float32)
@@ -200,12 +208,12 @@ class RefCycle:
         n_out = int(o.s.n_outlets)
         if n_out:
             flows = np.array([o.s.outlet_flow[k] for k in range(n_out)], np.float64)
-            ref_lib().ref_cycle_set_leaving(self.h, n_out, _p(flows))
+            self.L.ref_cycle_set_leaving(self.h, n_out, _p(flows))
         stats = np.zeros(8, np.uint64)
         ex = np.zeros(self.n_ctb * self.n_c)
         ab = np.zeros(self.n_ctb * self.n_c)
         sc = np.zeros(self.n_ctb * self.n_c, np.float32)
-        rc = ref_lib().ref_cycle_step(self.h, o.scen.dt, _p(conc), _p(tab["move0"]), _p(tab["move1"]),
+        rc = self.L.ref_cycle_step(self.h, o.scen.dt, _p(conc), _p(tab["move0"]), _p(tab["move1"]),
                                       _p(tab["exit"]), _p(tab["div"]), _p(self._keep["kinds"]), _p(stats), _p(ex),
                                       _p(ab), _p(sc))
         if rc != 0:
@@ -230,7 +238,7 @@ class RefCycle:
         for _ in range(n_steps):
             L.orc_liquid_step(ct.byref(o.s), o.scen.dt)
             conc = np.ascontiguousarray(o.C, np.float64)
-            if ref_lib().ref_cycle_step_stream(self.h, o.scen.dt, _p(conc), seed, _p(stats), _p(ex), _p(ab),
+            if self.L.ref_cycle_step_stream(self.h, o.scen.dt, _p(conc), seed, _p(stats), _p(ex), _p(ab),
                                                _p(sc)) != 0:
                 break
             o.src[:, :self.n_ctb] = ex.reshape(self.n_ctb, self.n_c).T
@@ -290,3 +298,12 @@ class RefCycle:
         out["moves_n"] = int(os_["moves"])
         out["compacted"] = int(os_["compacted"])
         return out
+
+
+    def probe(self, k: int) -> tuple[np.ndarray, bool]:
+        """Values probe k (0 leaving times, 1 division times) holds and
+        whether it needs exporting (Probes::get, need_export)."""
+        out = np.zeros(REF_PROBE_CAPACITY)
+        full = ct.c_int32()
+        n = int(self.L.ref_cycle_probe(self.h, k, _p(out), len(out), ct.byref(full)))
+        return out[:min(n, len(out))].copy(), bool(full.value)

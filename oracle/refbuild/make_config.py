@@ -10,6 +10,11 @@ compile-time flags (event counter on, probes off).
 
     python make_config.py <reference root> <output header>
     python make_config.py --variant <reference root> <output header>
+    python make_config.py --probe <reference root> <output header>
+
+With --probe the configuration has the reference's probes on (use_probe =
+true, its buffer of probe_buffer_size values), for the build of its cycle
+whose probe records pin the oracle's.
 
 With --variant it writes the model-variant header instead
 (apps/autogenerated/variant_model.hxx, which the reference's
@@ -47,8 +52,9 @@ DEFINES = {"_BIOMC_VERSION_MAJOR": "1", "_BIOMC_VERSION_MINOR": "2", "_BIOMC_VER
            "_BIOMC_BUILD_MODE": '"release"'}
 
 
-def main(ref_root: str, out: str) -> None:
+def main(ref_root: str, out: str, probes: bool = False) -> None:
     src = open(f"{ref_root}/apps/autogenerated/biocma_cst_config.hpp.in").read()
+    values = dict(VALUES, use_probe="true") if probes else VALUES
 
     def mesondefine(m):
         name = m.group(1)
@@ -58,9 +64,9 @@ def main(ref_root: str, out: str) -> None:
 
     def at(m):
         name = m.group(1)
-        if name not in VALUES:
+        if name not in values:
             raise KeyError(f"no value for @{name}@")
-        return VALUES[name]
+        return values[name]
 
     src = re.sub(r"@(\w+)@", at, src)
     with open(out, "w") as f:
@@ -82,5 +88,7 @@ def variant(ref_root: str, out: str) -> None:
 if __name__ == "__main__":
     if sys.argv[1] == "--variant":
         variant(sys.argv[2], sys.argv[3])
+    elif sys.argv[1] == "--probe":
+        main(sys.argv[2], sys.argv[3], probes=True)
     else:
         main(sys.argv[1], sys.argv[2])

@@ -171,6 +171,8 @@ struct CycleBase {
   virtual uint32_t n_ctb() const = 0;
   virtual void set_leaving(uint32_t n, const double* flow) = 0;
   virtual uint64_t capacity() const = 0;
+  // values the probe holds (Probes::get) and whether it needs exporting
+  virtual uint64_t probe(int k, double* out, uint64_t max, int32_t* full) const = 0;
 };
 
 template <class M>
@@ -184,6 +186,9 @@ struct Cycle final : CycleBase {
   MC::kernelContribution contribs;
   MC::ContributionView scatter;
   MC::EventContainer events;
+  // the functors get copies of these handles (Views share their storage):
+  // leaving times, division times; inactive unless built with use_probe
+  Simulation::ProbeAutogeneratedBuffer probe_leave, probe_div;
   KI::CycleFunctors<Exec, M> functors;
 
   static KernelDispatchOptions options(uint32_t ppt) {
@@ -225,7 +230,7 @@ struct Cycle final : CycleBase {
         opt(options(ppt)), container(runtime(min_removal, ratio), n, 0), contribs("contribs", M::n_c, n_c_),
         scatter(Kokkos::Experimental::create_scatter_view(contribs)),
         functors(opt, container, MC::pool_type(), MC::KernelConcentrationType(conc.data(), n_s_, n_c_), scatter,
-                 events, domain(), Simulation::ProbeAutogeneratedBuffer(), Simulation::ProbeAutogeneratedBuffer()) {
+                 events, domain(), probe_leave, probe_div) {
     for (uint64_t i = 0; i < n; ++i) {
       for (uint32_t v = 0; v < M::n_var; ++v) container.model(i, v) = state[(std::size_t)v * n + i];
       container.position(i) = pos[i];
@@ -321,6 +326,14 @@ struct Cycle final : CycleBase {
     for (uint32_t o = 0; o < n && o < lf.size(); ++o) lf[o].flow = flow[o];
   }
   uint64_t capacity() const override { return container.capacity(); }
+  uint64_t probe(int k, double* out, uint64_t max, int32_t* full) const override {
+    const auto& p = k == 0 ? probe_leave : probe_div;
+    const auto v = p.get();
+    const uint64_t n = std::min<uint64_t>(v.size(), max);
+    for (uint64_t i = 0; i < n; ++i) out[i] = v[i];
+    if (full) *full = p.need_export() ? 1 : 0;
+    return v.size();
+  }
 };
 
 struct Handle {
@@ -362,6 +375,12 @@ void ref_cycle_free(void* h) { delete static_cast<Handle*>(h); }
 uint32_t ref_cycle_n_var(void* h) { return static_cast<Handle*>(h)->c->n_var(); }
 uint32_t ref_cycle_n_ctb(void* h) { return static_cast<Handle*>(h)->c->n_ctb(); }
 uint64_t ref_cycle_capacity(void* h) { return static_cast<Handle*>(h)->c->capacity(); }
+// Probe k (0 leaving times, 1 division times): copies up to max of the
+// values it holds into out, sets *full when it needs exporting, returns how
+// many it holds (0 in the build without use_probe).
+uint64_t ref_cycle_probe(void* h, int32_t k, double* out, uint64_t max, int32_t* full) {
+  return static_cast<Handle*>(h)->c->probe(k, out, max, full);
+}
 long ref_cycle_misses(void* h) { return static_cast<Handle*>(h)->misses; }
 
 // One cycle with the concentrations conc [n_c][n_s] and the draws of every
