@@ -167,6 +167,14 @@ int main(int argc, char** argv) {
     put(out, pos.data(), n);
     put(out, status.data(), n);
     put(out, id.data(), n);
+    // the run's event tallies (the exporter's records/tallies) and every
+    // particle's Model::mass (the particle dump's mass column)
+    uint64_t events[BMC_N_EVENTS] = {};
+    if (bmc_read_events(backend.handle(), events, 0) != BMC_OK) throw std::runtime_error(bmc_last_error());
+    put(out, events, BMC_N_EVENTS);
+    std::vector<double> mass(n);
+    if (bmc_read_mass(backend.handle(), n, mass.data(), &got) != BMC_OK) throw std::runtime_error(bmc_last_error());
+    put(out, mass.data(), n);
     std::fclose(out);
   } catch (const std::exception& e) {
     std::fprintf(stderr, "backend_demo: %s\n", e.what());

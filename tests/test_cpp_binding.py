@@ -98,6 +98,11 @@ def test_cpp_binding_equals_python_binding(tmp_path):
     assert np.array_equal(np.frombuffer(raw, np.uint8, n, off), p["status"])
     off += n
     assert np.array_equal(np.frombuffer(raw, np.uint32, n, off), p["id"])
+    off += 4 * n
+    ev = np.frombuffer(raw, np.uint64, 6, off)
+    off += 48
+    assert list(ev) == list(g.events().values())
+    assert np.array_equal(np.frombuffer(raw, np.float64, n, off).view(np.uint64), g.mass().view(np.uint64))
     g.close()
 
 
