@@ -551,9 +551,11 @@ def served_form(window_s: float, rate: float = 50.0, budget: float = 160e9):
     """Poisson arrivals for `window_s` seconds, sizes as the batched workload,
     steps log-uniform on [100, 10000]; all requests are served to completion.
     The workload's 10-minute arrival window is shortened so the run stays
-    within minutes: p99 of an overloaded server grows with the window (the
-    queue grows), so the overloaded figure is a lower bound for 10 minutes;
-    at a sub-saturating rate the latencies are stationary."""
+    within minutes.  The seeded arrivals' first 10 s ask for more than their
+    10-minute average, which runs close to the server's capacity: the full
+    window (served_form(600.0)) sees longer queues near capacity, so its p99
+    is above the short window's; at a sub-saturating rate the latencies are
+    stationary."""
     from bmc import _lib, serve
 
     _lib.load()  # built and loaded before the arrival clock starts
